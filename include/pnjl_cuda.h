@@ -1,0 +1,191 @@
+/*
+ * pnjl_cuda.h -- C ABI of libpnjl_cuda, the GB300 (sm_103a) engine for the PNJL
+ * gap-equation parameter scan of w5851/Julia_RelaxTime.
+ *
+ * The reference has no native boundary (it is pure Julia).  These entry points are
+ * what its `ccall` shim binds in place of the Julia solver stack; each declaration
+ * names the reference function it stands in for.  Conventions:
+ *   - plain C types, SoA host (or device) arrays of FP64, int return codes
+ *     (PNJL_OK == 0), no exceptions across the boundary;
+ *   - units are the reference's: T, mu, M in fm^-1, phi in fm^-3, Omega in fm^-4;
+ *   - host buffers are caller-owned; device buffers are owned by the context;
+ *   - one context per host thread; every call on a context is serialised on its stream.
+ */
+#ifndef PNJL_CUDA_H
+#define PNJL_CUDA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- return codes ---- */
+#define PNJL_OK 0
+#define PNJL_ERR_INVALID_ARGUMENT 1
+#define PNJL_ERR_CUDA 2
+#define PNJL_ERR_NO_NODES 3
+#define PNJL_ERR_OUT_OF_MEMORY 4
+#define PNJL_ERR_NOT_TRAINED 5
+#define PNJL_ERR_TIMEOUT 6
+
+/* ---- per-point status (pnjl_result_soa.status) ---- */
+#define PNJL_POINT_CONVERGED 0        /* converged, physical, residual <= residual_norm_max */
+#define PNJL_POINT_NOT_CONVERGED 1    /* single-seed result kept, converged == 0            */
+#define PNJL_POINT_EXCEPTION 2        /* non-finite residual at the seed (NLsolve raises)   */
+#define PNJL_POINT_ALL_SEEDS_FAILED 3 /* solve_multi: "All seeds failed to converge ..."    */
+#define PNJL_POINT_INVALID_INPUT 4    /* T <= 0, xi <= -1 or a non-finite input             */
+
+/* ---- seed modes ---- */
+#define PNJL_SEEDS_TABLE 0     /* MultiSeed: every row of seed_table, min-Omega selection   */
+#define PNJL_SEEDS_PER_POINT 1 /* one seed per point (ContinuitySeed / DefaultSeed / learned),
+                                  MultiSeed over seed_table when it fails and
+                                  auto_multiseed_fallback != 0                               */
+
+/* ---- arithmetic of the node integrand ---- */
+#define PNJL_PREC_FP64 0  /* every pass in FP64 (the plain method)                          */
+#define PNJL_PREC_MIXED 1 /* Newton passes with an FP32 Kahan-compensated integrand; the
+                             residual that decides convergence, Omega and the thermo output
+                             come from FP64 passes                                          */
+
+/* Model constants in fm units; src/Constants_PNJL.jl:82-103 (hbarc, N_color, rho0,
+ * Lambda, G, K, m_ud0, m_s0, T0, a0, a1, a2, b3). */
+typedef struct pnjl_params {
+    double hbarc_MeV_fm;
+    double Lambda;
+    double G;
+    double K;
+    double m_ud0;
+    double m_s0;
+    double T0;
+    double a0, a1, a2, b3;
+    double N_color;
+    double rho0;
+} pnjl_params;
+
+typedef struct pnjl_ctx pnjl_ctx;
+
+/* Options of one batched solve; the fields mirror the keyword arguments of
+ * solve(::FixedMu, ...) (src/pnjl/solver/ImplicitSolver.jl:211-223) and the NLsolve
+ * tolerances fixed at :112/:144. */
+typedef struct pnjl_solve_opts {
+    int32_t seed_mode;           /* PNJL_SEEDS_TABLE or PNJL_SEEDS_PER_POINT                  */
+    int32_t n_seeds;             /* rows of seed_table (1..16)                               */
+    const double *seed_table;    /* [n_seeds*5] host, (phi_u, phi_d, phi_s, Phi, Phibar)     */
+    const double *seed_table_hot;/* NULL or [n_seeds*5]: row used instead when T*hbarc >= hot_T_MeV
+                                    (DefaultSeed(:quark) -> VERY_HIGH_TEMP, SeedStrategies.jl:212-220) */
+    double hot_T_MeV;            /* 300 in the reference                                      */
+    const double *point_seeds;   /* [n*5] for PNJL_SEEDS_PER_POINT (same memory space as T)  */
+    int32_t max_iter;            /* NLsolve iterations (reference default 1000; scan 40)     */
+    double ftol;                 /* 1e-9 in the reference                                     */
+    double xtol;                 /* 1e-9                                                      */
+    double residual_norm_max;    /* 1e-6                                                      */
+    double phi_tol;              /* 1e-8, physicality window of Phi, Phibar                   */
+    double omega_tie_rtol;       /* candidates within rtol*|Omega_min| of the minimum count as
+                                    tied; the earliest seed wins (0 = strict argmin)           */
+    int32_t trust_region_fallback;   /* ImplicitSolver.jl:130-151                            */
+    int32_t auto_multiseed_fallback; /* ImplicitSolver.jl:306-327                            */
+    int32_t precision;           /* PNJL_PREC_FP64 / PNJL_PREC_MIXED                          */
+    int32_t reserved;
+} pnjl_solve_opts;
+
+/* Per-point results, SoA; any NULL pointer skips that output.  Fields follow SolverResult
+ * (ImplicitSolver.jl:178-193) plus the number densities of calculate_number_densities
+ * (Thermodynamics.jl:255-281) and the per-flavour densities rho_f = dP/dmu_f. */
+typedef struct pnjl_result_soa {
+    double *x;             /* [5n] solution (phi_u, phi_d, phi_s, Phi, Phibar)       */
+    double *omega;         /* [n]                                                    */
+    double *pressure;      /* [n]                                                    */
+    double *rho_norm;      /* [n]  sum(rho_f)/(3 rho0)                               */
+    double *entropy;       /* [n]                                                    */
+    double *energy;        /* [n]                                                    */
+    double *masses;        /* [3n]                                                   */
+    double *rho;           /* [3n]                                                   */
+    double *n_q;           /* [3n] quark number densities n_u, n_d, n_s              */
+    double *n_aq;          /* [3n] antiquark number densities                        */
+    double *residual_norm; /* [n]  ||F||_inf of the chosen candidate                 */
+    int32_t *iterations;   /* [n]                                                    */
+    int32_t *chosen_seed;  /* [n]  row of seed_table, -1 for the per-point seed      */
+    int32_t *status;       /* [n]  PNJL_POINT_*                                      */
+    uint8_t *converged;    /* [n]                                                    */
+} pnjl_result_soa;
+
+/* Counters of the last solve on the context. */
+typedef struct pnjl_stats {
+    int64_t points;
+    int64_t passes_fp64;      /* full passes over the 3*p*t node-flavour mesh in FP64  */
+    int64_t passes_fp32;      /* ... in FP32                                          */
+    int64_t node_evals_fp64;  /* node-flavour evaluations actually executed (FP64)    */
+    int64_t node_evals_fp32;
+    int64_t seeds_run;        /* Newton (+ trust region) runs                          */
+    int64_t trust_region_runs;
+    int64_t multiseed_fallbacks;
+    int64_t kernel_launches;
+    double last_kernel_ms;    /* device time of the last solve kernel (CUDA events)    */
+} pnjl_stats;
+
+/* Default parameter set: config/pnjl/default.toml:1-21 through Constants_PNJL.jl:82-103. */
+int pnjl_params_default(pnjl_params *out);
+
+/* Context on one GPU; replaces the module-level constants of Constants_PNJL.jl (any
+ * profile loaded by load_pnjl_config, :57-73, is passed in here). */
+int pnjl_init(const pnjl_params *params, int device, pnjl_ctx **out);
+int pnjl_destroy(pnjl_ctx *ctx);
+/* Last error message of the context (thread-local to the context). */
+const char *pnjl_last_error(const pnjl_ctx *ctx);
+
+/* Gauss-Legendre meshes of cached_nodes(p_num, t_num) (src/pnjl/core/Integrals.jl:87-110,
+ * src/integration/GaussLegendre.jl:94-119): p on [0, p_max], cos(theta) on [0, 1] with
+ * doubled weights.  1 <= p_num <= 512, 1 <= t_num <= 64. */
+int pnjl_set_nodes(pnjl_ctx *ctx, int32_t p_num, int32_t t_num, double p_max);
+/* Copy the column-major meshes back (p_num*t_num each; any pointer may be NULL). */
+int pnjl_get_nodes(const pnjl_ctx *ctx, double *p_mesh, double *c_mesh, double *coef);
+
+/* Omega, grad_x Omega [5n] and Hessian_x Omega [25n, row-major] at given states:
+ * calculate_omega (Thermodynamics.jl:181-195) and the ForwardDiff gradient/Jacobian of
+ * gap_conditions (Conditions.jl:72-86; F = -grad_x Omega).  precision: PNJL_PREC_FP64 or
+ * PNJL_PREC_MIXED (FP32-Kahan integrand, FP64 assembly).  Host pointers; NULL skips. */
+int pnjl_eval_batch(pnjl_ctx *ctx, int64_t n, const double *x, const double *T,
+                    const double *mu_u, const double *mu_d, const double *mu_s,
+                    const double *xi, int32_t precision,
+                    double *omega, double *grad, double *hess);
+
+/* calculate_thermo + calculate_number_densities at given states
+ * (Thermodynamics.jl:233-244, :255-281).  Host pointers; fills pressure, rho_norm,
+ * entropy, energy, masses, rho, n_q, n_aq and omega of `out` (other fields untouched). */
+int pnjl_thermo_batch(pnjl_ctx *ctx, int64_t n, const double *x, const double *T,
+                      const double *mu_u, const double *mu_d, const double *mu_s,
+                      const double *xi, pnjl_result_soa *out);
+
+/* Batched solve(::FixedMu, T, mu; xi, seed_strategy, ...) over n points
+ * (ImplicitSolver.jl:211-328, solve_multi :532-559), flavour-resolved chemical
+ * potentials (Conditions.jl:205 takes mu_vec).  Host pointers, synchronous: the timed
+ * region of a caller includes the host<->device copies. */
+int pnjl_solve_batch(pnjl_ctx *ctx, int64_t n, const double *T, const double *mu_u,
+                     const double *mu_d, const double *mu_s, const double *xi,
+                     const pnjl_solve_opts *opts, pnjl_result_soa *out);
+
+/* Same with device pointers (inputs and outputs already in HBM); asynchronous on the
+ * context stream (see pnjl_stream).  opts->seed_table stays a host pointer;
+ * opts->point_seeds is a device pointer here. */
+int pnjl_solve_batch_device(pnjl_ctx *ctx, int64_t n, const double *d_T, const double *d_mu_u,
+                            const double *d_mu_d, const double *d_mu_s, const double *d_xi,
+                            const pnjl_solve_opts *opts, pnjl_result_soa *d_out);
+
+/* The context's CUDA stream (a cudaStream_t) and a blocking wait on it. */
+void *pnjl_stream(pnjl_ctx *ctx);
+int pnjl_synchronize(pnjl_ctx *ctx);
+int pnjl_get_stats(const pnjl_ctx *ctx, pnjl_stats *out);
+
+/* Number of streaming multiprocessors of the context's device. */
+int pnjl_device_sm_count(const pnjl_ctx *ctx);
+
+/* Launch shape of the solve kernel: lanes per point (8 or 32) and resident blocks
+ * per SM (0 = occupancy maximum).  Chosen by the autotuner; results do not depend on it. */
+int pnjl_set_tuning(pnjl_ctx *ctx, int32_t lanes_per_point, int32_t blocks_per_sm);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PNJL_CUDA_H */

@@ -1,0 +1,146 @@
+"""ctypes declarations of include/pnjl_cuda.h (the C ABI of libpnjl_cuda).
+
+This module only loads the in-tree library; it never falls back to anything else.  When
+the library is missing or cannot be loaded, :func:`lib` raises ``CudaLibraryError``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libpnjl_cuda.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "pnjl_cuda.h")
+
+PNJL_OK = 0
+PNJL_ERR_INVALID_ARGUMENT = 1
+PNJL_ERR_CUDA = 2
+PNJL_ERR_NO_NODES = 3
+PNJL_ERR_OUT_OF_MEMORY = 4
+PNJL_ERR_NOT_TRAINED = 5
+PNJL_ERR_TIMEOUT = 6
+
+PNJL_POINT_CONVERGED = 0
+PNJL_POINT_NOT_CONVERGED = 1
+PNJL_POINT_EXCEPTION = 2
+PNJL_POINT_ALL_SEEDS_FAILED = 3
+PNJL_POINT_INVALID_INPUT = 4
+
+PNJL_SEEDS_TABLE = 0
+PNJL_SEEDS_PER_POINT = 1
+
+PNJL_PREC_FP64 = 0
+PNJL_PREC_MIXED = 1
+
+dp = C.POINTER(C.c_double)
+i32p = C.POINTER(C.c_int32)
+u8p = C.POINTER(C.c_uint8)
+
+
+class CudaLibraryError(RuntimeError):
+    """libpnjl_cuda is missing, failed to load, or returned an error code."""
+
+
+class pnjl_params(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "hbarc_MeV_fm", "Lambda", "G", "K", "m_ud0", "m_s0", "T0", "a0", "a1", "a2", "b3", "N_color", "rho0")]
+
+
+class pnjl_solve_opts(C.Structure):
+    _fields_ = [
+        ("seed_mode", C.c_int32),
+        ("n_seeds", C.c_int32),
+        ("seed_table", dp),
+        ("seed_table_hot", dp),
+        ("hot_T_MeV", C.c_double),
+        ("point_seeds", dp),
+        ("max_iter", C.c_int32),
+        ("ftol", C.c_double),
+        ("xtol", C.c_double),
+        ("residual_norm_max", C.c_double),
+        ("phi_tol", C.c_double),
+        ("omega_tie_rtol", C.c_double),
+        ("trust_region_fallback", C.c_int32),
+        ("auto_multiseed_fallback", C.c_int32),
+        ("precision", C.c_int32),
+        ("reserved", C.c_int32),
+    ]
+
+
+class pnjl_result_soa(C.Structure):
+    _fields_ = [
+        ("x", dp), ("omega", dp), ("pressure", dp), ("rho_norm", dp), ("entropy", dp), ("energy", dp),
+        ("masses", dp), ("rho", dp), ("n_q", dp), ("n_aq", dp), ("residual_norm", dp),
+        ("iterations", i32p), ("chosen_seed", i32p), ("status", i32p), ("converged", u8p),
+    ]
+
+
+class pnjl_stats(C.Structure):
+    _fields_ = [
+        ("points", C.c_int64), ("passes_fp64", C.c_int64), ("passes_fp32", C.c_int64),
+        ("node_evals_fp64", C.c_int64), ("node_evals_fp32", C.c_int64), ("seeds_run", C.c_int64),
+        ("trust_region_runs", C.c_int64), ("multiseed_fallbacks", C.c_int64), ("kernel_launches", C.c_int64),
+        ("last_kernel_ms", C.c_double),
+    ]
+
+
+# name -> (restype, argtypes); every function declared in include/pnjl_cuda.h
+SIGNATURES = {
+    "pnjl_params_default": (C.c_int, [C.POINTER(pnjl_params)]),
+    "pnjl_init": (C.c_int, [C.POINTER(pnjl_params), C.c_int, C.POINTER(C.c_void_p)]),
+    "pnjl_destroy": (C.c_int, [C.c_void_p]),
+    "pnjl_last_error": (C.c_char_p, [C.c_void_p]),
+    "pnjl_set_nodes": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_double]),
+    "pnjl_get_nodes": (C.c_int, [C.c_void_p, dp, dp, dp]),
+    "pnjl_eval_batch": (C.c_int, [C.c_void_p, C.c_int64, dp, dp, dp, dp, dp, dp, C.c_int32, dp, dp, dp]),
+    "pnjl_thermo_batch": (C.c_int, [C.c_void_p, C.c_int64, dp, dp, dp, dp, dp, dp, C.POINTER(pnjl_result_soa)]),
+    "pnjl_solve_batch": (C.c_int, [C.c_void_p, C.c_int64, dp, dp, dp, dp, dp,
+                                   C.POINTER(pnjl_solve_opts), C.POINTER(pnjl_result_soa)]),
+    "pnjl_solve_batch_device": (C.c_int, [C.c_void_p, C.c_int64, dp, dp, dp, dp, dp,
+                                          C.POINTER(pnjl_solve_opts), C.POINTER(pnjl_result_soa)]),
+    "pnjl_stream": (C.c_void_p, [C.c_void_p]),
+    "pnjl_synchronize": (C.c_int, [C.c_void_p]),
+    "pnjl_get_stats": (C.c_int, [C.c_void_p, C.POINTER(pnjl_stats)]),
+    "pnjl_device_sm_count": (C.c_int, [C.c_void_p]),
+    "pnjl_set_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+}
+
+_lib = None
+
+
+def lib():
+    """Load libpnjl_cuda.so from the package tree (built by julia_relaxtime_gb300.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise CudaLibraryError(
+            f"{LIB_PATH} is missing: build it with `python -m julia_relaxtime_gb300.build` "
+            "(there is no CPU fallback)")
+    try:
+        L = C.CDLL(LIB_PATH)
+    except OSError as e:  # pragma: no cover - depends on the machine
+        raise CudaLibraryError(f"cannot load {LIB_PATH}: {e}") from e
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def declared_functions() -> list[str]:
+    """Names of the functions declared in include/pnjl_cuda.h (parsed from the header)."""
+    import re
+
+    with open(HEADER) as fh:
+        text = fh.read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(pnjl_[a-z0-9_]+)\s*\(", text)))
+
+
+def check(ctx, rc: int, what: str):
+    if rc != PNJL_OK:
+        msg = lib().pnjl_last_error(ctx)
+        msg = msg.decode() if msg else ""
+        raise CudaLibraryError(f"{what} failed with code {rc}: {msg}")

@@ -1,0 +1,553 @@
+// pnjl_capi.cu -- the extern "C" boundary of libpnjl_cuda (declared in include/pnjl_cuda.h).
+//
+// Owns the per-context state: device, stream, model constants, node meshes (FP64 and an
+// FP32 copy), a growable device workspace for the host-pointer entry points, the work-queue
+// head and the counters.  Every entry point returns a PNJL_* code and records a message
+// for pnjl_last_error(); no C++ exception crosses the boundary.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "pnjl_kernels.h"
+
+struct pnjl_ctx {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    pnjl_params params{};
+    pnjl::DevParams dp{};
+    // nodes
+    int p_num = 0, t_num = 0;
+    double p_max = 0.0;
+    std::vector<double> p_mesh, c_mesh, coef;
+    double *d_nodes = nullptr;  // p2 | pc2 | w
+    float *d_nodes_f = nullptr; // p2 | pc2 | w
+    // control block: [0] queue head, [1..15] counters
+    long long *d_ctrl = nullptr;
+    double *d_seed_tables = nullptr; // 2 * 16 * 5
+    // workspace for the host entry points
+    unsigned char *d_ws = nullptr;
+    size_t ws_cap = 0;
+    // tuning
+    int group = 32;
+    int blocks_per_sm = 0;  // 0 = occupancy maximum
+    pnjl_stats stats{};
+    std::string err;
+};
+
+namespace {
+
+int fail(pnjl_ctx *ctx, int code, const std::string &msg) {
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+int cuda_fail(pnjl_ctx *ctx, cudaError_t e, const char *what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    return fail(ctx, PNJL_ERR_CUDA, m);
+}
+
+#define PNJL_CUDA_TRY(ctx, call)                                   \
+    do {                                                           \
+        cudaError_t _e = (call);                                   \
+        if (_e != cudaSuccess) return cuda_fail((ctx), _e, #call); \
+    } while (0)
+
+// Gauss-Legendre rule on [a, b] (ascending): Newton's method on the Legendre polynomial
+// P_n evaluated by its three-term recurrence, started from cos(pi (k + 3/4) / (n + 1/2)),
+// weights 2 / ((1 - x^2) P_n'(x)^2).  Same published rule the reference obtains from
+// FastGaussQuadrature.gausslegendre (src/integration/GaussLegendre.jl:33-42, :94-119).
+void gauss_legendre(int n, double a, double b, std::vector<double> &x, std::vector<double> &w) {
+    x.assign(n, 0.0);
+    w.assign(n, 0.0);
+    const int half = (n + 1) / 2;
+    for (int k = 0; k < half; ++k) {
+        long double z = std::cos(M_PI * (k + 0.75) / (n + 0.5));
+        long double dp = 1.0L;
+        for (int iter = 0; iter < 64; ++iter) {
+            long double p0 = 1.0L, p1 = z;
+            for (int j = 2; j <= n; ++j) {
+                long double p2 = ((2.0L * j - 1.0L) * z * p1 - (j - 1.0L) * p0) / j;
+                p0 = p1;
+                p1 = p2;
+            }
+            if (n == 1) { p1 = z; p0 = 1.0L; }
+            dp = n * (z * p1 - p0) / (z * z - 1.0L);
+            long double dz = p1 / dp;
+            z -= dz;
+            if (std::fabs((double)dz) < 1e-19) break;
+        }
+        // derivative at the converged root
+        long double p0 = 1.0L, p1 = z;
+        for (int j = 2; j <= n; ++j) {
+            long double p2 = ((2.0L * j - 1.0L) * z * p1 - (j - 1.0L) * p0) / j;
+            p0 = p1;
+            p1 = p2;
+        }
+        if (n == 1) { p1 = z; p0 = 1.0L; }
+        dp = n * (z * p1 - p0) / (z * z - 1.0L);
+        const double wt = (double)(2.0L / ((1.0L - z * z) * dp * dp));
+        x[k] = -(double)z;
+        x[n - 1 - k] = (double)z;
+        w[k] = wt;
+        w[n - 1 - k] = wt;
+        if (2 * k + 1 == n) x[k] = 0.0;
+    }
+    const double scale = (b - a) / 2.0, shift = (b + a) / 2.0;
+    for (int i = 0; i < n; ++i) {
+        x[i] = scale * x[i] + shift;
+        w[i] = scale * w[i];
+    }
+}
+
+template <typename T>
+T *carve(unsigned char *&p, size_t count) {
+    T *r = reinterpret_cast<T *>(p);
+    size_t bytes = (count * sizeof(T) + 255) & ~size_t(255);
+    p += bytes;
+    return r;
+}
+size_t carve_size(size_t count, size_t elem) { return (count * elem + 255) & ~size_t(255); }
+
+int ensure_ws(pnjl_ctx *ctx, size_t bytes) {
+    if (bytes <= ctx->ws_cap) return PNJL_OK;
+    if (ctx->d_ws) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(ctx->d_ws);
+        ctx->d_ws = nullptr;
+        ctx->ws_cap = 0;
+    }
+    size_t cap = bytes + bytes / 4;
+    cudaError_t e = cudaMalloc(&ctx->d_ws, cap);
+    if (e != cudaSuccess) {
+        ctx->d_ws = nullptr;
+        return fail(ctx, PNJL_ERR_OUT_OF_MEMORY, std::string("workspace allocation failed: ") + cudaGetErrorString(e));
+    }
+    ctx->ws_cap = cap;
+    return PNJL_OK;
+}
+
+pnjl::KernelNodes kernel_nodes(const pnjl_ctx *ctx) {
+    pnjl::KernelNodes kn;
+    const int n = ctx->p_num * ctx->t_num;
+    kn.n = n;
+    kn.p2 = ctx->d_nodes;
+    kn.pc2 = ctx->d_nodes + n;
+    kn.w = ctx->d_nodes + 2 * n;
+    kn.p2f = ctx->d_nodes_f;
+    kn.pc2f = ctx->d_nodes_f + n;
+    kn.wf = ctx->d_nodes_f + 2 * n;
+    return kn;
+}
+
+int check_opts(pnjl_ctx *ctx, const pnjl_solve_opts *o) {
+    if (!o) return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "opts is NULL");
+    if (o->seed_mode != PNJL_SEEDS_TABLE && o->seed_mode != PNJL_SEEDS_PER_POINT)
+        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "unknown seed_mode");
+    const bool need_table = o->seed_mode == PNJL_SEEDS_TABLE || o->auto_multiseed_fallback;
+    if (need_table && (o->n_seeds < 1 || o->n_seeds > 16 || !o->seed_table))
+        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "seed table must have 1..16 rows");
+    if (o->seed_mode == PNJL_SEEDS_PER_POINT && !o->point_seeds)
+        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "point_seeds is NULL");
+    if (o->max_iter < 0 || o->max_iter > 100000) return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "max_iter out of range");
+    if (!(o->ftol > 0) || !(o->xtol >= 0) || !(o->residual_norm_max > 0) || !(o->phi_tol >= 0) ||
+        !(o->omega_tie_rtol >= 0))
+        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "tolerances must be positive");
+    if (o->precision != PNJL_PREC_FP64 && o->precision != PNJL_PREC_MIXED)
+        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "unknown precision");
+    return PNJL_OK;
+}
+
+int grid_for(pnjl_ctx *ctx, int group, size_t smem, int64_t n) {
+    int occ = pnjl::solve_kernel_occupancy(group, smem);
+    if (occ < 1) occ = 1;
+    int bps = ctx->blocks_per_sm > 0 ? std::min(ctx->blocks_per_sm, occ) : occ;
+    const int64_t groups_per_block = pnjl::kSolveThreads / group;
+    int64_t need = (n + groups_per_block - 1) / groups_per_block;
+    int64_t g = (int64_t)ctx->sm_count * bps;
+    if (need < g) g = need;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pnjl_params_default(pnjl_params *out) {
+    if (!out) return PNJL_ERR_INVALID_ARGUMENT;
+    const double hbarc = 197.327;
+    out->hbarc_MeV_fm = hbarc;
+    out->Lambda = 602.3 / hbarc;
+    out->m_ud0 = 5.5 / hbarc;
+    out->m_s0 = 140.7 / hbarc;
+    out->G = 1.835 / (out->Lambda * out->Lambda);
+    out->K = 12.36 / std::pow(out->Lambda, 5);
+    out->T0 = 210.0 / hbarc;
+    out->a0 = 3.51;
+    out->a1 = -2.47;
+    out->a2 = 15.2;
+    out->b3 = -1.75;
+    out->N_color = 3.0;
+    out->rho0 = 0.16;
+    return PNJL_OK;
+}
+
+int pnjl_init(const pnjl_params *params, int device, pnjl_ctx **out) {
+    if (!out) return PNJL_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    pnjl_ctx *ctx = new (std::nothrow) pnjl_ctx();
+    if (!ctx) return PNJL_ERR_OUT_OF_MEMORY;
+    if (params) ctx->params = *params;
+    else pnjl_params_default(&ctx->params);
+    const pnjl_params &p = ctx->params;
+    ctx->dp = pnjl::DevParams{p.hbarc_MeV_fm, p.Lambda, p.G, p.K, p.m_ud0, p.m_s0, p.T0,
+                              p.a0, p.a1, p.a2, p.b3, p.N_color, p.rho0};
+    ctx->device = device;
+    int rc = PNJL_OK;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_ctrl, 16 * sizeof(long long));
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_seed_tables, 2 * 16 * 5 * sizeof(double));
+    if (e != cudaSuccess) {
+        std::fprintf(stderr, "pnjl_init: %s\n", cudaGetErrorString(e));
+        rc = PNJL_ERR_CUDA;
+        pnjl_destroy(ctx);
+        return rc;
+    }
+    *out = ctx;
+    return PNJL_OK;
+}
+
+int pnjl_destroy(pnjl_ctx *ctx) {
+    if (!ctx) return PNJL_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    cudaFree(ctx->d_nodes);
+    cudaFree(ctx->d_nodes_f);
+    cudaFree(ctx->d_ctrl);
+    cudaFree(ctx->d_seed_tables);
+    cudaFree(ctx->d_ws);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return PNJL_OK;
+}
+
+const char *pnjl_last_error(const pnjl_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int pnjl_set_nodes(pnjl_ctx *ctx, int32_t p_num, int32_t t_num, double p_max) {
+    if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
+    if (p_num < 1 || p_num > 512 || t_num < 1 || t_num > 64 || !(p_max > 0.0))
+        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "node counts out of range (1..512 x 1..64, p_max > 0)");
+    cudaSetDevice(ctx->device);
+    std::vector<double> xp, wp, xc, wc;
+    gauss_legendre(p_num, 0.0, p_max, xp, wp);
+    gauss_legendre(t_num, 0.0, 1.0, xc, wc);
+    const int n = p_num * t_num;
+    ctx->p_mesh.resize(n);
+    ctx->c_mesh.resize(n);
+    ctx->coef.resize(n);
+    std::vector<double> h(3 * n);
+    std::vector<float> hf(3 * n);
+    const double fourpi2 = (2.0 * M_PI) * (2.0 * M_PI);
+    for (int it = 0; it < t_num; ++it)
+        for (int ip = 0; ip < p_num; ++ip) {
+            const int k = ip + p_num * it;  // column-major like Integrals.jl:87-97
+            const double p = xp[ip], c = xc[it];
+            ctx->p_mesh[k] = p;
+            ctx->c_mesh[k] = c;
+            ctx->coef[k] = (wp[ip] * (wc[it] * 2.0)) * (p * p) / fourpi2;
+            h[k] = p * p;
+            h[n + k] = (p * c) * (p * c);
+            h[2 * n + k] = ctx->coef[k];
+        }
+    for (int i = 0; i < 3 * n; ++i) hf[i] = (float)h[i];
+    PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    cudaFree(ctx->d_nodes);
+    cudaFree(ctx->d_nodes_f);
+    ctx->d_nodes = nullptr;
+    ctx->d_nodes_f = nullptr;
+    PNJL_CUDA_TRY(ctx, cudaMalloc(&ctx->d_nodes, 3 * n * sizeof(double)));
+    PNJL_CUDA_TRY(ctx, cudaMalloc(&ctx->d_nodes_f, 3 * n * sizeof(float)));
+    PNJL_CUDA_TRY(ctx, cudaMemcpy(ctx->d_nodes, h.data(), 3 * n * sizeof(double), cudaMemcpyHostToDevice));
+    PNJL_CUDA_TRY(ctx, cudaMemcpy(ctx->d_nodes_f, hf.data(), 3 * n * sizeof(float), cudaMemcpyHostToDevice));
+    ctx->p_num = p_num;
+    ctx->t_num = t_num;
+    ctx->p_max = p_max;
+    return PNJL_OK;
+}
+
+int pnjl_get_nodes(const pnjl_ctx *ctx, double *p_mesh, double *c_mesh, double *coef) {
+    if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
+    if (ctx->p_num == 0) return PNJL_ERR_NO_NODES;
+    const size_t n = ctx->p_mesh.size();
+    if (p_mesh) std::memcpy(p_mesh, ctx->p_mesh.data(), n * sizeof(double));
+    if (c_mesh) std::memcpy(c_mesh, ctx->c_mesh.data(), n * sizeof(double));
+    if (coef) std::memcpy(coef, ctx->coef.data(), n * sizeof(double));
+    return PNJL_OK;
+}
+
+static int eval_common(pnjl_ctx *ctx, int64_t n, const double *x, const double *T, const double *mu_u,
+                       const double *mu_d, const double *mu_s, const double *xi, int32_t precision, double *omega,
+                       double *grad, double *hess, pnjl_result_soa *out) {
+    if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
+    if (ctx->p_num == 0) return fail(ctx, PNJL_ERR_NO_NODES, "call pnjl_set_nodes first");
+    if (n < 0 || (n > 0 && (!x || !T || !mu_u || !mu_d || !mu_s || !xi)))
+        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "null input array");
+    if (precision != PNJL_PREC_FP64 && precision != PNJL_PREC_MIXED)
+        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "unknown precision");
+    if (n == 0) return PNJL_OK;
+    cudaSetDevice(ctx->device);
+    const size_t nn = (size_t)n;
+    size_t bytes = carve_size(5 * nn, 8) + 5 * carve_size(nn, 8) + carve_size(nn, 8) + carve_size(5 * nn, 8) +
+                   carve_size(25 * nn, 8) + 5 * carve_size(nn, 8) + 4 * carve_size(3 * nn, 8);
+    int rc = ensure_ws(ctx, bytes);
+    if (rc) return rc;
+    unsigned char *p = ctx->d_ws;
+    double *dx = carve<double>(p, 5 * nn), *dT = carve<double>(p, nn), *du = carve<double>(p, nn),
+           *dd = carve<double>(p, nn), *ds = carve<double>(p, nn), *dxi = carve<double>(p, nn);
+    double *dom = carve<double>(p, nn), *dg = carve<double>(p, 5 * nn), *dh = carve<double>(p, 25 * nn);
+    pnjl_result_soa dout{};
+    dout.omega = nullptr;
+    dout.pressure = carve<double>(p, nn);
+    dout.rho_norm = carve<double>(p, nn);
+    dout.entropy = carve<double>(p, nn);
+    dout.energy = carve<double>(p, nn);
+    double *dspare = carve<double>(p, nn);
+    (void)dspare;
+    dout.masses = carve<double>(p, 3 * nn);
+    dout.rho = carve<double>(p, 3 * nn);
+    dout.n_q = carve<double>(p, 3 * nn);
+    dout.n_aq = carve<double>(p, 3 * nn);
+    cudaStream_t s = ctx->stream;
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dx, x, 5 * nn * 8, cudaMemcpyHostToDevice, s));
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dT, T, nn * 8, cudaMemcpyHostToDevice, s));
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(du, mu_u, nn * 8, cudaMemcpyHostToDevice, s));
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dd, mu_d, nn * 8, cudaMemcpyHostToDevice, s));
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(ds, mu_s, nn * 8, cudaMemcpyHostToDevice, s));
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dxi, xi, nn * 8, cudaMemcpyHostToDevice, s));
+    pnjl::EvalArgs a{};
+    a.P = ctx->dp;
+    a.nodes = kernel_nodes(ctx);
+    const bool fp32 = precision == PNJL_PREC_MIXED;
+    size_t smem = pnjl::node_smem_bytes(a.nodes.n, fp32);
+    a.stage_nodes = smem <= 200 * 1024;
+    if (!a.stage_nodes) smem = 0;
+    a.n = n;
+    a.x = dx; a.T = dT; a.mu_u = du; a.mu_d = dd; a.mu_s = ds; a.xi = dxi;
+    a.omega = dom; a.grad = dg; a.hess = dh;
+    a.out = dout;
+    int64_t blocks = (n + 7) / 8;
+    int grid = (int)std::min<int64_t>(blocks, (int64_t)ctx->sm_count * 8);
+    cudaError_t e = pnjl::launch_eval(a, fp32, grid, smem, s);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "eval_kernel launch");
+    ctx->stats.kernel_launches += 1;
+    if (omega) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(omega, dom, nn * 8, cudaMemcpyDeviceToHost, s));
+    if (grad) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(grad, dg, 5 * nn * 8, cudaMemcpyDeviceToHost, s));
+    if (hess) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(hess, dh, 25 * nn * 8, cudaMemcpyDeviceToHost, s));
+    if (out) {
+        if (out->omega) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(out->omega, dom, nn * 8, cudaMemcpyDeviceToHost, s));
+        if (out->pressure) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(out->pressure, dout.pressure, nn * 8, cudaMemcpyDeviceToHost, s));
+        if (out->rho_norm) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(out->rho_norm, dout.rho_norm, nn * 8, cudaMemcpyDeviceToHost, s));
+        if (out->entropy) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(out->entropy, dout.entropy, nn * 8, cudaMemcpyDeviceToHost, s));
+        if (out->energy) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(out->energy, dout.energy, nn * 8, cudaMemcpyDeviceToHost, s));
+        if (out->masses) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(out->masses, dout.masses, 3 * nn * 8, cudaMemcpyDeviceToHost, s));
+        if (out->rho) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(out->rho, dout.rho, 3 * nn * 8, cudaMemcpyDeviceToHost, s));
+        if (out->n_q) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(out->n_q, dout.n_q, 3 * nn * 8, cudaMemcpyDeviceToHost, s));
+        if (out->n_aq) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(out->n_aq, dout.n_aq, 3 * nn * 8, cudaMemcpyDeviceToHost, s));
+    }
+    PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    return PNJL_OK;
+}
+
+int pnjl_eval_batch(pnjl_ctx *ctx, int64_t n, const double *x, const double *T, const double *mu_u,
+                    const double *mu_d, const double *mu_s, const double *xi, int32_t precision, double *omega,
+                    double *grad, double *hess) {
+    return eval_common(ctx, n, x, T, mu_u, mu_d, mu_s, xi, precision, omega, grad, hess, nullptr);
+}
+
+int pnjl_thermo_batch(pnjl_ctx *ctx, int64_t n, const double *x, const double *T, const double *mu_u,
+                      const double *mu_d, const double *mu_s, const double *xi, pnjl_result_soa *out) {
+    return eval_common(ctx, n, x, T, mu_u, mu_d, mu_s, xi, PNJL_PREC_FP64, nullptr, nullptr, nullptr, out);
+}
+
+int pnjl_solve_batch_device(pnjl_ctx *ctx, int64_t n, const double *d_T, const double *d_mu_u, const double *d_mu_d,
+                            const double *d_mu_s, const double *d_xi, const pnjl_solve_opts *opts,
+                            pnjl_result_soa *d_out) {
+    if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
+    if (ctx->p_num == 0) return fail(ctx, PNJL_ERR_NO_NODES, "call pnjl_set_nodes first");
+    int rc = check_opts(ctx, opts);
+    if (rc) return rc;
+    if (n < 0 || !d_out || (n > 0 && (!d_T || !d_mu_u || !d_mu_d || !d_mu_s || !d_xi)))
+        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "null array");
+    if (n == 0) return PNJL_OK;
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = ctx->stream;
+    const bool has_table = opts->n_seeds > 0 && opts->seed_table;
+    if (has_table) {
+        PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_seed_tables, opts->seed_table, opts->n_seeds * 5 * sizeof(double),
+                                           cudaMemcpyHostToDevice, s));
+        if (opts->seed_table_hot)
+            PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_seed_tables + 80, opts->seed_table_hot,
+                                               opts->n_seeds * 5 * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    PNJL_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_ctrl, 0, 16 * sizeof(long long), s));
+    pnjl::SolveArgs a{};
+    a.P = ctx->dp;
+    a.nodes = kernel_nodes(ctx);
+    size_t smem = pnjl::node_smem_bytes(a.nodes.n, false);
+    a.stage_nodes = smem <= 200 * 1024;
+    if (!a.stage_nodes) smem = 0;
+    a.n = n;
+    a.T = d_T; a.mu_u = d_mu_u; a.mu_d = d_mu_d; a.mu_s = d_mu_s; a.xi = d_xi;
+    a.seed_mode = opts->seed_mode;
+    a.n_seeds = has_table ? opts->n_seeds : 0;
+    a.seed_table = ctx->d_seed_tables;
+    a.seed_table_hot = (has_table && opts->seed_table_hot) ? ctx->d_seed_tables + 80 : nullptr;
+    a.hot_T_MeV = opts->hot_T_MeV;
+    a.point_seeds = opts->point_seeds;
+    a.opts.max_iter = opts->max_iter;
+    a.opts.ftol = opts->ftol;
+    a.opts.xtol = opts->xtol;
+    a.opts.residual_norm_max = opts->residual_norm_max;
+    a.opts.phi_tol = opts->phi_tol;
+    a.opts.omega_tie_rtol = opts->omega_tie_rtol;
+    a.opts.trust_region_fallback = opts->trust_region_fallback;
+    a.opts.auto_multiseed_fallback = opts->auto_multiseed_fallback;
+    a.out = *d_out;
+    a.queue = ctx->d_ctrl;
+    a.stats = ctx->d_ctrl + 1;
+    const int group = ctx->group;
+    const int grid = grid_for(ctx, group, smem, n);
+    PNJL_CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, s));
+    cudaError_t e = pnjl::launch_solve(a, group, grid, smem, s);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "solve_kernel launch");
+    PNJL_CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, s));
+    ctx->stats.kernel_launches += 1;
+    ctx->stats.points = n;
+    return PNJL_OK;
+}
+
+int pnjl_solve_batch(pnjl_ctx *ctx, int64_t n, const double *T, const double *mu_u, const double *mu_d,
+                     const double *mu_s, const double *xi, const pnjl_solve_opts *opts, pnjl_result_soa *out) {
+    if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
+    if (ctx->p_num == 0) return fail(ctx, PNJL_ERR_NO_NODES, "call pnjl_set_nodes first");
+    int rc = check_opts(ctx, opts);
+    if (rc) return rc;
+    if (n < 0 || !out || (n > 0 && (!T || !mu_u || !mu_d || !mu_s || !xi)))
+        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "null array");
+    if (n == 0) return PNJL_OK;
+    cudaSetDevice(ctx->device);
+    const size_t nn = (size_t)n;
+    const bool per_point = opts->seed_mode == PNJL_SEEDS_PER_POINT;
+    size_t bytes = 5 * carve_size(nn, 8) + (per_point ? carve_size(5 * nn, 8) : 0) + carve_size(5 * nn, 8) +
+                   6 * carve_size(nn, 8) + 4 * carve_size(3 * nn, 8) + 3 * carve_size(nn, 4) + carve_size(nn, 1);
+    rc = ensure_ws(ctx, bytes);
+    if (rc) return rc;
+    unsigned char *p = ctx->d_ws;
+    double *dT = carve<double>(p, nn), *du = carve<double>(p, nn), *dd = carve<double>(p, nn),
+           *ds = carve<double>(p, nn), *dxi = carve<double>(p, nn);
+    double *dseeds = per_point ? carve<double>(p, 5 * nn) : nullptr;
+    pnjl_result_soa d{};
+    d.x = carve<double>(p, 5 * nn);
+    d.omega = carve<double>(p, nn);
+    d.pressure = carve<double>(p, nn);
+    d.rho_norm = carve<double>(p, nn);
+    d.entropy = carve<double>(p, nn);
+    d.energy = carve<double>(p, nn);
+    d.residual_norm = carve<double>(p, nn);
+    d.masses = carve<double>(p, 3 * nn);
+    d.rho = carve<double>(p, 3 * nn);
+    d.n_q = carve<double>(p, 3 * nn);
+    d.n_aq = carve<double>(p, 3 * nn);
+    d.iterations = carve<int32_t>(p, nn);
+    d.chosen_seed = carve<int32_t>(p, nn);
+    d.status = carve<int32_t>(p, nn);
+    d.converged = carve<uint8_t>(p, nn);
+    cudaStream_t s = ctx->stream;
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dT, T, nn * 8, cudaMemcpyHostToDevice, s));
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(du, mu_u, nn * 8, cudaMemcpyHostToDevice, s));
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dd, mu_d, nn * 8, cudaMemcpyHostToDevice, s));
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(ds, mu_s, nn * 8, cudaMemcpyHostToDevice, s));
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dxi, xi, nn * 8, cudaMemcpyHostToDevice, s));
+    pnjl_solve_opts o2 = *opts;
+    if (per_point) {
+        PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dseeds, opts->point_seeds, 5 * nn * 8, cudaMemcpyHostToDevice, s));
+        o2.point_seeds = dseeds;
+    }
+    rc = pnjl_solve_batch_device(ctx, n, dT, du, dd, ds, dxi, &o2, &d);
+    if (rc) return rc;
+#define PNJL_D2H(field, count, elem)                                                                              \
+    if (out->field)                                                                                                \
+        PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(out->field, d.field, (count) * (elem), cudaMemcpyDeviceToHost, s));
+    PNJL_D2H(x, 5 * nn, 8)
+    PNJL_D2H(omega, nn, 8)
+    PNJL_D2H(pressure, nn, 8)
+    PNJL_D2H(rho_norm, nn, 8)
+    PNJL_D2H(entropy, nn, 8)
+    PNJL_D2H(energy, nn, 8)
+    PNJL_D2H(residual_norm, nn, 8)
+    PNJL_D2H(masses, 3 * nn, 8)
+    PNJL_D2H(rho, 3 * nn, 8)
+    PNJL_D2H(n_q, 3 * nn, 8)
+    PNJL_D2H(n_aq, 3 * nn, 8)
+    PNJL_D2H(iterations, nn, 4)
+    PNJL_D2H(chosen_seed, nn, 4)
+    PNJL_D2H(status, nn, 4)
+    PNJL_D2H(converged, nn, 1)
+#undef PNJL_D2H
+    PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    return pnjl_get_stats(ctx, &ctx->stats) == PNJL_OK ? PNJL_OK : PNJL_ERR_CUDA;
+}
+
+void *pnjl_stream(pnjl_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+int pnjl_synchronize(pnjl_ctx *ctx) {
+    if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
+    PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    return PNJL_OK;
+}
+
+int pnjl_get_stats(const pnjl_ctx *cctx, pnjl_stats *out) {
+    pnjl_ctx *ctx = const_cast<pnjl_ctx *>(cctx);
+    if (!ctx || !out) return PNJL_ERR_INVALID_ARGUMENT;
+    long long h[16];
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(h, ctx->d_ctrl, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+    PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    pnjl_stats st = ctx->stats;
+    st.passes_fp64 = h[1];
+    st.node_evals_fp64 = h[2];
+    st.seeds_run = h[3];
+    st.trust_region_runs = h[4];
+    st.multiseed_fallbacks = h[5];
+    st.passes_fp32 = h[6];
+    st.node_evals_fp32 = h[7];
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1) == cudaSuccess) st.last_kernel_ms = ms;
+    *out = st;
+    ctx->stats = st;
+    return PNJL_OK;
+}
+
+int pnjl_device_sm_count(const pnjl_ctx *ctx) { return ctx ? ctx->sm_count : 0; }
+
+int pnjl_set_tuning(pnjl_ctx *ctx, int32_t lanes_per_point, int32_t blocks_per_sm) {
+    if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
+    if (lanes_per_point != 8 && lanes_per_point != 32)
+        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "lanes_per_point must be 8 or 32");
+    if (blocks_per_sm < 0 || blocks_per_sm > 32) return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "blocks_per_sm out of range");
+    ctx->group = lanes_per_point;
+    ctx->blocks_per_sm = blocks_per_sm;
+    return PNJL_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,213 @@
+// pnjl_device.cuh -- device-side model of the PNJL grand potential for libpnjl_cuda.
+//
+// The integrand is restated from src/pnjl/core/Integrals.jl:178-259 (calculate_log_term,
+// calculate_log_sum) in a branch-free form that needs one exponential and one reciprocal
+// per node and flavour:
+//
+//   a = (mu - E)/T,  b = -(mu + E)/T = a - 2 mu/T,  t = exp(-|a|),  C = exp(-2 mu/T)  (mu >= 0)
+//   f+ (the quark log argument)     = P(alpha, beta;   Phi, Phibar) / alpha^3
+//   f- (the antiquark log argument) = P(alpha, C beta; Phibar, Phi) / alpha^3
+//   P(alpha, beta; u, v) = alpha^3 + 3u alpha^2 beta + 3v alpha beta^2 + beta^3
+//   (alpha, beta) = (1, t) for a <= 0 and (t, 1) for a > 0
+//
+// which is the reference's log-sum-exp rescaling (divide by e^{3a} when a > 0) applied to
+// both factors.  mu < 0 uses the exact symmetry f+(mu, Phi, Phibar) = f-(-mu, Phibar, Phi).
+// The reference's max(f, 1e-16) clamps (Integrals.jl:210,217,228,234) are kept: a clamped
+// factor contributes the constant log(1e-16) (+3a in the rescaled branch) and no Phi
+// derivatives, as ForwardDiff differentiates through max().
+//
+// Derivatives with respect to (M_f, Phi, Phibar) are analytic:
+//   dL/da = 3 n+,  n+ = (Phi y + 2 Phibar y^2 + y^3)/f+  (the Polyakov quark distribution of
+//   src/QuarkDistribution.jl:14-31), d2L/da2 = (3Phi y + 12Phibar y^2 + 9y^3)/f+ - 9 n+^2,
+//   dE/dM = M/E, d2E/dM2 = p^2(1 + xi c^2)/E^3, and the mixed terms by the quotient rule.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pnjl {
+
+struct DevParams {
+    double hbarc, Lambda, G, K, m_ud0, m_s0, T0, a0, a1, a2, b3, Nc, rho0;
+};
+
+// Sums of one pass over the node-flavour mesh (all in FP64 after the lane reduction).
+// Index f = flavour (u, d, s); "P" = Phi, "Pb" = Phibar.
+struct PassSums {
+    double DM[3], DMM[3], DMP[3], DMPb[3], Nq[3], Na[3];
+    double SL, SP, SPb, SPP, SPPb, SPbPb, SAN;
+};
+static constexpr int kPassSumCount = 6 * 3 + 7;
+
+// Solver options on the device (see pnjl_solve_opts).
+struct SolveOpts {
+    int max_iter;
+    double ftol, xtol, residual_norm_max, phi_tol, omega_tie_rtol;
+    int trust_region_fallback, auto_multiseed_fallback;
+};
+
+// The reference's POLYAKOV_EPS (Integrals.jl:151)
+static constexpr double kPolyakovEps = 1e-16;
+
+// Per-flavour constants of a pass.
+template <typename R>
+struct FlavourConst {
+    R M, M2, mu, invT, C, C2, C3;
+    R Pq, Pa;  // Phi on the quark side / antiquark side (swapped when mu < 0)
+    // quark cubic Horner coefficients ((t + k2) t + k1) t + 1 for a <= 0 (index 0) and a > 0 (1)
+    R k1_0, k2_0, k1_1, k2_1;
+    // antiquark cubic ((e3 t + e2) t + e1) t + e0
+    R e3_0, e2_0, e1_0, e0_0, e3_1, e2_1, e1_1, e0_1;
+};
+
+template <typename R>
+__device__ __forceinline__ FlavourConst<R> make_flavour(double M, double mu, double T, double Phi, double Phib,
+                                                      bool &swapped) {
+    FlavourConst<R> fc;
+    swapped = mu < 0.0;
+    const double mua = swapped ? -mu : mu;
+    const double Pq = swapped ? Phib : Phi;
+    const double Pa = swapped ? Phi : Phib;
+    const double C = exp(-2.0 * mua / T);
+    const double C2 = C * C, C3 = C2 * C;
+    fc.M = (R)M;
+    fc.M2 = (R)(M * M);
+    fc.mu = (R)mua;
+    fc.invT = (R)(1.0 / T);
+    fc.C = (R)C;
+    fc.C2 = (R)C2;
+    fc.C3 = (R)C3;
+    fc.Pq = (R)Pq;
+    fc.Pa = (R)Pa;
+    fc.k1_0 = (R)(3.0 * Pq);
+    fc.k2_0 = (R)(3.0 * Pa);
+    fc.k1_1 = (R)(3.0 * Pa);
+    fc.k2_1 = (R)(3.0 * Pq);
+    fc.e3_0 = (R)C3;
+    fc.e2_0 = (R)(3.0 * Pq * C2);
+    fc.e1_0 = (R)(3.0 * Pa * C);
+    fc.e0_0 = (R)1.0;
+    fc.e3_1 = (R)1.0;
+    fc.e2_1 = (R)(3.0 * Pa * C);
+    fc.e1_1 = (R)(3.0 * Pq * C2);
+    fc.e0_1 = (R)C3;
+    return fc;
+}
+
+__device__ __forceinline__ double fast_exp(double x) { return exp(x); }
+__device__ __forceinline__ float fast_exp(float x) { return __expf(x); }
+__device__ __forceinline__ double fast_rcp(double x) { return 1.0 / x; }
+__device__ __forceinline__ float fast_rcp(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double fast_rsqrt(double x) { return rsqrt(x); }
+__device__ __forceinline__ float fast_rsqrt(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double fast_log(double x) { return log(x); }
+__device__ __forceinline__ float fast_log(float x) { return __logf(x); }
+
+// Accumulator: plain sum (FP64) or Kahan-compensated sum (FP32).
+template <typename R, bool KAHAN>
+struct Acc {
+    R s;
+    __device__ __forceinline__ void zero() { s = R(0); }
+    __device__ __forceinline__ void add(R v) { s += v; }
+    __device__ __forceinline__ double value() const { return (double)s; }
+};
+template <>
+struct Acc<float, true> {
+    float s, c;
+    __device__ __forceinline__ void zero() { s = 0.f; c = 0.f; }
+    __device__ __forceinline__ void add(float v) {
+        float y = __fsub_rn(v, c);
+        float t = __fadd_rn(s, y);
+        c = __fsub_rn(__fsub_rn(t, s), y);
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+// Per-flavour accumulators of one lane over its share of the nodes.
+template <typename R, bool KAHAN, bool HESS, bool LOG>
+struct FlavourAcc {
+    Acc<R, KAHAN> DM, DMM, DMq, DMa, Nq, Na, SL, Sq, Sa, Sqq, Sqa, Saa, SAN;
+    __device__ __forceinline__ void zero() {
+        DM.zero(); DMM.zero(); DMq.zero(); DMa.zero(); Nq.zero(); Na.zero();
+        SL.zero(); Sq.zero(); Sa.zero(); Sqq.zero(); Sqa.zero(); Saa.zero(); SAN.zero();
+    }
+};
+
+// One node-flavour evaluation, accumulated with weight w.  q2 = p^2 (1 + xi c^2).
+template <typename R, bool KAHAN, bool HESS, bool LOG>
+__device__ __forceinline__ void node_flavour(const FlavourConst<R> &fc, R q2, R w,
+                                             FlavourAcc<R, KAHAN, HESS, LOG> &acc) {
+    const R E2 = q2 + fc.M2;
+    const R rE = fast_rsqrt(E2);
+    const R E = E2 * rE;
+    const R mE = fc.M * rE;  // dE/dM
+    const R a = (fc.mu - E) * fc.invT;
+    const bool sig = a > R(0);
+    const R t = fast_exp(sig ? -a : a);
+    const R t2 = t * t;
+    const R t3 = t2 * t;
+    const R k1 = sig ? fc.k1_1 : fc.k1_0;
+    const R k2 = sig ? fc.k2_1 : fc.k2_0;
+    const R fp = ((t + k2) * t + k1) * t + R(1);
+    const R e3 = sig ? fc.e3_1 : fc.e3_0;
+    const R e2 = sig ? fc.e2_1 : fc.e2_0;
+    const R e1 = sig ? fc.e1_1 : fc.e1_0;
+    const R e0 = sig ? fc.e0_1 : fc.e0_0;
+    const R gm = ((e3 * t + e2) * t + e1) * t + e0;
+    // clamps of the reference (max(f, 1e-16)); alpha^3 = t^3 when a > 0
+    const R alpha3 = sig ? t3 : R(1);
+    const bool clP = fp < R(kPolyakovEps);  // NaN is not clamped (Julia's max propagates it)
+    const bool clM = gm < R(kPolyakovEps) * alpha3;
+    const R fpc = clP ? R(1) : fp;
+    const R gmc = clM ? R(1) : gm;
+    const R prod = fpc * gmc;
+    const R Rr = fast_rcp(prod);
+    const R ip = clP ? R(0) : gmc * Rr;
+    const R im = clM ? R(0) : fpc * Rr;
+    const R u1 = sig ? t2 : t;
+    const R u2 = sig ? t : t2;
+    const R u3 = sig ? R(1) : t3;
+    const R r1 = u1 * ip, r2 = u2 * ip, r3 = u3 * ip;
+    const R s1 = fc.C * u1 * im, s2 = fc.C2 * u2 * im, s3 = fc.C3 * u3 * im;
+    const R Pq = fc.Pq, Pa = fc.Pa;
+    const R np = clP ? (sig ? R(1) : R(0)) : (Pq * r1 + R(2) * Pa * r2 + r3);
+    const R nm = clM ? R(0) : (Pa * s1 + R(2) * Pq * s2 + s3);
+    const R invT = fc.invT;
+    const R LE = R(-3) * (np + nm) * invT;
+    const R LM = LE * mE;
+    const R Lq = R(3) * (r1 + s2);
+    const R La = R(3) * (r2 + s1);
+    acc.DM.add(w * LM);
+    acc.Sq.add(w * Lq);
+    acc.Sa.add(w * La);
+    acc.Nq.add(w * np);
+    acc.Na.add(w * nm);
+    if (LOG) {
+        const R b = a - R(2) * fc.mu * invT;
+        acc.SAN.add(w * (a * np + b * nm));
+        // ln f+ + ln f- = 6 max(a,0) + ln(fp gm); a clamped factor is replaced by the
+        // reference's constant (log(1e-16), plus 3a in its rescaled quark branch)
+        const R logeps = R(-36.841361487904734);
+        R L = (sig ? R(6) * a : R(0)) + fast_log(prod);
+        if (clP) L += logeps;
+        if (clM) L += logeps - (sig ? R(3) * a : R(0));
+        acc.SL.add(w * L);
+    }
+    if (HESS) {
+        const R Laa = clP ? R(0) : (R(3) * Pq * r1 + R(12) * Pa * r2 + R(9) * r3 - R(9) * np * np);
+        const R Lbb = clM ? R(0) : (R(3) * Pa * s1 + R(12) * Pq * s2 + R(9) * s3 - R(9) * nm * nm);
+        const R LEE = (Laa + Lbb) * invT * invT;
+        const R LMM = LEE * mE * mE + LE * (R(1) - mE * mE) * rE;
+        const R LEq = -invT * (R(3) * r1 * (R(1) - R(3) * np) + R(3) * s2 * (R(2) - R(3) * nm));
+        const R LEa = -invT * (R(3) * r2 * (R(2) - R(3) * np) + R(3) * s1 * (R(1) - R(3) * nm));
+        acc.DMM.add(w * LMM);
+        acc.DMq.add(w * (LEq * mE));
+        acc.DMa.add(w * (LEa * mE));
+        acc.Sqq.add(w * (R(-9) * (r1 * r1 + s2 * s2)));
+        acc.Sqa.add(w * (R(-9) * (r1 * r2 + s1 * s2)));
+        acc.Saa.add(w * (R(-9) * (r2 * r2 + s1 * s1)));
+    }
+}
+
+}  // namespace pnjl

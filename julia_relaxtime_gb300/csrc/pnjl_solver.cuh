@@ -1,0 +1,347 @@
+// pnjl_solver.cuh -- passes, assembly and the NLsolve-style Newton / trust-region drivers
+// that run inside one lane group (G lanes cooperate on one point; G = 32 is one warp).
+//
+// Reference semantics restated here (w5851/Julia_RelaxTime):
+//   Omega and its parts ....... src/pnjl/core/Thermodynamics.jl:81-206, Integrals.jl:123-145
+//   F = grad_x P, J = dF/dx .... src/pnjl/solver/Conditions.jl:72-86 (ForwardDiff, here analytic)
+//   Newton ..................... ImplicitSolver.jl:112 -> NLsolve 4.5.1 :newton, static line
+//                                search: full step, converged iff ||F||_inf < ftol or
+//                                ||x - x_prev||_inf < xtol, singular J -> LM direction
+//   trust region ............... ImplicitSolver.jl:144 -> NLsolve :trust_region (dogleg,
+//                                autoscale, factor 1, eta 1e-4)
+//   physicality, candidate choice ImplicitSolver.jl:50-101
+//   thermo ..................... Thermodynamics.jl:215-244 (rho = dP/dmu, s = dP/dT analytic)
+#pragma once
+
+#include "pnjl_device.cuh"
+
+namespace pnjl {
+
+struct PointIn {
+    double T, mu[3], xi;
+};
+
+// Result of one evaluation at a state x (FP64 assembly).
+struct Eval {
+    double F[5];   // grad_x P = -grad_x Omega
+    double J[25];  // Hessian_x P, row-major
+    double omega;
+    double dOdT;   // dOmega/dT at fixed x, mu
+    double rho[3];
+    double nq[3], naq[3];
+};
+
+struct NodeView {
+    const double *p2, *pc2, *w;   // FP64 mesh (p^2, (p c)^2, weight)
+    const float *p2f, *pc2f, *wf; // FP32 copy
+    int n;
+};
+
+__device__ __forceinline__ void masses(const DevParams &P, const double *x, double *M) {
+    M[0] = P.m_ud0 - 4.0 * P.G * x[0] + 2.0 * P.K * x[1] * x[2];
+    M[1] = P.m_ud0 - 4.0 * P.G * x[1] + 2.0 * P.K * x[0] * x[2];
+    M[2] = P.m_s0 - 4.0 * P.G * x[2] + 2.0 * P.K * x[0] * x[1];
+}
+
+template <int G>
+__device__ __forceinline__ unsigned group_mask(int lane) {
+    if (G == 32) return 0xffffffffu;
+    const unsigned base = (unsigned)(lane & ~(G - 1));
+    return ((G == 32) ? 0xffffffffu : ((1u << G) - 1u)) << base;
+}
+
+// XOR butterfly: a + b == b + a bitwise, so every lane of the group ends with the
+// identical sum and the group's control flow stays uniform.
+template <int G>
+__device__ __forceinline__ double group_sum(double v, unsigned mask) {
+#pragma unroll
+    for (int m = G >> 1; m > 0; m >>= 1) v += __shfl_xor_sync(mask, v, m);
+    return v;
+}
+
+// One pass over the node-flavour mesh at state x; lane `gl` of a group of G lanes takes
+// nodes gl, gl+G, ...  Returns the group-reduced sums (identical in every lane).
+template <typename R, bool KAHAN, bool HESS, bool LOG, int G>
+__device__ void node_pass(const NodeView &nv, const PointIn &pt, const double *x, const double *M, int gl,
+                          unsigned mask, PassSums &S, int64_t &evals) {
+    double acc[kPassSumCount];
+#pragma unroll
+    for (int i = 0; i < kPassSumCount; ++i) acc[i] = 0.0;
+    const bool dedup = (M[1] == M[0]) && (pt.mu[1] == pt.mu[0]);
+    const R xi = (R)pt.xi;
+    const R *p2 = nullptr, *pc2 = nullptr, *w = nullptr;
+    if constexpr (sizeof(R) == 8) { p2 = (const R *)nv.p2; pc2 = (const R *)nv.pc2; w = (const R *)nv.w; }
+    else { p2 = (const R *)nv.p2f; pc2 = (const R *)nv.pc2f; w = (const R *)nv.wf; }
+#pragma unroll 1
+    for (int f = 0; f < 3; ++f) {
+        if (f == 1 && dedup) continue;
+        bool sw;
+        const FlavourConst<R> fc = make_flavour<R>(M[f], pt.mu[f], pt.T, x[3], x[4], sw);
+        FlavourAcc<R, KAHAN, HESS, LOG> fa;
+        fa.zero();
+#pragma unroll 2
+        for (int k = gl; k < nv.n; k += G) {
+            const R q2 = p2[k] + xi * pc2[k];
+            node_flavour<R, KAHAN, HESS, LOG>(fc, q2, w[k], fa);
+        }
+        const double mult = (f == 0 && dedup) ? 2.0 : 1.0;
+        const int fs[2] = {f, (f == 0 && dedup) ? 1 : f};
+        for (int j = 0; j < ((f == 0 && dedup) ? 2 : 1); ++j) {
+            const int ff = fs[j];
+            acc[0 + ff] = fa.DM.value();
+            acc[3 + ff] = HESS ? fa.DMM.value() : 0.0;
+            acc[6 + ff] = HESS ? (sw ? fa.DMa.value() : fa.DMq.value()) : 0.0;
+            acc[9 + ff] = HESS ? (sw ? fa.DMq.value() : fa.DMa.value()) : 0.0;
+            acc[12 + ff] = sw ? fa.Na.value() : fa.Nq.value();
+            acc[15 + ff] = sw ? fa.Nq.value() : fa.Na.value();
+        }
+        acc[18] += mult * (LOG ? fa.SL.value() : 0.0);
+        acc[19] += mult * (sw ? fa.Sa.value() : fa.Sq.value());
+        acc[20] += mult * (sw ? fa.Sq.value() : fa.Sa.value());
+        if (HESS) {
+            acc[21] += mult * (sw ? fa.Saa.value() : fa.Sqq.value());
+            acc[22] += mult * fa.Sqa.value();
+            acc[23] += mult * (sw ? fa.Sqq.value() : fa.Saa.value());
+        }
+        acc[24] += mult * (LOG ? fa.SAN.value() : 0.0);
+        if (gl == 0) evals += (int64_t)nv.n;
+    }
+#pragma unroll
+    for (int i = 0; i < kPassSumCount; ++i) acc[i] = group_sum<G>(acc[i], mask);
+    for (int f = 0; f < 3; ++f) {
+        S.DM[f] = acc[0 + f]; S.DMM[f] = acc[3 + f]; S.DMP[f] = acc[6 + f]; S.DMPb[f] = acc[9 + f];
+        S.Nq[f] = acc[12 + f]; S.Na[f] = acc[15 + f];
+    }
+    S.SL = acc[18]; S.SP = acc[19]; S.SPb = acc[20]; S.SPP = acc[21]; S.SPPb = acc[22]; S.SPbPb = acc[23];
+    S.SAN = acc[24];
+}
+
+// FP64 assembly of Omega, grad, Hessian and thermo from the pass sums.
+template <bool HESS, bool LOG>
+__device__ void assemble(const DevParams &P, const PointIn &pt, const double *x, const double *M, const PassSums &S,
+                         Eval &ev) {
+    const double T = pt.T;
+    const double pu = x[0], pd = x[1], ps = x[2], Ph = x[3], Pb = x[4];
+    const double G4 = 4.0 * P.G, K2 = 2.0 * P.K, K4 = 4.0 * P.K;
+    // chi (Thermodynamics.jl:112-114)
+    const double chi = 2.0 * P.G * (pu * pu + pd * pd + ps * ps) - K4 * (pu * pd * ps);
+    const double chig[3] = {G4 * pu - K4 * pd * ps, G4 * pd - K4 * pu * ps, G4 * ps - K4 * pu * pd};
+    // dM_f/dphi_a
+    const double Jm[3][3] = {{-G4, K2 * ps, K2 * pd}, {K2 * ps, -G4, K2 * pu}, {K2 * pd, K2 * pu, -G4}};
+    // Polyakov potential U (Thermodynamics.jl:124-130) with safe_log
+    const double r = P.T0 / T;
+    const double Ta = P.a0 + P.a1 * r + P.a2 * r * r;
+    const double Tb = P.b3 * r * r * r;
+    const double T4 = (T * T) * (T * T);
+    const double pp = Pb * Ph;
+    const double g = 1.0 - 6.0 * pp + 4.0 * (Pb * Pb * Pb + Ph * Ph * Ph) - 3.0 * pp * pp;
+    const bool gcl = (g <= 0.0) || (g < kPolyakovEps);  // safe_log, Integrals.jl:159-162
+    const double lg = gcl ? -36.841361487904734 : log(g);
+    const double U = T4 * (-0.5 * Ta * pp + Tb * lg);
+    const double gP = -6.0 * Pb + 12.0 * Ph * Ph - 6.0 * Ph * Pb * Pb;
+    const double gPb = -6.0 * Ph + 12.0 * Pb * Pb - 6.0 * Ph * Ph * Pb;
+    const double ig = gcl ? 0.0 : 1.0 / g;
+    const double UP = T4 * (-0.5 * Ta * Pb + Tb * gP * ig);
+    const double UPb = T4 * (-0.5 * Ta * Ph + Tb * gPb * ig);
+    // vacuum term -2 Nc sum_f I(|M_f| + 1e-12) (Integrals.jl:123-145)
+    const double L = P.Lambda;
+    const double inv4pi2 = 1.0 / (4.0 * M_PI * M_PI);
+    double V = 0.0, V1[3], V2[3];
+    for (int f = 0; f < 3; ++f) {
+        const double sgn = signbit(M[f]) ? -1.0 : 1.0;
+        const double ms = fabs(M[f]) + 1e-12;
+        const double ms2 = ms * ms;
+        const double Sq = sqrt(L * L + ms2);
+        const double lgv = log((L + Sq) / ms);
+        const double I = (L * Sq * (2.0 * L * L + ms2) - ms2 * ms2 * lgv) * (0.25 * inv4pi2);
+        const double I1 = (L * ms * Sq - ms2 * ms * lgv) * inv4pi2;
+        const double I2 = (L * Sq + 2.0 * L * ms2 / Sq - 3.0 * ms2 * lgv) * inv4pi2;
+        V += I;
+        V1[f] = -2.0 * P.Nc * I1 * sgn;
+        V2[f] = -2.0 * P.Nc * I2;
+    }
+    V *= -2.0 * P.Nc;
+    const double Dsc = -2.0 * T;
+    double gO[5];
+    for (int a = 0; a < 3; ++a) {
+        double s = chig[a];
+        for (int f = 0; f < 3; ++f) s += Jm[f][a] * (V1[f] + Dsc * S.DM[f]);
+        gO[a] = s;
+    }
+    gO[3] = UP + Dsc * S.SP;
+    gO[4] = UPb + Dsc * S.SPb;
+    for (int i = 0; i < 5; ++i) ev.F[i] = -gO[i];
+    if (LOG) ev.omega = chi + U + V + Dsc * S.SL;
+    else ev.omega = 0.0;
+    if (HESS) {
+        double H[5][5];
+        const double chih[3][3] = {{G4, -K4 * ps, -K4 * pd}, {-K4 * ps, G4, -K4 * pu}, {-K4 * pd, -K4 * pu, G4}};
+        for (int a = 0; a < 3; ++a)
+            for (int b = a; b < 3; ++b) {
+                double s = chih[a][b];
+                for (int f = 0; f < 3; ++f) s += Jm[f][a] * Jm[f][b] * (V2[f] + Dsc * S.DMM[f]);
+                H[a][b] = s;
+            }
+        H[0][1] += (V1[2] + Dsc * S.DM[2]) * K2;
+        H[0][2] += (V1[1] + Dsc * S.DM[1]) * K2;
+        H[1][2] += (V1[0] + Dsc * S.DM[0]) * K2;
+        for (int a = 0; a < 3; ++a) {
+            double s3 = 0.0, s4 = 0.0;
+            for (int f = 0; f < 3; ++f) {
+                s3 += Jm[f][a] * (Dsc * S.DMP[f]);
+                s4 += Jm[f][a] * (Dsc * S.DMPb[f]);
+            }
+            H[a][3] = s3;
+            H[a][4] = s4;
+        }
+        const double gPP = 24.0 * Ph - 6.0 * Pb * Pb;
+        const double gPbPb = 24.0 * Pb - 6.0 * Ph * Ph;
+        const double gPPb = -6.0 - 12.0 * Ph * Pb;
+        const double UPP = gcl ? 0.0 : T4 * Tb * (gPP * ig - gP * gP * ig * ig);
+        const double UPbPb = gcl ? 0.0 : T4 * Tb * (gPbPb * ig - gPb * gPb * ig * ig);
+        const double UPPb = T4 * (-0.5 * Ta + (gcl ? 0.0 : Tb * (gPPb * ig - gP * gPb * ig * ig)));
+        H[3][3] = UPP + Dsc * S.SPP;
+        H[3][4] = UPPb + Dsc * S.SPPb;
+        H[4][4] = UPbPb + Dsc * S.SPbPb;
+        for (int a = 0; a < 5; ++a)
+            for (int b = a; b < 5; ++b) {
+                ev.J[a * 5 + b] = -H[a][b];
+                ev.J[b * 5 + a] = -H[a][b];
+            }
+    }
+    if (LOG) {
+        // dU/dT (Thermodynamics.jl:142-163) and dD/dT = -2 sum wL + 6 sum w (a n+ + b n-)
+        const double dTa = -P.a1 * P.T0 / (T * T) - 2.0 * P.a2 * P.T0 * P.T0 / (T * T * T);
+        const double dTb = -3.0 * P.b3 * P.T0 * P.T0 * P.T0 / (T4);
+        const double UT = 4.0 * T * T * T * (-0.5 * Ta * pp + Tb * lg) + T4 * (dTa * (-0.5 * pp) + dTb * lg);
+        ev.dOdT = UT - 2.0 * S.SL + 6.0 * S.SAN;
+        for (int f = 0; f < 3; ++f) {
+            ev.rho[f] = 6.0 * (S.Nq[f] - S.Na[f]);
+            ev.nq[f] = 2.0 * P.Nc * S.Nq[f];
+            ev.naq[f] = 2.0 * P.Nc * S.Na[f];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// 5x5 dense LU with partial pivoting (first maximal pivot, as LAPACK getrf); returns
+// false when a pivot is exactly zero (Julia's SingularException).
+__device__ __forceinline__ bool lu_solve5(const double *Ain, const double *b, double *x) {
+    double A[25], y[5];
+#pragma unroll
+    for (int i = 0; i < 25; ++i) A[i] = Ain[i];
+#pragma unroll
+    for (int i = 0; i < 5; ++i) y[i] = b[i];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        int p = k;
+        double best = fabs(A[k * 5 + k]);
+#pragma unroll
+        for (int i = k + 1; i < 5; ++i) {
+            const double v = fabs(A[i * 5 + k]);
+            if (v > best) { best = v; p = i; }
+        }
+        if (A[p * 5 + k] == 0.0) return false;
+        if (p != k) {
+#pragma unroll
+            for (int j = 0; j < 5; ++j) {
+                const double t = A[k * 5 + j];
+                A[k * 5 + j] = A[p * 5 + j];
+                A[p * 5 + j] = t;
+            }
+            const double t = y[k];
+            y[k] = y[p];
+            y[p] = t;
+        }
+#pragma unroll
+        for (int i = k + 1; i < 5; ++i) {
+            const double l = A[i * 5 + k] / A[k * 5 + k];
+            A[i * 5 + k] = l;
+#pragma unroll
+            for (int j = k + 1; j < 5; ++j) A[i * 5 + j] -= l * A[k * 5 + j];
+            y[i] -= l * y[k];
+        }
+    }
+#pragma unroll
+    for (int i = 4; i >= 0; --i) {
+        double s = y[i];
+#pragma unroll
+        for (int j = i + 1; j < 5; ++j) s -= A[i * 5 + j] * y[j];
+        y[i] = s / A[i * 5 + i];
+    }
+#pragma unroll
+    for (int i = 0; i < 5; ++i) x[i] = y[i];
+    return true;
+}
+
+__device__ __forceinline__ double norm_inf5(const double *v) {
+    double m = 0.0;
+    bool nan = false;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        const double a = fabs(v[i]);
+        nan |= isnan(a);
+        m = a > m ? a : m;
+    }
+    return nan ? __longlong_as_double(0x7ff8000000000000ll) : m;
+}
+__device__ __forceinline__ bool any_nan5(const double *v) {
+    bool r = false;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) r |= isnan(v[i]);
+    return r;
+}
+__device__ __forceinline__ bool all_finite5(const double *v) {
+    bool r = true;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) r &= isfinite(v[i]);
+    return r;
+}
+
+// Outcome of one NLsolve run plus the postprocessed candidate at its final x.
+struct Candidate {
+    double x[5];
+    double residual_norm;
+    int iterations;
+    bool f_converged, exception, phys;
+    double omega, entropy, rho[3], nq[3], naq[3];
+};
+
+__device__ __forceinline__ void postprocess(const DevParams &P, const PointIn &pt, const SolveOpts &o, const Eval &ev,
+                                            Candidate &c) {
+    double M[3];
+    masses(P, c.x, M);
+    c.omega = ev.omega;
+    c.entropy = -ev.dOdT;
+    for (int f = 0; f < 3; ++f) { c.rho[f] = ev.rho[f]; c.nq[f] = ev.nq[f]; c.naq[f] = ev.naq[f]; }
+    const double pressure = -ev.omega;
+    const double rho_norm = (c.rho[0] + c.rho[1] + c.rho[2]) / (3.0 * P.rho0);
+    const double energy = -pressure + (pt.mu[0] * c.rho[0] + pt.mu[1] * c.rho[1] + pt.mu[2] * c.rho[2]) + pt.T * c.entropy;
+    const double Ph = c.x[3], Pb = c.x[4], tol = o.phi_tol;
+    bool ok = isfinite(Ph) && isfinite(Pb) && (-tol <= Ph) && (Ph <= 1.0 + tol) && (-tol <= Pb) && (Pb <= 1.0 + tol);
+    for (int f = 0; f < 3; ++f) ok = ok && isfinite(M[f]) && (M[f] > 0.0);
+    ok = ok && isfinite(c.omega) && isfinite(pressure) && isfinite(rho_norm) && isfinite(c.entropy) && isfinite(energy);
+    c.phys = ok;
+}
+
+__device__ __forceinline__ bool cand_good(const Candidate &c, double rmax) {
+    return c.f_converged && isfinite(c.residual_norm) && c.residual_norm <= rmax && c.phys;
+}
+
+// _choose_candidate (ImplicitSolver.jl:72-101): true -> take the fallback
+__device__ __forceinline__ bool choose_fallback(const Candidate &p, const Candidate &f, double rmax) {
+    const bool pg = cand_good(p, rmax), fg = cand_good(f, rmax);
+    if (fg && !pg) return true;
+    if (pg && !fg) return false;
+    if (fg && pg) {
+        if (f.omega < p.omega) return true;
+        if (f.omega > p.omega) return false;
+        return f.residual_norm < p.residual_norm;
+    }
+    if (f.f_converged && !p.f_converged) return true;
+    if (p.f_converged && !f.f_converged) return false;
+    if (isfinite(f.residual_norm) && isfinite(p.residual_norm)) return f.residual_norm < p.residual_norm;
+    return false;
+}
+
+}  // namespace pnjl

@@ -1,0 +1,236 @@
+"""GapEngine: host-side owner of one libpnjl_cuda context (one GPU, one stream).
+
+All compute goes through the C ABI (include/pnjl_cuda.h); numpy arrays are the host
+containers.  There is no CPU fallback: without the library every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _capi as api
+from .constants import PNJLParams
+
+PRECISIONS = {"fp64": api.PNJL_PREC_FP64, "mixed": api.PNJL_PREC_MIXED}
+
+
+@dataclass
+class SolveOptions:
+    """Keyword arguments of solve(::FixedMu, ...) (ImplicitSolver.jl:211-223) that reach the GPU.
+
+    ``iterations`` is NLsolve's iteration cap (NLsolve default 1000; the scan script passes 40).
+    ``ftol``/``xtol`` are fixed at 1e-9 in the reference (ImplicitSolver.jl:112,144).
+    ``omega_tie_rtol``: seeds whose converged Omega lies within rtol*|Omega| of the kept one are
+    treated as the same minimum and the earlier seed is kept (0 gives a strict argmin).
+    """
+    iterations: int = 1000
+    ftol: float = 1e-9
+    xtol: float = 1e-9
+    residual_norm_max: float = 1e-6
+    phi_tol: float = 1e-8
+    omega_tie_rtol: float = 1e-12
+    trust_region_fallback: bool = True
+    auto_multiseed_fallback: bool = True
+    precision: str = "fp64"
+
+
+def _dp(a):
+    return a.ctypes.data_as(api.dp) if a is not None else None
+
+
+def _f64(a, n=None, shape=None):
+    a = np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+    if shape is not None:
+        a = np.ascontiguousarray(np.broadcast_to(a, shape))
+    elif n is not None and a.ndim == 0:
+        a = np.full(n, float(a))
+    return a
+
+
+class BatchResult(dict):
+    """Per-point arrays of one batched solve (keys follow pnjl_result_soa)."""
+
+    def __getattr__(self, k):
+        try:
+            return self[k]
+        except KeyError as e:
+            raise AttributeError(k) from e
+
+
+class GapEngine:
+    def __init__(self, params: PNJLParams | None = None, device: int = 0, p_num: int = 64, t_num: int = 8,
+                 p_max: float = 10.0):
+        self._lib = api.lib()
+        self.params = params or PNJLParams.default()
+        cp = self.params.to_c()
+        ctx = C.c_void_p()
+        rc = self._lib.pnjl_init(C.byref(cp), device, C.byref(ctx))
+        if rc != api.PNJL_OK or not ctx.value:
+            raise api.CudaLibraryError(f"pnjl_init failed with code {rc} (device {device})")
+        self._ctx = ctx
+        self.device = device
+        self.p_num = self.t_num = 0
+        self.p_max = p_max
+        self.set_nodes(p_num, t_num, p_max)
+
+    # -- lifecycle ---------------------------------------------------------------------
+    def close(self):
+        if getattr(self, "_ctx", None) is not None and self._ctx.value:
+            self._lib.pnjl_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc, what):
+        api.check(self._ctx, rc, what)
+
+    # -- nodes -------------------------------------------------------------------------
+    def set_nodes(self, p_num: int, t_num: int, p_max: float = 10.0):
+        if (p_num, t_num, p_max) == (self.p_num, self.t_num, self.p_max):
+            return
+        self._check(self._lib.pnjl_set_nodes(self._ctx, int(p_num), int(t_num), float(p_max)), "pnjl_set_nodes")
+        self.p_num, self.t_num, self.p_max = int(p_num), int(t_num), float(p_max)
+
+    def nodes(self):
+        n = self.p_num * self.t_num
+        p, c, w = np.zeros(n), np.zeros(n), np.zeros(n)
+        self._check(self._lib.pnjl_get_nodes(self._ctx, _dp(p), _dp(c), _dp(w)), "pnjl_get_nodes")
+        return p, c, w
+
+    # -- evaluation ----------------------------------------------------------------------
+    def _point_arrays(self, T, mu, xi):
+        T = _f64(T).reshape(-1)
+        n = T.size
+        mu = np.asarray(mu, dtype=np.float64)
+        if mu.ndim <= 1 and mu.size in (1, n) and not (mu.ndim == 1 and mu.size == 3 and n != 3):
+            mu3 = np.repeat(np.broadcast_to(mu.reshape(-1), (n,))[:, None], 3, axis=1)
+        else:
+            mu3 = np.broadcast_to(mu.reshape(-1, 3), (n, 3))
+        mu_u = np.ascontiguousarray(mu3[:, 0])
+        mu_d = np.ascontiguousarray(mu3[:, 1])
+        mu_s = np.ascontiguousarray(mu3[:, 2])
+        xi = _f64(xi, shape=(n,))
+        return n, T, mu_u, mu_d, mu_s, xi
+
+    def evaluate(self, x, T, mu, xi, precision: str = "fp64"):
+        """Omega, grad_x Omega [n,5], Hessian_x Omega [n,5,5] at given states."""
+        n, T, mu_u, mu_d, mu_s, xi = self._point_arrays(T, mu, xi)
+        x = _f64(x, shape=(n, 5))
+        om, g, h = np.zeros(n), np.zeros((n, 5)), np.zeros((n, 5, 5))
+        rc = self._lib.pnjl_eval_batch(self._ctx, n, _dp(x), _dp(T), _dp(mu_u), _dp(mu_d), _dp(mu_s), _dp(xi),
+                                       PRECISIONS[precision], _dp(om), _dp(g), _dp(h))
+        self._check(rc, "pnjl_eval_batch")
+        return om, g, h
+
+    def thermo(self, x, T, mu, xi) -> BatchResult:
+        n, T, mu_u, mu_d, mu_s, xi = self._point_arrays(T, mu, xi)
+        x = _f64(x, shape=(n, 5))
+        out = BatchResult(omega=np.zeros(n), pressure=np.zeros(n), rho_norm=np.zeros(n), entropy=np.zeros(n),
+                          energy=np.zeros(n), masses=np.zeros((n, 3)), rho=np.zeros((n, 3)), n_q=np.zeros((n, 3)),
+                          n_aq=np.zeros((n, 3)))
+        soa = api.pnjl_result_soa()
+        for k in ("omega", "pressure", "rho_norm", "entropy", "energy", "masses", "rho", "n_q", "n_aq"):
+            setattr(soa, k, _dp(out[k]))
+        rc = self._lib.pnjl_thermo_batch(self._ctx, n, _dp(x), _dp(T), _dp(mu_u), _dp(mu_d), _dp(mu_s), _dp(xi),
+                                         C.byref(soa))
+        self._check(rc, "pnjl_thermo_batch")
+        return out
+
+    # -- solve -----------------------------------------------------------------------------
+    @staticmethod
+    def _opts_struct(opts: SolveOptions, seed_table, seed_table_hot, hot_T_MeV, per_point, point_seeds):
+        o = api.pnjl_solve_opts()
+        o.seed_mode = api.PNJL_SEEDS_PER_POINT if per_point else api.PNJL_SEEDS_TABLE
+        o.n_seeds = 0 if seed_table is None else seed_table.shape[0]
+        o.seed_table = _dp(seed_table)
+        o.seed_table_hot = _dp(seed_table_hot)
+        o.hot_T_MeV = hot_T_MeV
+        o.point_seeds = _dp(point_seeds) if isinstance(point_seeds, np.ndarray) else (
+            C.cast(C.c_void_p(point_seeds), api.dp) if point_seeds else None)
+        o.max_iter = int(opts.iterations)
+        o.ftol = opts.ftol
+        o.xtol = opts.xtol
+        o.residual_norm_max = opts.residual_norm_max
+        o.phi_tol = opts.phi_tol
+        o.omega_tie_rtol = opts.omega_tie_rtol
+        o.trust_region_fallback = int(bool(opts.trust_region_fallback))
+        o.auto_multiseed_fallback = int(bool(opts.auto_multiseed_fallback))
+        o.precision = PRECISIONS[opts.precision]
+        return o
+
+    def solve(self, T, mu, xi, *, seed_table=None, seed_table_hot=None, hot_T_MeV: float = 300.0,
+              point_seeds=None, opts: SolveOptions | None = None) -> BatchResult:
+        """Batched solve(::FixedMu) over host arrays (synchronous; includes the copies).
+
+        seed_table [S,5]: MultiSeed candidates (min-Omega selection) and the fallback table.
+        point_seeds [n,5]: one seed per point (ContinuitySeed-like); None selects table mode.
+        """
+        opts = opts or SolveOptions()
+        n, T, mu_u, mu_d, mu_s, xi = self._point_arrays(T, mu, xi)
+        st = None if seed_table is None else _f64(seed_table).reshape(-1, 5)
+        sth = None if seed_table_hot is None else _f64(seed_table_hot).reshape(-1, 5)
+        ps = None if point_seeds is None else _f64(point_seeds, shape=(n, 5))
+        o = self._opts_struct(opts, st, sth, hot_T_MeV, ps is not None, ps)
+        out = BatchResult(
+            x=np.zeros((n, 5)), omega=np.zeros(n), pressure=np.zeros(n), rho_norm=np.zeros(n), entropy=np.zeros(n),
+            energy=np.zeros(n), masses=np.zeros((n, 3)), rho=np.zeros((n, 3)), n_q=np.zeros((n, 3)),
+            n_aq=np.zeros((n, 3)), residual_norm=np.zeros(n), iterations=np.zeros(n, np.int32),
+            chosen_seed=np.zeros(n, np.int32), status=np.zeros(n, np.int32), converged=np.zeros(n, np.uint8))
+        soa = api.pnjl_result_soa()
+        for k, v in out.items():
+            ptr_t = api.i32p if v.dtype == np.int32 else (api.u8p if v.dtype == np.uint8 else api.dp)
+            setattr(soa, k, v.ctypes.data_as(ptr_t))
+        rc = self._lib.pnjl_solve_batch(self._ctx, n, _dp(T), _dp(mu_u), _dp(mu_d), _dp(mu_s), _dp(xi),
+                                        C.byref(o), C.byref(soa))
+        self._check(rc, "pnjl_solve_batch")
+        out["converged"] = out["converged"].astype(bool)
+        return out
+
+    def solve_device(self, n: int, d_T: int, d_mu_u: int, d_mu_d: int, d_mu_s: int, d_xi: int, d_out: dict, *,
+                     seed_table=None, seed_table_hot=None, hot_T_MeV: float = 300.0, d_point_seeds: int = 0,
+                     opts: SolveOptions | None = None):
+        """Asynchronous solve on device pointers (integers); d_out maps result fields to device pointers."""
+        opts = opts or SolveOptions()
+        st = None if seed_table is None else _f64(seed_table).reshape(-1, 5)
+        sth = None if seed_table_hot is None else _f64(seed_table_hot).reshape(-1, 5)
+        o = self._opts_struct(opts, st, sth, hot_T_MeV, bool(d_point_seeds), d_point_seeds or None)
+        soa = api.pnjl_result_soa()
+        for k, v in d_out.items():
+            ptr_t = dict(iterations=api.i32p, chosen_seed=api.i32p, status=api.i32p, converged=api.u8p).get(k, api.dp)
+            setattr(soa, k, C.cast(C.c_void_p(v), ptr_t))
+        cast = lambda p: C.cast(C.c_void_p(p), api.dp)  # noqa: E731
+        rc = self._lib.pnjl_solve_batch_device(self._ctx, n, cast(d_T), cast(d_mu_u), cast(d_mu_d), cast(d_mu_s),
+                                               cast(d_xi), C.byref(o), C.byref(soa))
+        self._check(rc, "pnjl_solve_batch_device")
+        self._keep = (st, sth)  # seed tables are read by the async host->device copy
+
+    # -- misc ------------------------------------------------------------------------------
+    def stream(self) -> int:
+        return int(self._lib.pnjl_stream(self._ctx) or 0)
+
+    def synchronize(self):
+        self._check(self._lib.pnjl_synchronize(self._ctx), "pnjl_synchronize")
+
+    def stats(self) -> dict:
+        st = api.pnjl_stats()
+        self._check(self._lib.pnjl_get_stats(self._ctx, C.byref(st)), "pnjl_get_stats")
+        return {k: getattr(st, k) for k, _ in api.pnjl_stats._fields_}
+
+    def sm_count(self) -> int:
+        return int(self._lib.pnjl_device_sm_count(self._ctx))
+
+    def set_tuning(self, lanes_per_point: int, blocks_per_sm: int = 0):
+        self._check(self._lib.pnjl_set_tuning(self._ctx, int(lanes_per_point), int(blocks_per_sm)),
+                    "pnjl_set_tuning")
