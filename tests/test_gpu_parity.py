@@ -1,0 +1,227 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle and the golden rows.
+
+Tolerances: FP64 kernel vs the jet-AD oracle -- Omega 1e-13 relative, gradient and Hessian
+1e-11 relative (different but exact derivative formulas, rounding only); solved states --
+|dphi|/|phi| <= 1e-9 and |dPhi| <= 1e-10 (the benchmark spec's bound), Omega 1e-12 relative.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from julia_relaxtime_gb300 import _capi as api
+from julia_relaxtime_gb300 import pnjl
+from julia_relaxtime_gb300.engine import SolveOptions
+from oracle import oracle as orc
+from oracle_adapter import GOLDEN, read_csv
+
+pytestmark = pytest.mark.gpu
+HBARC = 197.327
+
+
+@pytest.fixture(scope="module")
+def P():
+    return orc.default_params()
+
+
+def random_states(n, seed, mu_neg=False, asym=False):
+    rng = np.random.default_rng(seed)
+    T = rng.uniform(20, 350, n) / HBARC
+    mu1 = rng.uniform(-200 if mu_neg else 0, 450, n) / HBARC
+    mu = np.stack([mu1, mu1, mu1], axis=1)
+    if asym:
+        mu[:, 1] = mu1 * rng.uniform(0.8, 1.2, n)
+        mu[:, 2] = 0.5 * mu1
+    xi = rng.uniform(-0.8, 0.8, n)
+    x = np.column_stack([rng.uniform(-2.0, -0.05, (n, 3)), rng.uniform(0.0, 1.0, (n, 2))])
+    sym = rng.random(n) < 0.5
+    x[sym, 1] = x[sym, 0]
+    return x, T, mu, xi
+
+
+@pytest.mark.parametrize("p_num,t_num", [(12, 6), (64, 8), (128, 32), (256, 32)])
+def test_nodes_match_oracle(engine_factory, p_num, t_num):
+    eng = engine_factory(p_num, t_num)
+    p, c, w = eng.nodes()
+    nd = orc.Nodes(p_num, t_num)
+    np.testing.assert_allclose(p, nd.p, rtol=2e-15, atol=1e-15)
+    np.testing.assert_allclose(c, nd.c, rtol=2e-15, atol=1e-16)
+    np.testing.assert_allclose(w, nd.w, rtol=1e-13, atol=0)
+
+
+@pytest.mark.parametrize("p_num,t_num,mu_neg,asym", [(12, 6, False, False), (64, 8, True, False),
+                                                     (32, 16, False, True), (128, 32, True, True)])
+def test_eval_fp64_matches_oracle(engine_factory, P, p_num, t_num, mu_neg, asym):
+    eng = engine_factory(p_num, t_num)
+    nd = orc.Nodes(p_num, t_num)
+    x, T, mu, xi = random_states(48, p_num + t_num, mu_neg, asym)
+    om, g, h = eng.evaluate(x, T, mu, xi)
+    for i in range(len(T)):
+        o_ref, g_ref, h_ref = orc.evaluate(P, nd, x[i], mu[i], T[i], xi[i])
+        assert abs(om[i] - o_ref) <= 1e-13 * abs(o_ref), (i, om[i], o_ref)
+        sg = max(1.0, np.abs(g_ref).max())
+        assert np.abs(g[i] - g_ref).max() <= 1e-11 * sg, (i, g[i], g_ref)
+        sh = max(1.0, np.abs(h_ref).max())
+        assert np.abs(h[i] - h_ref).max() <= 1e-11 * sh, (i, h[i], h_ref)
+
+
+def test_eval_mixed_fp32_pass_close_to_fp64(engine_factory):
+    eng = engine_factory(128, 32)
+    x, T, mu, xi = random_states(64, 7)
+    om, g, h = eng.evaluate(x, T, mu, xi)
+    om32, g32, h32 = eng.evaluate(x, T, mu, xi, precision="mixed")
+    assert np.abs(om32 - om).max() <= 1e-5 * np.abs(om).max()
+    assert np.abs(g32 - g).max() <= 1e-4 * max(1.0, np.abs(g).max())
+    assert np.abs(h32 - h).max() <= 1e-4 * max(1.0, np.abs(h).max())
+
+
+def test_thermo_matches_oracle(engine_factory, P):
+    eng = engine_factory(64, 8)
+    nd = orc.Nodes(64, 8)
+    x, T, mu, xi = random_states(32, 11, mu_neg=True, asym=True)
+    th = eng.thermo(x, T, mu, xi)
+    for i in range(len(T)):
+        ref = orc.thermo(P, nd, x[i], mu[i], T[i], xi[i])
+        assert abs(th["pressure"][i] - ref["pressure"]) <= 1e-13 * abs(ref["pressure"])
+        assert abs(th["entropy"][i] - ref["entropy"]) <= 1e-11 * max(1.0, abs(ref["entropy"]))
+        assert abs(th["energy"][i] - ref["energy"]) <= 1e-11 * max(1.0, abs(ref["energy"]))
+        np.testing.assert_allclose(th["rho"][i], ref["rho"], rtol=1e-11, atol=1e-13)
+        np.testing.assert_allclose(th["n_q"][i], ref["nq"], rtol=1e-11, atol=1e-14)
+        np.testing.assert_allclose(th["n_aq"][i], ref["naq"], rtol=1e-11, atol=1e-14)
+
+
+def assert_solution_parity(res, i, ref, msg=""):
+    assert bool(res["converged"][i]) == ref["converged"], (msg, i, res["status"][i], ref["status"])
+    if not ref["converged"]:
+        return
+    x, xr = res["x"][i], ref["x"]
+    assert np.all(np.abs(x[:3] - xr[:3]) <= 1e-9 * np.abs(xr[:3]) + 1e-12), (msg, i, x, xr)
+    assert np.all(np.abs(x[3:] - xr[3:]) <= 1e-10), (msg, i, x, xr)
+    assert abs(res["omega"][i] - ref["omega"]) <= 1e-12 * abs(ref["omega"]), (msg, i)
+    assert abs(res["entropy"][i] - ref["entropy"]) <= 1e-9 * max(1.0, abs(ref["entropy"]))
+    np.testing.assert_allclose(res["n_q"][i], ref["nq"], rtol=1e-9, atol=1e-12)
+
+
+def test_multiseed_solve_matches_oracle(engine_factory, P):
+    """Config-1 shape (T x mu grid, xi = 0, p64/t8, MultiSeed) on a coarse 6 x 6 sub-grid."""
+    eng = engine_factory(64, 8)
+    nd = orc.Nodes(64, 8)
+    Tg, mg = np.meshgrid(np.linspace(50, 300, 6), np.linspace(0, 400, 6), indexing="ij")
+    T = Tg.ravel() / HBARC
+    mu = mg.ravel() / HBARC
+    table, hot = pnjl.multiseed_table()
+    opts = SolveOptions(iterations=40)
+    res = eng.solve(T, mu, 0.0, seed_table=table, seed_table_hot=hot, opts=opts)
+    refs = orc.solve_batch(P, nd, T, np.repeat(mu[:, None], 3, 1), 0.0, multi=True, opts=orc.default_opts(max_iter=40))
+    for i in range(T.size):
+        ref = orc.result_to_dict(refs[i])
+        assert_solution_parity(res, i, ref)
+        assert res["chosen_seed"][i] == ref["chosen_seed"]
+        assert res["iterations"][i] == ref["iterations"]
+        assert res["status"][i] == ref["status"]
+
+
+def test_anisotropic_asymmetric_solve_matches_oracle(engine_factory, P):
+    """Config-2/5 shapes: xi != 0, 4 seeds, flavour-asymmetric mu_s = mu/2, p32/t8."""
+    eng = engine_factory(32, 8)
+    nd = orc.Nodes(32, 8)
+    rng = np.random.default_rng(5)
+    n = 24
+    T = rng.uniform(20, 300, n) / HBARC
+    mu1 = rng.uniform(0, 450, n) / HBARC
+    mu = np.stack([mu1, mu1, 0.5 * mu1], axis=1)
+    xi = rng.uniform(-0.4, 0.4, n)
+    table, hot = pnjl.multiseed_table(4)
+    res = eng.solve(T, mu, xi, seed_table=table, seed_table_hot=hot, opts=SolveOptions(iterations=40))
+    refs = orc.solve_batch(P, nd, T, mu, xi, multi=True, n_seeds=4, opts=orc.default_opts(max_iter=40))
+    for i in range(n):
+        assert_solution_parity(res, i, orc.result_to_dict(refs[i]), "asym")
+
+
+def test_per_point_seeds_and_multiseed_fallback(engine_factory, P):
+    eng = engine_factory(24, 6)
+    nd = orc.Nodes(24, 6)
+    T = np.array([60.0, 100.0, 180.0, 250.0, 320.0]) / HBARC
+    mu = np.array([340.0, 0.0, 200.0, 100.0, 10.0]) / HBARC
+    seeds = np.array([pnjl.HADRON_SEED_5, pnjl.HIGH_DENSITY_SEED_5, (-3.0, -3.0, -3.0, 2.5, -1.0),
+                      pnjl.QUARK_SEED_5, (-2.5, -0.1, -0.2, 0.9, 0.1)])
+    table, hot = pnjl.multiseed_table()
+    for fb in (True, False):
+        opts = SolveOptions(iterations=40, auto_multiseed_fallback=fb)
+        res = eng.solve(T, mu, 0.0, seed_table=table, seed_table_hot=hot, point_seeds=seeds, opts=opts)
+        for i in range(T.size):
+            ref = orc.solve_point(P, nd, T[i], [mu[i]] * 3, 0.0, seeds[i], False,
+                                  orc.default_opts(max_iter=40, auto_multiseed_fallback=int(fb)))
+            assert_solution_parity(res, i, ref, f"fallback={fb}")
+            assert res["status"][i] == ref["status"], (i, fb)
+            assert res["iterations"][i] == ref["iterations"], (i, fb)
+
+
+def test_golden_scan_through_gpu(engine_factory):
+    """The reference's stored scan (xi = 0, p12/t6) reproduced through the GPU solver."""
+    from julia_relaxtime_gb300.scan import ScanOptions, gpu_point_solver, scan_rows
+    from test_oracle_golden import check_scan_rows
+
+    eng = engine_factory(12, 6)
+    for fname, xis, exact in (("gap_transport_scan_xi0.csv", [0.0], True),
+                              ("gap_transport_scan_xim0p6to0p6.csv", [-0.6, -0.4, -0.2, 0.0, 0.2, 0.4, 0.6], False)):
+        g = read_csv(fname)
+        gk = {(float(r["T_MeV"]), float(r["muB_MeV"]), float(r["xi"])): r for r in g}
+        opts = ScanOptions(xi_values=xis, tmin_mev=120, tmax_mev=400, tstep_mev=10, mubmin_mev=0, mubmax_mev=800,
+                           mubstep_mev=800, p_num=12, t_num=6, max_iter=40,
+                           boundary_path=os.path.join(GOLDEN, "boundary.csv"), cep_path=os.path.join(GOLDEN, "cep.csv"))
+        rows = scan_rows(opts, gpu_point_solver(12, 6, engine=eng))
+        mism = check_scan_rows(rows, gk, exact_iterations=exact)
+        assert mism <= 10
+
+
+def test_edge_cases(engine_factory, P):
+    eng = engine_factory(16, 4)
+    table, hot = pnjl.multiseed_table()
+    opts = SolveOptions(iterations=40)
+    # empty batch
+    r0 = eng.solve(np.zeros(0), np.zeros(0), np.zeros(0), seed_table=table, opts=opts)
+    assert r0["x"].shape == (0, 5)
+    # invalid inputs are flagged per point, valid neighbours still solve
+    T = np.array([0.0, -0.5, np.nan, 0.5, 0.5, 0.5]) / 1.0
+    mu = np.array([0.5, 0.5, 0.5, np.inf, 0.5, 0.5])
+    xi = np.array([0.0, 0.0, 0.0, 0.0, -1.0, 0.1])
+    r = eng.solve(T, mu, xi, seed_table=table, seed_table_hot=hot, opts=opts)
+    assert list(r["status"][:5]) == [api.PNJL_POINT_INVALID_INPUT] * 5
+    assert r["status"][5] == api.PNJL_POINT_CONVERGED and r["converged"][5]
+    # a non-finite seed raises inside the reference's nlsolve: status EXCEPTION, no fallback
+    seeds = np.array([[np.nan, -1.0, -2.0, 0.1, 0.1]])
+    r = eng.solve(np.array([0.5]), np.array([0.5]), 0.0, seed_table=table, seed_table_hot=hot, point_seeds=seeds,
+                  opts=opts)
+    assert r["status"][0] == api.PNJL_POINT_EXCEPTION and not r["converged"][0]
+    # iteration cap: max_iter = 1 gives the oracle's (unconverged) outcome
+    nd = orc.Nodes(16, 4)
+    r = eng.solve(np.array([0.5]), np.array([1.5]), 0.0, seed_table=table, seed_table_hot=hot,
+                  opts=SolveOptions(iterations=1, trust_region_fallback=False))
+    ref = orc.solve_point(P, nd, 0.5, [1.5] * 3, 0.0, orc.multiseed_seeds(P, 0.5), True,
+                          orc.default_opts(max_iter=1, trust_region_fallback=0))
+    assert r["status"][0] == ref["status"] and bool(r["converged"][0]) == ref["converged"]
+    # bad options are rejected with an error code and message
+    with pytest.raises(api.CudaLibraryError, match="seed table"):
+        eng.solve(np.array([0.5]), np.array([0.5]), 0.0, seed_table=np.zeros((0, 5)), opts=opts)
+    with pytest.raises(api.CudaLibraryError, match="node counts"):
+        eng.set_nodes(0, 4)
+
+
+def test_solve_api_mirrors_reference(engine_factory):
+    eng = engine_factory(24, 6)
+    T, mu = 100 / HBARC, 200 / HBARC
+    r = pnjl.solve(pnjl.FixedMu(), T, mu, p_num=24, t_num=6, engine=eng)
+    assert r.converged and r.iterations > 0
+    assert r.pressure == pytest.approx(-r.omega, rel=1e-12)          # test_solver_implicit.jl:56-59
+    assert r.masses[0] == pytest.approx(r.masses[1], rel=1e-6)       # :233-240
+    assert r.masses[2] > r.masses[0]
+    r2 = pnjl.solve(pnjl.FixedMu(), T, mu, xi=0.2, p_num=24, t_num=6, engine=eng)
+    assert r2.converged and r2.xi == 0.2
+    rm = pnjl.solve(pnjl.FixedMu(), T, mu, seed_strategy=pnjl.MultiSeed(), p_num=24, t_num=6, engine=eng)
+    assert rm.converged and abs(rm.omega - r.omega) < 1e-10
+    # the two regression points of test_solver_random_physical_smoke.jl:33-51 (p12/t4)
+    for T_MeV, muB, xi in ((48.269077, 972.6409, 0.479315), (288.453662, 563.275131, -0.652469)):
+        rr = pnjl.solve(pnjl.FixedMu(), T_MeV / HBARC, muB / 3 / HBARC, xi=xi, p_num=12, t_num=4, engine=eng)
+        assert rr.converged
+        assert -1e-8 <= rr.x_state[3] <= 1 + 1e-8 and np.all(rr.masses > 0)
