@@ -1,0 +1,320 @@
+#!/usr/bin/env python
+"""Throughput of the batched PNJL gap solve on one GB300 (bench contract of this repository).
+
+Workload (default ``--workload aniso_scan_256x256x9``): the batched anisotropic scan
+T = linspace(50, 300, 256) MeV x mu = linspace(0, 400, 256) MeV x xi in {-0.4, ..., 0.4}
+(589,824 points), 128 momentum x 32 cos(theta) Gauss-Legendre nodes, the first four
+MultiSeed candidates per point with min-Omega selection, FP64 Newton with the trust-region
+fallback, converged when ||grad_x Omega||_inf < 1e-10.  A "step" solves one strided slice
+of the grid (every n_chunks-th point, a different slice each step), so the timed steps are
+spread over the whole (T, mu, xi) box.  Inputs (T, mu, xi) are synthetic grid points: there
+is no dataset.
+
+value: converged solves per second with inputs already in HBM (pnjl_solve_batch_device),
+timed with CUDA events on the library's stream; e2e: the same metric through the host-pointer
+entry point pnjl_solve_batch, pinned host inputs, host<->device copies inside the timed region.
+``--impl reference`` times the reference algorithm's CPU restatement (the oracle: nested
+forward-mode derivatives like the reference's ForwardDiff, NLsolve-style Newton) on a bounded
+sample of the same workload with all host threads.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+HBARC = 197.327
+METRIC = "gap solves/s at ||dOmega|| <= 1e-10"
+# FP64 operations per node-flavour evaluation of the full Newton pass, counted from
+# pnjl_device.cuh::node_flavour with HESS and LOG (FMA = 2; the four transcendental
+# calls rsqrt, exp, rcp and log are counted separately, not as FLOPs).
+FLOP_PER_NODE_FLAVOUR_FP64 = 150
+TRANSCENDENTALS_PER_NODE_FLAVOUR = 4
+
+
+def workload_grid(name: str):
+    if name == "aniso_scan_256x256x9":
+        T = np.linspace(50.0, 300.0, 256)
+        mu = np.linspace(0.0, 400.0, 256)
+        xi = np.round(np.arange(-0.4, 0.4001, 0.1), 10)
+        Tg, mg, xg = np.meshgrid(T, mu, xi, indexing="ij")
+        return dict(T=Tg.ravel() / HBARC, mu=mg.ravel() / HBARC, xi=xg.ravel().copy(), p_num=128, t_num=32,
+                    n_seeds=4, desc="256x256 (T 50-300 MeV, mu 0-400 MeV) x 9 xi, p128 x t32, 4 seeds, min-Omega")
+    if name == "iso_scan_32x32":
+        T = np.linspace(50.0, 300.0, 32)
+        mu = np.linspace(0.0, 400.0, 32)
+        Tg, mg = np.meshgrid(T, mu, indexing="ij")
+        n = Tg.size
+        return dict(T=Tg.ravel() / HBARC, mu=mg.ravel() / HBARC, xi=np.zeros(n), p_num=64, t_num=8, n_seeds=6,
+                    desc="32x32 (T 50-300 MeV, mu 0-400 MeV), xi = 0, p64 x t8, MultiSeed (6), min-Omega")
+    raise SystemExit(f"unknown workload {name}")
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def run_reference(args, grid, sample_points: int):
+    """The reference algorithm on the CPU (oracle restatement), bounded sample, all threads."""
+    from oracle import oracle as orc
+
+    P = orc.default_params()
+    nd = orc.Nodes(grid["p_num"], grid["t_num"])
+    threads = os.cpu_count() or 1
+    n = grid["T"].size
+    rng = np.random.default_rng(1234)
+    idx = np.sort(rng.choice(n, size=min(sample_points, n), replace=False))
+    opts = orc.default_opts(max_iter=40, ftol=1e-10)
+    T = grid["T"][idx]
+    mu3 = np.repeat(grid["mu"][idx][:, None], 3, axis=1)
+    xi = grid["xi"][idx]
+    times, solved = [], 0
+    for it in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        rs = orc.solve_batch(P, nd, T, mu3, xi, multi=True, n_seeds=grid["n_seeds"], opts=opts, threads=threads)
+        dt = time.perf_counter() - t0
+        if it >= args.warmup:
+            times.append(dt)
+            solved += sum(1 for r in rs if r.converged and r.residual_norm <= 1e-10)
+    total = sum(times)
+    return dict(value=solved / total, seconds=total, cores=threads, points=len(idx),
+                sample=f"{len(idx)} points drawn uniformly (seed 1234) from the workload grid, per step")
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=4)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=("gpu", "reference"))
+    ap.add_argument("--workload", default="aniso_scan_256x256x9")
+    ap.add_argument("--chunks", type=int, default=64, help="the grid is solved in this many strided slices")
+    ap.add_argument("--precision", default="fp64", choices=("fp64", "mixed"))
+    ap.add_argument("--cpu-sample", type=int, default=48, help="points per step of the CPU baseline")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--lanes", type=int, default=32)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    grid = workload_grid(args.workload)
+    config = {"workload": args.workload, "grid": grid["desc"], "points": int(grid["T"].size),
+              "points_per_step": int(math.ceil(grid["T"].size / args.chunks)), "ftol": 1e-10, "max_iter": 40,
+              "precision": args.precision, "l2": "256 MiB device buffer written before every timed step"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        ref = run_reference(args, grid, args.cpu_sample)
+        line = {"metric": METRIC, "value": ref["value"], "unit": "solves/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * ref["seconds"] / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": config, "impl": "reference",
+                "cpu_baseline": {"value": ref["value"], "unit": "solves/s", "cores": ref["cores"], "kind": "port",
+                                 "sample": ref["sample"]},
+                "e2e": {"value": ref["value"], "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    torch.cuda.set_device(local_rank)
+    from julia_relaxtime_gb300.engine import GapEngine, SolveOptions
+    from julia_relaxtime_gb300.pnjl import multiseed_table
+
+    eng = GapEngine(device=local_rank, p_num=grid["p_num"], t_num=grid["t_num"])
+    eng.set_tuning(args.lanes, 0)
+    table, hot = multiseed_table(grid["n_seeds"])
+    opts = SolveOptions(iterations=40, ftol=1e-10, precision=args.precision)
+    # this rank's share of the points: a strided shard (no data exchange between ranks)
+    T_all, mu_all, xi_all = grid["T"][rank::world], grid["mu"][rank::world], grid["xi"][rank::world]
+    chunks = [np.arange(c, T_all.size, args.chunks) for c in range(args.chunks)]
+    dev = torch.device("cuda", local_rank)
+    stream = torch.cuda.ExternalStream(eng.stream(), device=dev)
+    maxn = max(len(c) for c in chunks)
+    d_in = {k: torch.empty(maxn, dtype=torch.float64, device=dev) for k in ("T", "mu", "xi")}
+    f64 = lambda *s: torch.empty(*s, dtype=torch.float64, device=dev)  # noqa: E731
+    d_out = {"x": f64(maxn * 5), "omega": f64(maxn), "pressure": f64(maxn), "rho_norm": f64(maxn),
+             "entropy": f64(maxn), "energy": f64(maxn), "residual_norm": f64(maxn), "masses": f64(maxn * 3),
+             "rho": f64(maxn * 3), "n_q": f64(maxn * 3), "n_aq": f64(maxn * 3),
+             "iterations": torch.empty(maxn, dtype=torch.int32, device=dev),
+             "chosen_seed": torch.empty(maxn, dtype=torch.int32, device=dev),
+             "status": torch.empty(maxn, dtype=torch.int32, device=dev),
+             "converged": torch.empty(maxn, dtype=torch.uint8, device=dev)}
+    ptrs = {k: v.data_ptr() for k, v in d_out.items()}
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+
+    def load_chunk(c):
+        idx = chunks[c]
+        n = idx.size
+        with torch.cuda.stream(stream):
+            d_in["T"][:n].copy_(torch.from_numpy(T_all[idx]))
+            d_in["mu"][:n].copy_(torch.from_numpy(mu_all[idx]))
+            d_in["xi"][:n].copy_(torch.from_numpy(xi_all[idx]))
+        stream.synchronize()
+        return n
+
+    def solve_chunk(n):
+        m = d_in["mu"].data_ptr()
+        eng.solve_device(n, d_in["T"].data_ptr(), m, m, m, d_in["xi"].data_ptr(), ptrs, seed_table=table,
+                         seed_table_hot=hot, opts=opts)
+
+    # warm-up (untimed) on the last chunks
+    for w in range(args.warmup):
+        n = load_chunk(args.chunks - 1 - (w % args.chunks))
+        solve_chunk(n)
+        eng.synchronize()
+
+    # timed region: K steps, device inputs already resident per step (loaded before the events)
+    sampler = ClockSampler(local_rank)
+    kernel_ms, step_ms, solved, evals, launches0 = [], [], 0, 0, eng.stats()["kernel_launches"]
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    for k in range(args.steps):
+        n = load_chunk(k % args.chunks)
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 0xFF)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        solve_chunk(n)
+        e1.record(stream)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        st = eng.stats()
+        kernel_ms.append(st["last_kernel_ms"])
+        evals += st["node_evals_fp64"]
+        conv = d_out["converged"][:n].cpu().numpy().astype(bool)
+        res = d_out["residual_norm"][:n].cpu().numpy()
+        solved += int(np.sum(conv & (res <= 1e-10)))
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    launches = eng.stats()["kernel_launches"] - launches0
+    total_ms = sum(step_ms)
+    if dist is not None:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+        s = torch.tensor([solved], device=dev, dtype=torch.float64)
+        dist.all_reduce(s)
+        solved = int(s.item())
+    value = solved / (total_ms * 1e-3)
+
+    # e2e: the host-pointer C-ABI call with pinned host buffers, copies inside the timed region
+    e2e_solved, e2e_s, h2d, d2h = 0, 0.0, 0, 0
+    for k in range(args.steps):
+        idx = chunks[k % args.chunks]
+        n = idx.size
+        Th = torch.from_numpy(T_all[idx]).pin_memory().numpy()
+        Mh = torch.from_numpy(mu_all[idx]).pin_memory().numpy()
+        Xh = torch.from_numpy(xi_all[idx]).pin_memory().numpy()
+        t0 = time.perf_counter()
+        r = eng.solve(Th, Mh, Xh, seed_table=table, seed_table_hot=hot, opts=opts)
+        e2e_s += time.perf_counter() - t0
+        e2e_solved += int(np.sum(r["converged"] & (r["residual_norm"] <= 1e-10)))
+        h2d = 3 * 8 * n + 2 * 8 * n  # T, mu (x3 arrays: mu_u, mu_d, mu_s), xi
+        h2d = 5 * 8 * n
+        d2h = sum(v.nbytes for v in r.values()) // 1
+    e2e = {"value": e2e_solved / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h)}
+
+    if rank != 0:
+        return
+    peak_fp64 = eng.probe_peak("fp64")
+    avg_kernel_s = (sum(kernel_ms) / len(kernel_ms)) * 1e-3
+    flops_per_launch = (evals / args.steps) * FLOP_PER_NODE_FLAVOUR_FP64
+    achieved = flops_per_launch / avg_kernel_s
+    line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+            "data": "synthetic", "config": config, "e2e": e2e, "gpu_launches": int(launches),
+            "roofline": {"bound": "fp64", "kernel": "solve_kernel<32>", "achieved": achieved / 1e12,
+                         "peak": peak_fp64 / 1e12, "unit": "TFLOP/s", "frac": achieved / peak_fp64,
+                         "peak_source": "measured in-run (pnjl_probe_peak FP64 FMA chains)",
+                         "flop_per_node_flavour": FLOP_PER_NODE_FLAVOUR_FP64,
+                         "node_flavour_evals_per_launch": evals / args.steps, "traffic": None},
+            "clocks": clocks, "solved": solved}
+    if not args.no_cpu_baseline:
+        class A:  # noqa: N801
+            warmup, steps = 0, 1
+        ref = run_reference(A, grid, args.cpu_sample)
+        line["cpu_baseline"] = {"value": ref["value"], "unit": "solves/s", "cores": ref["cores"], "kind": "port",
+                                "sample": ref["sample"]}
+    print(json.dumps(line))
+    eng.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

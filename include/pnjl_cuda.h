@@ -184,6 +184,11 @@ int pnjl_device_sm_count(const pnjl_ctx *ctx);
  * per SM (0 = occupancy maximum).  Chosen by the autotuner; results do not depend on it. */
 int pnjl_set_tuning(pnjl_ctx *ctx, int32_t lanes_per_point, int32_t blocks_per_sm);
 
+/* Measured pipe throughput of the context's device, the denominators of the kernels'
+ * rooflines (no counterpart in the reference, which has no GPU): kind 0 = FP64 FMA
+ * (FLOP/s, FMA = 2), 1 = FP32 FMA (FLOP/s), 2 = SFU ex2.approx.f32 (operations/s). */
+int pnjl_probe_peak(pnjl_ctx *ctx, int32_t kind, double *ops_per_s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -103,6 +103,7 @@ SIGNATURES = {
     "pnjl_get_stats": (C.c_int, [C.c_void_p, C.POINTER(pnjl_stats)]),
     "pnjl_device_sm_count": (C.c_int, [C.c_void_p]),
     "pnjl_set_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "pnjl_probe_peak": (C.c_int, [C.c_void_p, C.c_int32, dp]),
 }
 
 _lib = None

@@ -540,6 +540,16 @@ int pnjl_get_stats(const pnjl_ctx *cctx, pnjl_stats *out) {
 
 int pnjl_device_sm_count(const pnjl_ctx *ctx) { return ctx ? ctx->sm_count : 0; }
 
+extern "C" int pnjl_probe_peak_impl(int device, int kind, double *ops_per_s);
+
+int pnjl_probe_peak(pnjl_ctx *ctx, int32_t kind, double *ops_per_s) {
+    if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
+    PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    int rc = pnjl_probe_peak_impl(ctx->device, kind, ops_per_s);
+    if (rc) return fail(ctx, rc, "peak probe failed");
+    return PNJL_OK;
+}
+
 int pnjl_set_tuning(pnjl_ctx *ctx, int32_t lanes_per_point, int32_t blocks_per_sm) {
     if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
     if (lanes_per_point != 8 && lanes_per_point != 32)

@@ -1,0 +1,80 @@
+// pnjl_probe.cu -- pipe-throughput probes used as roofline denominators.
+//
+// Each probe runs independent dependency chains of one instruction type on every lane of a
+// full grid (a multiple of the SM count) and reports operations per second from CUDA-event
+// time.  kind 0: FP64 FMA, 1: FP32 FMA, 2: FP32 ex2.approx (the SFU).  The chains are
+// seeded from the thread index and written back so the compiler cannot drop them.
+#include <cuda_runtime.h>
+
+#include "../../include/pnjl_cuda.h"
+
+namespace pnjl {
+
+template <typename R>
+__global__ void __launch_bounds__(256) fma_probe(R *out, int iters, R a, R b) {
+    R x[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = (R)(threadIdx.x + k) * (R)1e-3;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) x[k] = x[k] * a + b;
+    }
+    R s = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += x[k];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(256) ex2_probe(float *out, int iters) {
+    float x[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = -(float)(threadIdx.x + k) * 1e-4f;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            float y;
+            asm volatile("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x[k]));
+            x[k] = -y;  // stays in (-1, 0]: 2^x in (0.5, 1]
+        }
+    }
+    float s = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += x[k];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+}  // namespace pnjl
+
+extern "C" int pnjl_probe_peak_impl(int device, int kind, double *ops_per_s) {
+    if (!ops_per_s || kind < 0 || kind > 2) return PNJL_ERR_INVALID_ARGUMENT;
+    if (cudaSetDevice(device) != cudaSuccess) return PNJL_ERR_CUDA;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    const int blocks = sms * 8, threads = 256;
+    void *buf = nullptr;
+    if (cudaMalloc(&buf, (size_t)blocks * threads * sizeof(double)) != cudaSuccess) return PNJL_ERR_OUT_OF_MEMORY;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int iters = kind == 0 ? 2048 : 16384;
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; ++rep) {
+        cudaEventRecord(e0);
+        if (kind == 0) pnjl::fma_probe<double><<<blocks, threads>>>((double *)buf, iters, 0.999999, 1e-7);
+        else if (kind == 1) pnjl::fma_probe<float><<<blocks, threads>>>((float *)buf, iters, 0.9999f, 1e-5f);
+        else pnjl::ex2_probe<<<blocks, threads>>>((float *)buf, iters);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && ms < best) best = ms;  // first launch is the warm-up
+    }
+    cudaError_t err = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(buf);
+    if (err != cudaSuccess) return PNJL_ERR_CUDA;
+    const double ops = (double)blocks * threads * iters * 8.0 * (kind == 2 ? 1.0 : 2.0);
+    *ops_per_s = ops / (best * 1e-3);
+    return PNJL_OK;
+}

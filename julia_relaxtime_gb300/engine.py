@@ -231,6 +231,13 @@ class GapEngine:
     def sm_count(self) -> int:
         return int(self._lib.pnjl_device_sm_count(self._ctx))
 
+    def probe_peak(self, kind: str) -> float:
+        """Measured pipe throughput: "fp64" / "fp32" FLOP/s (FMA = 2) or "sfu" ex2 ops/s."""
+        v = C.c_double()
+        k = {"fp64": 0, "fp32": 1, "sfu": 2}[kind]
+        self._check(self._lib.pnjl_probe_peak(self._ctx, k, C.byref(v)), "pnjl_probe_peak")
+        return float(v.value)
+
     def set_tuning(self, lanes_per_point: int, blocks_per_sm: int = 0):
         self._check(self._lib.pnjl_set_tuning(self._ctx, int(lanes_per_point), int(blocks_per_sm)),
                     "pnjl_set_tuning")

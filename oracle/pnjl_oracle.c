@@ -85,35 +85,35 @@ void or_params_default(or_params *p) {
 int or_gauleg(double a, double b, int n, double *x, double *w) {
     if (n <= 0 || !(a < b)) return -1;
     const double scale = (b - a) / 2.0, shift = (b + a) / 2.0;
+    /* extended precision keeps the endpoint weights 2/((1-x^2)P'^2) accurate to ~1 ulp */
     for (int i = 0; i < (n + 1) / 2; ++i) {
-        double z = cos(M_PI * (i + 0.75) / (n + 0.5));
-        double pp = 0.0;
+        long double z = cosl(3.14159265358979323846264338327950288L * (i + 0.75L) / (n + 0.5L));
+        long double pp = 0.0L;
         for (int it = 0; it < 100; ++it) {
-            double p1 = 1.0, p2 = 0.0;
+            long double p1 = 1.0L, p2 = 0.0L;
             for (int j = 1; j <= n; ++j) {
-                double p3 = p2;
+                long double p3 = p2;
                 p2 = p1;
-                p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / j;
+                p1 = ((2.0L * j - 1.0L) * z * p2 - (j - 1.0L) * p3) / j;
             }
-            pp = n * (z * p1 - p2) / (z * z - 1.0);
-            double dz = p1 / pp;
+            pp = n * (z * p1 - p2) / (z * z - 1.0L);
+            long double dz = p1 / pp;
             z -= dz;
-            if (fabs(dz) < 1e-16) {
-                /* one more polish step with the final derivative */
-                p1 = 1.0; p2 = 0.0;
-                for (int j = 1; j <= n; ++j) {
-                    double p3 = p2;
-                    p2 = p1;
-                    p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / j;
-                }
-                pp = n * (z * p1 - p2) / (z * z - 1.0);
-                break;
-            }
+            if (fabsl(dz) < 1e-19L) break;
         }
-        double wt = 2.0 / ((1.0 - z * z) * pp * pp);
-        /* z is the (i+1)-th largest root: place symmetric pair in ascending order */
+        {
+            long double p1 = 1.0L, p2 = 0.0L;
+            for (int j = 1; j <= n; ++j) {
+                long double p3 = p2;
+                p2 = p1;
+                p1 = ((2.0L * j - 1.0L) * z * p2 - (j - 1.0L) * p3) / j;
+            }
+            pp = n * (z * p1 - p2) / (z * z - 1.0L);
+        }
+        double wt = (double)(2.0L / ((1.0L - z * z) * pp * pp));
+        /* z is the (i+1)-th largest root: place the symmetric pair in ascending order */
         int lo = i, hi = n - 1 - i;
-        x[lo] = -z; x[hi] = z;
+        x[lo] = -(double)z; x[hi] = (double)z;
         w[lo] = wt; w[hi] = wt;
         if (lo == hi) x[lo] = 0.0;
     }

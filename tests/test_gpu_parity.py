@@ -46,7 +46,7 @@ def test_nodes_match_oracle(engine_factory, p_num, t_num):
     nd = orc.Nodes(p_num, t_num)
     np.testing.assert_allclose(p, nd.p, rtol=2e-15, atol=1e-15)
     np.testing.assert_allclose(c, nd.c, rtol=2e-15, atol=1e-16)
-    np.testing.assert_allclose(w, nd.w, rtol=1e-13, atol=0)
+    np.testing.assert_allclose(w, nd.w, rtol=2e-14, atol=0)
 
 
 @pytest.mark.parametrize("p_num,t_num,mu_neg,asym", [(12, 6, False, False), (64, 8, True, False),
