@@ -37,11 +37,14 @@ if ROOT not in sys.path:
 
 HBARC = 197.327
 METRIC = "gap solves/s at ||dOmega|| <= 1e-10"
-# FP64 operations per node-flavour evaluation of the full Newton pass, counted from
-# pnjl_device.cuh::node_flavour with HESS and LOG (FMA = 2; the four transcendental
-# calls rsqrt, exp, rcp and log are counted separately, not as FLOPs).
-FLOP_PER_NODE_FLAVOUR_FP64 = 150
-TRANSCENDENTALS_PER_NODE_FLAVOUR = 4
+# Floating-point operations per node-flavour evaluation, counted from the source of
+# pnjl_device.cuh::node_flavour (FMA = 2, loop invariants hoisted, selects and compares not
+# counted; the transcendental calls -- rsqrt, exp, rcp, and log in thermo passes -- are
+# counted separately and not as FLOPs):
+#   Newton pass (residual + Jacobian):        123 FLOP + 3 transcendentals
+#   thermo pass (Omega, s, rho, n_f at the end): 58 FLOP + 4 transcendentals
+FLOP_NEWTON = 123
+FLOP_THERMO = 58
 
 
 def workload_grid(name: str):
@@ -235,7 +238,7 @@ def main():
 
     # timed region: K steps, device inputs already resident per step (loaded before the events)
     sampler = ClockSampler(local_rank)
-    kernel_ms, step_ms, solved, evals, launches0 = [], [], 0, 0, eng.stats()["kernel_launches"]
+    kernel_ms, step_ms, solved, evals, flops, launches0 = [], [], 0, 0, 0, eng.stats()["kernel_launches"]
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
@@ -254,6 +257,8 @@ def main():
         st = eng.stats()
         kernel_ms.append(st["last_kernel_ms"])
         evals += st["node_evals_fp64"]
+        flops += (st["node_evals_fp64"] - st["node_evals_fp64_thermo"]) * FLOP_NEWTON + \
+            st["node_evals_fp64_thermo"] * FLOP_THERMO
         conv = d_out["converged"][:n].cpu().numpy().astype(bool)
         res = d_out["residual_norm"][:n].cpu().numpy()
         solved += int(np.sum(conv & (res <= 1e-10)))
@@ -282,8 +287,7 @@ def main():
         r = eng.solve(Th, Mh, Xh, seed_table=table, seed_table_hot=hot, opts=opts)
         e2e_s += time.perf_counter() - t0
         e2e_solved += int(np.sum(r["converged"] & (r["residual_norm"] <= 1e-10)))
-        h2d = 3 * 8 * n + 2 * 8 * n  # T, mu (x3 arrays: mu_u, mu_d, mu_s), xi
-        h2d = 5 * 8 * n
+        h2d = 5 * 8 * n  # T, mu_u, mu_d, mu_s, xi
         d2h = sum(v.nbytes for v in r.values()) // 1
     e2e = {"value": e2e_solved / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
            "d2h_bytes_per_step": int(d2h)}
@@ -292,7 +296,7 @@ def main():
         return
     peak_fp64 = eng.probe_peak("fp64")
     avg_kernel_s = (sum(kernel_ms) / len(kernel_ms)) * 1e-3
-    flops_per_launch = (evals / args.steps) * FLOP_PER_NODE_FLAVOUR_FP64
+    flops_per_launch = flops / args.steps
     achieved = flops_per_launch / avg_kernel_s
     line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -301,7 +305,7 @@ def main():
             "roofline": {"bound": "fp64", "kernel": "solve_kernel<32>", "achieved": achieved / 1e12,
                          "peak": peak_fp64 / 1e12, "unit": "TFLOP/s", "frac": achieved / peak_fp64,
                          "peak_source": "measured in-run (pnjl_probe_peak FP64 FMA chains)",
-                         "flop_per_node_flavour": FLOP_PER_NODE_FLAVOUR_FP64,
+                         "flop_per_node_flavour": {"newton_pass": FLOP_NEWTON, "thermo_pass": FLOP_THERMO},
                          "node_flavour_evals_per_launch": evals / args.steps, "traffic": None},
             "clocks": clocks, "solved": solved}
     if not args.no_cpu_baseline:

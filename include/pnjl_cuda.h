@@ -116,6 +116,7 @@ typedef struct pnjl_stats {
     int64_t passes_fp64;      /* full passes over the 3*p*t node-flavour mesh in FP64  */
     int64_t passes_fp32;      /* ... in FP32                                          */
     int64_t node_evals_fp64;  /* node-flavour evaluations actually executed (FP64)    */
+    int64_t node_evals_fp64_thermo; /* ... of them in thermo passes (Omega, s, rho, n_f) */
     int64_t node_evals_fp32;
     int64_t seeds_run;        /* Newton (+ trust region) runs                          */
     int64_t trust_region_runs;

@@ -24,14 +24,17 @@ struct pnjl_ctx {
     int p_num = 0, t_num = 0;
     double p_max = 0.0;
     std::vector<double> p_mesh, c_mesh, coef;
-    double *d_nodes = nullptr;  // p2 | pc2 | w
-    float *d_nodes_f = nullptr; // p2 | pc2 | w
+    double *d_nodes = nullptr;  // p2[p] | A[p] | c2[t] | B[t]
+    float *d_nodes_f = nullptr; // the same in FP32
     // control block: [0] queue head, [1..15] counters
     long long *d_ctrl = nullptr;
     double *d_seed_tables = nullptr; // 2 * 16 * 5
     // workspace for the host entry points
     unsigned char *d_ws = nullptr;
     size_t ws_cap = 0;
+    // solver scratch: candidate records and per-point completion counters (MultiSeed mode)
+    unsigned char *d_scratch = nullptr;
+    size_t scratch_cap = 0;
     // tuning
     int group = 32;
     int blocks_per_sm = 0;  // 0 = occupancy maximum
@@ -133,15 +136,36 @@ int ensure_ws(pnjl_ctx *ctx, size_t bytes) {
 
 pnjl::KernelNodes kernel_nodes(const pnjl_ctx *ctx) {
     pnjl::KernelNodes kn;
-    const int n = ctx->p_num * ctx->t_num;
-    kn.n = n;
+    const int np = ctx->p_num, nt = ctx->t_num;
+    kn.p_num = np;
+    kn.t_num = nt;
     kn.p2 = ctx->d_nodes;
-    kn.pc2 = ctx->d_nodes + n;
-    kn.w = ctx->d_nodes + 2 * n;
+    kn.A = ctx->d_nodes + np;
+    kn.c2 = ctx->d_nodes + 2 * np;
+    kn.B = ctx->d_nodes + 2 * np + nt;
     kn.p2f = ctx->d_nodes_f;
-    kn.pc2f = ctx->d_nodes_f + n;
-    kn.wf = ctx->d_nodes_f + 2 * n;
+    kn.Af = ctx->d_nodes_f + np;
+    kn.c2f = ctx->d_nodes_f + 2 * np;
+    kn.Bf = ctx->d_nodes_f + 2 * np + nt;
     return kn;
+}
+
+int ensure_scratch(pnjl_ctx *ctx, size_t bytes) {
+    if (bytes <= ctx->scratch_cap) return PNJL_OK;
+    if (ctx->d_scratch) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(ctx->d_scratch);
+        ctx->d_scratch = nullptr;
+        ctx->scratch_cap = 0;
+    }
+    size_t cap = bytes + bytes / 4;
+    cudaError_t e = cudaMalloc(&ctx->d_scratch, cap);
+    if (e != cudaSuccess) {
+        ctx->d_scratch = nullptr;
+        return fail(ctx, PNJL_ERR_OUT_OF_MEMORY, std::string("scratch allocation failed: ") + cudaGetErrorString(e));
+    }
+    ctx->scratch_cap = cap;
+    return PNJL_OK;
 }
 
 int check_opts(pnjl_ctx *ctx, const pnjl_solve_opts *o) {
@@ -235,6 +259,7 @@ int pnjl_destroy(pnjl_ctx *ctx) {
     cudaFree(ctx->d_ctrl);
     cudaFree(ctx->d_seed_tables);
     cudaFree(ctx->d_ws);
+    cudaFree(ctx->d_scratch);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -256,30 +281,36 @@ int pnjl_set_nodes(pnjl_ctx *ctx, int32_t p_num, int32_t t_num, double p_max) {
     ctx->p_mesh.resize(n);
     ctx->c_mesh.resize(n);
     ctx->coef.resize(n);
-    std::vector<double> h(3 * n);
-    std::vector<float> hf(3 * n);
     const double fourpi2 = (2.0 * M_PI) * (2.0 * M_PI);
     for (int it = 0; it < t_num; ++it)
         for (int ip = 0; ip < p_num; ++ip) {
             const int k = ip + p_num * it;  // column-major like Integrals.jl:87-97
-            const double p = xp[ip], c = xc[it];
-            ctx->p_mesh[k] = p;
-            ctx->c_mesh[k] = c;
-            ctx->coef[k] = (wp[ip] * (wc[it] * 2.0)) * (p * p) / fourpi2;
-            h[k] = p * p;
-            h[n + k] = (p * c) * (p * c);
-            h[2 * n + k] = ctx->coef[k];
+            ctx->p_mesh[k] = xp[ip];
+            ctx->c_mesh[k] = xc[it];
+            ctx->coef[k] = (wp[ip] * (wc[it] * 2.0)) * (xp[ip] * xp[ip]) / fourpi2;
         }
-    for (int i = 0; i < 3 * n; ++i) hf[i] = (float)h[i];
+    // separable device tables: p2[p] | A[p] = w_p p^2/(2 pi)^2 | c2[t] | B[t] = 2 w_c
+    const int m = 2 * (p_num + t_num);
+    std::vector<double> h(m);
+    std::vector<float> hf(m);
+    for (int ip = 0; ip < p_num; ++ip) {
+        h[ip] = xp[ip] * xp[ip];
+        h[p_num + ip] = wp[ip] * (xp[ip] * xp[ip]) / fourpi2;
+    }
+    for (int it = 0; it < t_num; ++it) {
+        h[2 * p_num + it] = xc[it] * xc[it];
+        h[2 * p_num + t_num + it] = 2.0 * wc[it];
+    }
+    for (int i = 0; i < m; ++i) hf[i] = (float)h[i];
     PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     cudaFree(ctx->d_nodes);
     cudaFree(ctx->d_nodes_f);
     ctx->d_nodes = nullptr;
     ctx->d_nodes_f = nullptr;
-    PNJL_CUDA_TRY(ctx, cudaMalloc(&ctx->d_nodes, 3 * n * sizeof(double)));
-    PNJL_CUDA_TRY(ctx, cudaMalloc(&ctx->d_nodes_f, 3 * n * sizeof(float)));
-    PNJL_CUDA_TRY(ctx, cudaMemcpy(ctx->d_nodes, h.data(), 3 * n * sizeof(double), cudaMemcpyHostToDevice));
-    PNJL_CUDA_TRY(ctx, cudaMemcpy(ctx->d_nodes_f, hf.data(), 3 * n * sizeof(float), cudaMemcpyHostToDevice));
+    PNJL_CUDA_TRY(ctx, cudaMalloc(&ctx->d_nodes, m * sizeof(double)));
+    PNJL_CUDA_TRY(ctx, cudaMalloc(&ctx->d_nodes_f, m * sizeof(float)));
+    PNJL_CUDA_TRY(ctx, cudaMemcpy(ctx->d_nodes, h.data(), m * sizeof(double), cudaMemcpyHostToDevice));
+    PNJL_CUDA_TRY(ctx, cudaMemcpy(ctx->d_nodes_f, hf.data(), m * sizeof(float), cudaMemcpyHostToDevice));
     ctx->p_num = p_num;
     ctx->t_num = t_num;
     ctx->p_max = p_max;
@@ -339,9 +370,7 @@ static int eval_common(pnjl_ctx *ctx, int64_t n, const double *x, const double *
     a.P = ctx->dp;
     a.nodes = kernel_nodes(ctx);
     const bool fp32 = precision == PNJL_PREC_MIXED;
-    size_t smem = pnjl::node_smem_bytes(a.nodes.n, fp32);
-    a.stage_nodes = smem <= 200 * 1024;
-    if (!a.stage_nodes) smem = 0;
+    const size_t smem = pnjl::node_smem_bytes(ctx->p_num, ctx->t_num);
     a.n = n;
     a.x = dx; a.T = dT; a.mu_u = du; a.mu_d = dd; a.mu_s = ds; a.xi = dxi;
     a.omega = dom; a.grad = dg; a.hess = dh;
@@ -400,13 +429,20 @@ int pnjl_solve_batch_device(pnjl_ctx *ctx, int64_t n, const double *d_T, const d
             PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_seed_tables + 80, opts->seed_table_hot,
                                                opts->n_seeds * 5 * sizeof(double), cudaMemcpyHostToDevice, s));
     }
-    PNJL_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_ctrl, 0, 16 * sizeof(long long), s));
     pnjl::SolveArgs a{};
+    if (opts->seed_mode == PNJL_SEEDS_TABLE) {
+        const size_t rec = (size_t)n * opts->n_seeds * sizeof(pnjl::CandRec);
+        const size_t cnt = ((size_t)n * sizeof(int) + 255) & ~size_t(255);
+        int rc2 = ensure_scratch(ctx, cnt + rec);
+        if (rc2) return rc2;
+        a.done = (int *)ctx->d_scratch;
+        a.cand = (pnjl::CandRec *)(ctx->d_scratch + cnt);
+        PNJL_CUDA_TRY(ctx, cudaMemsetAsync(a.done, 0, (size_t)n * sizeof(int), s));
+    }
+    PNJL_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_ctrl, 0, 16 * sizeof(long long), s));
     a.P = ctx->dp;
     a.nodes = kernel_nodes(ctx);
-    size_t smem = pnjl::node_smem_bytes(a.nodes.n, false);
-    a.stage_nodes = smem <= 200 * 1024;
-    if (!a.stage_nodes) smem = 0;
+    const size_t smem = pnjl::node_smem_bytes(ctx->p_num, ctx->t_num);
     a.n = n;
     a.T = d_T; a.mu_u = d_mu_u; a.mu_d = d_mu_d; a.mu_s = d_mu_s; a.xi = d_xi;
     a.seed_mode = opts->seed_mode;
@@ -427,7 +463,8 @@ int pnjl_solve_batch_device(pnjl_ctx *ctx, int64_t n, const double *d_T, const d
     a.queue = ctx->d_ctrl;
     a.stats = ctx->d_ctrl + 1;
     const int group = ctx->group;
-    const int grid = grid_for(ctx, group, smem, n);
+    const int64_t n_tasks = opts->seed_mode == PNJL_SEEDS_TABLE ? n * (int64_t)opts->n_seeds : n;
+    const int grid = grid_for(ctx, group, smem, n_tasks);
     PNJL_CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, s));
     cudaError_t e = pnjl::launch_solve(a, group, grid, smem, s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "solve_kernel launch");
@@ -524,13 +561,15 @@ int pnjl_get_stats(const pnjl_ctx *cctx, pnjl_stats *out) {
     PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(h, ctx->d_ctrl, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
     PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     pnjl_stats st = ctx->stats;
-    st.passes_fp64 = h[1];
-    st.node_evals_fp64 = h[2];
-    st.seeds_run = h[3];
-    st.trust_region_runs = h[4];
-    st.multiseed_fallbacks = h[5];
-    st.passes_fp32 = h[6];
-    st.node_evals_fp32 = h[7];
+    const long long *c = h + 1;
+    st.passes_fp64 = c[pnjl::kStatPasses64];
+    st.node_evals_fp64 = c[pnjl::kStatEvalsNewton64] + c[pnjl::kStatEvalsThermo64];
+    st.node_evals_fp64_thermo = c[pnjl::kStatEvalsThermo64];
+    st.seeds_run = c[pnjl::kStatSeeds];
+    st.trust_region_runs = c[pnjl::kStatTrRuns];
+    st.multiseed_fallbacks = c[pnjl::kStatMsFallbacks];
+    st.passes_fp32 = c[pnjl::kStatPasses32];
+    st.node_evals_fp32 = c[pnjl::kStatEvals32];
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1) == cudaSuccess) st.last_kernel_ms = ms;
     *out = st;

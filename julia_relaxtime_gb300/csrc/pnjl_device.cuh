@@ -2,7 +2,7 @@
 //
 // The integrand is restated from src/pnjl/core/Integrals.jl:178-259 (calculate_log_term,
 // calculate_log_sum) in a branch-free form that needs one exponential and one reciprocal
-// per node and flavour:
+// per node and flavour (plus one logarithm when Omega itself is wanted):
 //
 //   a = (mu - E)/T,  b = -(mu + E)/T = a - 2 mu/T,  t = exp(-|a|),  C = exp(-2 mu/T)  (mu >= 0)
 //   f+ (the quark log argument)     = P(alpha, beta;   Phi, Phibar) / alpha^3
@@ -20,6 +20,10 @@
 //   dL/da = 3 n+,  n+ = (Phi y + 2 Phibar y^2 + y^3)/f+  (the Polyakov quark distribution of
 //   src/QuarkDistribution.jl:14-31), d2L/da2 = (3Phi y + 12Phibar y^2 + 9y^3)/f+ - 9 n+^2,
 //   dE/dM = M/E, d2E/dM2 = p^2(1 + xi c^2)/E^3, and the mixed terms by the quotient rule.
+//
+// Node mesh: the reference's coefficient w_p (2 w_c) p^2/(2 pi)^2 (Integrals.jl:94) is kept
+// separable, w = A[ip] * B[it] with A = w_p p^2/(2 pi)^2 and B = 2 w_c, and
+// p^2 (1 + xi c^2) = p2[ip] * (1 + xi c2[it]); the tables are (p_num + t_num) entries.
 #pragma once
 
 #include <cstdint>
@@ -37,7 +41,6 @@ struct PassSums {
     double DM[3], DMM[3], DMP[3], DMPb[3], Nq[3], Na[3];
     double SL, SP, SPb, SPP, SPPb, SPbPb, SAN;
 };
-static constexpr int kPassSumCount = 6 * 3 + 7;
 
 // Solver options on the device (see pnjl_solve_opts).
 struct SolveOpts {
@@ -46,8 +49,9 @@ struct SolveOpts {
     int trust_region_fallback, auto_multiseed_fallback;
 };
 
-// The reference's POLYAKOV_EPS (Integrals.jl:151)
+// The reference's POLYAKOV_EPS (Integrals.jl:151) and log(POLYAKOV_EPS)
 static constexpr double kPolyakovEps = 1e-16;
+static constexpr double kLogPolyakovEps = -36.841361487904734;
 
 // Per-flavour constants of a pass.
 template <typename R>
@@ -125,7 +129,7 @@ struct Acc<float, true> {
 };
 
 // Per-flavour accumulators of one lane over its share of the nodes.
-template <typename R, bool KAHAN, bool HESS, bool LOG>
+template <typename R, bool KAHAN>
 struct FlavourAcc {
     Acc<R, KAHAN> DM, DMM, DMq, DMa, Nq, Na, SL, Sq, Sa, Sqq, Sqa, Saa, SAN;
     __device__ __forceinline__ void zero() {
@@ -135,9 +139,12 @@ struct FlavourAcc {
 };
 
 // One node-flavour evaluation, accumulated with weight w.  q2 = p^2 (1 + xi c^2).
-template <typename R, bool KAHAN, bool HESS, bool LOG>
-__device__ __forceinline__ void node_flavour(const FlavourConst<R> &fc, R q2, R w,
-                                             FlavourAcc<R, KAHAN, HESS, LOG> &acc) {
+//   GRAD:   dD/dM_f, dD/dPhi, dD/dPhibar        (the residual F)
+//   HESS:   the second derivatives              (the Jacobian J)
+//   THERMO: ln f+ + ln f- (for Omega), sum w (a n+ + b n-) (entropy) and the per-flavour
+//           sums of n+ and n- (rho_f and the number densities)
+template <typename R, bool KAHAN, bool GRAD, bool HESS, bool THERMO>
+__device__ __forceinline__ void node_flavour(const FlavourConst<R> &fc, R q2, R w, FlavourAcc<R, KAHAN> &acc) {
     const R E2 = q2 + fc.M2;
     const R rE = fast_rsqrt(E2);
     const R E = E2 * rE;
@@ -155,9 +162,10 @@ __device__ __forceinline__ void node_flavour(const FlavourConst<R> &fc, R q2, R 
     const R e1 = sig ? fc.e1_1 : fc.e1_0;
     const R e0 = sig ? fc.e0_1 : fc.e0_0;
     const R gm = ((e3 * t + e2) * t + e1) * t + e0;
-    // clamps of the reference (max(f, 1e-16)); alpha^3 = t^3 when a > 0
+    // clamps of the reference (max(f, 1e-16)); alpha^3 = t^3 when a > 0.  NaN is not
+    // clamped (Julia's max propagates it).
     const R alpha3 = sig ? t3 : R(1);
-    const bool clP = fp < R(kPolyakovEps);  // NaN is not clamped (Julia's max propagates it)
+    const bool clP = fp < R(kPolyakovEps);
     const bool clM = gm < R(kPolyakovEps) * alpha3;
     const R fpc = clP ? R(1) : fp;
     const R gmc = clM ? R(1) : gm;
@@ -169,29 +177,28 @@ __device__ __forceinline__ void node_flavour(const FlavourConst<R> &fc, R q2, R 
     const R u2 = sig ? t : t2;
     const R u3 = sig ? R(1) : t3;
     const R r1 = u1 * ip, r2 = u2 * ip, r3 = u3 * ip;
-    const R s1 = fc.C * u1 * im, s2 = fc.C2 * u2 * im, s3 = fc.C3 * u3 * im;
+    const R Cim = fc.C * im;
+    const R s1 = u1 * Cim, s2 = fc.C * (u2 * Cim), s3 = fc.C2 * (u3 * Cim);
     const R Pq = fc.Pq, Pa = fc.Pa;
     const R np = clP ? (sig ? R(1) : R(0)) : (Pq * r1 + R(2) * Pa * r2 + r3);
     const R nm = clM ? R(0) : (Pa * s1 + R(2) * Pq * s2 + s3);
     const R invT = fc.invT;
     const R LE = R(-3) * (np + nm) * invT;
-    const R LM = LE * mE;
-    const R Lq = R(3) * (r1 + s2);
-    const R La = R(3) * (r2 + s1);
-    acc.DM.add(w * LM);
-    acc.Sq.add(w * Lq);
-    acc.Sa.add(w * La);
-    acc.Nq.add(w * np);
-    acc.Na.add(w * nm);
-    if (LOG) {
+    if (GRAD) {
+        acc.DM.add(w * (LE * mE));
+        acc.Sq.add(w * (R(3) * (r1 + s2)));
+        acc.Sa.add(w * (R(3) * (r2 + s1)));
+    }
+    if (THERMO) {
+        acc.Nq.add(w * np);
+        acc.Na.add(w * nm);
         const R b = a - R(2) * fc.mu * invT;
         acc.SAN.add(w * (a * np + b * nm));
         // ln f+ + ln f- = 6 max(a,0) + ln(fp gm); a clamped factor is replaced by the
         // reference's constant (log(1e-16), plus 3a in its rescaled quark branch)
-        const R logeps = R(-36.841361487904734);
         R L = (sig ? R(6) * a : R(0)) + fast_log(prod);
-        if (clP) L += logeps;
-        if (clM) L += logeps - (sig ? R(3) * a : R(0));
+        if (clP) L += R(kLogPolyakovEps);
+        if (clM) L += R(kLogPolyakovEps) - (sig ? R(3) * a : R(0));
         acc.SL.add(w * L);
     }
     if (HESS) {

@@ -1,10 +1,14 @@
 // pnjl_kernels.cu -- sm_103a kernels of libpnjl_cuda.
 //
-//   solve_kernel<G>   persistent: lane groups of G lanes pop points from a device work
-//                     queue (one atomic per point) and run every seed of the point --
-//                     Newton, trust-region fallback, candidate choice and min-Omega
-//                     selection -- entirely in registers; FP64 throughout.
-//   eval_kernel<G>    one pass + assembly per given state (parity checks, thermo).
+//   solve_kernel<G>   persistent: lane groups of G lanes pop tasks from a device work queue.
+//                     MultiSeed mode: a task is one (point, seed) pair -- Newton,
+//                     trust-region fallback and candidate choice (ImplicitSolver.jl:103-151)
+//                     -- whose candidate record goes to a scratch slot; the task that
+//                     completes a point's last seed applies the min-Omega selection
+//                     (solve_multi, :532-559) and writes the point.  Per-point-seed mode: a
+//                     task is one point (single seed, with the MultiSeed fallback inline).
+//                     FP64 throughout.
+//   eval_kernel<G>    one full pass + assembly per given state (parity checks, thermo).
 //
 // Host launch wrappers are at the end (called from pnjl_capi.cu).
 #include "pnjl_kernels.h"
@@ -13,39 +17,30 @@
 namespace pnjl {
 
 // ---------------------------------------------------------------------------------------
-// Stage the node tables into shared memory when they fit, else read them from global.
-__device__ __forceinline__ NodeView stage_nodes(const KernelNodes &kn, bool fp32_too, void *smem, bool use_smem) {
+// Stage the separable node tables (a few KB) into shared memory.
+__device__ __forceinline__ NodeView stage_nodes(const KernelNodes &kn, void *smem) {
     NodeView nv;
-    nv.n = kn.n;
-    if (!use_smem) {
-        nv.p2 = kn.p2; nv.pc2 = kn.pc2; nv.w = kn.w;
-        nv.p2f = kn.p2f; nv.pc2f = kn.pc2f; nv.wf = kn.wf;
-        return nv;
-    }
+    nv.p_num = kn.p_num;
+    nv.t_num = kn.t_num;
+    const int np = kn.p_num, nt = kn.t_num;
     double *sd = (double *)smem;
-    for (int i = threadIdx.x; i < kn.n; i += blockDim.x) {
-        sd[i] = kn.p2[i];
-        sd[kn.n + i] = kn.pc2[i];
-        sd[2 * kn.n + i] = kn.w[i];
-    }
-    nv.p2 = sd; nv.pc2 = sd + kn.n; nv.w = sd + 2 * kn.n;
-    if (fp32_too) {
-        float *sf = (float *)(sd + 3 * kn.n);
-        for (int i = threadIdx.x; i < kn.n; i += blockDim.x) {
-            sf[i] = kn.p2f[i];
-            sf[kn.n + i] = kn.pc2f[i];
-            sf[2 * kn.n + i] = kn.wf[i];
-        }
-        nv.p2f = sf; nv.pc2f = sf + kn.n; nv.wf = sf + 2 * kn.n;
-    } else {
-        nv.p2f = kn.p2f; nv.pc2f = kn.pc2f; nv.wf = kn.wf;
-    }
+    for (int i = threadIdx.x; i < np; i += blockDim.x) { sd[i] = kn.p2[i]; sd[np + i] = kn.A[i]; }
+    for (int i = threadIdx.x; i < nt; i += blockDim.x) { sd[2 * np + i] = kn.c2[i]; sd[2 * np + nt + i] = kn.B[i]; }
+    float *sf = (float *)(sd + 2 * (np + nt));
+    for (int i = threadIdx.x; i < np; i += blockDim.x) { sf[i] = kn.p2f[i]; sf[np + i] = kn.Af[i]; }
+    for (int i = threadIdx.x; i < nt; i += blockDim.x) { sf[2 * np + i] = kn.c2f[i]; sf[2 * np + nt + i] = kn.Bf[i]; }
+    nv.p2 = sd; nv.A = sd + np; nv.c2 = sd + 2 * np; nv.B = sd + 2 * np + nt;
+    nv.p2f = sf; nv.Af = sf + np; nv.c2f = sf + 2 * np; nv.Bf = sf + 2 * np + nt;
     return nv;
 }
 
+size_t node_smem_bytes(int p_num, int t_num) { return (size_t)(p_num + t_num) * 2 * (sizeof(double) + sizeof(float)) + 16; }
+
 struct Counters {
-    int64_t passes64, evals64, seeds, tr_runs, ms_fallbacks;
+    int64_t v[kStatCount];
 };
+
+__device__ __forceinline__ double qnan() { return __longlong_as_double(0x7ff8000000000000ll); }
 
 template <int G>
 struct Group {
@@ -55,63 +50,61 @@ struct Group {
     unsigned mask;
     Counters &cnt;
 
-    __device__ void eval_full(const PointIn &pt, const double *x, Eval &ev) {
+    // residual and Jacobian at x (one Newton pass)
+    __device__ __noinline__ void eval_newton(const PointIn &pt, const double *x, double *F, double *J) {
         double M[3];
         masses(P, x, M);
         PassSums S;
-        node_pass<double, false, true, true, G>(nv, pt, x, M, gl, mask, S, cnt.evals64);
-        assemble<true, true>(P, pt, x, M, S, ev);
-        cnt.passes64 += 1;
+        node_pass<double, false, true, true, false, G>(nv, pt, x, M, gl, mask, S, cnt.v[kStatEvalsNewton64]);
+        Eval ev;
+        assemble<true, true, false>(P, pt, x, M, S, ev);
+        for (int i = 0; i < 5; ++i) F[i] = ev.F[i];
+        for (int i = 0; i < 25; ++i) J[i] = ev.J[i];
+        cnt.v[kStatPasses64] += 1;
+    }
+
+    // Omega, entropy, rho_f and number densities at x (one thermo pass) -> candidate fields
+    __device__ __noinline__ void eval_thermo(const PointIn &pt, const SolveOpts &o, Candidate &c) {
+        double M[3];
+        masses(P, c.x, M);
+        PassSums S;
+        node_pass<double, false, false, false, true, G>(nv, pt, c.x, M, gl, mask, S, cnt.v[kStatEvalsThermo64]);
+        Eval ev;
+        assemble<false, false, true>(P, pt, c.x, M, S, ev);
+        cnt.v[kStatPasses64] += 1;
+        postprocess(P, pt, o, ev, c);
     }
 
     // NLsolve :newton (static line search) from x0
     __device__ void newton(const PointIn &pt, const double *x0, const SolveOpts &o, Candidate &c) {
-        Eval ev;
-        double x[5], xold[5], p[5];
+        double x[5], xold[5], p[5], F[5], J[25];
 #pragma unroll
-        for (int i = 0; i < 5; ++i) { x[i] = x0[i]; xold[i] = __longlong_as_double(0x7ff8000000000000ll); }
-        eval_full(pt, x, ev);
-        c.exception = !all_finite5(ev.F);
+        for (int i = 0; i < 5; ++i) { x[i] = x0[i]; xold[i] = qnan(); }
+        eval_newton(pt, x, F, J);
+        c.exception = !all_finite5(F);
         if (c.exception) {
             for (int i = 0; i < 5; ++i) c.x[i] = x0[i];
-            c.residual_norm = __longlong_as_double(0x7ff8000000000000ll);
+            c.residual_norm = qnan();
             c.iterations = 0;
             c.f_converged = false;
             c.phys = false;
             return;
         }
         int it = 0;
-        bool xconv = false, fconv = norm_inf5(ev.F) < o.ftol;
-        bool stopped = any_nan5(x) || any_nan5(ev.F);
+        bool xconv = false, fconv = norm_inf5(F) < o.ftol;
+        bool stopped = any_nan5(x) || any_nan5(F);
         bool converged = fconv;
         while (!stopped && !converged && it < o.max_iter) {
             ++it;
-            if (lu_solve5(ev.J, ev.F, p)) {
+            if (lu_solve5(J, F, p)) {
 #pragma unroll
                 for (int i = 0; i < 5; ++i) p[i] = -p[i];
             } else {
-                // singular Jacobian: p = -(J'J + lambda I) \ J'F
-                double g[5], A[25], s = 0.0;
-                for (int i = 0; i < 5; ++i) {
-                    double a = 0.0;
-                    for (int k = 0; k < 5; ++k) a += ev.J[k * 5 + i] * ev.F[k];
-                    g[i] = a;
-                }
-                for (int i = 0; i < 5; ++i)
-                    for (int j = 0; j < 5; ++j) {
-                        double a = 0.0;
-                        for (int k = 0; k < 5; ++k) a += ev.J[k * 5 + i] * ev.J[k * 5 + j];
-                        A[i * 5 + j] = -a;
-                        s += fabs(a);
-                    }
-                const double lambda = 1e6 * sqrt(5.0 * 2.220446049250313e-16) * s;
-                for (int i = 0; i < 5; ++i) A[i * 5 + i] -= lambda;
-                if (!lu_solve5(A, g, p))
-                    for (int i = 0; i < 5; ++i) p[i] = __longlong_as_double(0x7ff8000000000000ll);
+                levenberg_step(J, F, p);
             }
 #pragma unroll
             for (int i = 0; i < 5; ++i) { xold[i] = x[i]; x[i] += p[i]; }
-            eval_full(pt, x, ev);
+            eval_newton(pt, x, F, J);
             double dx = 0.0;
             bool dxn = false;
 #pragma unroll
@@ -121,40 +114,59 @@ struct Group {
                 dx = d > dx ? d : dx;
             }
             xconv = !any_nan5(xold) && !dxn && dx < o.xtol;
-            fconv = norm_inf5(ev.F) < o.ftol;
-            stopped = any_nan5(x) || any_nan5(ev.F);
+            fconv = norm_inf5(F) < o.ftol;
+            stopped = any_nan5(x) || any_nan5(F);
             converged = xconv || fconv;
         }
         for (int i = 0; i < 5; ++i) c.x[i] = x[i];
-        c.residual_norm = norm_inf5(ev.F);
+        c.residual_norm = norm_inf5(F);
         c.iterations = it;
         c.f_converged = fconv;
-        postprocess(P, pt, o, ev, c);
+        eval_thermo(pt, o, c);
+    }
+
+    // singular Jacobian: p = -(J'J + lambda I) \ J'F, lambda = 1e6 sqrt(n eps) sum|J'J|
+    __device__ static void levenberg_step(const double *J, const double *F, double *p) {
+        double g[5], A[25], s = 0.0;
+        for (int i = 0; i < 5; ++i) {
+            double a = 0.0;
+            for (int k = 0; k < 5; ++k) a += J[k * 5 + i] * F[k];
+            g[i] = a;
+        }
+        for (int i = 0; i < 5; ++i)
+            for (int j = 0; j < 5; ++j) {
+                double a = 0.0;
+                for (int k = 0; k < 5; ++k) a += J[k * 5 + i] * J[k * 5 + j];
+                A[i * 5 + j] = -a;
+                s += fabs(a);
+            }
+        const double lambda = 1e6 * sqrt(5.0 * 2.220446049250313e-16) * s;
+        for (int i = 0; i < 5; ++i) A[i * 5 + i] -= lambda;
+        if (!lu_solve5(A, g, p))
+            for (int i = 0; i < 5; ++i) p[i] = qnan();
     }
 
     // NLsolve :trust_region (dogleg, autoscale) from x0
     __device__ void trust_region(const PointIn &pt, const double *x0, const SolveOpts &o, Candidate &c) {
-        Eval acc, trial;
-        double x[5], xold[5], d[5], p[5];
-        for (int i = 0; i < 5; ++i) { x[i] = x0[i]; xold[i] = __longlong_as_double(0x7ff8000000000000ll); }
-        eval_full(pt, x, acc);
-        cnt.tr_runs += 1;
-        c.exception = !all_finite5(acc.F);
+        double x[5], xold[5], d[5], p[5], r[5], Jacc[25], F[5], J[25];
+        for (int i = 0; i < 5; ++i) { x[i] = x0[i]; xold[i] = qnan(); }
+        eval_newton(pt, x, r, Jacc);
+        cnt.v[kStatTrRuns] += 1;
+        c.exception = !all_finite5(r);
         if (c.exception) {
             for (int i = 0; i < 5; ++i) c.x[i] = x0[i];
-            c.residual_norm = __longlong_as_double(0x7ff8000000000000ll);
+            c.residual_norm = qnan();
             c.iterations = 0; c.f_converged = false; c.phys = false;
             return;
         }
         int it = 0;
-        bool xconv = false, fconv = norm_inf5(acc.F) < o.ftol;
-        bool stopped = any_nan5(x) || any_nan5(acc.F);
+        bool fconv = norm_inf5(r) < o.ftol;
+        bool stopped = any_nan5(x) || any_nan5(r);
         bool converged = fconv;
-        bool last_nan_F = any_nan5(acc.F);
         if (!converged) {
             for (int j = 0; j < 5; ++j) {
                 double s = 0.0;
-                for (int i = 0; i < 5; ++i) s += acc.J[i * 5 + j] * acc.J[i * 5 + j];
+                for (int i = 0; i < 5; ++i) s += Jacc[i * 5 + j] * Jacc[i * 5 + j];
                 d[j] = sqrt(s);
                 if (d[j] == 0.0) d[j] = 1.0;
             }
@@ -164,24 +176,25 @@ struct Group {
             if (delta == 0.0) delta = 1.0;
             while (!stopped && !converged && it < o.max_iter) {
                 ++it;
-                dogleg(p, acc.F, d, acc.J, delta);
+                dogleg(p, r, d, Jacc, delta);
                 for (int i = 0; i < 5; ++i) { xold[i] = x[i]; x[i] += p[i]; }
-                eval_full(pt, x, trial);
+                eval_newton(pt, x, F, J);
                 double sr = 0.0, sf = 0.0, sp = 0.0;
                 for (int k = 0; k < 5; ++k) {
                     double a = 0.0;
-                    for (int i = 0; i < 5; ++i) a += acc.J[k * 5 + i] * p[i];
-                    const double rp = a + acc.F[k];
-                    sr += acc.F[k] * acc.F[k];
-                    sf += trial.F[k] * trial.F[k];
+                    for (int i = 0; i < 5; ++i) a += Jacc[k * 5 + i] * p[i];
+                    const double rp = a + r[k];
+                    sr += r[k] * r[k];
+                    sf += F[k] * F[k];
                     sp += rp * rp;
                 }
                 const double rho = (sr - sf) / (sr - sp);
                 if (rho > 1e-4) {
-                    acc = trial;
+                    for (int i = 0; i < 5; ++i) r[i] = F[i];
+                    for (int i = 0; i < 25; ++i) Jacc[i] = J[i];
                     for (int j = 0; j < 5; ++j) {
                         double s = 0.0;
-                        for (int i = 0; i < 5; ++i) s += acc.J[i * 5 + j] * acc.J[i * 5 + j];
+                        for (int i = 0; i < 5; ++i) s += Jacc[i * 5 + j] * Jacc[i * 5 + j];
                         const double cn = sqrt(s);
                         d[j] = (0.1 * d[j] > cn) ? 0.1 * d[j] : cn;
                     }
@@ -192,12 +205,11 @@ struct Group {
                         dxn |= isnan(dd);
                         dx = dd > dx ? dd : dx;
                     }
-                    xconv = !dxn && dx < o.xtol;
-                    fconv = norm_inf5(acc.F) < o.ftol;
+                    const bool xconv = !dxn && dx < o.xtol;
+                    fconv = norm_inf5(r) < o.ftol;
                     converged = xconv || fconv;
                 } else {
                     for (int i = 0; i < 5; ++i) x[i] -= p[i];
-                    xconv = false;
                     converged = false;
                 }
                 double wp = 0.0;
@@ -206,19 +218,17 @@ struct Group {
                 if (rho < 0.1) delta = delta / 2.0;
                 else if (rho >= 0.9) delta = 2.0 * wp;
                 else if (rho >= 0.5) delta = fmax(delta, 2.0 * wp);
-                last_nan_F = any_nan5(trial.F);
-                stopped = any_nan5(x) || last_nan_F;
+                stopped = any_nan5(x) || any_nan5(F);
             }
         }
         for (int i = 0; i < 5; ++i) c.x[i] = x[i];
-        c.residual_norm = norm_inf5(acc.F);
+        c.residual_norm = norm_inf5(r);
         c.iterations = it;
         c.f_converged = fconv;
-        // acc holds the evaluation at the last accepted x, which is the returned x
-        postprocess(P, pt, o, acc, c);
+        eval_thermo(pt, o, c);
     }
 
-    // Powell dogleg inside ||D p|| <= delta (Nocedal & Wright, algorithm 4.1 family)
+    // Powell dogleg inside ||D p|| <= delta (Nocedal & Wright, section 4.1)
     __device__ static void dogleg(double *p, const double *r, const double *d, const double *J, double delta) {
         double pi[5], pc[5], g[5];
         if (!lu_solve5(J, r, pi)) {
@@ -279,7 +289,7 @@ struct Group {
 
     // solve(::FixedMu) single-seed path without the MultiSeed fallback (ImplicitSolver.jl:261-304)
     __device__ void solve_seed(const PointIn &pt, const double *x0, const SolveOpts &o, Candidate &out, bool &converged) {
-        cnt.seeds += 1;
+        cnt.v[kStatSeeds] += 1;
         newton(pt, x0, o, out);
         converged = false;
         if (out.exception) return;
@@ -301,16 +311,30 @@ __device__ __forceinline__ bool valid_point(const PointIn &pt) {
            isfinite(pt.xi) && pt.xi > -1.0;
 }
 
-template <int G>
-__device__ void write_point(const DevParams &P, const PointIn &pt, const SolveArgs &a, int64_t i, int gl,
+__device__ __forceinline__ void load_point(const SolveArgs &a, int64_t i, PointIn &pt) {
+    pt.T = a.T[i];
+    pt.mu[0] = a.mu_u[i];
+    pt.mu[1] = a.mu_d[i];
+    pt.mu[2] = a.mu_s[i];
+    pt.xi = a.xi[i];
+}
+
+__device__ __forceinline__ void nan_candidate(Candidate &c, const double *x) {
+    for (int k = 0; k < 5; ++k) c.x[k] = x ? x[k] : qnan();
+    c.residual_norm = c.omega = c.entropy = qnan();
+    for (int k = 0; k < 3; ++k) c.rho[k] = c.nq[k] = c.naq[k] = qnan();
+    c.iterations = 0;
+    c.f_converged = c.phys = false;
+    c.exception = false;
+}
+
+__device__ void write_point(const DevParams &P, const PointIn &pt, const pnjl_result_soa &o, int64_t i,
                             const Candidate &c, bool converged, int chosen, int status) {
-    if (gl != 0) return;
     double M[3];
     masses(P, c.x, M);
     const double pressure = -c.omega;
     const double rho_norm = (c.rho[0] + c.rho[1] + c.rho[2]) / (3.0 * P.rho0);
     const double energy = -pressure + (pt.mu[0] * c.rho[0] + pt.mu[1] * c.rho[1] + pt.mu[2] * c.rho[2]) + pt.T * c.entropy;
-    const pnjl_result_soa &o = a.out;
     if (o.x) for (int k = 0; k < 5; ++k) o.x[5 * i + k] = c.x[k];
     if (o.omega) o.omega[i] = c.omega;
     if (o.pressure) o.pressure[i] = pressure;
@@ -328,117 +352,176 @@ __device__ void write_point(const DevParams &P, const PointIn &pt, const SolveAr
     if (o.converged) o.converged[i] = converged ? 1 : 0;
 }
 
-// MultiSeed over the seed table with the streaming tie rule: a later converged candidate
-// replaces the kept one only when its Omega is lower by more than omega_tie_rtol*|Omega|
-// (rtol = 0 is the reference's argmin with the first minimum kept).
-template <int G>
-__device__ bool solve_table(Group<G> &grp, const PointIn &pt, const SolveArgs &a, const SolveOpts &o, Candidate &best,
-                            int &chosen, Candidate &first, int &first_idx) {
-    bool have = false;
-    first_idx = -1;
+// Candidate record in the scratch buffer (one slot per (point, seed) task).
+__device__ __forceinline__ void store_record(CandRec *r, const Candidate &c, bool converged) {
+    for (int k = 0; k < 5; ++k) r->x[k] = c.x[k];
+    r->residual_norm = c.residual_norm;
+    r->omega = c.omega;
+    r->entropy = c.entropy;
+    for (int k = 0; k < 3; ++k) { r->rho[k] = c.rho[k]; r->nq[k] = c.nq[k]; r->naq[k] = c.naq[k]; }
+    r->iterations = c.iterations;
+    r->flags = (c.f_converged ? 1 : 0) | (c.phys ? 2 : 0) | (c.exception ? 4 : 0) | (converged ? 8 : 0);
+}
+
+__device__ __forceinline__ void load_record(const CandRec *r, Candidate &c, bool &converged) {
+    for (int k = 0; k < 5; ++k) c.x[k] = __ldcg(&r->x[k]);
+    c.residual_norm = __ldcg(&r->residual_norm);
+    c.omega = __ldcg(&r->omega);
+    c.entropy = __ldcg(&r->entropy);
+    for (int k = 0; k < 3; ++k) { c.rho[k] = __ldcg(&r->rho[k]); c.nq[k] = __ldcg(&r->nq[k]); c.naq[k] = __ldcg(&r->naq[k]); }
+    c.iterations = __ldcg(&r->iterations);
+    const int fl = __ldcg(&r->flags);
+    c.f_converged = fl & 1;
+    c.phys = (fl & 2) != 0;
+    c.exception = (fl & 4) != 0;
+    converged = (fl & 8) != 0;
+}
+
+__device__ __forceinline__ const double *table_row(const SolveArgs &a, const PointIn &pt, int s) {
     const bool hot = pt.T * a.P.hbarc >= a.hot_T_MeV;
+    return (hot && a.seed_table_hot) ? a.seed_table_hot + 5 * s : a.seed_table + 5 * s;
+}
+
+// Streaming min-Omega rule over seeds in order: a later converged candidate replaces the
+// kept one only when its Omega is lower by more than omega_tie_rtol*|Omega| (rtol = 0 is
+// the reference's argmin, first minimum kept, SeedStrategies.jl:236-240).
+__device__ __forceinline__ bool better(const Candidate &c, const Candidate &best, bool have, double rtol) {
+    return !have || c.omega < best.omega - rtol * fabs(best.omega);
+}
+
+// MultiSeed over the table inside one group (used by the per-point fallback).
+template <int G>
+__device__ bool solve_table_inline(Group<G> &grp, const PointIn &pt, const SolveArgs &a, Candidate &best, int &chosen) {
+    bool have = false;
     for (int s = 0; s < a.n_seeds; ++s) {
-        const double *row = (hot && a.seed_table_hot) ? a.seed_table_hot + 5 * s : a.seed_table + 5 * s;
+        const double *row = table_row(a, pt, s);
         double x0[5];
         for (int k = 0; k < 5; ++k) x0[k] = row[k];
         Candidate c;
         bool conv;
-        grp.solve_seed(pt, x0, o, c, conv);
-        if (c.exception) continue;
-        if (first_idx < 0) { first = c; first_idx = s; }
-        if (!conv) continue;
-        if (!have || c.omega < best.omega - o.omega_tie_rtol * fabs(best.omega)) {
-            best = c;
-            chosen = s;
-            have = true;
-        }
+        grp.solve_seed(pt, x0, a.opts, c, conv);
+        if (c.exception || !conv) continue;
+        if (better(c, best, have, a.opts.omega_tie_rtol)) { best = c; chosen = s; have = true; }
     }
     return have;
 }
 
 template <int G>
-__global__ void __launch_bounds__(kSolveThreads) solve_kernel(SolveArgs a) {
+__global__ void __launch_bounds__(kSolveThreads, 2) solve_kernel(SolveArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const NodeView nv = stage_nodes(a.nodes, false, smem_raw, a.stage_nodes);
+    const NodeView nv = stage_nodes(a.nodes, smem_raw);
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const int gl = lane & (G - 1);
     const unsigned mask = group_mask<G>(lane);
     const int leader = lane & ~(G - 1);
-    Counters cnt = {0, 0, 0, 0, 0};
+    Counters cnt;
+    for (int k = 0; k < kStatCount; ++k) cnt.v[k] = 0;
     Group<G> grp{a.P, nv, gl, mask, cnt};
     const SolveOpts &o = a.opts;
+    const bool table_mode = a.seed_mode == PNJL_SEEDS_TABLE;
+    const int S = a.n_seeds;
+    const int64_t n_tasks = table_mode ? a.n * S : a.n;
     while (true) {
-        long long idx = 0;
-        if (gl == 0) idx = atomicAdd((unsigned long long *)a.queue, 1ull);
-        idx = __shfl_sync(mask, idx, leader);
-        if (idx >= a.n) break;
-        const int64_t i = idx;
-        PointIn pt;
-        pt.T = a.T[i];
-        pt.mu[0] = a.mu_u[i];
-        pt.mu[1] = a.mu_d[i];
-        pt.mu[2] = a.mu_s[i];
-        pt.xi = a.xi[i];
-        if (!valid_point(pt)) {
+        long long t = 0;
+        if (gl == 0) t = atomicAdd((unsigned long long *)a.queue, 1ull);
+        t = __shfl_sync(mask, t, leader);
+        if (t >= n_tasks) break;
+        if (table_mode) {
+            const int64_t i = t / S;
+            const int s = (int)(t - i * S);
+            PointIn pt;
+            load_point(a, i, pt);
+            if (!valid_point(pt)) {
+                if (s == 0 && gl == 0) {
+                    Candidate c;
+                    nan_candidate(c, nullptr);
+                    write_point(a.P, pt, a.out, i, c, false, -1, PNJL_POINT_INVALID_INPUT);
+                }
+                continue;
+            }
+            const double *row = table_row(a, pt, s);
+            double x0[5];
+            for (int k = 0; k < 5; ++k) x0[k] = row[k];
             Candidate c;
-            for (int k = 0; k < 5; ++k) c.x[k] = __longlong_as_double(0x7ff8000000000000ll);
-            c.residual_norm = c.omega = c.entropy = __longlong_as_double(0x7ff8000000000000ll);
-            for (int k = 0; k < 3; ++k) c.rho[k] = c.nq[k] = c.naq[k] = __longlong_as_double(0x7ff8000000000000ll);
-            c.iterations = 0;
-            write_point<G>(a.P, pt, a, i, gl, c, false, -1, PNJL_POINT_INVALID_INPUT);
-            continue;
-        }
-        Candidate best, first;
-        int chosen = -1, first_idx = -1;
-        if (a.seed_mode == PNJL_SEEDS_PER_POINT) {
+            bool conv;
+            grp.solve_seed(pt, x0, o, c, conv);
+            int old = 0;
+            if (gl == 0) {
+                store_record(&a.cand[t], c, conv);
+                __threadfence();
+                old = atomicAdd(&a.done[i], 1);
+            }
+            old = __shfl_sync(mask, old, leader);
+            if (old != S - 1) continue;
+            // this task completed the point: select among its S candidate records
+            __threadfence();
+            if (gl != 0) continue;
+            Candidate best, first;
+            bool have = false;
+            int chosen = -1, first_idx = -1;
+            for (int q = 0; q < S; ++q) {
+                Candidate cq;
+                bool cv;
+                load_record(&a.cand[i * S + q], cq, cv);
+                if (cq.exception) continue;
+                if (first_idx < 0) { first = cq; first_idx = q; }
+                if (!cv) continue;
+                if (better(cq, best, have, o.omega_tie_rtol)) { best = cq; chosen = q; have = true; }
+            }
+            if (have) write_point(a.P, pt, a.out, i, best, true, chosen, PNJL_POINT_CONVERGED);
+            else if (first_idx >= 0) write_point(a.P, pt, a.out, i, first, false, first_idx, PNJL_POINT_ALL_SEEDS_FAILED);
+            else {
+                Candidate cz;
+                nan_candidate(cz, table_row(a, pt, 0));
+                write_point(a.P, pt, a.out, i, cz, false, -1, PNJL_POINT_ALL_SEEDS_FAILED);
+            }
+        } else {
+            const int64_t i = t;
+            PointIn pt;
+            load_point(a, i, pt);
+            if (!valid_point(pt)) {
+                if (gl == 0) {
+                    Candidate c;
+                    nan_candidate(c, nullptr);
+                    write_point(a.P, pt, a.out, i, c, false, -1, PNJL_POINT_INVALID_INPUT);
+                }
+                continue;
+            }
             double x0[5];
             for (int k = 0; k < 5; ++k) x0[k] = a.point_seeds[5 * i + k];
             Candidate single;
             bool conv;
             grp.solve_seed(pt, x0, o, single, conv);
             if (single.exception) {
-                write_point<G>(a.P, pt, a, i, gl, single, false, -1, PNJL_POINT_EXCEPTION);
+                if (gl == 0) write_point(a.P, pt, a.out, i, single, false, -1, PNJL_POINT_EXCEPTION);
                 continue;
             }
-            if (conv || !o.auto_multiseed_fallback) {
-                write_point<G>(a.P, pt, a, i, gl, single, conv, -1, conv ? PNJL_POINT_CONVERGED : PNJL_POINT_NOT_CONVERGED);
+            if (conv || !o.auto_multiseed_fallback || S == 0) {
+                if (gl == 0)
+                    write_point(a.P, pt, a.out, i, single, conv, -1, conv ? PNJL_POINT_CONVERGED : PNJL_POINT_NOT_CONVERGED);
                 continue;
             }
-            cnt.ms_fallbacks += 1;
-            if (solve_table<G>(grp, pt, a, o, best, chosen, first, first_idx))
-                write_point<G>(a.P, pt, a, i, gl, best, true, chosen, PNJL_POINT_CONVERGED);
-            else
-                write_point<G>(a.P, pt, a, i, gl, single, false, -1, PNJL_POINT_NOT_CONVERGED);
-        } else {
-            if (solve_table<G>(grp, pt, a, o, best, chosen, first, first_idx)) {
-                write_point<G>(a.P, pt, a, i, gl, best, true, chosen, PNJL_POINT_CONVERGED);
-            } else if (first_idx >= 0) {
-                write_point<G>(a.P, pt, a, i, gl, first, false, first_idx, PNJL_POINT_ALL_SEEDS_FAILED);
-            } else {
-                Candidate c;
-                for (int k = 0; k < 5; ++k) c.x[k] = a.seed_table[k];
-                c.residual_norm = c.omega = c.entropy = __longlong_as_double(0x7ff8000000000000ll);
-                for (int k = 0; k < 3; ++k) c.rho[k] = c.nq[k] = c.naq[k] = __longlong_as_double(0x7ff8000000000000ll);
-                c.iterations = 0;
-                write_point<G>(a.P, pt, a, i, gl, c, false, -1, PNJL_POINT_ALL_SEEDS_FAILED);
+            cnt.v[kStatMsFallbacks] += 1;
+            Candidate best;
+            int chosen = -1;
+            const bool have = solve_table_inline<G>(grp, pt, a, best, chosen);
+            if (gl == 0) {
+                if (have) write_point(a.P, pt, a.out, i, best, true, chosen, PNJL_POINT_CONVERGED);
+                else write_point(a.P, pt, a.out, i, single, false, -1, PNJL_POINT_NOT_CONVERGED);
             }
         }
     }
-    if (gl == 0) {
-        atomicAdd((unsigned long long *)&a.stats[0], (unsigned long long)cnt.passes64);
-        atomicAdd((unsigned long long *)&a.stats[1], (unsigned long long)cnt.evals64);
-        atomicAdd((unsigned long long *)&a.stats[2], (unsigned long long)cnt.seeds);
-        atomicAdd((unsigned long long *)&a.stats[3], (unsigned long long)cnt.tr_runs);
-        atomicAdd((unsigned long long *)&a.stats[4], (unsigned long long)cnt.ms_fallbacks);
-    }
+    if (gl == 0)
+        for (int k = 0; k < kStatCount; ++k)
+            if (cnt.v[k]) atomicAdd((unsigned long long *)&a.stats[k], (unsigned long long)cnt.v[k]);
 }
 
-// One pass + assembly per state: Omega, grad_x Omega, Hessian_x Omega and thermo.
+// One full pass + assembly per state: Omega, grad_x Omega, Hessian_x Omega and thermo.
 template <int G, bool FP32>
 __global__ void __launch_bounds__(kSolveThreads) eval_kernel(EvalArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const NodeView nv = stage_nodes(a.nodes, FP32, smem_raw, a.stage_nodes);
+    const NodeView nv = stage_nodes(a.nodes, smem_raw);
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const int gl = lane & (G - 1);
@@ -459,10 +542,10 @@ __global__ void __launch_bounds__(kSolveThreads) eval_kernel(EvalArgs a) {
         double M[3];
         masses(a.P, x, M);
         PassSums S;
-        if (FP32) node_pass<float, true, true, true, G>(nv, pt, x, M, gl, mask, S, evals);
-        else node_pass<double, false, true, true, G>(nv, pt, x, M, gl, mask, S, evals);
+        if (FP32) node_pass<float, true, true, true, true, G>(nv, pt, x, M, gl, mask, S, evals);
+        else node_pass<double, false, true, true, true, G>(nv, pt, x, M, gl, mask, S, evals);
         Eval ev;
-        assemble<true, true>(a.P, pt, x, M, S, ev);
+        assemble<true, true, true>(a.P, pt, x, M, S, ev);
         if (gl == 0) {
             if (a.omega) a.omega[i] = ev.omega;
             if (a.grad) for (int k = 0; k < 5; ++k) a.grad[5 * i + k] = -ev.F[k];
@@ -488,14 +571,8 @@ __global__ void __launch_bounds__(kSolveThreads) eval_kernel(EvalArgs a) {
 
 // ---------------------------------------------------------------------------------------
 // launch wrappers
-size_t node_smem_bytes(int n, bool fp32_too) { return (size_t)n * 3 * (sizeof(double) + (fp32_too ? sizeof(float) : 0)); }
-
 template <int G>
 static cudaError_t launch_solve_g(const SolveArgs &a, int grid, size_t smem, cudaStream_t s) {
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(solve_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-    }
     solve_kernel<G><<<grid, kSolveThreads, smem, s>>>(a);
     return cudaGetLastError();
 }
@@ -510,10 +587,6 @@ cudaError_t launch_solve(const SolveArgs &a, int group, int grid, size_t smem, c
 
 template <int G, bool FP32>
 static cudaError_t launch_eval_g(const EvalArgs &a, int grid, size_t smem, cudaStream_t s) {
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(eval_kernel<G, FP32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-    }
     eval_kernel<G, FP32><<<grid, kSolveThreads, smem, s>>>(a);
     return cudaGetLastError();
 }
@@ -526,10 +599,8 @@ int solve_kernel_occupancy(int group, size_t smem) {
     int nb = 0;
     cudaError_t e = cudaSuccess;
     switch (group) {
-        case 32: cudaFuncSetAttribute(solve_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                 e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, solve_kernel<32>, kSolveThreads, smem); break;
-        case 8: cudaFuncSetAttribute(solve_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, solve_kernel<8>, kSolveThreads, smem); break;
+        case 32: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, solve_kernel<32>, kSolveThreads, smem); break;
+        case 8: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, solve_kernel<8>, kSolveThreads, smem); break;
         default: return 0;
     }
     return e == cudaSuccess ? nb : 0;

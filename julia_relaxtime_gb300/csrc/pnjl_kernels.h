@@ -12,16 +12,30 @@ namespace pnjl {
 
 static constexpr int kSolveThreads = 256;
 
+// Separable node tables on the device (FP64 and an FP32 copy).
 struct KernelNodes {
-    const double *p2, *pc2, *w;
-    const float *p2f, *pc2f, *wf;
-    int n;
+    const double *p2, *A, *c2, *B;
+    const float *p2f, *Af, *c2f, *Bf;
+    int p_num, t_num;
+};
+
+// Scratch record of one (point, seed) task in MultiSeed mode (176 bytes).
+struct CandRec {
+    double x[5];
+    double residual_norm, omega, entropy;
+    double rho[3], nq[3], naq[3];
+    int iterations, flags;
+};
+
+// Counter slots of SolveArgs::stats
+enum StatSlot {
+    kStatPasses64 = 0, kStatEvalsNewton64, kStatEvalsThermo64, kStatSeeds, kStatTrRuns, kStatMsFallbacks,
+    kStatPasses32, kStatEvals32, kStatCount
 };
 
 struct SolveArgs {
     DevParams P;
     KernelNodes nodes;
-    bool stage_nodes;
     int64_t n;
     const double *T, *mu_u, *mu_d, *mu_s, *xi;
     int seed_mode, n_seeds;
@@ -31,21 +45,22 @@ struct SolveArgs {
     const double *point_seeds;    // device [n*5]
     SolveOpts opts;
     pnjl_result_soa out;          // device pointers
+    CandRec *cand;                // scratch [n*n_seeds] (MultiSeed mode)
+    int *done;                    // scratch [n], zeroed before the launch
     long long *queue;             // device work-queue head (zeroed before the launch)
-    long long *stats;             // device counters [8]
+    long long *stats;             // device counters [kStatCount]
 };
 
 struct EvalArgs {
     DevParams P;
     KernelNodes nodes;
-    bool stage_nodes;
     int64_t n;
     const double *x, *T, *mu_u, *mu_d, *mu_s, *xi;
     double *omega, *grad, *hess;
     pnjl_result_soa out;
 };
 
-size_t node_smem_bytes(int n, bool fp32_too);
+size_t node_smem_bytes(int p_num, int t_num);
 cudaError_t launch_solve(const SolveArgs &a, int group, int grid, size_t smem, cudaStream_t s);
 cudaError_t launch_eval(const EvalArgs &a, bool fp32, int grid, size_t smem, cudaStream_t s);
 int solve_kernel_occupancy(int group, size_t smem);

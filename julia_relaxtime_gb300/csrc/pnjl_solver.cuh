@@ -31,10 +31,11 @@ struct Eval {
     double nq[3], naq[3];
 };
 
+// Separable node tables (see pnjl_device.cuh): p2[ip], A[ip] over p; c2[it], B[it] over t.
 struct NodeView {
-    const double *p2, *pc2, *w;   // FP64 mesh (p^2, (p c)^2, weight)
-    const float *p2f, *pc2f, *wf; // FP32 copy
-    int n;
+    const double *p2, *A, *c2, *B;
+    const float *p2f, *Af, *c2f, *Bf;
+    int p_num, t_num;
 };
 
 __device__ __forceinline__ void masses(const DevParams &P, const double *x, double *M) {
@@ -47,7 +48,7 @@ template <int G>
 __device__ __forceinline__ unsigned group_mask(int lane) {
     if (G == 32) return 0xffffffffu;
     const unsigned base = (unsigned)(lane & ~(G - 1));
-    return ((G == 32) ? 0xffffffffu : ((1u << G) - 1u)) << base;
+    return ((1u << G) - 1u) << base;
 }
 
 // XOR butterfly: a + b == b + a bitwise, so every lane of the group ends with the
@@ -60,54 +61,80 @@ __device__ __forceinline__ double group_sum(double v, unsigned mask) {
 }
 
 // One pass over the node-flavour mesh at state x; lane `gl` of a group of G lanes takes
-// nodes gl, gl+G, ...  Returns the group-reduced sums (identical in every lane).
-template <typename R, bool KAHAN, bool HESS, bool LOG, int G>
+// the flattened nodes k = gl, gl+G, ... (k = ip + p_num*it).  Returns the group-reduced
+// sums (identical in every lane of the group); entries a pass does not compute are 0.
+template <typename R, bool KAHAN, bool GRAD, bool HESS, bool THERMO, int G>
 __device__ void node_pass(const NodeView &nv, const PointIn &pt, const double *x, const double *M, int gl,
                           unsigned mask, PassSums &S, int64_t &evals) {
-    double acc[kPassSumCount];
+    constexpr int NS = 25;
+    double acc[NS];
 #pragma unroll
-    for (int i = 0; i < kPassSumCount; ++i) acc[i] = 0.0;
+    for (int i = 0; i < NS; ++i) acc[i] = 0.0;
     const bool dedup = (M[1] == M[0]) && (pt.mu[1] == pt.mu[0]);
+    const R *p2, *A, *c2, *B;
+    if constexpr (sizeof(R) == 8) { p2 = (const R *)nv.p2; A = (const R *)nv.A; c2 = (const R *)nv.c2; B = (const R *)nv.B; }
+    else { p2 = (const R *)nv.p2f; A = (const R *)nv.Af; c2 = (const R *)nv.c2f; B = (const R *)nv.Bf; }
+    const int pn = nv.p_num, n = nv.p_num * nv.t_num;
     const R xi = (R)pt.xi;
-    const R *p2 = nullptr, *pc2 = nullptr, *w = nullptr;
-    if constexpr (sizeof(R) == 8) { p2 = (const R *)nv.p2; pc2 = (const R *)nv.pc2; w = (const R *)nv.w; }
-    else { p2 = (const R *)nv.p2f; pc2 = (const R *)nv.pc2f; w = (const R *)nv.wf; }
 #pragma unroll 1
     for (int f = 0; f < 3; ++f) {
         if (f == 1 && dedup) continue;
         bool sw;
         const FlavourConst<R> fc = make_flavour<R>(M[f], pt.mu[f], pt.T, x[3], x[4], sw);
-        FlavourAcc<R, KAHAN, HESS, LOG> fa;
+        FlavourAcc<R, KAHAN> fa;
         fa.zero();
-#pragma unroll 2
-        for (int k = gl; k < nv.n; k += G) {
-            const R q2 = p2[k] + xi * pc2[k];
-            node_flavour<R, KAHAN, HESS, LOG>(fc, q2, w[k], fa);
+        int ip = gl, it = 0;
+        while (ip >= pn) { ip -= pn; ++it; }
+        R sxi = R(1), bw = R(0);
+        if (it < nv.t_num) { sxi = xi * c2[it] + R(1); bw = B[it]; }
+#pragma unroll 1
+        for (int k = gl; k < n; k += G) {
+            const R pp = p2[ip];
+            node_flavour<R, KAHAN, GRAD, HESS, THERMO>(fc, pp * sxi, A[ip] * bw, fa);
+            ip += G;
+            if (ip >= pn) {
+                do { ip -= pn; ++it; } while (ip >= pn);
+                if (it < nv.t_num) { sxi = xi * c2[it] + R(1); bw = B[it]; }
+            }
         }
-        const double mult = (f == 0 && dedup) ? 2.0 : 1.0;
-        const int fs[2] = {f, (f == 0 && dedup) ? 1 : f};
-        for (int j = 0; j < ((f == 0 && dedup) ? 2 : 1); ++j) {
-            const int ff = fs[j];
-            acc[0 + ff] = fa.DM.value();
-            acc[3 + ff] = HESS ? fa.DMM.value() : 0.0;
-            acc[6 + ff] = HESS ? (sw ? fa.DMa.value() : fa.DMq.value()) : 0.0;
-            acc[9 + ff] = HESS ? (sw ? fa.DMq.value() : fa.DMa.value()) : 0.0;
-            acc[12 + ff] = sw ? fa.Na.value() : fa.Nq.value();
-            acc[15 + ff] = sw ? fa.Nq.value() : fa.Na.value();
+        const bool two = (f == 0 && dedup);
+        const double mult = two ? 2.0 : 1.0;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            if (j == 1 && !two) break;
+            const int ff = j == 0 ? f : 1;
+            if (GRAD) acc[0 + ff] = fa.DM.value();
+            if (HESS) {
+                acc[3 + ff] = fa.DMM.value();
+                acc[6 + ff] = sw ? fa.DMa.value() : fa.DMq.value();
+                acc[9 + ff] = sw ? fa.DMq.value() : fa.DMa.value();
+            }
+            if (THERMO) {
+                acc[12 + ff] = sw ? fa.Na.value() : fa.Nq.value();
+                acc[15 + ff] = sw ? fa.Nq.value() : fa.Na.value();
+            }
         }
-        acc[18] += mult * (LOG ? fa.SL.value() : 0.0);
-        acc[19] += mult * (sw ? fa.Sa.value() : fa.Sq.value());
-        acc[20] += mult * (sw ? fa.Sq.value() : fa.Sa.value());
+        if (GRAD) {
+            acc[19] += mult * (sw ? fa.Sa.value() : fa.Sq.value());
+            acc[20] += mult * (sw ? fa.Sq.value() : fa.Sa.value());
+        }
         if (HESS) {
             acc[21] += mult * (sw ? fa.Saa.value() : fa.Sqq.value());
             acc[22] += mult * fa.Sqa.value();
             acc[23] += mult * (sw ? fa.Sqq.value() : fa.Saa.value());
         }
-        acc[24] += mult * (LOG ? fa.SAN.value() : 0.0);
-        if (gl == 0) evals += (int64_t)nv.n;
+        if (THERMO) {
+            acc[18] += mult * fa.SL.value();
+            acc[24] += mult * fa.SAN.value();
+        }
+        if (gl == 0) evals += (int64_t)n;
     }
 #pragma unroll
-    for (int i = 0; i < kPassSumCount; ++i) acc[i] = group_sum<G>(acc[i], mask);
+    for (int i = 0; i < NS; ++i) {
+        const bool used = (i < 3 || i == 19 || i == 20) ? GRAD
+                          : (i < 12 || (i >= 21 && i <= 23)) ? HESS : THERMO;
+        if (used) acc[i] = group_sum<G>(acc[i], mask);
+    }
     for (int f = 0; f < 3; ++f) {
         S.DM[f] = acc[0 + f]; S.DMM[f] = acc[3 + f]; S.DMP[f] = acc[6 + f]; S.DMPb[f] = acc[9 + f];
         S.Nq[f] = acc[12 + f]; S.Na[f] = acc[15 + f];
@@ -117,7 +144,7 @@ __device__ void node_pass(const NodeView &nv, const PointIn &pt, const double *x
 }
 
 // FP64 assembly of Omega, grad, Hessian and thermo from the pass sums.
-template <bool HESS, bool LOG>
+template <bool GRAD, bool HESS, bool LOG>
 __device__ void assemble(const DevParams &P, const PointIn &pt, const double *x, const double *M, const PassSums &S,
                          Eval &ev) {
     const double T = pt.T;
