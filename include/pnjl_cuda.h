@@ -181,7 +181,7 @@ int pnjl_get_stats(const pnjl_ctx *ctx, pnjl_stats *out);
 /* Number of streaming multiprocessors of the context's device. */
 int pnjl_device_sm_count(const pnjl_ctx *ctx);
 
-/* Launch shape of the solve kernel: lanes per point (8 or 32) and resident blocks
+/* Launch shape of the solve kernel: lanes per task (32: one warp) and resident blocks
  * per SM (0 = occupancy maximum).  Chosen by the autotuner; results do not depend on it. */
 int pnjl_set_tuning(pnjl_ctx *ctx, int32_t lanes_per_point, int32_t blocks_per_sm);
 

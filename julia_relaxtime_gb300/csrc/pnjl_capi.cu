@@ -591,8 +591,8 @@ int pnjl_probe_peak(pnjl_ctx *ctx, int32_t kind, double *ops_per_s) {
 
 int pnjl_set_tuning(pnjl_ctx *ctx, int32_t lanes_per_point, int32_t blocks_per_sm) {
     if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
-    if (lanes_per_point != 8 && lanes_per_point != 32)
-        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "lanes_per_point must be 8 or 32");
+    if (lanes_per_point != 32)
+        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "lanes_per_point must be 32");
     if (blocks_per_sm < 0 || blocks_per_sm > 32) return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "blocks_per_sm out of range");
     ctx->group = lanes_per_point;
     ctx->blocks_per_sm = blocks_per_sm;

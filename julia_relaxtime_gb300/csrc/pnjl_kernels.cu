@@ -580,7 +580,6 @@ static cudaError_t launch_solve_g(const SolveArgs &a, int grid, size_t smem, cud
 cudaError_t launch_solve(const SolveArgs &a, int group, int grid, size_t smem, cudaStream_t s) {
     switch (group) {
         case 32: return launch_solve_g<32>(a, grid, smem, s);
-        case 8: return launch_solve_g<8>(a, grid, smem, s);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -600,7 +599,6 @@ int solve_kernel_occupancy(int group, size_t smem) {
     cudaError_t e = cudaSuccess;
     switch (group) {
         case 32: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, solve_kernel<32>, kSolveThreads, smem); break;
-        case 8: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, solve_kernel<8>, kSolveThreads, smem); break;
         default: return 0;
     }
     return e == cudaSuccess ? nb : 0;
