@@ -28,6 +28,7 @@ extern "C" {
 #define PNJL_ERR_OUT_OF_MEMORY 4
 #define PNJL_ERR_NOT_TRAINED 5
 #define PNJL_ERR_TIMEOUT 6
+#define PNJL_ERR_TOO_LARGE 7 /* batch beyond the fixed scratch of pnjl_solve_batch_noalloc */
 
 /* ---- per-point status (pnjl_result_soa.status) ---- */
 #define PNJL_POINT_CONVERGED 0        /* converged, physical, residual <= residual_norm_max */
@@ -189,6 +190,31 @@ int pnjl_set_tuning(pnjl_ctx *ctx, int32_t lanes_per_point, int32_t blocks_per_s
  * rooflines (no counterpart in the reference, which has no GPU): kind 0 = FP64 FMA
  * (FLOP/s, FMA = 2), 1 = FP32 FMA (FLOP/s), 2 = SFU ex2.approx.f32 (operations/s). */
 int pnjl_probe_peak(pnjl_ctx *ctx, int32_t kind, double *ops_per_s);
+
+/* Largest batch of pnjl_solve_batch_noalloc, counted in tasks: n * n_seeds in
+ * PNJL_SEEDS_TABLE mode, n in PNJL_SEEDS_PER_POINT mode (and n itself at most this). */
+#define PNJL_NOALLOC_MAX_TASKS 32768
+
+/* Batched solve that allocates nothing (no counterpart in the reference, which has no GPU
+ * code; it is an allocation-free twin of pnjl_solve_batch_device).  For callers that may not
+ * allocate device memory when they solve: code running inside a CUDA stream capture, hosts
+ * whose device memory belongs to another allocator's pool, services that reserve all memory
+ * at start-up.  They pass device inputs and outputs (same layout and meaning as
+ * pnjl_solve_batch_device; opts->seed_table stays a host pointer, opts->point_seeds is a
+ * device pointer) and a stream; no context is used and the call makes no cudaMalloc,
+ * cudaFree or other allocating call.  The scratch it needs (candidate records, completion
+ * counters, queue head, node and seed tables) is one static device array of about 6 MB that
+ * every GPU loading this library holds until exit; batches beyond PNJL_NOALLOC_MAX_TASKS
+ * tasks return PNJL_ERR_TOO_LARGE.  The call is asynchronous on `stream` (NULL = the legacy
+ * default stream) and runs on the current device.  Its first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress) and loads the kernel module, so make that
+ * first call before any stream capture.  All calls share the one array and it keeps the last
+ * call's contents (the counters are cleared by each call): calls that overlap on the GPU --
+ * on two streams, or from two threads -- race and must not be issued. */
+int pnjl_solve_batch_noalloc(const pnjl_params *params, int32_t p_num, int32_t t_num, double p_max, int64_t n,
+                             const double *d_T, const double *d_mu_u, const double *d_mu_d, const double *d_mu_s,
+                             const double *d_xi, const pnjl_solve_opts *opts, pnjl_result_soa *d_out,
+                             void *stream);
 
 #ifdef __cplusplus
 }

@@ -19,6 +19,8 @@ PNJL_ERR_NO_NODES = 3
 PNJL_ERR_OUT_OF_MEMORY = 4
 PNJL_ERR_NOT_TRAINED = 5
 PNJL_ERR_TIMEOUT = 6
+PNJL_ERR_TOO_LARGE = 7
+PNJL_NOALLOC_MAX_TASKS = 32768
 
 PNJL_POINT_CONVERGED = 0
 PNJL_POINT_NOT_CONVERGED = 1
@@ -105,6 +107,9 @@ SIGNATURES = {
     "pnjl_device_sm_count": (C.c_int, [C.c_void_p]),
     "pnjl_set_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "pnjl_probe_peak": (C.c_int, [C.c_void_p, C.c_int32, dp]),
+    "pnjl_solve_batch_noalloc": (C.c_int, [C.POINTER(pnjl_params), C.c_int32, C.c_int32, C.c_double, C.c_int64,
+                                           dp, dp, dp, dp, dp, C.POINTER(pnjl_solve_opts),
+                                           C.POINTER(pnjl_result_soa), C.c_void_p]),
 }
 
 _lib = None

@@ -11,6 +11,7 @@
 #include <string>
 #include <vector>
 
+#include "pnjl_host_common.h"
 #include "pnjl_kernels.h"
 
 struct pnjl_ctx {
@@ -60,51 +61,10 @@ int cuda_fail(pnjl_ctx *ctx, cudaError_t e, const char *what) {
         if (_e != cudaSuccess) return cuda_fail((ctx), _e, #call); \
     } while (0)
 
-// Gauss-Legendre rule on [a, b] (ascending): Newton's method on the Legendre polynomial
-// P_n evaluated by its three-term recurrence, started from cos(pi (k + 3/4) / (n + 1/2)),
-// weights 2 / ((1 - x^2) P_n'(x)^2).  Same published rule the reference obtains from
-// FastGaussQuadrature.gausslegendre (src/integration/GaussLegendre.jl:33-42, :94-119).
 void gauss_legendre(int n, double a, double b, std::vector<double> &x, std::vector<double> &w) {
     x.assign(n, 0.0);
     w.assign(n, 0.0);
-    const int half = (n + 1) / 2;
-    for (int k = 0; k < half; ++k) {
-        long double z = std::cos(M_PI * (k + 0.75) / (n + 0.5));
-        long double dp = 1.0L;
-        for (int iter = 0; iter < 64; ++iter) {
-            long double p0 = 1.0L, p1 = z;
-            for (int j = 2; j <= n; ++j) {
-                long double p2 = ((2.0L * j - 1.0L) * z * p1 - (j - 1.0L) * p0) / j;
-                p0 = p1;
-                p1 = p2;
-            }
-            if (n == 1) { p1 = z; p0 = 1.0L; }
-            dp = n * (z * p1 - p0) / (z * z - 1.0L);
-            long double dz = p1 / dp;
-            z -= dz;
-            if (std::fabs((double)dz) < 1e-19) break;
-        }
-        // derivative at the converged root
-        long double p0 = 1.0L, p1 = z;
-        for (int j = 2; j <= n; ++j) {
-            long double p2 = ((2.0L * j - 1.0L) * z * p1 - (j - 1.0L) * p0) / j;
-            p0 = p1;
-            p1 = p2;
-        }
-        if (n == 1) { p1 = z; p0 = 1.0L; }
-        dp = n * (z * p1 - p0) / (z * z - 1.0L);
-        const double wt = (double)(2.0L / ((1.0L - z * z) * dp * dp));
-        x[k] = -(double)z;
-        x[n - 1 - k] = (double)z;
-        w[k] = wt;
-        w[n - 1 - k] = wt;
-        if (2 * k + 1 == n) x[k] = 0.0;
-    }
-    const double scale = (b - a) / 2.0, shift = (b + a) / 2.0;
-    for (int i = 0; i < n; ++i) {
-        x[i] = scale * x[i] + shift;
-        w[i] = scale * w[i];
-    }
+    pnjl::gauss_legendre_into(n, a, b, x.data(), w.data());
 }
 
 template <typename T>
@@ -169,21 +129,9 @@ int ensure_scratch(pnjl_ctx *ctx, size_t bytes) {
 }
 
 int check_opts(pnjl_ctx *ctx, const pnjl_solve_opts *o) {
-    if (!o) return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "opts is NULL");
-    if (o->seed_mode != PNJL_SEEDS_TABLE && o->seed_mode != PNJL_SEEDS_PER_POINT)
-        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "unknown seed_mode");
-    const bool need_table = o->seed_mode == PNJL_SEEDS_TABLE || o->auto_multiseed_fallback;
-    if (need_table && (o->n_seeds < 1 || o->n_seeds > 16 || !o->seed_table))
-        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "seed table must have 1..16 rows");
-    if (o->seed_mode == PNJL_SEEDS_PER_POINT && !o->point_seeds)
-        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "point_seeds is NULL");
-    if (o->max_iter < 0 || o->max_iter > 100000) return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "max_iter out of range");
-    if (!(o->ftol > 0) || !(o->xtol >= 0) || !(o->residual_norm_max > 0) || !(o->phi_tol >= 0) ||
-        !(o->omega_tie_rtol >= 0))
-        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "tolerances must be positive");
-    if (o->precision != PNJL_PREC_FP64 && o->precision != PNJL_PREC_MIXED)
-        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "unknown precision");
-    return PNJL_OK;
+    const char *msg = "";
+    const int rc = pnjl::validate_opts(o, &msg);
+    return rc ? fail(ctx, rc, msg) : PNJL_OK;
 }
 
 int grid_for(pnjl_ctx *ctx, int group, size_t smem, int64_t n) {
@@ -229,8 +177,7 @@ int pnjl_init(const pnjl_params *params, int device, pnjl_ctx **out) {
     if (params) ctx->params = *params;
     else pnjl_params_default(&ctx->params);
     const pnjl_params &p = ctx->params;
-    ctx->dp = pnjl::DevParams{p.hbarc_MeV_fm, p.Lambda, p.G, p.K, p.m_ud0, p.m_s0, p.T0,
-                              p.a0, p.a1, p.a2, p.b3, p.N_color, p.rho0};
+    ctx->dp = pnjl::dev_params(p);
     ctx->device = device;
     int rc = PNJL_OK;
     cudaError_t e = cudaSetDevice(device);
@@ -271,7 +218,7 @@ const char *pnjl_last_error(const pnjl_ctx *ctx) { return ctx ? ctx->err.c_str()
 
 int pnjl_set_nodes(pnjl_ctx *ctx, int32_t p_num, int32_t t_num, double p_max) {
     if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
-    if (p_num < 1 || p_num > 512 || t_num < 1 || t_num > 64 || !(p_max > 0.0))
+    if (p_num < 1 || p_num > pnjl::kMaxPNodes || t_num < 1 || t_num > pnjl::kMaxTNodes || !(p_max > 0.0))
         return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "node counts out of range (1..512 x 1..64, p_max > 0)");
     cudaSetDevice(ctx->device);
     std::vector<double> xp, wp, xc, wc;
@@ -293,15 +240,7 @@ int pnjl_set_nodes(pnjl_ctx *ctx, int32_t p_num, int32_t t_num, double p_max) {
     const int m = 2 * (p_num + t_num);
     std::vector<double> h(m);
     std::vector<float> hf(m);
-    for (int ip = 0; ip < p_num; ++ip) {
-        h[ip] = xp[ip] * xp[ip];
-        h[p_num + ip] = wp[ip] * (xp[ip] * xp[ip]) / fourpi2;
-    }
-    for (int it = 0; it < t_num; ++it) {
-        h[2 * p_num + it] = xc[it] * xc[it];
-        h[2 * p_num + t_num + it] = 2.0 * wc[it];
-    }
-    for (int i = 0; i < m; ++i) hf[i] = (float)h[i];
+    pnjl::separable_tables(p_num, t_num, xp.data(), wp.data(), xc.data(), wc.data(), h.data(), hf.data());
     PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     cudaFree(ctx->d_nodes);
     cudaFree(ctx->d_nodes_f);
@@ -451,14 +390,7 @@ int pnjl_solve_batch_device(pnjl_ctx *ctx, int64_t n, const double *d_T, const d
     a.seed_table_hot = (has_table && opts->seed_table_hot) ? ctx->d_seed_tables + 80 : nullptr;
     a.hot_T_MeV = opts->hot_T_MeV;
     a.point_seeds = opts->point_seeds;
-    a.opts.max_iter = opts->max_iter;
-    a.opts.ftol = opts->ftol;
-    a.opts.xtol = opts->xtol;
-    a.opts.residual_norm_max = opts->residual_norm_max;
-    a.opts.phi_tol = opts->phi_tol;
-    a.opts.omega_tie_rtol = opts->omega_tie_rtol;
-    a.opts.trust_region_fallback = opts->trust_region_fallback;
-    a.opts.auto_multiseed_fallback = opts->auto_multiseed_fallback;
+    pnjl::fill_solve_opts(opts, a.opts);
     a.out = *d_out;
     a.queue = ctx->d_ctrl;
     a.stats = ctx->d_ctrl + 1;
