@@ -43,8 +43,21 @@ METRIC = "gap solves/s at ||dOmega|| <= 1e-10"
 # counted separately and not as FLOPs):
 #   Newton pass (residual + Jacobian):        123 FLOP + 3 transcendentals
 #   thermo pass (Omega, s, rho, n_f at the end): 58 FLOP + 4 transcendentals
+#   residual-only pass (mixed-precision refinement):  53 FLOP + 3 transcendentals
+#   residual + thermo pass (mixed refinement):        69 FLOP + 4 transcendentals
+#   FP32 Newton pass: 123 FLOP + 27 for the Kahan compensation of 9 sums = 150 FLOP
 FLOP_NEWTON = 123
 FLOP_THERMO = 58
+FLOP_GRAD = 53
+FLOP_GRAD_THERMO = 69
+FLOP_NEWTON32 = 150
+
+
+def pass_flops(st: dict):
+    """(FP64 FLOP, FP32 FLOP) of one solve from the library's node-evaluation counters."""
+    f64 = (st["node_evals_fp64_newton"] * FLOP_NEWTON + st["node_evals_fp64_thermo"] * FLOP_THERMO +
+           st["node_evals_fp64_grad"] * FLOP_GRAD + st["node_evals_fp64_grad_thermo"] * FLOP_GRAD_THERMO)
+    return f64, st["node_evals_fp32"] * FLOP_NEWTON32
 
 
 def workload_grid(name: str):
@@ -238,7 +251,8 @@ def main():
 
     # timed region: K steps, device inputs already resident per step (loaded before the events)
     sampler = ClockSampler(local_rank)
-    kernel_ms, step_ms, solved, evals, flops, launches0 = [], [], 0, 0, 0, eng.stats()["kernel_launches"]
+    kernel_ms, step_ms, solved, evals, flops, flops32 = [], [], 0, 0, 0, 0
+    launches0 = eng.stats()["kernel_launches"]
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
@@ -256,9 +270,10 @@ def main():
         step_ms.append(e0.elapsed_time(e1))
         st = eng.stats()
         kernel_ms.append(st["last_kernel_ms"])
-        evals += st["node_evals_fp64"]
-        flops += (st["node_evals_fp64"] - st["node_evals_fp64_thermo"]) * FLOP_NEWTON + \
-            st["node_evals_fp64_thermo"] * FLOP_THERMO
+        evals += st["node_evals_fp64"] + st["node_evals_fp32"]
+        f64, f32 = pass_flops(st)
+        flops += f64
+        flops32 += f32
         conv = d_out["converged"][:n].cpu().numpy().astype(bool)
         res = d_out["residual_norm"][:n].cpu().numpy()
         solved += int(np.sum(conv & (res <= 1e-10)))
@@ -295,19 +310,24 @@ def main():
     if rank != 0:
         return
     peak_fp64 = eng.probe_peak("fp64")
+    peak_fp32 = eng.probe_peak("fp32")
     avg_kernel_s = (sum(kernel_ms) / len(kernel_ms)) * 1e-3
-    flops_per_launch = flops / args.steps
-    achieved = flops_per_launch / avg_kernel_s
+    ach64 = flops / args.steps / avg_kernel_s
+    ach32 = flops32 / args.steps / avg_kernel_s
+    kname = "solve_kernel<32>" if args.precision == "fp64" else "solve_kernel_mixed<32>"
+    roof = {"bound": "fp64", "kernel": kname, "achieved": ach64 / 1e12, "peak": peak_fp64 / 1e12,
+            "unit": "TFLOP/s", "frac": ach64 / peak_fp64,
+            "peak_source": "measured in-run (pnjl_probe_peak, FMA chains on every lane of the GPU)",
+            "flop_per_node_flavour": {"newton_pass": FLOP_NEWTON, "thermo_pass": FLOP_THERMO,
+                                      "residual_pass": FLOP_GRAD, "residual_thermo_pass": FLOP_GRAD_THERMO,
+                                      "newton_pass_fp32": FLOP_NEWTON32},
+            "node_flavour_evals_per_launch": evals / args.steps, "traffic": None,
+            "fp32": {"achieved": ach32 / 1e12, "peak": peak_fp32 / 1e12, "frac": ach32 / peak_fp32}}
     line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
             "data": "synthetic", "config": config, "e2e": e2e, "gpu_launches": int(launches),
-            "roofline": {"bound": "fp64", "kernel": "solve_kernel<32>", "achieved": achieved / 1e12,
-                         "peak": peak_fp64 / 1e12, "unit": "TFLOP/s", "frac": achieved / peak_fp64,
-                         "peak_source": "measured in-run (pnjl_probe_peak FP64 FMA chains)",
-                         "flop_per_node_flavour": {"newton_pass": FLOP_NEWTON, "thermo_pass": FLOP_THERMO},
-                         "node_flavour_evals_per_launch": evals / args.steps, "traffic": None},
-            "clocks": clocks, "solved": solved}
+            "roofline": roof, "clocks": clocks, "solved": solved}
     if not args.no_cpu_baseline:
         class A:  # noqa: N801
             warmup, steps = 0, 1

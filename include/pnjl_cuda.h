@@ -111,19 +111,23 @@ typedef struct pnjl_result_soa {
     uint8_t *converged;    /* [n]                                                    */
 } pnjl_result_soa;
 
-/* Counters of the last solve on the context. */
+/* Counters of the last solve on the context.  A node-flavour evaluation is one (p, cos(theta),
+ * flavour) term of the thermal integral; the kinds differ in what a pass computes. */
 typedef struct pnjl_stats {
     int64_t points;
-    int64_t passes_fp64;      /* full passes over the 3*p*t node-flavour mesh in FP64  */
-    int64_t passes_fp32;      /* ... in FP32                                          */
-    int64_t node_evals_fp64;  /* node-flavour evaluations actually executed (FP64)    */
-    int64_t node_evals_fp64_thermo; /* ... of them in thermo passes (Omega, s, rho, n_f) */
-    int64_t node_evals_fp32;
-    int64_t seeds_run;        /* Newton (+ trust region) runs                          */
+    int64_t passes_fp64;      /* passes over the 3*p*t node-flavour mesh in FP64        */
+    int64_t passes_fp32;      /* ... in FP32 (mixed precision)                          */
+    int64_t node_evals_fp64;  /* all FP64 node-flavour evaluations                      */
+    int64_t node_evals_fp64_newton;      /* residual + Jacobian passes                  */
+    int64_t node_evals_fp64_thermo;      /* Omega, entropy, rho, n_f passes             */
+    int64_t node_evals_fp64_grad;        /* residual-only passes (mixed refinement)     */
+    int64_t node_evals_fp64_grad_thermo; /* residual + thermo passes (mixed refinement) */
+    int64_t node_evals_fp32;  /* FP32 residual + Jacobian passes                        */
+    int64_t seeds_run;        /* Newton (+ trust region) runs                           */
     int64_t trust_region_runs;
     int64_t multiseed_fallbacks;
     int64_t kernel_launches;
-    double last_kernel_ms;    /* device time of the last solve kernel (CUDA events)    */
+    double last_kernel_ms;    /* device time of the last solve kernel (CUDA events)     */
 } pnjl_stats;
 
 /* Default parameter set: config/pnjl/default.toml:1-21 through Constants_PNJL.jl:82-103. */

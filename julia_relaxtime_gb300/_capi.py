@@ -80,10 +80,10 @@ class pnjl_result_soa(C.Structure):
 class pnjl_stats(C.Structure):
     _fields_ = [
         ("points", C.c_int64), ("passes_fp64", C.c_int64), ("passes_fp32", C.c_int64),
-        ("node_evals_fp64", C.c_int64), ("node_evals_fp64_thermo", C.c_int64), ("node_evals_fp32", C.c_int64),
-        ("seeds_run", C.c_int64),
-        ("trust_region_runs", C.c_int64), ("multiseed_fallbacks", C.c_int64), ("kernel_launches", C.c_int64),
-        ("last_kernel_ms", C.c_double),
+        ("node_evals_fp64", C.c_int64), ("node_evals_fp64_newton", C.c_int64), ("node_evals_fp64_thermo", C.c_int64),
+        ("node_evals_fp64_grad", C.c_int64), ("node_evals_fp64_grad_thermo", C.c_int64),
+        ("node_evals_fp32", C.c_int64), ("seeds_run", C.c_int64), ("trust_region_runs", C.c_int64),
+        ("multiseed_fallbacks", C.c_int64), ("kernel_launches", C.c_int64), ("last_kernel_ms", C.c_double),
     ]
 
 

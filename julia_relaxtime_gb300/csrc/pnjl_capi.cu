@@ -369,7 +369,8 @@ int pnjl_solve_batch_device(pnjl_ctx *ctx, int64_t n, const double *d_T, const d
                                                opts->n_seeds * 5 * sizeof(double), cudaMemcpyHostToDevice, s));
     }
     pnjl::SolveArgs a{};
-    if (opts->seed_mode == PNJL_SEEDS_TABLE) {
+    const bool mixed = opts->precision == PNJL_PREC_MIXED;
+    if (opts->seed_mode == PNJL_SEEDS_TABLE && !mixed) {
         const size_t rec = (size_t)n * opts->n_seeds * sizeof(pnjl::CandRec);
         const size_t cnt = ((size_t)n * sizeof(int) + 255) & ~size_t(255);
         int rc2 = ensure_scratch(ctx, cnt + rec);
@@ -395,11 +396,20 @@ int pnjl_solve_batch_device(pnjl_ctx *ctx, int64_t n, const double *d_T, const d
     a.queue = ctx->d_ctrl;
     a.stats = ctx->d_ctrl + 1;
     const int group = ctx->group;
-    const int64_t n_tasks = opts->seed_mode == PNJL_SEEDS_TABLE ? n * (int64_t)opts->n_seeds : n;
-    const int grid = grid_for(ctx, group, smem, n_tasks);
+    int grid = 0;
+    if (mixed) {
+        int occ = pnjl::solve_mixed_occupancy(smem);
+        if (occ < 1) occ = 1;
+        if (ctx->blocks_per_sm > 0 && ctx->blocks_per_sm < occ) occ = ctx->blocks_per_sm;
+        const int64_t need = (n + pnjl::kSolveThreads / 32 - 1) / (pnjl::kSolveThreads / 32);
+        grid = (int)std::min<int64_t>((int64_t)ctx->sm_count * occ, need);
+    } else {
+        const int64_t n_tasks = opts->seed_mode == PNJL_SEEDS_TABLE ? n * (int64_t)opts->n_seeds : n;
+        grid = grid_for(ctx, group, smem, n_tasks);
+    }
     PNJL_CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, s));
-    cudaError_t e = pnjl::launch_solve(a, group, grid, smem, s);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "solve_kernel launch");
+    cudaError_t e = mixed ? pnjl::launch_solve_mixed(a, grid, smem, s) : pnjl::launch_solve(a, group, grid, smem, s);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "solve kernel launch");
     PNJL_CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, s));
     ctx->stats.kernel_launches += 1;
     ctx->stats.points = n;
@@ -495,8 +505,12 @@ int pnjl_get_stats(const pnjl_ctx *cctx, pnjl_stats *out) {
     pnjl_stats st = ctx->stats;
     const long long *c = h + 1;
     st.passes_fp64 = c[pnjl::kStatPasses64];
-    st.node_evals_fp64 = c[pnjl::kStatEvalsNewton64] + c[pnjl::kStatEvalsThermo64];
+    st.node_evals_fp64_newton = c[pnjl::kStatEvalsNewton64];
     st.node_evals_fp64_thermo = c[pnjl::kStatEvalsThermo64];
+    st.node_evals_fp64_grad = c[pnjl::kStatEvalsGrad64];
+    st.node_evals_fp64_grad_thermo = c[pnjl::kStatEvalsGradThermo64];
+    st.node_evals_fp64 = st.node_evals_fp64_newton + st.node_evals_fp64_thermo + st.node_evals_fp64_grad +
+                         st.node_evals_fp64_grad_thermo;
     st.seeds_run = c[pnjl::kStatSeeds];
     st.trust_region_runs = c[pnjl::kStatTrRuns];
     st.multiseed_fallbacks = c[pnjl::kStatMsFallbacks];

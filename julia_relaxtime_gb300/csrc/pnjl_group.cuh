@@ -1,0 +1,622 @@
+// pnjl_group.cuh -- the per-task solver of libpnjl_cuda: a group of G lanes (G = 32, one
+// warp) that runs NLsolve-style Newton and trust-region solves of one (point, seed) on top of
+// the node passes of pnjl_solver.cuh, plus the helpers the solve kernels share (node-table
+// staging, candidate records, output writing).  Included by the kernel translation units.
+#pragma once
+
+#include "pnjl_kernels.h"
+#include "pnjl_solver.cuh"
+
+namespace pnjl {
+
+// ---------------------------------------------------------------------------------------
+// Stage the separable node tables (a few KB) into shared memory.
+__device__ __forceinline__ NodeView stage_nodes(const KernelNodes &kn, void *smem) {
+    NodeView nv;
+    nv.p_num = kn.p_num;
+    nv.t_num = kn.t_num;
+    const int np = kn.p_num, nt = kn.t_num;
+    double *sd = (double *)smem;
+    for (int i = threadIdx.x; i < np; i += blockDim.x) { sd[i] = kn.p2[i]; sd[np + i] = kn.A[i]; }
+    for (int i = threadIdx.x; i < nt; i += blockDim.x) { sd[2 * np + i] = kn.c2[i]; sd[2 * np + nt + i] = kn.B[i]; }
+    float *sf = (float *)(sd + 2 * (np + nt));
+    for (int i = threadIdx.x; i < np; i += blockDim.x) { sf[i] = kn.p2f[i]; sf[np + i] = kn.Af[i]; }
+    for (int i = threadIdx.x; i < nt; i += blockDim.x) { sf[2 * np + i] = kn.c2f[i]; sf[2 * np + nt + i] = kn.Bf[i]; }
+    nv.p2 = sd; nv.A = sd + np; nv.c2 = sd + 2 * np; nv.B = sd + 2 * np + nt;
+    nv.p2f = sf; nv.Af = sf + np; nv.c2f = sf + 2 * np; nv.Bf = sf + 2 * np + nt;
+    return nv;
+}
+
+
+struct Counters {
+    int64_t v[kStatCount];
+};
+
+__device__ __forceinline__ double qnan() { return __longlong_as_double(0x7ff8000000000000ll); }
+
+template <int G>
+struct Group {
+    const DevParams &P;
+    const NodeView &nv;
+    int gl;
+    unsigned mask;
+    Counters &cnt;
+
+    // residual and Jacobian at x (one Newton pass)
+    __device__ __noinline__ void eval_newton(const PointIn &pt, const double *x, double *F, double *J) {
+        double M[3];
+        masses(P, x, M);
+        PassSums S;
+        node_pass<double, false, true, true, false, G>(nv, pt, x, M, gl, mask, S, cnt.v[kStatEvalsNewton64]);
+        Eval ev;
+        assemble<true, true, false>(P, pt, x, M, S, ev);
+        for (int i = 0; i < 5; ++i) F[i] = ev.F[i];
+        for (int i = 0; i < 25; ++i) J[i] = ev.J[i];
+        cnt.v[kStatPasses64] += 1;
+    }
+
+    // Omega, entropy, rho_f and number densities at x (one thermo pass) -> candidate fields
+    __device__ __noinline__ void eval_thermo(const PointIn &pt, const SolveOpts &o, Candidate &c) {
+        double M[3];
+        masses(P, c.x, M);
+        PassSums S;
+        node_pass<double, false, false, false, true, G>(nv, pt, c.x, M, gl, mask, S, cnt.v[kStatEvalsThermo64]);
+        Eval ev;
+        assemble<false, false, true>(P, pt, c.x, M, S, ev);
+        cnt.v[kStatPasses64] += 1;
+        postprocess(P, pt, o, ev, c);
+    }
+
+    // NLsolve :newton (static line search) from x0
+    __device__ void newton(const PointIn &pt, const double *x0, const SolveOpts &o, Candidate &c) {
+        double x[5], xold[5], p[5], F[5], J[25];
+#pragma unroll
+        for (int i = 0; i < 5; ++i) { x[i] = x0[i]; xold[i] = qnan(); }
+        eval_newton(pt, x, F, J);
+        c.exception = !all_finite5(F);
+        if (c.exception) {
+            for (int i = 0; i < 5; ++i) c.x[i] = x0[i];
+            c.residual_norm = qnan();
+            c.iterations = 0;
+            c.f_converged = false;
+            c.phys = false;
+            return;
+        }
+        int it = 0;
+        bool xconv = false, fconv = norm_inf5(F) < o.ftol;
+        bool stopped = any_nan5(x) || any_nan5(F);
+        bool converged = fconv;
+        while (!stopped && !converged && it < o.max_iter) {
+            ++it;
+            if (lu_solve5(J, F, p)) {
+#pragma unroll
+                for (int i = 0; i < 5; ++i) p[i] = -p[i];
+            } else {
+                levenberg_step(J, F, p);
+            }
+#pragma unroll
+            for (int i = 0; i < 5; ++i) { xold[i] = x[i]; x[i] += p[i]; }
+            eval_newton(pt, x, F, J);
+            double dx = 0.0;
+            bool dxn = false;
+#pragma unroll
+            for (int i = 0; i < 5; ++i) {
+                const double d = fabs(x[i] - xold[i]);
+                dxn |= isnan(d);
+                dx = d > dx ? d : dx;
+            }
+            xconv = !any_nan5(xold) && !dxn && dx < o.xtol;
+            fconv = norm_inf5(F) < o.ftol;
+            stopped = any_nan5(x) || any_nan5(F);
+            converged = xconv || fconv;
+        }
+        for (int i = 0; i < 5; ++i) c.x[i] = x[i];
+        c.residual_norm = norm_inf5(F);
+        c.iterations = it;
+        c.f_converged = fconv;
+        eval_thermo(pt, o, c);
+    }
+
+    // singular Jacobian: p = -(J'J + lambda I) \ J'F, lambda = 1e6 sqrt(n eps) sum|J'J|
+    __device__ static void levenberg_step(const double *J, const double *F, double *p) {
+        double g[5], A[25], s = 0.0;
+        for (int i = 0; i < 5; ++i) {
+            double a = 0.0;
+            for (int k = 0; k < 5; ++k) a += J[k * 5 + i] * F[k];
+            g[i] = a;
+        }
+        for (int i = 0; i < 5; ++i)
+            for (int j = 0; j < 5; ++j) {
+                double a = 0.0;
+                for (int k = 0; k < 5; ++k) a += J[k * 5 + i] * J[k * 5 + j];
+                A[i * 5 + j] = -a;
+                s += fabs(a);
+            }
+        const double lambda = 1e6 * sqrt(5.0 * 2.220446049250313e-16) * s;
+        for (int i = 0; i < 5; ++i) A[i * 5 + i] -= lambda;
+        if (!lu_solve5(A, g, p))
+            for (int i = 0; i < 5; ++i) p[i] = qnan();
+    }
+
+    // NLsolve :trust_region (dogleg, autoscale) from x0
+    __device__ void trust_region(const PointIn &pt, const double *x0, const SolveOpts &o, Candidate &c) {
+        double x[5], xold[5], d[5], p[5], r[5], Jacc[25], F[5], J[25];
+        for (int i = 0; i < 5; ++i) { x[i] = x0[i]; xold[i] = qnan(); }
+        eval_newton(pt, x, r, Jacc);
+        cnt.v[kStatTrRuns] += 1;
+        c.exception = !all_finite5(r);
+        if (c.exception) {
+            for (int i = 0; i < 5; ++i) c.x[i] = x0[i];
+            c.residual_norm = qnan();
+            c.iterations = 0; c.f_converged = false; c.phys = false;
+            return;
+        }
+        int it = 0;
+        bool fconv = norm_inf5(r) < o.ftol;
+        bool stopped = any_nan5(x) || any_nan5(r);
+        bool converged = fconv;
+        if (!converged) {
+            for (int j = 0; j < 5; ++j) {
+                double s = 0.0;
+                for (int i = 0; i < 5; ++i) s += Jacc[i * 5 + j] * Jacc[i * 5 + j];
+                d[j] = sqrt(s);
+                if (d[j] == 0.0) d[j] = 1.0;
+            }
+            double delta = 0.0;
+            for (int i = 0; i < 5; ++i) delta += (d[i] * x[i]) * (d[i] * x[i]);
+            delta = sqrt(delta);
+            if (delta == 0.0) delta = 1.0;
+            while (!stopped && !converged && it < o.max_iter) {
+                ++it;
+                dogleg(p, r, d, Jacc, delta);
+                for (int i = 0; i < 5; ++i) { xold[i] = x[i]; x[i] += p[i]; }
+                eval_newton(pt, x, F, J);
+                double sr = 0.0, sf = 0.0, sp = 0.0;
+                for (int k = 0; k < 5; ++k) {
+                    double a = 0.0;
+                    for (int i = 0; i < 5; ++i) a += Jacc[k * 5 + i] * p[i];
+                    const double rp = a + r[k];
+                    sr += r[k] * r[k];
+                    sf += F[k] * F[k];
+                    sp += rp * rp;
+                }
+                const double rho = (sr - sf) / (sr - sp);
+                if (rho > 1e-4) {
+                    for (int i = 0; i < 5; ++i) r[i] = F[i];
+                    for (int i = 0; i < 25; ++i) Jacc[i] = J[i];
+                    for (int j = 0; j < 5; ++j) {
+                        double s = 0.0;
+                        for (int i = 0; i < 5; ++i) s += Jacc[i * 5 + j] * Jacc[i * 5 + j];
+                        const double cn = sqrt(s);
+                        d[j] = (0.1 * d[j] > cn) ? 0.1 * d[j] : cn;
+                    }
+                    double dx = 0.0;
+                    bool dxn = false;
+                    for (int i = 0; i < 5; ++i) {
+                        const double dd = fabs(x[i] - xold[i]);
+                        dxn |= isnan(dd);
+                        dx = dd > dx ? dd : dx;
+                    }
+                    const bool xconv = !dxn && dx < o.xtol;
+                    fconv = norm_inf5(r) < o.ftol;
+                    converged = xconv || fconv;
+                } else {
+                    for (int i = 0; i < 5; ++i) x[i] -= p[i];
+                    converged = false;
+                }
+                double wp = 0.0;
+                for (int i = 0; i < 5; ++i) wp += (d[i] * p[i]) * (d[i] * p[i]);
+                wp = sqrt(wp);
+                if (rho < 0.1) delta = delta / 2.0;
+                else if (rho >= 0.9) delta = 2.0 * wp;
+                else if (rho >= 0.5) delta = fmax(delta, 2.0 * wp);
+                stopped = any_nan5(x) || any_nan5(F);
+            }
+        }
+        for (int i = 0; i < 5; ++i) c.x[i] = x[i];
+        c.residual_norm = norm_inf5(r);
+        c.iterations = it;
+        c.f_converged = fconv;
+        eval_thermo(pt, o, c);
+    }
+
+    // Powell dogleg inside ||D p|| <= delta (Nocedal & Wright, section 4.1)
+    __device__ static void dogleg(double *p, const double *r, const double *d, const double *J, double delta) {
+        double pi[5], pc[5], g[5];
+        if (!lu_solve5(J, r, pi)) {
+            double JJ[25], Jr[5];
+            for (int i = 0; i < 5; ++i) {
+                double a = 0.0;
+                for (int k = 0; k < 5; ++k) a += J[k * 5 + i] * r[k];
+                Jr[i] = a;
+            }
+            for (int i = 0; i < 5; ++i)
+                for (int j = 0; j < 5; ++j) {
+                    double a = 0.0;
+                    for (int k = 0; k < 5; ++k) a += J[k * 5 + i] * J[k * 5 + j];
+                    JJ[i * 5 + j] = a;
+                }
+            for (int i = 0; i < 5; ++i) JJ[i * 5 + i] += 2.220446049250313e-16 * (1.0 + JJ[i * 5 + i]);
+            if (!lu_solve5(JJ, Jr, pi))
+                for (int i = 0; i < 5; ++i) pi[i] = 0.0;
+        }
+        for (int i = 0; i < 5; ++i) pi[i] = -pi[i];
+        double wpi = 0.0;
+        for (int i = 0; i < 5; ++i) wpi += (d[i] * pi[i]) * (d[i] * pi[i]);
+        if (sqrt(wpi) <= delta) {
+            for (int i = 0; i < 5; ++i) p[i] = pi[i];
+            return;
+        }
+        for (int i = 0; i < 5; ++i) {
+            double a = 0.0;
+            for (int k = 0; k < 5; ++k) a += J[k * 5 + i] * r[k];
+            g[i] = a / (d[i] * d[i]);
+        }
+        double Jg2 = 0.0, wg = 0.0;
+        for (int k = 0; k < 5; ++k) {
+            double a = 0.0;
+            for (int i = 0; i < 5; ++i) a += J[k * 5 + i] * g[i];
+            Jg2 += a * a;
+        }
+        for (int i = 0; i < 5; ++i) wg += (d[i] * g[i]) * (d[i] * g[i]);
+        wg = sqrt(wg);
+        for (int i = 0; i < 5; ++i) pc[i] = -(wg * wg) / Jg2 * g[i];
+        double wpc = 0.0;
+        for (int i = 0; i < 5; ++i) wpc += (d[i] * pc[i]) * (d[i] * pc[i]);
+        wpc = sqrt(wpc);
+        if (wpc >= delta) {
+            for (int i = 0; i < 5; ++i) p[i] = g[i] * (-delta / wg);
+            return;
+        }
+        double pd[5], bq = 0.0, aq = 0.0;
+        for (int i = 0; i < 5; ++i) {
+            pd[i] = pi[i] - pc[i];
+            bq += (d[i] * pc[i]) * (d[i] * pd[i]);
+            aq += (d[i] * pd[i]) * (d[i] * pd[i]);
+        }
+        bq *= 2.0;
+        const double tau = (-bq + sqrt(bq * bq - 4.0 * aq * (wpc * wpc - delta * delta))) / (2.0 * aq);
+        for (int i = 0; i < 5; ++i) p[i] = pc[i] + tau * pd[i];
+    }
+
+    // ---- mixed precision ---------------------------------------------------------------
+    // Newton passes with the FP32 Kahan-compensated integrand (the 5x5 solve and the update
+    // stay FP64), then FP64 refinement steps x <- x - J32^{-1} F64(x) until the FP64 residual
+    // ||grad_x Omega||_inf is below ftol; Omega and the thermo output come from FP64 passes.
+    static constexpr double kFtol32 = 1e-7;   // FP32 residual that ends the FP32 phase
+    static constexpr double kStall32 = 1e-6;  // ... or a relative step this small ...
+    static constexpr double kLoose32 = 1e-3;  // ... with the FP32 residual below this
+    static constexpr int kMaxRefine = 6;
+
+    __device__ __noinline__ void eval_newton32(const PointIn &pt, const double *x, double *F, double *J) {
+        double M[3];
+        masses(P, x, M);
+        PassSums S;
+        node_pass<float, true, true, true, false, G>(nv, pt, x, M, gl, mask, S, cnt.v[kStatEvals32]);
+        Eval ev;
+        assemble<true, true, false>(P, pt, x, M, S, ev);
+        for (int i = 0; i < 5; ++i) F[i] = ev.F[i];
+        for (int i = 0; i < 25; ++i) J[i] = ev.J[i];
+        cnt.v[kStatPasses32] += 1;
+    }
+
+    __device__ __noinline__ void eval_grad64(const PointIn &pt, const double *x, double *F) {
+        double M[3];
+        masses(P, x, M);
+        PassSums S;
+        node_pass<double, false, true, false, false, G>(nv, pt, x, M, gl, mask, S, cnt.v[kStatEvalsGrad64]);
+        Eval ev;
+        assemble<true, false, false>(P, pt, x, M, S, ev);
+        for (int i = 0; i < 5; ++i) F[i] = ev.F[i];
+        cnt.v[kStatPasses64] += 1;
+    }
+
+    __device__ __noinline__ void eval_grad_thermo64(const PointIn &pt, const SolveOpts &o, Candidate &c, double *F) {
+        double M[3];
+        masses(P, c.x, M);
+        PassSums S;
+        node_pass<double, false, true, false, true, G>(nv, pt, c.x, M, gl, mask, S, cnt.v[kStatEvalsGradThermo64]);
+        Eval ev;
+        assemble<true, false, true>(P, pt, c.x, M, S, ev);
+        for (int i = 0; i < 5; ++i) F[i] = ev.F[i];
+        cnt.v[kStatPasses64] += 1;
+        postprocess(P, pt, o, ev, c);
+    }
+
+    // 1: reached the FP32 floor, 0: did not converge, -1: residual at x0 not finite
+    __device__ int newton32(const PointIn &pt, const double *x0, const SolveOpts &o, double *x, double *J, int &iters) {
+        double F[5], p[5];
+        for (int i = 0; i < 5; ++i) x[i] = x0[i];
+        eval_newton32(pt, x, F, J);
+        iters = 0;
+        if (!all_finite5(F)) return -1;
+        for (;;) {
+            if (norm_inf5(F) < kFtol32) return 1;
+            if (iters >= o.max_iter) return 0;
+            if (lu_solve5(J, F, p)) {
+                for (int i = 0; i < 5; ++i) p[i] = -p[i];
+            } else {
+                levenberg_step(J, F, p);
+            }
+            const double pn = norm_inf5(p), xn = norm_inf5(x);
+            for (int i = 0; i < 5; ++i) x[i] += p[i];
+            ++iters;
+            eval_newton32(pt, x, F, J);
+            if (any_nan5(x) || any_nan5(F)) return 0;
+            if (pn <= kStall32 * (1.0 + xn) && norm_inf5(F) < kLoose32) return 1;
+        }
+    }
+
+    // NLsolve-style dogleg trust region on FP32 passes; same return codes as newton32
+    __device__ int tr32(const PointIn &pt, const double *x0, const SolveOpts &o, double *x, double *Jacc, int &iters) {
+        double d[5], p[5], r[5], F[5], J[25];
+        for (int i = 0; i < 5; ++i) x[i] = x0[i];
+        eval_newton32(pt, x, r, Jacc);
+        iters = 0;
+        if (!all_finite5(r)) return -1;
+        if (norm_inf5(r) < kFtol32) return 1;
+        for (int j = 0; j < 5; ++j) {
+            double s = 0.0;
+            for (int i = 0; i < 5; ++i) s += Jacc[i * 5 + j] * Jacc[i * 5 + j];
+            d[j] = sqrt(s);
+            if (d[j] == 0.0) d[j] = 1.0;
+        }
+        double delta = 0.0;
+        for (int i = 0; i < 5; ++i) delta += (d[i] * x[i]) * (d[i] * x[i]);
+        delta = sqrt(delta);
+        if (delta == 0.0) delta = 1.0;
+        while (iters < o.max_iter) {
+            ++iters;
+            dogleg(p, r, d, Jacc, delta);
+            for (int i = 0; i < 5; ++i) x[i] += p[i];
+            eval_newton32(pt, x, F, J);
+            double sr = 0.0, sf = 0.0, sp = 0.0;
+            for (int k = 0; k < 5; ++k) {
+                double a = 0.0;
+                for (int i = 0; i < 5; ++i) a += Jacc[k * 5 + i] * p[i];
+                const double rp = a + r[k];
+                sr += r[k] * r[k];
+                sf += F[k] * F[k];
+                sp += rp * rp;
+            }
+            const double rho = (sr - sf) / (sr - sp);
+            double wp = 0.0;
+            for (int i = 0; i < 5; ++i) wp += (d[i] * p[i]) * (d[i] * p[i]);
+            wp = sqrt(wp);
+            if (rho > 1e-4) {
+                for (int i = 0; i < 5; ++i) r[i] = F[i];
+                for (int i = 0; i < 25; ++i) Jacc[i] = J[i];
+                for (int j = 0; j < 5; ++j) {
+                    double s = 0.0;
+                    for (int i = 0; i < 5; ++i) s += Jacc[i * 5 + j] * Jacc[i * 5 + j];
+                    const double cn = sqrt(s);
+                    d[j] = (0.1 * d[j] > cn) ? 0.1 * d[j] : cn;
+                }
+                const double fn = norm_inf5(r);
+                if (fn < kFtol32) return 1;
+                if (norm_inf5(p) <= kStall32 * (1.0 + norm_inf5(x)) && fn < kLoose32) return 1;
+            } else {
+                for (int i = 0; i < 5; ++i) x[i] -= p[i];
+            }
+            if (rho < 0.1) delta = delta / 2.0;
+            else if (rho >= 0.9) delta = 2.0 * wp;
+            else if (rho >= 0.5) delta = fmax(delta, 2.0 * wp);
+            if (any_nan5(x) || any_nan5(F)) return 0;
+        }
+        return 0;
+    }
+
+    // FP64 refinement + certification of an FP32 solution; fills c.  A certified candidate
+    // gets its thermo from an FP64 pass at its final x; an uncertified one is reported with
+    // f_converged = false and no thermo.
+    __device__ void refine64(const PointIn &pt, const SolveOpts &o, const double *J32, const double *x32, Candidate &c,
+                             int &steps) {
+        double F[5], p[5];
+        for (int i = 0; i < 5; ++i) c.x[i] = x32[i];
+        c.exception = false;
+        c.phys = false;
+        c.omega = c.entropy = qnan();
+        eval_grad64(pt, c.x, F);
+        steps = 0;
+        bool thermo_at_x = false;
+        for (;;) {
+            const double fn = norm_inf5(F);
+            c.residual_norm = fn;
+            if (!(fn == fn) || any_nan5(c.x)) { c.f_converged = false; break; }
+            if (fn < o.ftol) { c.f_converged = true; break; }
+            if (steps >= kMaxRefine) { c.f_converged = false; break; }
+            if (lu_solve5(J32, F, p)) {
+                for (int i = 0; i < 5; ++i) p[i] = -p[i];
+            } else {
+                levenberg_step(J32, F, p);
+            }
+            for (int i = 0; i < 5; ++i) c.x[i] += p[i];
+            ++steps;
+            eval_grad_thermo64(pt, o, c, F);
+            thermo_at_x = true;
+        }
+        if (c.f_converged && !thermo_at_x) eval_thermo(pt, o, c);
+        if (!c.f_converged) c.phys = false;
+    }
+
+    // Mixed-precision counterpart of solve_seed.  `dup` is set when the FP32 solution equals
+    // one in seen[0..n_seen) (the same FP64 root, which a later seed cannot replace under the
+    // min-Omega tie rule); then no FP64 work is spent on it.
+    __device__ void mixed_solve_seed(const PointIn &pt, const double *x0, const SolveOpts &o, Candidate &out,
+                                     bool &converged, double *seen, int &n_seen, bool &dup) {
+        cnt.v[kStatSeeds] += 1;
+        dup = false;
+        double x32[5], J32[25];
+        int it32 = 0;
+        const int r = newton32(pt, x0, o, x32, J32, it32);
+        if (r < 0) {  // decide a non-finite FP32 residual at the seed with the FP64 path
+            cnt.v[kStatSeeds] -= 1;
+            solve_seed(pt, x0, o, out, converged);
+            return;
+        }
+        out.exception = false;
+        if (r > 0) {
+            if (is_seen(x32, seen, n_seen)) { dup = true; converged = false; return; }
+            remember(x32, seen, n_seen);
+            int st = 0;
+            refine64(pt, o, J32, x32, out, st);
+            out.iterations = it32 + st;
+        } else {
+            for (int i = 0; i < 5; ++i) out.x[i] = x32[i];
+            out.f_converged = false;
+            out.phys = false;
+            out.residual_norm = out.omega = out.entropy = qnan();
+            for (int k = 0; k < 3; ++k) out.rho[k] = out.nq[k] = out.naq[k] = qnan();
+            out.iterations = it32;
+        }
+        if (!cand_good(out, o.residual_norm_max) && o.trust_region_fallback) {
+            cnt.v[kStatTrRuns] += 1;
+            double y32[5], K32[25];
+            int itt = 0;
+            if (tr32(pt, x0, o, y32, K32, itt) > 0 && !is_seen(y32, seen, n_seen)) {
+                remember(y32, seen, n_seen);
+                Candidate f;
+                int st = 0;
+                refine64(pt, o, K32, y32, f, st);
+                f.iterations = itt + st;
+                if (choose_fallback(out, f, o.residual_norm_max)) out = f;
+            }
+        }
+        converged = cand_good(out, o.residual_norm_max);
+    }
+
+    static constexpr int kMaxSeen = 34;
+    __device__ static bool is_seen(const double *x, const double *seen, int n_seen) {
+        for (int k = 0; k < n_seen; ++k) {
+            bool same = true;
+            for (int i = 0; i < 5; ++i) same = same && fabs(x[i] - seen[5 * k + i]) <= 1e-6 * (1.0 + fabs(x[i]));
+            if (same) return true;
+        }
+        return false;
+    }
+    __device__ static void remember(const double *x, double *seen, int &n_seen) {
+        if (n_seen >= kMaxSeen) return;
+        for (int i = 0; i < 5; ++i) seen[5 * n_seen + i] = x[i];
+        ++n_seen;
+    }
+
+    // solve(::FixedMu) single-seed path without the MultiSeed fallback (ImplicitSolver.jl:261-304)
+    __device__ void solve_seed(const PointIn &pt, const double *x0, const SolveOpts &o, Candidate &out, bool &converged) {
+        cnt.v[kStatSeeds] += 1;
+        newton(pt, x0, o, out);
+        converged = false;
+        if (out.exception) return;
+        const bool need = o.trust_region_fallback &&
+                          (!out.f_converged || !isfinite(out.residual_norm) || out.residual_norm > o.residual_norm_max ||
+                           !out.phys);
+        if (need) {
+            Candidate f;
+            trust_region(pt, x0, o, f);
+            if (!f.exception && choose_fallback(out, f, o.residual_norm_max)) out = f;
+        }
+        converged = cand_good(out, o.residual_norm_max);
+    }
+};
+
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ bool valid_point(const PointIn &pt) {
+    return isfinite(pt.T) && pt.T > 0.0 && isfinite(pt.mu[0]) && isfinite(pt.mu[1]) && isfinite(pt.mu[2]) &&
+           isfinite(pt.xi) && pt.xi > -1.0;
+}
+
+__device__ __forceinline__ void load_point(const SolveArgs &a, int64_t i, PointIn &pt) {
+    pt.T = a.T[i];
+    pt.mu[0] = a.mu_u[i];
+    pt.mu[1] = a.mu_d[i];
+    pt.mu[2] = a.mu_s[i];
+    pt.xi = a.xi[i];
+}
+
+__device__ __forceinline__ void nan_candidate(Candidate &c, const double *x) {
+    for (int k = 0; k < 5; ++k) c.x[k] = x ? x[k] : qnan();
+    c.residual_norm = c.omega = c.entropy = qnan();
+    for (int k = 0; k < 3; ++k) c.rho[k] = c.nq[k] = c.naq[k] = qnan();
+    c.iterations = 0;
+    c.f_converged = c.phys = false;
+    c.exception = false;
+}
+
+__device__ inline void write_point(const DevParams &P, const PointIn &pt, const pnjl_result_soa &o, int64_t i,
+                            const Candidate &c, bool converged, int chosen, int status) {
+    double M[3];
+    masses(P, c.x, M);
+    const double pressure = -c.omega;
+    const double rho_norm = (c.rho[0] + c.rho[1] + c.rho[2]) / (3.0 * P.rho0);
+    const double energy = -pressure + (pt.mu[0] * c.rho[0] + pt.mu[1] * c.rho[1] + pt.mu[2] * c.rho[2]) + pt.T * c.entropy;
+    if (o.x) for (int k = 0; k < 5; ++k) o.x[5 * i + k] = c.x[k];
+    if (o.omega) o.omega[i] = c.omega;
+    if (o.pressure) o.pressure[i] = pressure;
+    if (o.rho_norm) o.rho_norm[i] = rho_norm;
+    if (o.entropy) o.entropy[i] = c.entropy;
+    if (o.energy) o.energy[i] = energy;
+    if (o.masses) for (int k = 0; k < 3; ++k) o.masses[3 * i + k] = M[k];
+    if (o.rho) for (int k = 0; k < 3; ++k) o.rho[3 * i + k] = c.rho[k];
+    if (o.n_q) for (int k = 0; k < 3; ++k) o.n_q[3 * i + k] = c.nq[k];
+    if (o.n_aq) for (int k = 0; k < 3; ++k) o.n_aq[3 * i + k] = c.naq[k];
+    if (o.residual_norm) o.residual_norm[i] = c.residual_norm;
+    if (o.iterations) o.iterations[i] = c.iterations;
+    if (o.chosen_seed) o.chosen_seed[i] = chosen;
+    if (o.status) o.status[i] = status;
+    if (o.converged) o.converged[i] = converged ? 1 : 0;
+}
+
+// Candidate record in the scratch buffer (one slot per (point, seed) task).
+__device__ __forceinline__ void store_record(CandRec *r, const Candidate &c, bool converged) {
+    for (int k = 0; k < 5; ++k) r->x[k] = c.x[k];
+    r->residual_norm = c.residual_norm;
+    r->omega = c.omega;
+    r->entropy = c.entropy;
+    for (int k = 0; k < 3; ++k) { r->rho[k] = c.rho[k]; r->nq[k] = c.nq[k]; r->naq[k] = c.naq[k]; }
+    r->iterations = c.iterations;
+    r->flags = (c.f_converged ? 1 : 0) | (c.phys ? 2 : 0) | (c.exception ? 4 : 0) | (converged ? 8 : 0);
+}
+
+__device__ __forceinline__ void load_record(const CandRec *r, Candidate &c, bool &converged) {
+    for (int k = 0; k < 5; ++k) c.x[k] = __ldcg(&r->x[k]);
+    c.residual_norm = __ldcg(&r->residual_norm);
+    c.omega = __ldcg(&r->omega);
+    c.entropy = __ldcg(&r->entropy);
+    for (int k = 0; k < 3; ++k) { c.rho[k] = __ldcg(&r->rho[k]); c.nq[k] = __ldcg(&r->nq[k]); c.naq[k] = __ldcg(&r->naq[k]); }
+    c.iterations = __ldcg(&r->iterations);
+    const int fl = __ldcg(&r->flags);
+    c.f_converged = fl & 1;
+    c.phys = (fl & 2) != 0;
+    c.exception = (fl & 4) != 0;
+    converged = (fl & 8) != 0;
+}
+
+__device__ __forceinline__ const double *table_row(const SolveArgs &a, const PointIn &pt, int s) {
+    const bool hot = pt.T * a.P.hbarc >= a.hot_T_MeV;
+    return (hot && a.seed_table_hot) ? a.seed_table_hot + 5 * s : a.seed_table + 5 * s;
+}
+
+// Streaming min-Omega rule over seeds in order: a later converged candidate replaces the
+// kept one only when its Omega is lower by more than omega_tie_rtol*|Omega| (rtol = 0 is
+// the reference's argmin, first minimum kept, SeedStrategies.jl:236-240).
+__device__ __forceinline__ bool better(const Candidate &c, const Candidate &best, bool have, double rtol) {
+    return !have || c.omega < best.omega - rtol * fabs(best.omega);
+}
+
+// MultiSeed over the table inside one group (used by the per-point fallback).
+template <int G>
+__device__ bool solve_table_inline(Group<G> &grp, const PointIn &pt, const SolveArgs &a, Candidate &best, int &chosen) {
+    bool have = false;
+    for (int s = 0; s < a.n_seeds; ++s) {
+        const double *row = table_row(a, pt, s);
+        double x0[5];
+        for (int k = 0; k < 5; ++k) x0[k] = row[k];
+        Candidate c;
+        bool conv;
+        grp.solve_seed(pt, x0, a.opts, c, conv);
+        if (c.exception || !conv) continue;
+        if (better(c, best, have, a.opts.omega_tie_rtol)) { best = c; chosen = s; have = true; }
+    }
+    return have;
+}
+
+}  // namespace pnjl

@@ -30,7 +30,7 @@ struct CandRec {
 // Counter slots of SolveArgs::stats
 enum StatSlot {
     kStatPasses64 = 0, kStatEvalsNewton64, kStatEvalsThermo64, kStatSeeds, kStatTrRuns, kStatMsFallbacks,
-    kStatPasses32, kStatEvals32, kStatCount
+    kStatPasses32, kStatEvals32, kStatEvalsGrad64, kStatEvalsGradThermo64, kStatCount
 };
 
 struct SolveArgs {
@@ -62,6 +62,8 @@ struct EvalArgs {
 
 size_t node_smem_bytes(int p_num, int t_num);
 cudaError_t launch_solve(const SolveArgs &a, int group, int grid, size_t smem, cudaStream_t s);
+cudaError_t launch_solve_mixed(const SolveArgs &a, int grid, size_t smem, cudaStream_t s);
+int solve_mixed_occupancy(size_t smem);
 cudaError_t launch_eval(const EvalArgs &a, bool fp32, int grid, size_t smem, cudaStream_t s);
 int solve_kernel_occupancy(int group, size_t smem);
 

@@ -225,3 +225,57 @@ def test_solve_api_mirrors_reference(engine_factory):
         rr = pnjl.solve(pnjl.FixedMu(), T_MeV / HBARC, muB / 3 / HBARC, xi=xi, p_num=12, t_num=4, engine=eng)
         assert rr.converged
         assert -1e-8 <= rr.x_state[3] <= 1 + 1e-8 and np.all(rr.masses > 0)
+
+
+@pytest.mark.parametrize("p_num,t_num,asym", [(64, 8, False), (32, 8, True)])
+def test_mixed_precision_matches_fp64_oracle(engine_factory, P, p_num, t_num, asym):
+    """PNJL_PREC_MIXED: FP32 Kahan-compensated Newton passes, FP64 refinement and certification.
+    The certified roots and the selected phase must match the FP64 oracle (spec bound
+    |dphi|/|phi| <= 1e-9, |dPhi| <= 1e-10; Omega 1e-12 relative); iteration counts differ by
+    construction and are not compared."""
+    eng = engine_factory(p_num, t_num)
+    nd = orc.Nodes(p_num, t_num)
+    rng = np.random.default_rng(23 + p_num)
+    n = 40
+    T = rng.uniform(40, 320, n) / HBARC
+    mu1 = rng.uniform(0, 420, n) / HBARC
+    mu = np.stack([mu1, mu1, (0.5 if asym else 1.0) * mu1], axis=1)
+    xi = rng.uniform(-0.5, 0.5, n) if asym else np.zeros(n)
+    ns = 4 if asym else 6
+    table, hot = pnjl.multiseed_table(ns)
+    ftol = 1e-11
+    res = eng.solve(T, mu, xi, seed_table=table, seed_table_hot=hot,
+                    opts=SolveOptions(iterations=40, ftol=ftol, precision="mixed"))
+    refs = orc.solve_batch(P, nd, T, mu, xi, multi=True, n_seeds=ns, opts=orc.default_opts(max_iter=40, ftol=ftol))
+    st = eng.stats()
+    assert st["passes_fp32"] > 0 and st["node_evals_fp32"] > 0
+    for i in range(n):
+        ref = orc.result_to_dict(refs[i])
+        assert bool(res["converged"][i]) == ref["converged"], (i, res["status"][i], ref["status"])
+        if not ref["converged"]:
+            continue
+        assert res["residual_norm"][i] < ftol
+        x, xr = res["x"][i], ref["x"]
+        assert np.all(np.abs(x[:3] - xr[:3]) <= 1e-9 * np.abs(xr[:3]) + 1e-12), (i, x, xr)
+        assert np.all(np.abs(x[3:] - xr[3:]) <= 1e-10), (i, x, xr)
+        assert abs(res["omega"][i] - ref["omega"]) <= 1e-12 * abs(ref["omega"]), i
+        np.testing.assert_allclose(res["n_q"][i], ref["nq"], rtol=1e-9, atol=1e-12)
+
+
+def test_mixed_per_point_seed_and_fallback(engine_factory, P):
+    eng = engine_factory(24, 6)
+    nd = orc.Nodes(24, 6)
+    T = np.array([60.0, 100.0, 180.0, 250.0, 320.0]) / HBARC
+    mu = np.array([340.0, 0.0, 200.0, 100.0, 10.0]) / HBARC
+    seeds = np.array([pnjl.HADRON_SEED_5, pnjl.HIGH_DENSITY_SEED_5, (-3.0, -3.0, -3.0, 2.5, -1.0),
+                      pnjl.QUARK_SEED_5, (-2.5, -0.1, -0.2, 0.9, 0.1)])
+    table, hot = pnjl.multiseed_table()
+    res = eng.solve(T, mu, 0.0, seed_table=table, seed_table_hot=hot, point_seeds=seeds,
+                    opts=SolveOptions(iterations=40, ftol=1e-11, precision="mixed"))
+    for i in range(T.size):
+        ref = orc.solve_point(P, nd, T[i], [mu[i]] * 3, 0.0, seeds[i], False,
+                              orc.default_opts(max_iter=40, ftol=1e-11))
+        assert bool(res["converged"][i]) == ref["converged"], i
+        if ref["converged"]:
+            assert abs(res["omega"][i] - ref["omega"]) <= 1e-12 * abs(ref["omega"]), i
+            assert np.all(np.abs(res["x"][i][3:] - ref["x"][3:]) <= 1e-10), i
