@@ -192,7 +192,8 @@ int pnjl_set_tuning(pnjl_ctx *ctx, int32_t lanes_per_point, int32_t blocks_per_s
 
 /* Measured pipe throughput of the context's device, the denominators of the kernels'
  * rooflines (no counterpart in the reference, which has no GPU): kind 0 = FP64 FMA
- * (FLOP/s, FMA = 2), 1 = FP32 FMA (FLOP/s), 2 = SFU ex2.approx.f32 (operations/s). */
+ * (FLOP/s, FMA = 2), 1 = FP32 FMA (FLOP/s), 2 = SFU ex2.approx.f32 (operations/s), 3 = FP64 FMA
+ * issued by one lane per warp (FLOP/s of the active lanes). */
 int pnjl_probe_peak(pnjl_ctx *ctx, int32_t kind, double *ops_per_s);
 
 /* Largest batch of pnjl_solve_batch_noalloc, counted in tasks: n * n_seeds in

@@ -42,6 +42,8 @@ struct Group {
     unsigned mask;
     Counters &cnt;
 
+    __device__ __forceinline__ int leader() const { return (int)(threadIdx.x & 31) & ~(G - 1); }
+
     // residual and Jacobian at x (one Newton pass)
     __device__ __noinline__ void eval_newton(const PointIn &pt, const double *x, double *F, double *J) {
         double M[3];
@@ -49,7 +51,9 @@ struct Group {
         PassSums S;
         node_pass<double, false, true, true, false, G>(nv, pt, x, M, gl, mask, S, cnt.v[kStatEvalsNewton64]);
         Eval ev;
-        assemble<true, true, false>(P, pt, x, M, S, ev);
+        double V, V1[3], V2[3];
+        vacuum_terms<G>(P, M, gl, mask, leader(), V, V1, V2);
+        assemble<true, true, false>(P, pt, x, M, S, V, V1, V2, ev);
         for (int i = 0; i < 5; ++i) F[i] = ev.F[i];
         for (int i = 0; i < 25; ++i) J[i] = ev.J[i];
         cnt.v[kStatPasses64] += 1;
@@ -62,7 +66,9 @@ struct Group {
         PassSums S;
         node_pass<double, false, false, false, true, G>(nv, pt, c.x, M, gl, mask, S, cnt.v[kStatEvalsThermo64]);
         Eval ev;
-        assemble<false, false, true>(P, pt, c.x, M, S, ev);
+        double V, V1[3], V2[3];
+        vacuum_terms<G>(P, M, gl, mask, leader(), V, V1, V2);
+        assemble<false, false, true>(P, pt, c.x, M, S, V, V1, V2, ev);
         cnt.v[kStatPasses64] += 1;
         postprocess(P, pt, o, ev, c);
     }
@@ -294,7 +300,9 @@ struct Group {
         PassSums S;
         node_pass<float, true, true, true, false, G>(nv, pt, x, M, gl, mask, S, cnt.v[kStatEvals32]);
         Eval ev;
-        assemble<true, true, false>(P, pt, x, M, S, ev);
+        double V, V1[3], V2[3];
+        vacuum_terms<G>(P, M, gl, mask, leader(), V, V1, V2);
+        assemble<true, true, false, true>(P, pt, x, M, S, V, V1, V2, ev);
         for (int i = 0; i < 5; ++i) F[i] = ev.F[i];
         for (int i = 0; i < 25; ++i) J[i] = ev.J[i];
         cnt.v[kStatPasses32] += 1;
@@ -306,7 +314,9 @@ struct Group {
         PassSums S;
         node_pass<double, false, true, false, false, G>(nv, pt, x, M, gl, mask, S, cnt.v[kStatEvalsGrad64]);
         Eval ev;
-        assemble<true, false, false>(P, pt, x, M, S, ev);
+        double V, V1[3], V2[3];
+        vacuum_terms<G>(P, M, gl, mask, leader(), V, V1, V2);
+        assemble<true, false, false>(P, pt, x, M, S, V, V1, V2, ev);
         for (int i = 0; i < 5; ++i) F[i] = ev.F[i];
         cnt.v[kStatPasses64] += 1;
     }
@@ -317,7 +327,9 @@ struct Group {
         PassSums S;
         node_pass<double, false, true, false, true, G>(nv, pt, c.x, M, gl, mask, S, cnt.v[kStatEvalsGradThermo64]);
         Eval ev;
-        assemble<true, false, true>(P, pt, c.x, M, S, ev);
+        double V, V1[3], V2[3];
+        vacuum_terms<G>(P, M, gl, mask, leader(), V, V1, V2);
+        assemble<true, false, true>(P, pt, c.x, M, S, V, V1, V2, ev);
         for (int i = 0; i < 5; ++i) F[i] = ev.F[i];
         cnt.v[kStatPasses64] += 1;
         postprocess(P, pt, o, ev, c);
@@ -411,7 +423,9 @@ struct Group {
     // f_converged = false and no thermo.
     __device__ void refine64(const PointIn &pt, const SolveOpts &o, const double *J32, const double *x32, Candidate &c,
                              int &steps) {
-        double F[5], p[5];
+        double F[5], p[5], LU[25];
+        int piv[5];
+        const bool factored = lu_factor5(J32, LU, piv);
         for (int i = 0; i < 5; ++i) c.x[i] = x32[i];
         c.exception = false;
         c.phys = false;
@@ -425,7 +439,8 @@ struct Group {
             if (!(fn == fn) || any_nan5(c.x)) { c.f_converged = false; break; }
             if (fn < o.ftol) { c.f_converged = true; break; }
             if (steps >= kMaxRefine) { c.f_converged = false; break; }
-            if (lu_solve5(J32, F, p)) {
+            if (factored) {
+                lu_solve_factored5(LU, piv, F, p);
                 for (int i = 0; i < 5; ++i) p[i] = -p[i];
             } else {
                 levenberg_step(J32, F, p);

@@ -156,7 +156,9 @@ __global__ void __launch_bounds__(kSolveThreads) eval_kernel(EvalArgs a) {
         if (FP32) node_pass<float, true, true, true, true, G>(nv, pt, x, M, gl, mask, S, evals);
         else node_pass<double, false, true, true, true, G>(nv, pt, x, M, gl, mask, S, evals);
         Eval ev;
-        assemble<true, true, true>(a.P, pt, x, M, S, ev);
+        double V, V1[3], V2[3];
+        vacuum_terms<G>(a.P, M, gl, mask, lane & ~(G - 1), V, V1, V2);
+        assemble<true, true, true>(a.P, pt, x, M, S, V, V1, V2, ev);
         if (gl == 0) {
             if (a.omega) a.omega[i] = ev.omega;
             if (a.grad) for (int k = 0; k < 5; ++k) a.grad[5 * i + k] = -ev.F[k];

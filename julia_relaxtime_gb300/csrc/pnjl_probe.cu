@@ -4,6 +4,8 @@
 // full grid (a multiple of the SM count) and reports operations per second from CUDA-event
 // time.  kind 0: FP64 FMA, 1: FP32 FMA, 2: FP32 ex2.approx (the SFU).  The chains are
 // seeded from the thread index and written back so the compiler cannot drop them.
+// kind 3: FP64 FMA chains on lane 0 of every warp only (the other lanes are predicated off),
+// reported per active lane -- whether the FP64 pipe skips inactive lanes.
 #include <cuda_runtime.h>
 
 #include "../../include/pnjl_cuda.h"
@@ -11,7 +13,8 @@
 namespace pnjl {
 
 template <typename R>
-__global__ void __launch_bounds__(256) fma_probe(R *out, int iters, R a, R b) {
+__global__ void __launch_bounds__(256) fma_probe(R *out, int iters, R a, R b, int lanes) {
+    if ((int)(threadIdx.x & 31) >= lanes) return;
     R x[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) x[k] = (R)(threadIdx.x + k) * (R)1e-3;
@@ -46,7 +49,7 @@ __global__ void __launch_bounds__(256) ex2_probe(float *out, int iters) {
 }  // namespace pnjl
 
 extern "C" int pnjl_probe_peak_impl(int device, int kind, double *ops_per_s) {
-    if (!ops_per_s || kind < 0 || kind > 2) return PNJL_ERR_INVALID_ARGUMENT;
+    if (!ops_per_s || kind < 0 || kind > 3) return PNJL_ERR_INVALID_ARGUMENT;
     if (cudaSetDevice(device) != cudaSuccess) return PNJL_ERR_CUDA;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
@@ -56,12 +59,13 @@ extern "C" int pnjl_probe_peak_impl(int device, int kind, double *ops_per_s) {
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    const int iters = kind == 0 ? 2048 : 16384;
+    const int iters = kind == 0 ? 2048 : (kind == 3 ? 8192 : 16384);
     float best = 1e30f;
     for (int rep = 0; rep < 4; ++rep) {
         cudaEventRecord(e0);
-        if (kind == 0) pnjl::fma_probe<double><<<blocks, threads>>>((double *)buf, iters, 0.999999, 1e-7);
-        else if (kind == 1) pnjl::fma_probe<float><<<blocks, threads>>>((float *)buf, iters, 0.9999f, 1e-5f);
+        if (kind == 0) pnjl::fma_probe<double><<<blocks, threads>>>((double *)buf, iters, 0.999999, 1e-7, 32);
+        else if (kind == 1) pnjl::fma_probe<float><<<blocks, threads>>>((float *)buf, iters, 0.9999f, 1e-5f, 32);
+        else if (kind == 3) pnjl::fma_probe<double><<<blocks, threads>>>((double *)buf, iters, 0.999999, 1e-7, 1);
         else pnjl::ex2_probe<<<blocks, threads>>>((float *)buf, iters);
         cudaEventRecord(e1);
         cudaEventSynchronize(e1);
@@ -74,7 +78,8 @@ extern "C" int pnjl_probe_peak_impl(int device, int kind, double *ops_per_s) {
     cudaEventDestroy(e1);
     cudaFree(buf);
     if (err != cudaSuccess) return PNJL_ERR_CUDA;
-    const double ops = (double)blocks * threads * iters * 8.0 * (kind == 2 ? 1.0 : 2.0);
+    const double lanes = kind == 3 ? (double)blocks * threads / 32.0 : (double)blocks * threads;
+    const double ops = lanes * iters * 8.0 * (kind == 2 ? 1.0 : 2.0);
     *ops_per_s = ops / (best * 1e-3);
     return PNJL_OK;
 }

@@ -60,6 +60,61 @@ __device__ __forceinline__ double group_sum(double v, unsigned mask) {
     return v;
 }
 
+// Float-float XOR butterfly: TwoSum gives the exact rounding error of h_a + h_b, which does
+// not depend on the operand order, so every lane again ends with identical bits.
+template <int G>
+__device__ __forceinline__ void group_sum_ff(float &h, float &l, unsigned mask) {
+#pragma unroll
+    for (int m = G >> 1; m > 0; m >>= 1) {
+        const float bh = __shfl_xor_sync(mask, h, m);
+        const float bl = __shfl_xor_sync(mask, l, m);
+        const float sum = __fadd_rn(h, bh);
+        const float hp = __fsub_rn(sum, bh);
+        const float bp = __fsub_rn(sum, hp);
+        const float err = __fadd_rn(__fsub_rn(h, hp), __fsub_rn(bh, bp));
+        l = __fadd_rn(__fadd_rn(l, bl), err);
+        h = sum;
+    }
+}
+
+// Vacuum term -2 Nc sum_f I(|M_f| + 1e-12) and its first two derivatives in M_f
+// (Integrals.jl:123-145), FP64, lane-parallel: lane f of the group computes flavour f and the
+// results are broadcast, so the three evaluations cost one instruction stream.
+template <int G>
+__device__ __forceinline__ void vacuum_terms(const DevParams &P, const double *M, int gl, unsigned mask, int leader,
+                                             double &V, double *V1, double *V2) {
+    const int f = (G >= 4) ? (gl % 3) : 0;
+    const double L = P.Lambda;
+    const double inv4pi2 = 1.0 / (4.0 * M_PI * M_PI);
+    auto one = [&](double m, double &I, double &I1, double &I2) {
+        const double sgn = signbit(m) ? -1.0 : 1.0;
+        const double ms = fabs(m) + 1e-12;
+        const double ms2 = ms * ms;
+        const double Sq = sqrt(L * L + ms2);
+        const double lgv = log((L + Sq) / ms);
+        I = (L * Sq * (2.0 * L * L + ms2) - ms2 * ms2 * lgv) * (0.25 * inv4pi2);
+        I1 = -2.0 * P.Nc * ((L * ms * Sq - ms2 * ms * lgv) * inv4pi2) * sgn;
+        I2 = -2.0 * P.Nc * ((L * Sq + 2.0 * L * ms2 / Sq - 3.0 * ms2 * lgv) * inv4pi2);
+    };
+    if (G >= 4) {
+        const double mf = f == 0 ? M[0] : (f == 1 ? M[1] : M[2]);
+        double I, I1, I2;
+        one(mf, I, I1, I2);
+        double Is[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            Is[k] = __shfl_sync(mask, I, leader + k);
+            V1[k] = __shfl_sync(mask, I1, leader + k);
+            V2[k] = __shfl_sync(mask, I2, leader + k);
+        }
+        V = ((Is[0] + Is[1]) + Is[2]) * (-2.0 * P.Nc);
+    } else {
+        double Is[3];
+        for (int k = 0; k < 3; ++k) one(M[k], Is[k], V1[k], V2[k]);
+        V = ((Is[0] + Is[1]) + Is[2]) * (-2.0 * P.Nc);
+    }
+}
+
 // One pass over the node-flavour mesh at state x; lane `gl` of a group of G lanes takes
 // the flattened nodes k = gl, gl+G, ... (k = ip + p_num*it).  Returns the group-reduced
 // sums (identical in every lane of the group); entries a pass does not compute are 0.
@@ -133,7 +188,17 @@ __device__ void node_pass(const NodeView &nv, const PointIn &pt, const double *x
     for (int i = 0; i < NS; ++i) {
         const bool used = (i < 3 || i == 19 || i == 20) ? GRAD
                           : (i < 12 || (i >= 21 && i <= 23)) ? HESS : THERMO;
-        if (used) acc[i] = group_sum<G>(acc[i], mask);
+        if (!used) continue;
+        if constexpr (sizeof(R) == 4) {
+            // FP32 pass: reduce the compensated sums as float pairs (exact TwoSum on the
+            // high parts), so the lane reduction costs no FP64 instructions
+            float h = (float)acc[i];
+            float l = (float)(acc[i] - (double)h);
+            group_sum_ff<G>(h, l, mask);
+            acc[i] = (double)h + (double)l;
+        } else {
+            acc[i] = group_sum<G>(acc[i], mask);
+        }
     }
     for (int f = 0; f < 3; ++f) {
         S.DM[f] = acc[0 + f]; S.DMM[f] = acc[3 + f]; S.DMP[f] = acc[6 + f]; S.DMPb[f] = acc[9 + f];
@@ -143,10 +208,13 @@ __device__ void node_pass(const NodeView &nv, const PointIn &pt, const double *x
     S.SAN = acc[24];
 }
 
-// FP64 assembly of Omega, grad, Hessian and thermo from the pass sums.
-template <bool GRAD, bool HESS, bool LOG>
+// Assembly of Omega, grad, Hessian and thermo from the pass sums and the vacuum terms.
+// FP64 throughout, except that HESS32 assembles the Jacobian in FP32 arithmetic (the FP32
+// Newton passes of the mixed mode, whose sums carry FP32 accuracy anyway); the 5x5 solve
+// that consumes it stays FP64.
+template <bool GRAD, bool HESS, bool LOG, bool HESS32 = false>
 __device__ void assemble(const DevParams &P, const PointIn &pt, const double *x, const double *M, const PassSums &S,
-                         Eval &ev) {
+                         double V, const double *V1, const double *V2, Eval &ev) {
     const double T = pt.T;
     const double pu = x[0], pd = x[1], ps = x[2], Ph = x[3], Pb = x[4];
     const double G4 = 4.0 * P.G, K2 = 2.0 * P.K, K4 = 4.0 * P.K;
@@ -170,24 +238,6 @@ __device__ void assemble(const DevParams &P, const PointIn &pt, const double *x,
     const double ig = gcl ? 0.0 : 1.0 / g;
     const double UP = T4 * (-0.5 * Ta * Pb + Tb * gP * ig);
     const double UPb = T4 * (-0.5 * Ta * Ph + Tb * gPb * ig);
-    // vacuum term -2 Nc sum_f I(|M_f| + 1e-12) (Integrals.jl:123-145)
-    const double L = P.Lambda;
-    const double inv4pi2 = 1.0 / (4.0 * M_PI * M_PI);
-    double V = 0.0, V1[3], V2[3];
-    for (int f = 0; f < 3; ++f) {
-        const double sgn = signbit(M[f]) ? -1.0 : 1.0;
-        const double ms = fabs(M[f]) + 1e-12;
-        const double ms2 = ms * ms;
-        const double Sq = sqrt(L * L + ms2);
-        const double lgv = log((L + Sq) / ms);
-        const double I = (L * Sq * (2.0 * L * L + ms2) - ms2 * ms2 * lgv) * (0.25 * inv4pi2);
-        const double I1 = (L * ms * Sq - ms2 * ms * lgv) * inv4pi2;
-        const double I2 = (L * Sq + 2.0 * L * ms2 / Sq - 3.0 * ms2 * lgv) * inv4pi2;
-        V += I;
-        V1[f] = -2.0 * P.Nc * I1 * sgn;
-        V2[f] = -2.0 * P.Nc * I2;
-    }
-    V *= -2.0 * P.Nc;
     const double Dsc = -2.0 * T;
     double gO[5];
     for (int a = 0; a < 3; ++a) {
@@ -200,7 +250,7 @@ __device__ void assemble(const DevParams &P, const PointIn &pt, const double *x,
     for (int i = 0; i < 5; ++i) ev.F[i] = -gO[i];
     if (LOG) ev.omega = chi + U + V + Dsc * S.SL;
     else ev.omega = 0.0;
-    if (HESS) {
+    if (HESS && !HESS32) {
         double H[5][5];
         const double chih[3][3] = {{G4, -K4 * ps, -K4 * pd}, {-K4 * ps, G4, -K4 * pu}, {-K4 * pd, -K4 * pu, G4}};
         for (int a = 0; a < 3; ++a)
@@ -234,6 +284,52 @@ __device__ void assemble(const DevParams &P, const PointIn &pt, const double *x,
             for (int b = a; b < 5; ++b) {
                 ev.J[a * 5 + b] = -H[a][b];
                 ev.J[b * 5 + a] = -H[a][b];
+            }
+    }
+    if (HESS && HESS32) {
+        float H[5][5];
+        const float fG4 = (float)G4, fK2 = (float)K2, fK4 = (float)K4, fDsc = (float)Dsc;
+        const float fpu = (float)pu, fpd = (float)pd, fps = (float)ps, fPh = (float)Ph, fPb = (float)Pb;
+        const float Jf[3][3] = {{-fG4, fK2 * fps, fK2 * fpd}, {fK2 * fps, -fG4, fK2 * fpu}, {fK2 * fpd, fK2 * fpu, -fG4}};
+        const float chih[3][3] = {{fG4, -fK4 * fps, -fK4 * fpd}, {-fK4 * fps, fG4, -fK4 * fpu}, {-fK4 * fpd, -fK4 * fpu, fG4}};
+        float W2[3], W1[3];
+        for (int f = 0; f < 3; ++f) {
+            W2[f] = (float)(V2[f] + Dsc * S.DMM[f]);
+            W1[f] = (float)(V1[f] + Dsc * S.DM[f]);
+        }
+        for (int a = 0; a < 3; ++a)
+            for (int b = a; b < 3; ++b) {
+                float s = chih[a][b];
+                for (int f = 0; f < 3; ++f) s += Jf[f][a] * Jf[f][b] * W2[f];
+                H[a][b] = s;
+            }
+        H[0][1] += W1[2] * fK2;
+        H[0][2] += W1[1] * fK2;
+        H[1][2] += W1[0] * fK2;
+        for (int a = 0; a < 3; ++a) {
+            float s3 = 0.f, s4 = 0.f;
+            for (int f = 0; f < 3; ++f) {
+                s3 += Jf[f][a] * (fDsc * (float)S.DMP[f]);
+                s4 += Jf[f][a] * (fDsc * (float)S.DMPb[f]);
+            }
+            H[a][3] = s3;
+            H[a][4] = s4;
+        }
+        const float fT4 = (float)T4, fTb = (float)Tb, fTa = (float)Ta, fig = (float)ig;
+        const float fgP = (float)gP, fgPb = (float)gPb;
+        const float gPP = 24.f * fPh - 6.f * fPb * fPb;
+        const float gPbPb = 24.f * fPb - 6.f * fPh * fPh;
+        const float gPPb = -6.f - 12.f * fPh * fPb;
+        const float UPP = gcl ? 0.f : fT4 * fTb * (gPP * fig - fgP * fgP * fig * fig);
+        const float UPbPb = gcl ? 0.f : fT4 * fTb * (gPbPb * fig - fgPb * fgPb * fig * fig);
+        const float UPPb = fT4 * (-0.5f * fTa + (gcl ? 0.f : fTb * (gPPb * fig - fgP * fgPb * fig * fig)));
+        H[3][3] = UPP + fDsc * (float)S.SPP;
+        H[3][4] = UPPb + fDsc * (float)S.SPPb;
+        H[4][4] = UPbPb + fDsc * (float)S.SPbPb;
+        for (int a = 0; a < 5; ++a)
+            for (int b = a; b < 5; ++b) {
+                ev.J[a * 5 + b] = -(double)H[a][b];
+                ev.J[b * 5 + a] = -(double)H[a][b];
             }
     }
     if (LOG) {
@@ -299,6 +395,64 @@ __device__ __forceinline__ bool lu_solve5(const double *Ain, const double *b, do
 #pragma unroll
     for (int i = 0; i < 5; ++i) x[i] = y[i];
     return true;
+}
+
+// LU factorization with partial pivoting kept for repeated solves (mixed-precision
+// refinement reuses one FP32-assembled Jacobian); false when a pivot is exactly zero.
+__device__ __forceinline__ bool lu_factor5(const double *Ain, double *A, int *piv) {
+#pragma unroll
+    for (int i = 0; i < 25; ++i) A[i] = Ain[i];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        int p = k;
+        double best = fabs(A[k * 5 + k]);
+#pragma unroll
+        for (int i = k + 1; i < 5; ++i) {
+            const double v = fabs(A[i * 5 + k]);
+            if (v > best) { best = v; p = i; }
+        }
+        piv[k] = p;
+        if (A[p * 5 + k] == 0.0) return false;
+        if (p != k) {
+#pragma unroll
+            for (int j = 0; j < 5; ++j) {
+                const double t = A[k * 5 + j];
+                A[k * 5 + j] = A[p * 5 + j];
+                A[p * 5 + j] = t;
+            }
+        }
+        const double inv = 1.0 / A[k * 5 + k];
+#pragma unroll
+        for (int i = k + 1; i < 5; ++i) {
+            const double l = A[i * 5 + k] * inv;
+            A[i * 5 + k] = l;
+#pragma unroll
+            for (int j = k + 1; j < 5; ++j) A[i * 5 + j] -= l * A[k * 5 + j];
+        }
+    }
+    return true;
+}
+
+__device__ __forceinline__ void lu_solve_factored5(const double *A, const int *piv, const double *b, double *x) {
+    double y[5];
+#pragma unroll
+    for (int i = 0; i < 5; ++i) y[i] = b[i];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        const int p = piv[k];
+        if (p != k) { const double t = y[k]; y[k] = y[p]; y[p] = t; }
+#pragma unroll
+        for (int i = k + 1; i < 5; ++i) y[i] -= A[i * 5 + k] * y[k];
+    }
+#pragma unroll
+    for (int i = 4; i >= 0; --i) {
+        double s = y[i];
+#pragma unroll
+        for (int j = i + 1; j < 5; ++j) s -= A[i * 5 + j] * y[j];
+        y[i] = s / A[i * 5 + i];
+    }
+#pragma unroll
+    for (int i = 0; i < 5; ++i) x[i] = y[i];
 }
 
 __device__ __forceinline__ double norm_inf5(const double *v) {

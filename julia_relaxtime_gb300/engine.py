@@ -234,7 +234,7 @@ class GapEngine:
     def probe_peak(self, kind: str) -> float:
         """Measured pipe throughput: "fp64" / "fp32" FLOP/s (FMA = 2) or "sfu" ex2 ops/s."""
         v = C.c_double()
-        k = {"fp64": 0, "fp32": 1, "sfu": 2}[kind]
+        k = {"fp64": 0, "fp32": 1, "sfu": 2, "fp64_one_lane": 3}[kind]
         self._check(self._lib.pnjl_probe_peak(self._ctx, k, C.byref(v)), "pnjl_probe_peak")
         return float(v.value)
 
