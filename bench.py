@@ -252,6 +252,7 @@ def main():
     # timed region: K steps, device inputs already resident per step (loaded before the events)
     sampler = ClockSampler(local_rank)
     kernel_ms, step_ms, solved, evals, flops, flops32 = [], [], 0, 0, 0, 0
+    kinds = {}
     launches0 = eng.stats()["kernel_launches"]
     if dist is not None:
         dist.barrier()
@@ -272,6 +273,10 @@ def main():
         kernel_ms.append(st["last_kernel_ms"])
         evals += st["node_evals_fp64"] + st["node_evals_fp32"]
         f64, f32 = pass_flops(st)
+        for kk in ("node_evals_fp64_newton", "node_evals_fp64_thermo", "node_evals_fp64_grad",
+                   "node_evals_fp64_grad_thermo", "node_evals_fp32", "seeds_run", "trust_region_runs",
+                   "multiseed_fallbacks"):
+            kinds[kk] = kinds.get(kk, 0) + st[kk]
         flops += f64
         flops32 += f32
         conv = d_out["converged"][:n].cpu().numpy().astype(bool)
@@ -327,7 +332,8 @@ def main():
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
             "data": "synthetic", "config": config, "e2e": e2e, "gpu_launches": int(launches),
-            "roofline": roof, "clocks": clocks, "solved": solved}
+            "roofline": roof, "clocks": clocks, "solved": solved,
+            "work_per_step": {k: v / args.steps for k, v in kinds.items()}}
     if not args.no_cpu_baseline:
         class A:  # noqa: N801
             warmup, steps = 0, 1

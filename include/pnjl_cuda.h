@@ -196,6 +196,45 @@ int pnjl_set_tuning(pnjl_ctx *ctx, int32_t lanes_per_point, int32_t blocks_per_s
  * issued by one lane per warp (FLOP/s of the active lanes). */
 int pnjl_probe_peak(pnjl_ctx *ctx, int32_t kind, double *ops_per_s);
 
+/* ---- learned seed: MLP (T, mu, xi) -> (phi_u, phi_d, phi_s, Phi, Phibar) ----------------
+ * 3 -> 128 -> 128 -> 128 -> 5, SiLU, BF16 weights, FP32 accumulation, trained with Adam by
+ * the library's own BF16 tensor-core kernels on solutions the solver produced.  It replaces
+ * the initial guess of get_seed(::SeedStrategy, ...) (src/pnjl/solver/SeedStrategies.jl:118):
+ * the reference has no learned seed, so these entry points have no single reference
+ * counterpart; the multi-seed solve stays their fallback (pnjl_solve_batch_learned*). */
+
+/* Number of FP32 parameters (packed W1[128][3], b1, W2[128][128], b2, W3, b3, W4[5][128], b4). */
+int pnjl_mlp_param_count(void);
+/* (Re)initialise the weights (Kaiming-uniform from `seed`) and clear the optimiser state. */
+int pnjl_mlp_init(pnjl_ctx *ctx, uint64_t seed);
+/* Standardisation: input k = (v_k - in_shift[k]) / in_scale[k] for (T, mu, xi) in fm^-1,
+ * output x_j = y_j * out_scale[j] + out_shift[j]. */
+int pnjl_mlp_set_scaling(pnjl_ctx *ctx, const double *in_shift, const double *in_scale, const double *out_shift,
+                         const double *out_scale);
+/* Train on n labelled points (host arrays; targets [n*5]); Adam with a cosine-decayed learning
+ * rate over epochs x ceil(n/batch) steps, one CUDA graph replay per step; batch is a multiple
+ * of 32; last_loss receives the mean squared standardised error of the final step. */
+int pnjl_mlp_train(pnjl_ctx *ctx, int64_t n, const double *T, const double *mu, const double *xi,
+                   const double *targets, int32_t epochs, int32_t batch, double lr, uint64_t shuffle_seed,
+                   double *last_loss);
+/* Loss and gradient (FP32, packed like the parameters) over n points without an update. */
+int pnjl_mlp_loss_grad(pnjl_ctx *ctx, int64_t n, const double *T, const double *mu, const double *xi,
+                       const double *targets, double *loss, float *grad);
+/* Seeds [n*5] for n points: host arrays (synchronous) or device arrays (asynchronous). */
+int pnjl_mlp_infer(pnjl_ctx *ctx, int64_t n, const double *T, const double *mu, const double *xi, double *seeds);
+int pnjl_mlp_infer_device(pnjl_ctx *ctx, int64_t n, const double *d_T, const double *d_mu, const double *d_xi,
+                          double *d_seeds);
+/* Read or replace the FP32 parameters (count = pnjl_mlp_param_count()). */
+int pnjl_mlp_get_params(pnjl_ctx *ctx, float *out, int64_t count);
+int pnjl_mlp_set_params(pnjl_ctx *ctx, const float *in, int64_t count);
+/* Learned-seed solve on device arrays: the network's seed per point, then
+ * pnjl_solve_batch_device in PNJL_SEEDS_PER_POINT mode with opts' MultiSeed table as the
+ * fallback when the learned seed does not give a converged physical solution
+ * (solve(FixedMu) with auto_multiseed_fallback, ImplicitSolver.jl:306-327). */
+int pnjl_solve_batch_learned_device(pnjl_ctx *ctx, int64_t n, const double *d_T, const double *d_mu_u,
+                                    const double *d_mu_d, const double *d_mu_s, const double *d_xi,
+                                    const pnjl_solve_opts *opts, pnjl_result_soa *d_out);
+
 /* Largest batch of pnjl_solve_batch_noalloc, counted in tasks: n * n_seeds in
  * PNJL_SEEDS_TABLE mode, n in PNJL_SEEDS_PER_POINT mode (and n itself at most this). */
 #define PNJL_NOALLOC_MAX_TASKS 32768

@@ -107,6 +107,18 @@ SIGNATURES = {
     "pnjl_device_sm_count": (C.c_int, [C.c_void_p]),
     "pnjl_set_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "pnjl_probe_peak": (C.c_int, [C.c_void_p, C.c_int32, dp]),
+    "pnjl_mlp_param_count": (C.c_int, []),
+    "pnjl_mlp_init": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "pnjl_mlp_set_scaling": (C.c_int, [C.c_void_p, dp, dp, dp, dp]),
+    "pnjl_mlp_train": (C.c_int, [C.c_void_p, C.c_int64, dp, dp, dp, dp, C.c_int32, C.c_int32, C.c_double,
+                                 C.c_uint64, dp]),
+    "pnjl_mlp_loss_grad": (C.c_int, [C.c_void_p, C.c_int64, dp, dp, dp, dp, dp, C.POINTER(C.c_float)]),
+    "pnjl_mlp_infer": (C.c_int, [C.c_void_p, C.c_int64, dp, dp, dp, dp]),
+    "pnjl_mlp_infer_device": (C.c_int, [C.c_void_p, C.c_int64, dp, dp, dp, dp]),
+    "pnjl_mlp_get_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int64]),
+    "pnjl_mlp_set_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int64]),
+    "pnjl_solve_batch_learned_device": (C.c_int, [C.c_void_p, C.c_int64, dp, dp, dp, dp, dp,
+                                                  C.POINTER(pnjl_solve_opts), C.POINTER(pnjl_result_soa)]),
     "pnjl_solve_batch_noalloc": (C.c_int, [C.POINTER(pnjl_params), C.c_int32, C.c_int32, C.c_double, C.c_int64,
                                            dp, dp, dp, dp, dp, C.POINTER(pnjl_solve_opts),
                                            C.POINTER(pnjl_result_soa), C.c_void_p]),

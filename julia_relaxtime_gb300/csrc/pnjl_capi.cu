@@ -4,6 +4,7 @@
 // FP32 copy), a growable device workspace for the host-pointer entry points, the work-queue
 // head and the counters.  Every entry point returns a PNJL_* code and records a message
 // for pnjl_last_error(); no C++ exception crosses the boundary.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -13,6 +14,7 @@
 
 #include "pnjl_host_common.h"
 #include "pnjl_kernels.h"
+#include "pnjl_mlp.h"
 
 struct pnjl_ctx {
     int device = 0;
@@ -41,6 +43,20 @@ struct pnjl_ctx {
     int blocks_per_sm = 0;  // 0 = occupancy maximum
     pnjl_stats stats{};
     std::string err;
+    // learned seed
+    struct Mlp {
+        bool ready = false, scaled = false, trained = false;
+        float *params = nullptr;  // master | grad | adam m | adam v  (4 x kParamCount)
+        __nv_bfloat16 *wb = nullptr;
+        long long *step = nullptr;
+        float *loss = nullptr;
+        float *x = nullptr, *y = nullptr;
+        long long *perm = nullptr;
+        size_t cap = 0;
+        double *seeds = nullptr;  // per-point seeds of pnjl_solve_batch_learned*
+        size_t seeds_cap = 0;
+        pnjl::Scaling sc{};
+    } mlp;
 };
 
 namespace {
@@ -146,6 +162,51 @@ int grid_for(pnjl_ctx *ctx, int group, size_t smem, int64_t n) {
     return (int)g;
 }
 
+
+pnjl::MlpDev mlp_dev(pnjl_ctx *ctx) {
+    pnjl::MlpDev m;
+    m.master = ctx->mlp.params;
+    m.grad = ctx->mlp.params + pnjl::kParamCount;
+    m.adam_m = ctx->mlp.params + 2 * pnjl::kParamCount;
+    m.adam_v = ctx->mlp.params + 3 * pnjl::kParamCount;
+    const int H = pnjl::mlp::H, IN = pnjl::mlp::IN, OUT = pnjl::mlp::OUT;
+    m.w1b = ctx->mlp.wb;
+    m.w2b = ctx->mlp.wb + H * IN;
+    m.w3b = m.w2b + H * H;
+    m.w4b = m.w3b + H * H;
+    return m;
+}
+
+int mlp_require(pnjl_ctx *ctx, bool need_scaling) {
+    if (!ctx->mlp.ready) return fail(ctx, PNJL_ERR_NOT_TRAINED, "call pnjl_mlp_init first");
+    if (need_scaling && !ctx->mlp.scaled) return fail(ctx, PNJL_ERR_NOT_TRAINED, "call pnjl_mlp_set_scaling first");
+    return PNJL_OK;
+}
+
+int mlp_ensure_data(pnjl_ctx *ctx, size_t n) {
+    if (n <= ctx->mlp.cap) return PNJL_OK;
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(ctx->mlp.x);
+    cudaFree(ctx->mlp.y);
+    cudaFree(ctx->mlp.perm);
+    ctx->mlp.x = nullptr; ctx->mlp.y = nullptr; ctx->mlp.perm = nullptr; ctx->mlp.cap = 0;
+    if (cudaMalloc(&ctx->mlp.x, n * pnjl::mlp::IN * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&ctx->mlp.y, n * pnjl::mlp::OUT * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&ctx->mlp.perm, n * sizeof(long long)) != cudaSuccess)
+        return fail(ctx, PNJL_ERR_OUT_OF_MEMORY, "MLP data allocation failed");
+    ctx->mlp.cap = n;
+    return PNJL_OK;
+}
+
+// splitmix64: deterministic host RNG for the initial weights and the epoch shuffles
+uint64_t splitmix64(uint64_t &s) {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+double uniform01(uint64_t &s) { return (splitmix64(s) >> 11) * (1.0 / 9007199254740992.0); }
+
 }  // namespace
 
 extern "C" {
@@ -207,6 +268,14 @@ int pnjl_destroy(pnjl_ctx *ctx) {
     cudaFree(ctx->d_seed_tables);
     cudaFree(ctx->d_ws);
     cudaFree(ctx->d_scratch);
+    cudaFree(ctx->mlp.params);
+    cudaFree(ctx->mlp.wb);
+    cudaFree(ctx->mlp.step);
+    cudaFree(ctx->mlp.loss);
+    cudaFree(ctx->mlp.x);
+    cudaFree(ctx->mlp.y);
+    cudaFree(ctx->mlp.perm);
+    cudaFree(ctx->mlp.seeds);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -414,6 +483,242 @@ int pnjl_solve_batch_device(pnjl_ctx *ctx, int64_t n, const double *d_T, const d
     ctx->stats.kernel_launches += 1;
     ctx->stats.points = n;
     return PNJL_OK;
+}
+
+
+int pnjl_mlp_param_count(void) { return pnjl::kParamCount; }
+
+int pnjl_mlp_init(pnjl_ctx *ctx, uint64_t seed) {
+    if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    auto &M = ctx->mlp;
+    if (!M.params) {
+        PNJL_CUDA_TRY(ctx, cudaMalloc(&M.params, 4 * (size_t)pnjl::kParamCount * sizeof(float)));
+        PNJL_CUDA_TRY(ctx, cudaMalloc(&M.wb, (size_t)pnjl::kParamCount * sizeof(__nv_bfloat16)));
+        PNJL_CUDA_TRY(ctx, cudaMalloc(&M.step, sizeof(long long)));
+        PNJL_CUDA_TRY(ctx, cudaMalloc(&M.loss, sizeof(float)));
+        PNJL_CUDA_TRY(ctx, pnjl::mlp_setup_attributes());
+    }
+    // Kaiming-uniform weights (bound sqrt(6 / fan_in)), zero biases
+    const int H = pnjl::mlp::H, IN = pnjl::mlp::IN, OUT = pnjl::mlp::OUT;
+    std::vector<float> w(pnjl::kParamCount, 0.0f);
+    uint64_t s = seed;
+    auto fill = [&](int off, int rows, int cols) {
+        const double bound = std::sqrt(6.0 / cols);
+        for (int i = 0; i < rows * cols; ++i) w[off + i] = (float)((2.0 * uniform01(s) - 1.0) * bound);
+    };
+    int off = 0;
+    fill(off, H, IN); off += H * IN + H;
+    fill(off, H, H); off += H * H + H;
+    fill(off, H, H); off += H * H + H;
+    fill(off, OUT, H);
+    for (int i = 0; i < OUT * H; ++i) w[off + i] *= 0.1f;  // small output layer
+    PNJL_CUDA_TRY(ctx, cudaMemcpy(M.params, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice));
+    PNJL_CUDA_TRY(ctx, cudaMemset(M.params + pnjl::kParamCount, 0, 3 * (size_t)pnjl::kParamCount * sizeof(float)));
+    PNJL_CUDA_TRY(ctx, cudaMemset(M.step, 0, sizeof(long long)));
+    PNJL_CUDA_TRY(ctx, pnjl::mlp_refresh_bf16(mlp_dev(ctx), ctx->stream));
+    PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    M.ready = true;
+    M.trained = false;
+    return PNJL_OK;
+}
+
+int pnjl_mlp_set_scaling(pnjl_ctx *ctx, const double *in_shift, const double *in_scale, const double *out_shift,
+                         const double *out_scale) {
+    if (!ctx || !in_shift || !in_scale || !out_shift || !out_scale) return PNJL_ERR_INVALID_ARGUMENT;
+    auto &sc = ctx->mlp.sc;
+    for (int k = 0; k < 3; ++k) {
+        if (!(in_scale[k] != 0.0) || !std::isfinite(in_scale[k]) || !std::isfinite(in_shift[k]))
+            return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "input scaling must be finite and non-zero");
+        sc.in_shift[k] = in_shift[k];
+        sc.in_scale[k] = in_scale[k];
+    }
+    for (int k = 0; k < 5; ++k) {
+        if (!(out_scale[k] != 0.0) || !std::isfinite(out_scale[k]) || !std::isfinite(out_shift[k]))
+            return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "output scaling must be finite and non-zero");
+        sc.out_shift[k] = out_shift[k];
+        sc.out_scale[k] = out_scale[k];
+    }
+    ctx->mlp.scaled = true;
+    return PNJL_OK;
+}
+
+static int mlp_upload(pnjl_ctx *ctx, int64_t n, const double *T, const double *mu, const double *xi,
+                      const double *targets) {
+    int rc = mlp_ensure_data(ctx, (size_t)n);
+    if (rc) return rc;
+    const size_t nn = (size_t)n;
+    rc = ensure_ws(ctx, 8 * nn * sizeof(double) + 1024);
+    if (rc) return rc;
+    double *dT = (double *)ctx->d_ws, *dmu = dT + nn, *dxi = dmu + nn, *dt = dxi + nn;
+    cudaStream_t s = ctx->stream;
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dT, T, nn * 8, cudaMemcpyHostToDevice, s));
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dmu, mu, nn * 8, cudaMemcpyHostToDevice, s));
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dxi, xi, nn * 8, cudaMemcpyHostToDevice, s));
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dt, targets, 5 * nn * 8, cudaMemcpyHostToDevice, s));
+    PNJL_CUDA_TRY(ctx, pnjl::mlp_prepare(ctx->mlp.sc, n, dT, dmu, dxi, dt, ctx->mlp.x, ctx->mlp.y, s));
+    return PNJL_OK;
+}
+
+int pnjl_mlp_loss_grad(pnjl_ctx *ctx, int64_t n, const double *T, const double *mu, const double *xi,
+                       const double *targets, double *loss, float *grad) {
+    if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
+    int rc = mlp_require(ctx, true);
+    if (rc) return rc;
+    if (n <= 0 || n > (1 << 24) || !T || !mu || !xi || !targets) return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "bad batch");
+    cudaSetDevice(ctx->device);
+    rc = mlp_upload(ctx, n, T, mu, xi, targets);
+    if (rc) return rc;
+    pnjl::TrainBatch b{ctx->mlp.x, ctx->mlp.y, nullptr, n, (int)n, 0, ctx->mlp.step, ctx->mlp.loss};
+    pnjl::AdamCfg c{};
+    PNJL_CUDA_TRY(ctx, pnjl::mlp_launch_step(mlp_dev(ctx), b, c, false, ctx->stream));
+    float l = 0.f;
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(&l, ctx->mlp.loss, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    if (grad)
+        PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(grad, ctx->mlp.params + pnjl::kParamCount, pnjl::kParamCount * sizeof(float),
+                                           cudaMemcpyDeviceToHost, ctx->stream));
+    PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    if (loss) *loss = l;
+    ctx->stats.kernel_launches += 2;
+    return PNJL_OK;
+}
+
+int pnjl_mlp_train(pnjl_ctx *ctx, int64_t n, const double *T, const double *mu, const double *xi,
+                   const double *targets, int32_t epochs, int32_t batch, double lr, uint64_t shuffle_seed,
+                   double *last_loss) {
+    if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
+    int rc = mlp_require(ctx, true);
+    if (rc) return rc;
+    if (n <= 0 || epochs < 1 || batch < 32 || batch % 32 || !(lr > 0) || !T || !mu || !xi || !targets)
+        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "bad training arguments (batch: multiple of 32)");
+    cudaSetDevice(ctx->device);
+    rc = mlp_upload(ctx, n, T, mu, xi, targets);
+    if (rc) return rc;
+    cudaStream_t s = ctx->stream;
+    const long long spe = (n + batch - 1) / batch;
+    pnjl::TrainBatch b{ctx->mlp.x, ctx->mlp.y, ctx->mlp.perm, n, batch, spe, ctx->mlp.step, ctx->mlp.loss};
+    pnjl::AdamCfg c{lr, lr * 0.01, 0.9f, 0.999f, 1e-8f, spe * (long long)epochs};
+    PNJL_CUDA_TRY(ctx, cudaMemsetAsync(ctx->mlp.params + 2 * pnjl::kParamCount, 0,
+                                       2 * (size_t)pnjl::kParamCount * sizeof(float), s));
+    PNJL_CUDA_TRY(ctx, cudaMemsetAsync(ctx->mlp.step, 0, sizeof(long long), s));
+    // one training step as a CUDA graph, replayed steps_per_epoch x epochs times
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    PNJL_CUDA_TRY(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    cudaError_t ce = pnjl::mlp_launch_step(mlp_dev(ctx), b, c, true, s);
+    cudaError_t ee = cudaStreamEndCapture(s, &graph);
+    if (ce != cudaSuccess || ee != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return cuda_fail(ctx, ce != cudaSuccess ? ce : ee, "MLP step capture");
+    }
+    ce = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) return cuda_fail(ctx, ce, "MLP graph instantiate");
+    std::vector<long long> perm(n);
+    uint64_t rs = shuffle_seed;
+    float l = 0.f;
+    for (int ep = 0; ep < epochs && ce == cudaSuccess; ++ep) {
+        for (long long i = 0; i < n; ++i) perm[i] = i;
+        for (long long i = n - 1; i > 0; --i) {  // Fisher-Yates
+            const long long j = (long long)(splitmix64(rs) % (uint64_t)(i + 1));
+            std::swap(perm[i], perm[j]);
+        }
+        ce = cudaMemcpyAsync(ctx->mlp.perm, perm.data(), n * sizeof(long long), cudaMemcpyHostToDevice, s);
+        for (long long k = 0; k < spe && ce == cudaSuccess; ++k) ce = cudaGraphLaunch(exec, s);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);  // perm is host memory reused next epoch
+    }
+    if (ce == cudaSuccess) ce = cudaMemcpy(&l, ctx->mlp.loss, sizeof(float), cudaMemcpyDeviceToHost);
+    cudaGraphExecDestroy(exec);
+    if (ce != cudaSuccess) return cuda_fail(ctx, ce, "MLP training");
+    ctx->stats.kernel_launches += 4 * spe * (long long)epochs;
+    if (last_loss) *last_loss = l;
+    ctx->mlp.trained = true;
+    return PNJL_OK;
+}
+
+int pnjl_mlp_infer_device(pnjl_ctx *ctx, int64_t n, const double *d_T, const double *d_mu, const double *d_xi,
+                          double *d_seeds) {
+    if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
+    int rc = mlp_require(ctx, true);
+    if (rc) return rc;
+    if (n < 0 || (n > 0 && (!d_T || !d_mu || !d_xi || !d_seeds))) return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "null array");
+    if (n == 0) return PNJL_OK;
+    cudaSetDevice(ctx->device);
+    PNJL_CUDA_TRY(ctx, pnjl::mlp_launch_infer(mlp_dev(ctx), ctx->mlp.sc, n, d_T, d_mu, d_xi, d_seeds, ctx->sm_count,
+                                              ctx->stream));
+    ctx->stats.kernel_launches += 1;
+    return PNJL_OK;
+}
+
+int pnjl_mlp_infer(pnjl_ctx *ctx, int64_t n, const double *T, const double *mu, const double *xi, double *seeds) {
+    if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
+    int rc = mlp_require(ctx, true);
+    if (rc) return rc;
+    if (n < 0 || (n > 0 && (!T || !mu || !xi || !seeds))) return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "null array");
+    if (n == 0) return PNJL_OK;
+    cudaSetDevice(ctx->device);
+    const size_t nn = (size_t)n;
+    rc = ensure_ws(ctx, 8 * nn * sizeof(double) + 1024);
+    if (rc) return rc;
+    double *dT = (double *)ctx->d_ws, *dmu = dT + nn, *dxi = dmu + nn, *ds = dxi + nn;
+    cudaStream_t s = ctx->stream;
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dT, T, nn * 8, cudaMemcpyHostToDevice, s));
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dmu, mu, nn * 8, cudaMemcpyHostToDevice, s));
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dxi, xi, nn * 8, cudaMemcpyHostToDevice, s));
+    rc = pnjl_mlp_infer_device(ctx, n, dT, dmu, dxi, ds);
+    if (rc) return rc;
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(seeds, ds, 5 * nn * 8, cudaMemcpyDeviceToHost, s));
+    PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    return PNJL_OK;
+}
+
+int pnjl_mlp_get_params(pnjl_ctx *ctx, float *out, int64_t count) {
+    if (!ctx || !out || count != pnjl::kParamCount) return PNJL_ERR_INVALID_ARGUMENT;
+    int rc = mlp_require(ctx, false);
+    if (rc) return rc;
+    PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    PNJL_CUDA_TRY(ctx, cudaMemcpy(out, ctx->mlp.params, count * sizeof(float), cudaMemcpyDeviceToHost));
+    return PNJL_OK;
+}
+
+int pnjl_mlp_set_params(pnjl_ctx *ctx, const float *in, int64_t count) {
+    if (!ctx || !in || count != pnjl::kParamCount) return PNJL_ERR_INVALID_ARGUMENT;
+    int rc = mlp_require(ctx, false);
+    if (rc) return rc;
+    PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    PNJL_CUDA_TRY(ctx, cudaMemcpy(ctx->mlp.params, in, count * sizeof(float), cudaMemcpyHostToDevice));
+    PNJL_CUDA_TRY(ctx, pnjl::mlp_refresh_bf16(mlp_dev(ctx), ctx->stream));
+    PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->mlp.trained = true;
+    return PNJL_OK;
+}
+
+int pnjl_solve_batch_learned_device(pnjl_ctx *ctx, int64_t n, const double *d_T, const double *d_mu_u,
+                                    const double *d_mu_d, const double *d_mu_s, const double *d_xi,
+                                    const pnjl_solve_opts *opts, pnjl_result_soa *d_out) {
+    if (!ctx || !opts) return PNJL_ERR_INVALID_ARGUMENT;
+    int rc = mlp_require(ctx, true);
+    if (rc) return rc;
+    if (n <= 0) return n == 0 ? PNJL_OK : fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "n < 0");
+    cudaSetDevice(ctx->device);
+    auto &M = ctx->mlp;
+    const size_t need = (size_t)n * 5;
+    if (need > M.seeds_cap) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(M.seeds);
+        M.seeds = nullptr;
+        M.seeds_cap = 0;
+        if (cudaMalloc(&M.seeds, need * sizeof(double)) != cudaSuccess)
+            return fail(ctx, PNJL_ERR_OUT_OF_MEMORY, "seed buffer allocation failed");
+        M.seeds_cap = need;
+    }
+    rc = pnjl_mlp_infer_device(ctx, n, d_T, d_mu_u, d_xi, M.seeds);
+    if (rc) return rc;
+    pnjl_solve_opts o = *opts;
+    o.seed_mode = PNJL_SEEDS_PER_POINT;
+    o.point_seeds = M.seeds;
+    return pnjl_solve_batch_device(ctx, n, d_T, d_mu_u, d_mu_d, d_mu_s, d_xi, &o, d_out);
 }
 
 int pnjl_solve_batch(pnjl_ctx *ctx, int64_t n, const double *T, const double *mu_u, const double *mu_d,

@@ -69,32 +69,38 @@ __device__ __forceinline__ FlavourConst<R> make_flavour(double M, double mu, dou
                                                       bool &swapped) {
     FlavourConst<R> fc;
     swapped = mu < 0.0;
-    const double mua = swapped ? -mu : mu;
-    const double Pq = swapped ? Phib : Phi;
-    const double Pa = swapped ? Phi : Phib;
-    const double C = exp(-2.0 * mua / T);
-    const double C2 = C * C, C3 = C2 * C;
+    // the per-flavour constants are computed in the pass's own precision (an FP32 pass
+    // spends no FP64 instructions here)
+    const R mua = (R)(swapped ? -mu : mu);
+    const R Pq = (R)(swapped ? Phib : Phi);
+    const R Pa = (R)(swapped ? Phi : Phib);
+    const R Tr = (R)T;
+    R C;
+    if constexpr (sizeof(R) == 4) C = __expf(-2.0f * mua / Tr);
+    else C = exp(-2.0 * mua / Tr);
+    const R C2 = C * C, C3 = C2 * C;
     fc.M = (R)M;
-    fc.M2 = (R)(M * M);
-    fc.mu = (R)mua;
-    fc.invT = (R)(1.0 / T);
-    fc.C = (R)C;
-    fc.C2 = (R)C2;
-    fc.C3 = (R)C3;
-    fc.Pq = (R)Pq;
-    fc.Pa = (R)Pa;
-    fc.k1_0 = (R)(3.0 * Pq);
-    fc.k2_0 = (R)(3.0 * Pa);
-    fc.k1_1 = (R)(3.0 * Pa);
-    fc.k2_1 = (R)(3.0 * Pq);
-    fc.e3_0 = (R)C3;
-    fc.e2_0 = (R)(3.0 * Pq * C2);
-    fc.e1_0 = (R)(3.0 * Pa * C);
-    fc.e0_0 = (R)1.0;
-    fc.e3_1 = (R)1.0;
-    fc.e2_1 = (R)(3.0 * Pa * C);
-    fc.e1_1 = (R)(3.0 * Pq * C2);
-    fc.e0_1 = (R)C3;
+    fc.M2 = (R)M * (R)M;
+    if constexpr (sizeof(R) == 8) fc.M2 = M * M;
+    fc.mu = mua;
+    fc.invT = R(1) / Tr;
+    fc.C = C;
+    fc.C2 = C2;
+    fc.C3 = C3;
+    fc.Pq = Pq;
+    fc.Pa = Pa;
+    fc.k1_0 = R(3) * Pq;
+    fc.k2_0 = R(3) * Pa;
+    fc.k1_1 = R(3) * Pa;
+    fc.k2_1 = R(3) * Pq;
+    fc.e3_0 = C3;
+    fc.e2_0 = R(3) * Pq * C2;
+    fc.e1_0 = R(3) * Pa * C;
+    fc.e0_0 = R(1);
+    fc.e3_1 = R(1);
+    fc.e2_1 = R(3) * Pa * C;
+    fc.e1_1 = R(3) * Pq * C2;
+    fc.e0_1 = C3;
     return fc;
 }
 

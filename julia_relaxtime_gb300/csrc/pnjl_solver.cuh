@@ -208,11 +208,10 @@ __device__ void node_pass(const NodeView &nv, const PointIn &pt, const double *x
     S.SAN = acc[24];
 }
 
-// Assembly of Omega, grad, Hessian and thermo from the pass sums and the vacuum terms.
-// FP64 throughout, except that HESS32 assembles the Jacobian in FP32 arithmetic (the FP32
-// Newton passes of the mixed mode, whose sums carry FP32 accuracy anyway); the 5x5 solve
-// that consumes it stays FP64.
-template <bool GRAD, bool HESS, bool LOG, bool HESS32 = false>
+// FP64 assembly of Omega, grad, Hessian and thermo from the pass sums and the vacuum terms.
+// (An FP32 assembly of the Jacobian for the mixed mode was measured slower: the less
+// accurate J32 costs extra FP64 refinement passes.)
+template <bool GRAD, bool HESS, bool LOG>
 __device__ void assemble(const DevParams &P, const PointIn &pt, const double *x, const double *M, const PassSums &S,
                          double V, const double *V1, const double *V2, Eval &ev) {
     const double T = pt.T;
@@ -250,7 +249,7 @@ __device__ void assemble(const DevParams &P, const PointIn &pt, const double *x,
     for (int i = 0; i < 5; ++i) ev.F[i] = -gO[i];
     if (LOG) ev.omega = chi + U + V + Dsc * S.SL;
     else ev.omega = 0.0;
-    if (HESS && !HESS32) {
+    if (HESS) {
         double H[5][5];
         const double chih[3][3] = {{G4, -K4 * ps, -K4 * pd}, {-K4 * ps, G4, -K4 * pu}, {-K4 * pd, -K4 * pu, G4}};
         for (int a = 0; a < 3; ++a)
@@ -284,52 +283,6 @@ __device__ void assemble(const DevParams &P, const PointIn &pt, const double *x,
             for (int b = a; b < 5; ++b) {
                 ev.J[a * 5 + b] = -H[a][b];
                 ev.J[b * 5 + a] = -H[a][b];
-            }
-    }
-    if (HESS && HESS32) {
-        float H[5][5];
-        const float fG4 = (float)G4, fK2 = (float)K2, fK4 = (float)K4, fDsc = (float)Dsc;
-        const float fpu = (float)pu, fpd = (float)pd, fps = (float)ps, fPh = (float)Ph, fPb = (float)Pb;
-        const float Jf[3][3] = {{-fG4, fK2 * fps, fK2 * fpd}, {fK2 * fps, -fG4, fK2 * fpu}, {fK2 * fpd, fK2 * fpu, -fG4}};
-        const float chih[3][3] = {{fG4, -fK4 * fps, -fK4 * fpd}, {-fK4 * fps, fG4, -fK4 * fpu}, {-fK4 * fpd, -fK4 * fpu, fG4}};
-        float W2[3], W1[3];
-        for (int f = 0; f < 3; ++f) {
-            W2[f] = (float)(V2[f] + Dsc * S.DMM[f]);
-            W1[f] = (float)(V1[f] + Dsc * S.DM[f]);
-        }
-        for (int a = 0; a < 3; ++a)
-            for (int b = a; b < 3; ++b) {
-                float s = chih[a][b];
-                for (int f = 0; f < 3; ++f) s += Jf[f][a] * Jf[f][b] * W2[f];
-                H[a][b] = s;
-            }
-        H[0][1] += W1[2] * fK2;
-        H[0][2] += W1[1] * fK2;
-        H[1][2] += W1[0] * fK2;
-        for (int a = 0; a < 3; ++a) {
-            float s3 = 0.f, s4 = 0.f;
-            for (int f = 0; f < 3; ++f) {
-                s3 += Jf[f][a] * (fDsc * (float)S.DMP[f]);
-                s4 += Jf[f][a] * (fDsc * (float)S.DMPb[f]);
-            }
-            H[a][3] = s3;
-            H[a][4] = s4;
-        }
-        const float fT4 = (float)T4, fTb = (float)Tb, fTa = (float)Ta, fig = (float)ig;
-        const float fgP = (float)gP, fgPb = (float)gPb;
-        const float gPP = 24.f * fPh - 6.f * fPb * fPb;
-        const float gPbPb = 24.f * fPb - 6.f * fPh * fPh;
-        const float gPPb = -6.f - 12.f * fPh * fPb;
-        const float UPP = gcl ? 0.f : fT4 * fTb * (gPP * fig - fgP * fgP * fig * fig);
-        const float UPbPb = gcl ? 0.f : fT4 * fTb * (gPbPb * fig - fgPb * fgPb * fig * fig);
-        const float UPPb = fT4 * (-0.5f * fTa + (gcl ? 0.f : fTb * (gPPb * fig - fgP * fgPb * fig * fig)));
-        H[3][3] = UPP + fDsc * (float)S.SPP;
-        H[3][4] = UPPb + fDsc * (float)S.SPPb;
-        H[4][4] = UPbPb + fDsc * (float)S.SPbPb;
-        for (int a = 0; a < 5; ++a)
-            for (int b = a; b < 5; ++b) {
-                ev.J[a * 5 + b] = -(double)H[a][b];
-                ev.J[b * 5 + a] = -(double)H[a][b];
             }
     }
     if (LOG) {

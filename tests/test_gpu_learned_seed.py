@@ -1,0 +1,83 @@
+"""The learned seed: BF16 tensor-core MLP kernels against the CPU FP64 oracle, training, and
+what the trained network gains over the multi-seed method it falls back to."""
+import numpy as np
+import pytest
+
+from julia_relaxtime_gb300 import pnjl
+from julia_relaxtime_gb300.engine import SolveOptions
+from oracle import mlp_oracle as mo
+
+pytestmark = pytest.mark.gpu
+HBARC = 197.327
+
+
+def _standardised(ls, T, mu, xi, targets=None):
+    ins, insc, outs, outsc = ls.scaling
+    v = np.stack([T, mu, xi], axis=1)
+    x = ((v - ins) / insc).astype(np.float32).astype(np.float64)
+    y = None if targets is None else ((targets - outs) / outsc).astype(np.float32).astype(np.float64)
+    return x, y
+
+
+@pytest.mark.parametrize("n", [32, 80])
+def test_mlp_loss_and_gradient_match_cpu_oracle(engine_factory, n):
+    from julia_relaxtime_gb300.learned_seed import LearnedSeed, param_count
+
+    assert param_count() == mo.PARAM_COUNT
+    eng = engine_factory(16, 4)
+    ls = LearnedSeed(eng, seed=11)
+    rng = np.random.default_rng(n)
+    T = rng.uniform(50, 300, n) / HBARC
+    mu = rng.uniform(0, 400, n) / HBARC
+    xi = rng.uniform(-0.5, 0.5, n)
+    targets = np.column_stack([rng.normal(-1.0, 0.6, (n, 3)), rng.uniform(0, 1, (n, 2))])
+    ls.default_scaling(targets)
+    loss, g = ls.loss_grad(T, mu, xi, targets)
+    p = ls.params().astype(np.float64)
+    x, y = _standardised(ls, T, mu, xi, targets)
+    loss_ref, g_ref = mo.loss_grad(p, x, y)
+    assert abs(loss - loss_ref) <= 1e-3 * abs(loss_ref)
+    gu, gr = mo.unpack(g.astype(np.float64)), mo.unpack(g_ref)
+    for k, _ in mo.SIZES:
+        a, b = gu[k].ravel(), gr[k].ravel()
+        rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+        assert rel < 2e-2, (k, rel)
+    cos = np.dot(g, g_ref) / (np.linalg.norm(g) * np.linalg.norm(g_ref))
+    assert cos > 0.9999, cos
+    # inference equals the oracle forward pass (BF16 rounding emulated), de-standardised
+    seeds = ls.seeds(T, mu, xi)
+    ref = mo.forward(p, x) * ls.scaling[3] + ls.scaling[2]
+    np.testing.assert_allclose(seeds, ref, rtol=2e-2, atol=2e-2 * np.abs(ref).max())
+
+
+def test_learned_seed_trains_and_beats_multiseed(engine_factory):
+    """Train on a solver-labelled (T, mu, xi) grid, then solve held-out points: same roots and
+    phases as the multi-seed method (its fallback), at a fraction of the node evaluations."""
+    from julia_relaxtime_gb300.learned_seed import LearnedSeed, TrainConfig, label_grid
+
+    eng = engine_factory(32, 8)
+    cfg = TrainConfig(T_MeV=(50.0, 300.0, 24), mu_MeV=(0.0, 400.0, 24), xi=(-0.5, 0.5, 3), epochs=300, batch=256)
+    T, mu, xi, x, _ = label_grid(eng, cfg)
+    assert T.size > 0.95 * 24 * 24 * 3
+    ls = LearnedSeed(eng, seed=3)
+    loss0, _ = (ls.default_scaling(x), ls.loss_grad(T, mu, xi, x))[1]
+    loss = ls.fit(T, mu, xi, x, epochs=cfg.epochs, batch=cfg.batch, lr=cfg.lr)
+    assert loss < 0.05 * loss0, (loss0, loss)
+    rng = np.random.default_rng(99)
+    m = 400
+    Tt = rng.uniform(50, 300, m) / HBARC
+    mt = rng.uniform(0, 400, m) / HBARC
+    xt = rng.uniform(-0.5, 0.5, m)
+    table, hot = pnjl.multiseed_table(6)
+    opts = SolveOptions(iterations=40, ftol=1e-10, precision="mixed")
+    ref = eng.solve(Tt, mt, xt, seed_table=table, seed_table_hot=hot, opts=opts)
+    st_ref = eng.stats()
+    got = ls.solve(Tt, mt, xt, opts=opts)
+    st = eng.stats()
+    both = ref["converged"] & got["converged"]
+    assert both.mean() > 0.98
+    same_phase = np.abs(got["omega"] - ref["omega"]) <= 1e-10 * np.abs(ref["omega"])
+    assert same_phase[both].mean() >= 0.98, np.sum(~same_phase[both])
+    work_ref = st_ref["node_evals_fp32"] + 64 * st_ref["node_evals_fp64"]
+    work = st["node_evals_fp32"] + 64 * st["node_evals_fp64"]
+    assert work < 0.5 * work_ref, (work, work_ref)
