@@ -87,7 +87,12 @@ typedef struct pnjl_solve_opts {
     int32_t trust_region_fallback;   /* ImplicitSolver.jl:130-151                            */
     int32_t auto_multiseed_fallback; /* ImplicitSolver.jl:306-327                            */
     int32_t precision;           /* PNJL_PREC_FP64 / PNJL_PREC_MIXED                          */
-    int32_t reserved;
+    int32_t verify_seeds;        /* PNJL_SEEDS_PER_POINT only: a converged per-point solution is
+                                    also checked against the first verify_seeds rows of the seed
+                                    table at T*hbarc < verify_T_max_MeV (where a first-order line
+                                    allows a lower-Omega branch); min-Omega with the per-point
+                                    seed first.  0 disables (the reference's single-seed path). */
+    double verify_T_max_MeV;
 } pnjl_solve_opts;
 
 /* Per-point results, SoA; any NULL pointer skips that output.  Fields follow SolverResult

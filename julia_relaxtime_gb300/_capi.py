@@ -65,7 +65,8 @@ class pnjl_solve_opts(C.Structure):
         ("trust_region_fallback", C.c_int32),
         ("auto_multiseed_fallback", C.c_int32),
         ("precision", C.c_int32),
-        ("reserved", C.c_int32),
+        ("verify_seeds", C.c_int32),
+        ("verify_T_max_MeV", C.c_double),
     ]
 
 

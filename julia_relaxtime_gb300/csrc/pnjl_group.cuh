@@ -44,6 +44,17 @@ struct Group {
 
     __device__ __forceinline__ int leader() const { return (int)(threadIdx.x & 31) & ~(G - 1); }
 
+    // Isospin symmetry: with mu_u == mu_d and phi_u == phi_d the exact Newton (or dogleg) step
+    // has p_u == p_d; the 5x5 elimination leaves them unequal in the last bit.  Projecting the
+    // step keeps the state symmetric, so every pass evaluates the u and d flavours once.
+    __device__ static __forceinline__ void symmetrize_step(const PointIn &pt, const double *x, double *p) {
+        if (pt.mu[0] == pt.mu[1] && x[0] == x[1]) {
+            const double m = 0.5 * (p[0] + p[1]);
+            p[0] = m;
+            p[1] = m;
+        }
+    }
+
     // residual and Jacobian at x (one Newton pass)
     __device__ __noinline__ void eval_newton(const PointIn &pt, const double *x, double *F, double *J) {
         double M[3];
@@ -100,6 +111,7 @@ struct Group {
             } else {
                 levenberg_step(J, F, p);
             }
+            symmetrize_step(pt, x, p);
 #pragma unroll
             for (int i = 0; i < 5; ++i) { xold[i] = x[i]; x[i] += p[i]; }
             eval_newton(pt, x, F, J);
@@ -175,6 +187,7 @@ struct Group {
             while (!stopped && !converged && it < o.max_iter) {
                 ++it;
                 dogleg(p, r, d, Jacc, delta);
+                symmetrize_step(pt, x, p);
                 for (int i = 0; i < 5; ++i) { xold[i] = x[i]; x[i] += p[i]; }
                 eval_newton(pt, x, F, J);
                 double sr = 0.0, sf = 0.0, sp = 0.0;
@@ -289,8 +302,8 @@ struct Group {
     // Newton passes with the FP32 Kahan-compensated integrand (the 5x5 solve and the update
     // stay FP64), then FP64 refinement steps x <- x - J32^{-1} F64(x) until the FP64 residual
     // ||grad_x Omega||_inf is below ftol; Omega and the thermo output come from FP64 passes.
-    static constexpr double kFtol32 = 1e-7;   // FP32 residual that ends the FP32 phase
-    static constexpr double kStall32 = 1e-6;  // ... or a relative step this small ...
+    static constexpr double kFtol32 = 1e-8;   // FP32 residual that ends the FP32 phase
+    static constexpr double kStall32 = 1e-7;  // ... or a relative step this small ...
     static constexpr double kLoose32 = 1e-3;  // ... with the FP32 residual below this
     static constexpr int kMaxRefine = 6;
 
@@ -350,6 +363,7 @@ struct Group {
             } else {
                 levenberg_step(J, F, p);
             }
+            symmetrize_step(pt, x, p);
             const double pn = norm_inf5(p), xn = norm_inf5(x);
             for (int i = 0; i < 5; ++i) x[i] += p[i];
             ++iters;
@@ -380,6 +394,7 @@ struct Group {
         while (iters < o.max_iter) {
             ++iters;
             dogleg(p, r, d, Jacc, delta);
+            symmetrize_step(pt, x, p);
             for (int i = 0; i < 5; ++i) x[i] += p[i];
             eval_newton32(pt, x, F, J);
             double sr = 0.0, sf = 0.0, sp = 0.0;
@@ -445,6 +460,7 @@ struct Group {
             } else {
                 levenberg_step(J32, F, p);
             }
+            symmetrize_step(pt, c.x, p);
             for (int i = 0; i < 5; ++i) c.x[i] += p[i];
             ++steps;
             eval_grad_thermo64(pt, o, c, F);

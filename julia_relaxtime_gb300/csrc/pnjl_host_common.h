@@ -100,6 +100,10 @@ inline int validate_opts(const pnjl_solve_opts *o, const char **msg) {
         *msg = "tolerances must be positive";
         return PNJL_ERR_INVALID_ARGUMENT;
     }
+    if (o->verify_seeds < 0 || (o->verify_seeds > 0 && (!o->seed_table || o->verify_seeds > o->n_seeds))) {
+        *msg = "verify_seeds must be 0..n_seeds (rows of the seed table)";
+        return PNJL_ERR_INVALID_ARGUMENT;
+    }
     if (o->precision != PNJL_PREC_FP64 && o->precision != PNJL_PREC_MIXED) {
         *msg = "unknown precision";
         return PNJL_ERR_INVALID_ARGUMENT;
@@ -116,6 +120,8 @@ inline void fill_solve_opts(const pnjl_solve_opts *o, SolveOpts &d) {
     d.omega_tie_rtol = o->omega_tie_rtol;
     d.trust_region_fallback = o->trust_region_fallback;
     d.auto_multiseed_fallback = o->auto_multiseed_fallback;
+    d.verify_seeds = o->seed_mode == PNJL_SEEDS_PER_POINT ? o->verify_seeds : 0;
+    d.verify_T_max_MeV = o->verify_T_max_MeV;
 }
 
 inline DevParams dev_params(const pnjl_params &p) {

@@ -108,6 +108,22 @@ __global__ void __launch_bounds__(kSolveThreads, 2) solve_kernel(SolveArgs a) {
                 if (gl == 0) write_point(a.P, pt, a.out, i, single, false, -1, PNJL_POINT_EXCEPTION);
                 continue;
             }
+            if (conv && o.verify_seeds > 0 && pt.T * a.P.hbarc < o.verify_T_max_MeV) {
+                Candidate best = single;
+                int chosen = -1;
+                for (int s = 0; s < o.verify_seeds; ++s) {
+                    const double *row = table_row(a, pt, s);
+                    double x1[5];
+                    for (int k = 0; k < 5; ++k) x1[k] = row[k];
+                    Candidate c;
+                    bool cv;
+                    grp.solve_seed(pt, x1, o, c, cv);
+                    if (c.exception || !cv) continue;
+                    if (better(c, best, true, o.omega_tie_rtol)) { best = c; chosen = s; }
+                }
+                if (gl == 0) write_point(a.P, pt, a.out, i, best, true, chosen, PNJL_POINT_CONVERGED);
+                continue;
+            }
             if (conv || !o.auto_multiseed_fallback || S == 0) {
                 if (gl == 0)
                     write_point(a.P, pt, a.out, i, single, conv, -1, conv ? PNJL_POINT_CONVERGED : PNJL_POINT_NOT_CONVERGED);

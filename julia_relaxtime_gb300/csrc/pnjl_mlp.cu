@@ -418,7 +418,13 @@ __global__ void __launch_bounds__(NT) mlp_infer_kernel(MlpDev m, Scaling sc, lon
         forward_tile(m, X, valid, smem, out);
         for (int i = threadIdx.x; i < valid * OUT; i += NT) {
             const int s = i / OUT, o = i % OUT;
-            seeds[(base + s) * OUT + o] = (double)out[i] * sc.out_scale[o] + sc.out_shift[o];
+            double v = (double)out[i] * sc.out_scale[o] + sc.out_shift[o];
+            if (o < 2) {  // phi_u = phi_d: the network sees mu_u only, so its seed is isospin symmetric
+                const double vu = (double)out[s * OUT + 0] * sc.out_scale[0] + sc.out_shift[0];
+                const double vd = (double)out[s * OUT + 1] * sc.out_scale[1] + sc.out_shift[1];
+                v = 0.5 * (vu + vd);
+            }
+            seeds[(base + s) * OUT + o] = v;
         }
         __syncthreads();
     }

@@ -34,6 +34,9 @@ class SolveOptions:
     trust_region_fallback: bool = True
     auto_multiseed_fallback: bool = True
     precision: str = "fp64"
+    # per-point seeds only: also try the first `verify_seeds` table rows below this temperature
+    verify_seeds: int = 0
+    verify_T_max_MeV: float = 170.0
 
 
 def _dp(a):
@@ -168,6 +171,8 @@ class GapEngine:
         o.trust_region_fallback = int(bool(opts.trust_region_fallback))
         o.auto_multiseed_fallback = int(bool(opts.auto_multiseed_fallback))
         o.precision = PRECISIONS[opts.precision]
+        o.verify_seeds = int(opts.verify_seeds)
+        o.verify_T_max_MeV = float(opts.verify_T_max_MeV)
         return o
 
     def solve(self, T, mu, xi, *, seed_table=None, seed_table_hot=None, hot_T_MeV: float = 300.0,
