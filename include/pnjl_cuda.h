@@ -93,6 +93,9 @@ typedef struct pnjl_solve_opts {
                                     allows a lower-Omega branch); min-Omega with the per-point
                                     seed first.  0 disables (the reference's single-seed path). */
     double verify_T_max_MeV;
+    double verify_max_step;      /* ... and, at any T, when the converged state lies farther than
+                                    this (infinity norm) from its per-point seed: the seed did not
+                                    predict the branch it converged to.  <= 0 disables. */
 } pnjl_solve_opts;
 
 /* Per-point results, SoA; any NULL pointer skips that output.  Fields follow SolverResult

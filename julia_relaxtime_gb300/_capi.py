@@ -67,6 +67,7 @@ class pnjl_solve_opts(C.Structure):
         ("precision", C.c_int32),
         ("verify_seeds", C.c_int32),
         ("verify_T_max_MeV", C.c_double),
+        ("verify_max_step", C.c_double),
     ]
 
 

@@ -48,7 +48,7 @@ struct SolveOpts {
     double ftol, xtol, residual_norm_max, phi_tol, omega_tie_rtol;
     int trust_region_fallback, auto_multiseed_fallback;
     int verify_seeds;
-    double verify_T_max_MeV;
+    double verify_T_max_MeV, verify_max_step;
 };
 
 // The reference's POLYAKOV_EPS (Integrals.jl:151) and log(POLYAKOV_EPS)

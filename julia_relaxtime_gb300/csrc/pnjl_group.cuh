@@ -348,16 +348,20 @@ struct Group {
         postprocess(P, pt, o, ev, c);
     }
 
-    // 1: reached the FP32 floor, 0: did not converge, -1: residual at x0 not finite
+    // 1: reached the FP32 floor, 0: did not converge, -1: residual at x0 not finite.
+    // The FP32 phase ends at its noise floor: the residual is tiny, or it is small and no
+    // longer halves per Newton step (so the FP64 refinement starts from the best x FP32
+    // can give and usually certifies after one step).
     __device__ int newton32(const PointIn &pt, const double *x0, const SolveOpts &o, double *x, double *J, int &iters) {
         double F[5], p[5];
         for (int i = 0; i < 5; ++i) x[i] = x0[i];
         eval_newton32(pt, x, F, J);
         iters = 0;
         if (!all_finite5(F)) return -1;
+        double fn = norm_inf5(F);
         for (;;) {
-            if (norm_inf5(F) < kFtol32) return 1;
-            if (iters >= o.max_iter) return 0;
+            if (fn < kFtol32) return 1;
+            if (iters >= o.max_iter) return fn < kLoose32 ? 1 : 0;
             if (lu_solve5(J, F, p)) {
                 for (int i = 0; i < 5; ++i) p[i] = -p[i];
             } else {
@@ -369,7 +373,9 @@ struct Group {
             ++iters;
             eval_newton32(pt, x, F, J);
             if (any_nan5(x) || any_nan5(F)) return 0;
-            if (pn <= kStall32 * (1.0 + xn) && norm_inf5(F) < kLoose32) return 1;
+            const double fnew = norm_inf5(F);
+            if (fnew < kLoose32 && (fnew > 0.5 * fn || pn <= kStall32 * (1.0 + xn))) return 1;
+            fn = fnew;
         }
     }
 
@@ -381,6 +387,7 @@ struct Group {
         iters = 0;
         if (!all_finite5(r)) return -1;
         if (norm_inf5(r) < kFtol32) return 1;
+        double fprev = norm_inf5(r);
         for (int j = 0; j < 5; ++j) {
             double s = 0.0;
             for (int i = 0; i < 5; ++i) s += Jacc[i * 5 + j] * Jacc[i * 5 + j];
@@ -419,9 +426,11 @@ struct Group {
                     const double cn = sqrt(s);
                     d[j] = (0.1 * d[j] > cn) ? 0.1 * d[j] : cn;
                 }
+                const double fold = fprev;
                 const double fn = norm_inf5(r);
                 if (fn < kFtol32) return 1;
-                if (norm_inf5(p) <= kStall32 * (1.0 + norm_inf5(x)) && fn < kLoose32) return 1;
+                if (fn < kLoose32 && (fn > 0.5 * fold || norm_inf5(p) <= kStall32 * (1.0 + norm_inf5(x)))) return 1;
+                fprev = fn;
             } else {
                 for (int i = 0; i < 5; ++i) x[i] -= p[i];
             }
@@ -430,7 +439,7 @@ struct Group {
             else if (rho >= 0.5) delta = fmax(delta, 2.0 * wp);
             if (any_nan5(x) || any_nan5(F)) return 0;
         }
-        return 0;
+        return fprev < kLoose32 ? 1 : 0;
     }
 
     // FP64 refinement + certification of an FP32 solution; fills c.  A certified candidate
@@ -624,6 +633,20 @@ __device__ __forceinline__ void load_record(const CandRec *r, Candidate &c, bool
 __device__ __forceinline__ const double *table_row(const SolveArgs &a, const PointIn &pt, int s) {
     const bool hot = pt.T * a.P.hbarc >= a.hot_T_MeV;
     return (hot && a.seed_table_hot) ? a.seed_table_hot + 5 * s : a.seed_table + 5 * s;
+}
+
+// Whether a converged per-point solution gets the verification seeds: in the first-order
+// region (T below verify_T_max_MeV) or when the root lies far from the seed.
+__device__ __forceinline__ bool needs_verification(const SolveOpts &o, const PointIn &pt, double hbarc,
+                                                   const double *x0, const double *x) {
+    if (o.verify_seeds <= 0) return false;
+    if (pt.T * hbarc < o.verify_T_max_MeV) return true;
+    if (o.verify_max_step > 0.0) {
+        double d = 0.0;
+        for (int k = 0; k < 5; ++k) d = fmax(d, fabs(x[k] - x0[k]));
+        if (!(d <= o.verify_max_step)) return true;
+    }
+    return false;
 }
 
 // Streaming min-Omega rule over seeds in order: a later converged candidate replaces the

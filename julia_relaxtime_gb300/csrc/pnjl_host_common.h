@@ -122,6 +122,7 @@ inline void fill_solve_opts(const pnjl_solve_opts *o, SolveOpts &d) {
     d.auto_multiseed_fallback = o->auto_multiseed_fallback;
     d.verify_seeds = o->seed_mode == PNJL_SEEDS_PER_POINT ? o->verify_seeds : 0;
     d.verify_T_max_MeV = o->verify_T_max_MeV;
+    d.verify_max_step = o->verify_max_step;
 }
 
 inline DevParams dev_params(const pnjl_params &p) {

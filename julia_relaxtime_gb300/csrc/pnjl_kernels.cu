@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(kSolveThreads, 2) solve_kernel(SolveArgs a) {
                 if (gl == 0) write_point(a.P, pt, a.out, i, single, false, -1, PNJL_POINT_EXCEPTION);
                 continue;
             }
-            if (conv && o.verify_seeds > 0 && pt.T * a.P.hbarc < o.verify_T_max_MeV) {
+            if (conv && needs_verification(o, pt, a.P.hbarc, x0, single.x)) {
                 Candidate best = single;
                 int chosen = -1;
                 for (int s = 0; s < o.verify_seeds; ++s) {

@@ -59,17 +59,17 @@ __global__ void __launch_bounds__(kSolveThreads, 2) solve_kernel_mixed(SolveArgs
                 if (gl == 0) write_point(a.P, pt, a.out, i, single, false, -1, PNJL_POINT_EXCEPTION);
                 continue;
             }
-            if (single_conv && o.verify_seeds > 0 && pt.T * a.P.hbarc < o.verify_T_max_MeV) {
-                // first-order region: a table seed may reach a lower-Omega branch
+            if (single_conv && needs_verification(o, pt, a.P.hbarc, x0, single.x)) {
+                // a table seed may reach a lower-Omega branch
                 Candidate best = single;
                 int chosen = -1;
                 for (int s = 0; s < o.verify_seeds; ++s) {
                     const double *row = table_row(a, pt, s);
-                    double x0[5];
-                    for (int k = 0; k < 5; ++k) x0[k] = row[k];
+                    double xv[5];
+                    for (int k = 0; k < 5; ++k) xv[k] = row[k];
                     Candidate c;
                     bool conv, dup;
-                    grp.mixed_solve_seed(pt, x0, o, c, conv, seen, n_seen, dup);
+                    grp.mixed_solve_seed(pt, xv, o, c, conv, seen, n_seen, dup);
                     if (dup || c.exception || !conv) continue;
                     if (better(c, best, true, o.omega_tie_rtol)) { best = c; chosen = s; }
                 }

@@ -37,6 +37,7 @@ class SolveOptions:
     # per-point seeds only: also try the first `verify_seeds` table rows below this temperature
     verify_seeds: int = 0
     verify_T_max_MeV: float = 170.0
+    verify_max_step: float = 0.0
 
 
 def _dp(a):
@@ -173,6 +174,7 @@ class GapEngine:
         o.precision = PRECISIONS[opts.precision]
         o.verify_seeds = int(opts.verify_seeds)
         o.verify_T_max_MeV = float(opts.verify_T_max_MeV)
+        o.verify_max_step = float(opts.verify_max_step)
         return o
 
     def solve(self, T, mu, xi, *, seed_table=None, seed_table_hot=None, hot_T_MeV: float = 300.0,

@@ -47,6 +47,7 @@ def test_mlp_loss_and_gradient_match_cpu_oracle(engine_factory, n):
     # inference equals the oracle forward pass (BF16 rounding emulated), de-standardised
     seeds = ls.seeds(T, mu, xi)
     ref = mo.forward(p, x) * ls.scaling[3] + ls.scaling[2]
+    ref[:, :2] = 0.5 * (ref[:, 0] + ref[:, 1])[:, None]  # the solver seed is isospin symmetric
     np.testing.assert_allclose(seeds, ref, rtol=2e-2, atol=2e-2 * np.abs(ref).max())
 
 
