@@ -303,7 +303,7 @@ struct Group {
     // stay FP64), then FP64 refinement steps x <- x - J32^{-1} F64(x) until the FP64 residual
     // ||grad_x Omega||_inf is below ftol; Omega and the thermo output come from FP64 passes.
     static constexpr double kFtol32 = 1e-8;   // FP32 residual that ends the FP32 phase
-    static constexpr double kStall32 = 1e-7;  // ... or a relative step this small ...
+    static constexpr double kStall32 = 1e-6;  // ... or a relative step this small ...
     static constexpr double kLoose32 = 1e-3;  // ... with the FP32 residual below this
     static constexpr int kMaxRefine = 6;
 
@@ -349,19 +349,19 @@ struct Group {
     }
 
     // 1: reached the FP32 floor, 0: did not converge, -1: residual at x0 not finite.
-    // The FP32 phase ends at its noise floor: the residual is tiny, or it is small and no
-    // longer halves per Newton step (so the FP64 refinement starts from the best x FP32
-    // can give and usually certifies after one step).
+    // The FP32 phase ends when the residual is tiny, or when the Newton step has become small
+    // (relative 1e-6) with a small residual -- then one more FP32 step is taken, which brings
+    // x to the FP32 noise floor, so the FP64 refinement usually certifies after one step.
     __device__ int newton32(const PointIn &pt, const double *x0, const SolveOpts &o, double *x, double *J, int &iters) {
         double F[5], p[5];
         for (int i = 0; i < 5; ++i) x[i] = x0[i];
         eval_newton32(pt, x, F, J);
         iters = 0;
         if (!all_finite5(F)) return -1;
-        double fn = norm_inf5(F);
+        bool polish = false;
         for (;;) {
-            if (fn < kFtol32) return 1;
-            if (iters >= o.max_iter) return fn < kLoose32 ? 1 : 0;
+            if (norm_inf5(F) < kFtol32) return 1;
+            if (iters >= o.max_iter) return 0;
             if (lu_solve5(J, F, p)) {
                 for (int i = 0; i < 5; ++i) p[i] = -p[i];
             } else {
@@ -373,9 +373,8 @@ struct Group {
             ++iters;
             eval_newton32(pt, x, F, J);
             if (any_nan5(x) || any_nan5(F)) return 0;
-            const double fnew = norm_inf5(F);
-            if (fnew < kLoose32 && (fnew > 0.5 * fn || pn <= kStall32 * (1.0 + xn))) return 1;
-            fn = fnew;
+            if (polish) return 1;
+            if (pn <= kStall32 * (1.0 + xn) && norm_inf5(F) < kLoose32) polish = true;
         }
     }
 
@@ -429,7 +428,8 @@ struct Group {
                 const double fold = fprev;
                 const double fn = norm_inf5(r);
                 if (fn < kFtol32) return 1;
-                if (fn < kLoose32 && (fn > 0.5 * fold || norm_inf5(p) <= kStall32 * (1.0 + norm_inf5(x)))) return 1;
+                if (fn < kLoose32 && norm_inf5(p) <= kStall32 * (1.0 + norm_inf5(x))) return 1;
+                (void)fold;
                 fprev = fn;
             } else {
                 for (int i = 0; i < 5; ++i) x[i] -= p[i];
@@ -439,7 +439,7 @@ struct Group {
             else if (rho >= 0.5) delta = fmax(delta, 2.0 * wp);
             if (any_nan5(x) || any_nan5(F)) return 0;
         }
-        return fprev < kLoose32 ? 1 : 0;
+        return 0;
     }
 
     // FP64 refinement + certification of an FP32 solution; fills c.  A certified candidate
