@@ -136,6 +136,8 @@ typedef struct pnjl_stats {
     int64_t multiseed_fallbacks;
     int64_t kernel_launches;
     double last_kernel_ms;    /* device time of the last solve kernel (CUDA events)     */
+    int64_t fp64_rescues;     /* mixed mode: FP32-Jacobian refinements that stopped
+                                 contracting and were finished by FP64 Newton steps     */
 } pnjl_stats;
 
 /* Default parameter set: config/pnjl/default.toml:1-21 through Constants_PNJL.jl:82-103. */

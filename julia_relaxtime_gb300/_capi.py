@@ -86,6 +86,7 @@ class pnjl_stats(C.Structure):
         ("node_evals_fp64_grad", C.c_int64), ("node_evals_fp64_grad_thermo", C.c_int64),
         ("node_evals_fp32", C.c_int64), ("seeds_run", C.c_int64), ("trust_region_runs", C.c_int64),
         ("multiseed_fallbacks", C.c_int64), ("kernel_launches", C.c_int64), ("last_kernel_ms", C.c_double),
+        ("fp64_rescues", C.c_int64),
     ]
 
 

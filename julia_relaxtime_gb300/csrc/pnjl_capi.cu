@@ -821,6 +821,7 @@ int pnjl_get_stats(const pnjl_ctx *cctx, pnjl_stats *out) {
     st.multiseed_fallbacks = c[pnjl::kStatMsFallbacks];
     st.passes_fp32 = c[pnjl::kStatPasses32];
     st.node_evals_fp32 = c[pnjl::kStatEvals32];
+    st.fp64_rescues = c[pnjl::kStatRescue64];
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1) == cudaSuccess) st.last_kernel_ms = ms;
     *out = st;

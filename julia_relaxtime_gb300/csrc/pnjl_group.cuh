@@ -349,19 +349,22 @@ struct Group {
     }
 
     // 1: reached the FP32 floor, 0: did not converge, -1: residual at x0 not finite.
-    // The FP32 phase ends when the residual is tiny, or when the Newton step has become small
-    // (relative 1e-6) with a small residual -- then one more FP32 step is taken, which brings
-    // x to the FP32 noise floor, so the FP64 refinement usually certifies after one step.
+    // The FP32 phase ends at the first of: a tiny residual; a Newton step at the FP32
+    // resolution (relative kStall32) with a small residual; a small residual that stopped
+    // halving for two steps (the FP32 noise floor, or the linear convergence of a nearly
+    // singular Jacobian, which the FP64 phase then finishes); the iteration limit with a
+    // small residual.
     __device__ int newton32(const PointIn &pt, const double *x0, const SolveOpts &o, double *x, double *J, int &iters) {
         double F[5], p[5];
         for (int i = 0; i < 5; ++i) x[i] = x0[i];
         eval_newton32(pt, x, F, J);
         iters = 0;
         if (!all_finite5(F)) return -1;
-        bool polish = false;
+        int slow = 0;
         for (;;) {
-            if (norm_inf5(F) < kFtol32) return 1;
-            if (iters >= o.max_iter) return 0;
+            const double fn = norm_inf5(F);
+            if (fn < kFtol32) return 1;
+            if (iters >= o.max_iter) return fn < kLoose32 ? 1 : 0;
             if (lu_solve5(J, F, p)) {
                 for (int i = 0; i < 5; ++i) p[i] = -p[i];
             } else {
@@ -373,20 +376,25 @@ struct Group {
             ++iters;
             eval_newton32(pt, x, F, J);
             if (any_nan5(x) || any_nan5(F)) return 0;
-            if (polish) return 1;
-            if (pn <= kStall32 * (1.0 + xn) && norm_inf5(F) < kLoose32) polish = true;
+            const double fnew = norm_inf5(F);
+            if (fnew < kLoose32) {
+                if (pn <= kStall32 * (1.0 + xn)) return 1;
+                slow = fnew > 0.5 * fn ? slow + 1 : 0;
+                if (slow >= 2) return 1;
+            }
         }
     }
 
-    // NLsolve-style dogleg trust region on FP32 passes; same return codes as newton32
+    // NLsolve-style dogleg trust region on FP32 passes; same return codes and stop rules as
+    // newton32, plus a trust radius collapsed to the FP32 resolution with a small residual.
     __device__ int tr32(const PointIn &pt, const double *x0, const SolveOpts &o, double *x, double *Jacc, int &iters) {
-        double d[5], p[5], r[5], F[5], J[25];
+        double d[5], p[5], r[5], F[5], J[25], xt[5];
         for (int i = 0; i < 5; ++i) x[i] = x0[i];
         eval_newton32(pt, x, r, Jacc);
         iters = 0;
         if (!all_finite5(r)) return -1;
-        if (norm_inf5(r) < kFtol32) return 1;
-        double fprev = norm_inf5(r);
+        double fr = norm_inf5(r);
+        if (fr < kFtol32) return 1;
         for (int j = 0; j < 5; ++j) {
             double s = 0.0;
             for (int i = 0; i < 5; ++i) s += Jacc[i * 5 + j] * Jacc[i * 5 + j];
@@ -397,12 +405,13 @@ struct Group {
         for (int i = 0; i < 5; ++i) delta += (d[i] * x[i]) * (d[i] * x[i]);
         delta = sqrt(delta);
         if (delta == 0.0) delta = 1.0;
+        int slow = 0;
         while (iters < o.max_iter) {
             ++iters;
             dogleg(p, r, d, Jacc, delta);
             symmetrize_step(pt, x, p);
-            for (int i = 0; i < 5; ++i) x[i] += p[i];
-            eval_newton32(pt, x, F, J);
+            for (int i = 0; i < 5; ++i) xt[i] = x[i] + p[i];
+            eval_newton32(pt, xt, F, J);
             double sr = 0.0, sf = 0.0, sp = 0.0;
             for (int k = 0; k < 5; ++k) {
                 double a = 0.0;
@@ -416,8 +425,9 @@ struct Group {
             double wp = 0.0;
             for (int i = 0; i < 5; ++i) wp += (d[i] * p[i]) * (d[i] * p[i]);
             wp = sqrt(wp);
+            const double xn = norm_inf5(x);
             if (rho > 1e-4) {
-                for (int i = 0; i < 5; ++i) r[i] = F[i];
+                for (int i = 0; i < 5; ++i) { x[i] = xt[i]; r[i] = F[i]; }
                 for (int i = 0; i < 25; ++i) Jacc[i] = J[i];
                 for (int j = 0; j < 5; ++j) {
                     double s = 0.0;
@@ -425,44 +435,60 @@ struct Group {
                     const double cn = sqrt(s);
                     d[j] = (0.1 * d[j] > cn) ? 0.1 * d[j] : cn;
                 }
-                const double fold = fprev;
                 const double fn = norm_inf5(r);
+                if (any_nan5(x) || !(fn == fn)) return 0;
                 if (fn < kFtol32) return 1;
-                if (fn < kLoose32 && norm_inf5(p) <= kStall32 * (1.0 + norm_inf5(x))) return 1;
-                (void)fold;
-                fprev = fn;
-            } else {
-                for (int i = 0; i < 5; ++i) x[i] -= p[i];
+                if (fn < kLoose32) {
+                    if (norm_inf5(p) <= kStall32 * (1.0 + xn)) return 1;
+                    slow = fn > 0.5 * fr ? slow + 1 : 0;
+                    if (slow >= 2) return 1;
+                }
+                fr = fn;
             }
             if (rho < 0.1) delta = delta / 2.0;
             else if (rho >= 0.9) delta = 2.0 * wp;
             else if (rho >= 0.5) delta = fmax(delta, 2.0 * wp);
-            if (any_nan5(x) || any_nan5(F)) return 0;
+            if (fr < kLoose32 && delta <= kStall32 * (1.0 + xn)) return 1;
+            if (!(delta > 0.0)) return 0;
         }
-        return 0;
+        return fr < kLoose32 ? 1 : 0;
     }
 
-    // FP64 refinement + certification of an FP32 solution; fills c.  A certified candidate
-    // gets its thermo from an FP64 pass at its final x; an uncertified one is reported with
-    // f_converged = false and no thermo.
+    // FP64 refinement + certification of an FP32 solution; fills c.  Steps use the FP32
+    // Jacobian; when they stop contracting (residual not halved) or reach kMaxRefine, FP64
+    // Newton steps (FP64 Hessian passes) continue from the best state, so the mixed mode
+    // converges wherever the FP64 path does.  A certified candidate gets its thermo from an
+    // FP64 pass at its final x.
     __device__ void refine64(const PointIn &pt, const SolveOpts &o, const double *J32, const double *x32, Candidate &c,
                              int &steps) {
-        double F[5], p[5], LU[25];
+        double F[5], p[5], LU[25], xb[5];
         int piv[5];
         const bool factored = lu_factor5(J32, LU, piv);
-        for (int i = 0; i < 5; ++i) c.x[i] = x32[i];
+        for (int i = 0; i < 5; ++i) c.x[i] = xb[i] = x32[i];
         c.exception = false;
         c.phys = false;
         c.omega = c.entropy = qnan();
         eval_grad64(pt, c.x, F);
         steps = 0;
         bool thermo_at_x = false;
+        double fb = 0.0, fprev = 0.0;
         for (;;) {
             const double fn = norm_inf5(F);
             c.residual_norm = fn;
-            if (!(fn == fn) || any_nan5(c.x)) { c.f_converged = false; break; }
-            if (fn < o.ftol) { c.f_converged = true; break; }
-            if (steps >= kMaxRefine) { c.f_converged = false; break; }
+            const bool bad = !(fn == fn) || any_nan5(c.x);
+            if (!bad && fn < o.ftol) { c.f_converged = true; break; }
+            if (!bad && (steps == 0 || fn < fb)) {
+                for (int i = 0; i < 5; ++i) xb[i] = c.x[i];
+                fb = fn;
+            }
+            if (bad || steps >= kMaxRefine || (steps > 0 && !(fn <= 0.5 * fprev))) {
+                const int used = steps;
+                cnt.v[kStatRescue64] += 1;
+                newton(pt, xb, o, c);
+                steps = used + c.iterations;
+                return;
+            }
+            fprev = fn;
             if (factored) {
                 lu_solve_factored5(LU, piv, F, p);
                 for (int i = 0; i < 5; ++i) p[i] = -p[i];
@@ -475,8 +501,7 @@ struct Group {
             eval_grad_thermo64(pt, o, c, F);
             thermo_at_x = true;
         }
-        if (c.f_converged && !thermo_at_x) eval_thermo(pt, o, c);
-        if (!c.f_converged) c.phys = false;
+        if (!thermo_at_x) eval_thermo(pt, o, c);
     }
 
     // Mixed-precision counterpart of solve_seed.  `dup` is set when the FP32 solution equals

@@ -30,7 +30,7 @@ struct CandRec {
 // Counter slots of SolveArgs::stats
 enum StatSlot {
     kStatPasses64 = 0, kStatEvalsNewton64, kStatEvalsThermo64, kStatSeeds, kStatTrRuns, kStatMsFallbacks,
-    kStatPasses32, kStatEvals32, kStatEvalsGrad64, kStatEvalsGradThermo64, kStatCount
+    kStatPasses32, kStatEvals32, kStatEvalsGrad64, kStatEvalsGradThermo64, kStatRescue64, kStatCount
 };
 
 struct SolveArgs {
