@@ -3,18 +3,28 @@
 
 Workload (default ``--workload aniso_scan_256x256x9``): the batched anisotropic scan
 T = linspace(50, 300, 256) MeV x mu = linspace(0, 400, 256) MeV x xi in {-0.4, ..., 0.4}
-(589,824 points), 128 momentum x 32 cos(theta) Gauss-Legendre nodes, the first four
-MultiSeed candidates per point with min-Omega selection, FP64 Newton with the trust-region
-fallback, converged when ||grad_x Omega||_inf < 1e-10.  A "step" solves one strided slice
-of the grid (every n_chunks-th point, a different slice each step), so the timed steps are
-spread over the whole (T, mu, xi) box.  Inputs (T, mu, xi) are synthetic grid points: there
-is no dataset.
+(589,824 points), 128 momentum x 32 cos(theta) Gauss-Legendre nodes, converged when
+||grad_x Omega||_inf < 1e-10.  A "step" solves one strided slice of the grid (every
+n_chunks-th point, a different slice each step), so the timed steps are spread over the whole
+(T, mu, xi) box.  Inputs (T, mu, xi) are synthetic grid points: there is no dataset.
 
-value: converged solves per second with inputs already in HBM (pnjl_solve_batch_device),
-timed with CUDA events on the library's stream; e2e: the same metric through the host-pointer
-entry point pnjl_solve_batch, pinned host inputs, host<->device copies inside the timed region.
-``--impl reference`` times the reference algorithm's CPU restatement (the oracle: nested
-forward-mode derivatives like the reference's ForwardDiff, NLsolve-style Newton) on a bounded
+Headline (``--mode surrogate``): surrogate-seeded mixed-precision solves -- the trained
+network's seed per point (BF16 tensor-core inference kernel), one mixed-precision Newton solve
+(FP32 Kahan node passes, FP64 solve/update/residual), verification by two MultiSeed
+candidates where a second phase can exist, MultiSeed fallback where the learned seed fails.
+The network is trained in an untimed set-up on this GPU (labels: a 64 x 64 x 5 (T, mu, xi)
+multi-seed solve; 400 epochs), reported as ``surrogate.train``.  The same chunks are then
+solved by the plain FP64 multi-seed Newton (the first four MultiSeed candidates, min-Omega
+selection, trust-region fallback): ``plain_fp64`` holds its rate, the speed-up, and the phase
+misassignments of the surrogate path against it.  ``--mode multiseed --precision fp64|mixed``
+times the MultiSeed table path alone.
+
+value: converged solves per second with inputs already in HBM (pnjl_solve_batch_learned_device
+or pnjl_solve_batch_device), timed with CUDA events on the library's stream; e2e: the same
+metric through the host-array entry point (pnjl_solve_batch_learned / pnjl_solve_batch),
+pinned host inputs, host<->device copies inside the timed region.  ``--impl reference``
+times the reference algorithm's CPU restatement (the oracle: nested forward-mode derivatives
+like the reference's ForwardDiff, NLsolve-style Newton, MultiSeed min-Omega) on a bounded
 sample of the same workload with all host threads.
 """
 from __future__ import annotations
@@ -36,7 +46,7 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 HBARC = 197.327
-METRIC = "gap solves/s at ||dOmega|| <= 1e-10"
+METRIC = "gap solves/s at \u2016\u2202\u03a9\u2016\u22641e-10: surrogate-seeded vs plain FP64 Newton, 1 GB300"
 # Floating-point operations per node-flavour evaluation, counted from the source of
 # pnjl_device.cuh::node_flavour (FMA = 2, loop invariants hoisted, selects and compares not
 # counted; the transcendental calls -- rsqrt, exp, rcp, and log in thermo passes -- are
@@ -157,6 +167,18 @@ def run_reference(args, grid, sample_points: int):
                 sample=f"{len(idx)} points drawn uniformly (seed 1234) from the workload grid, per step")
 
 
+class Arm:
+    """One solve configuration timed over the same strided chunks of the grid."""
+
+    def __init__(self, name, eng, table, hot, opts, learned):
+        self.name, self.eng, self.table, self.hot, self.opts, self.learned = name, eng, table, hot, opts, learned
+
+    def launch(self, n, d_in, ptrs):
+        m = d_in["mu"].data_ptr()
+        self.eng.solve_device(n, d_in["T"].data_ptr(), m, m, m, d_in["xi"].data_ptr(), ptrs, seed_table=self.table,
+                              seed_table_hot=self.hot, opts=self.opts, learned=self.learned)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__)
     ap.add_argument("--gpus", type=int, default=1)
@@ -164,22 +186,28 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=("gpu", "reference"))
     ap.add_argument("--workload", default="aniso_scan_256x256x9")
-    ap.add_argument("--chunks", type=int, default=64, help="the grid is solved in this many strided slices")
-    ap.add_argument("--precision", default="fp64", choices=("fp64", "mixed"))
+    ap.add_argument("--mode", default="surrogate", choices=("surrogate", "multiseed"),
+                    help="surrogate: learned seed + mixed precision (headline); multiseed: the MultiSeed table")
+    ap.add_argument("--precision", default=None, choices=("fp64", "mixed"),
+                    help="precision of the timed arm (default: mixed for surrogate, fp64 for multiseed)")
+    ap.add_argument("--chunks", type=int, default=32, help="the grid is solved in this many strided slices")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 multi-seed comparison arm")
     ap.add_argument("--cpu-sample", type=int, default=48, help="points per step of the CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--lanes", type=int, default=32)
+    ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    precision = args.precision or ("mixed" if args.mode == "surrogate" else "fp64")
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     grid = workload_grid(args.workload)
     config = {"workload": args.workload, "grid": grid["desc"], "points": int(grid["T"].size),
-              "points_per_step": int(math.ceil(grid["T"].size / args.chunks)), "ftol": 1e-10, "max_iter": 40,
-              "precision": args.precision, "l2": "256 MiB device buffer written before every timed step"}
+              "points_per_step": int(math.ceil(grid["T"].size / world / args.chunks)), "ftol": 1e-10,
+              "max_iter": 40, "mode": args.mode, "precision": precision,
+              "l2": "256 MiB device buffer written before every timed step"}
 
     if args.impl == "reference":
         if rank != 0:
@@ -204,12 +232,25 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
     torch.cuda.set_device(local_rank)
     from julia_relaxtime_gb300.engine import GapEngine, SolveOptions
+    from julia_relaxtime_gb300.learned_seed import TrainConfig, default_learned_opts, train_learned_seed
     from julia_relaxtime_gb300.pnjl import multiseed_table
 
     eng = GapEngine(device=local_rank, p_num=grid["p_num"], t_num=grid["t_num"])
-    eng.set_tuning(args.lanes, 0)
     table, hot = multiseed_table(grid["n_seeds"])
-    opts = SolveOptions(iterations=40, ftol=1e-10, precision=args.precision)
+    train = None
+    if args.mode == "surrogate":
+        # set-up, untimed: label the 64 x 64 x 5 training grid with the multi-seed solver and
+        # train the network on it (both on this GPU); reported as train_s
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ls = train_learned_seed(eng, TrainConfig())
+        train = {"seconds": time.perf_counter() - t0, "labels": "64 x 64 x 5 (T, mu, xi) grid, MultiSeed (6) mixed",
+                 "epochs": TrainConfig().epochs}
+        arm = Arm("surrogate", eng, table, hot, default_learned_opts(ftol=1e-10, precision=precision), True)
+    else:
+        arm = Arm("multiseed", eng, table, hot, SolveOptions(iterations=40, ftol=1e-10, precision=precision), False)
+    plain = Arm("plain_fp64", eng, table, hot, SolveOptions(iterations=40, ftol=1e-10, precision="fp64"), False)
+
     # this rank's share of the points: a strided shard (no data exchange between ranks)
     T_all, mu_all, xi_all = grid["T"][rank::world], grid["mu"][rank::world], grid["xi"][rank::world]
     chunks = [np.arange(c, T_all.size, args.chunks) for c in range(args.chunks)]
@@ -238,102 +279,146 @@ def main():
         stream.synchronize()
         return n
 
-    def solve_chunk(n):
-        m = d_in["mu"].data_ptr()
-        eng.solve_device(n, d_in["T"].data_ptr(), m, m, m, d_in["xi"].data_ptr(), ptrs, seed_table=table,
-                         seed_table_hot=hot, opts=opts)
+    def run_arm(a: Arm, steps: int, warmup: int, sample_clocks: bool):
+        for w in range(warmup):
+            n = load_chunk(args.chunks - 1 - (w % args.chunks))
+            a.launch(n, d_in, ptrs)
+            eng.synchronize()
+        sampler = ClockSampler(local_rank) if sample_clocks else None
+        rec = {"step_ms": [], "kernel_ms": [], "solved": 0, "flops64": 0.0, "flops32": 0.0, "evals": 0, "kinds": {},
+               "results": []}
+        launches0 = eng.stats()["kernel_launches"]
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+        if sampler:
+            sampler.start()
+        for k in range(steps):
+            n = load_chunk(k % args.chunks)
+            with torch.cuda.stream(stream):
+                flush.fill_(k & 0xFF)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            a.launch(n, d_in, ptrs)
+            e1.record(stream)
+            e1.synchronize()
+            rec["step_ms"].append(e0.elapsed_time(e1))
+            st = eng.stats()
+            rec["kernel_ms"].append(st["last_kernel_ms"])
+            rec["evals"] += st["node_evals_fp64"] + st["node_evals_fp32"]
+            f64_, f32_ = pass_flops(st)
+            rec["flops64"] += f64_
+            rec["flops32"] += f32_
+            for kk in ("node_evals_fp64_newton", "node_evals_fp64_thermo", "node_evals_fp64_grad",
+                       "node_evals_fp64_grad_thermo", "node_evals_fp32", "seeds_run", "trust_region_runs",
+                       "multiseed_fallbacks", "fp64_rescues"):
+                rec["kinds"][kk] = rec["kinds"].get(kk, 0) + st[kk]
+            conv = d_out["converged"][:n].cpu().numpy().astype(bool)
+            res = d_out["residual_norm"][:n].cpu().numpy()
+            rec["solved"] += int(np.sum(conv & (res <= 1e-10)))
+            rec["results"].append({"converged": conv, "x": d_out["x"][:5 * n].cpu().numpy().reshape(n, 5),
+                                   "omega": d_out["omega"][:n].cpu().numpy()})
+        torch.cuda.synchronize()
+        rec["clocks"] = sampler.stop() if sampler else None
+        rec["launches"] = eng.stats()["kernel_launches"] - launches0
+        total_ms = sum(rec["step_ms"])
+        solved = rec["solved"]
+        if dist is not None:
+            t = torch.tensor([total_ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            total_ms = float(t.item())
+            s_ = torch.tensor([solved], device=dev, dtype=torch.float64)
+            dist.all_reduce(s_)
+            solved = int(s_.item())
+        rec["total_ms"] = total_ms
+        rec["value"] = solved / (total_ms * 1e-3)
+        return rec
 
-    # warm-up (untimed) on the last chunks
-    for w in range(args.warmup):
-        n = load_chunk(args.chunks - 1 - (w % args.chunks))
-        solve_chunk(n)
-        eng.synchronize()
+    main_rec = run_arm(arm, args.steps, args.warmup, True)
 
-    # timed region: K steps, device inputs already resident per step (loaded before the events)
-    sampler = ClockSampler(local_rank)
-    kernel_ms, step_ms, solved, evals, flops, flops32 = [], [], 0, 0, 0, 0
-    kinds = {}
-    launches0 = eng.stats()["kernel_launches"]
-    if dist is not None:
-        dist.barrier()
-    torch.cuda.synchronize()
-    sampler.start()
-    for k in range(args.steps):
-        n = load_chunk(k % args.chunks)
-        with torch.cuda.stream(stream):
-            flush.fill_(k & 0xFF)
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        solve_chunk(n)
-        e1.record(stream)
-        e1.synchronize()
-        step_ms.append(e0.elapsed_time(e1))
-        st = eng.stats()
-        kernel_ms.append(st["last_kernel_ms"])
-        evals += st["node_evals_fp64"] + st["node_evals_fp32"]
-        f64, f32 = pass_flops(st)
-        for kk in ("node_evals_fp64_newton", "node_evals_fp64_thermo", "node_evals_fp64_grad",
-                   "node_evals_fp64_grad_thermo", "node_evals_fp32", "seeds_run", "trust_region_runs",
-                   "multiseed_fallbacks"):
-            kinds[kk] = kinds.get(kk, 0) + st[kk]
-        flops += f64
-        flops32 += f32
-        conv = d_out["converged"][:n].cpu().numpy().astype(bool)
-        res = d_out["residual_norm"][:n].cpu().numpy()
-        solved += int(np.sum(conv & (res <= 1e-10)))
-    torch.cuda.synchronize()
-    clocks = sampler.stop()
-    launches = eng.stats()["kernel_launches"] - launches0
-    total_ms = sum(step_ms)
-    if dist is not None:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-        s = torch.tensor([solved], device=dev, dtype=torch.float64)
-        dist.all_reduce(s)
-        solved = int(s.item())
-    value = solved / (total_ms * 1e-3)
+    # the plain FP64 multi-seed Newton on the same chunks: the denominator of the speed-up and
+    # the FP64 judge of the surrogate's phase selection
+    plain_line = None
+    if args.mode == "surrogate" and not args.no_plain:
+        prec = run_arm(plain, args.steps, 1, False)
+        mis, dphi, dPhi, both_n = 0, 0.0, 0.0, 0
+        for r, q in zip(main_rec["results"], prec["results"]):
+            both = r["converged"] & q["converged"]
+            both_n += int(both.sum())
+            om, oq = r["omega"][both], q["omega"][both]
+            mis += int(np.sum(np.abs(om - oq) > 1e-10 * np.maximum(np.abs(oq), 1.0)))
+            xr, xq = r["x"][both], q["x"][both]
+            same = np.abs(om - oq) <= 1e-10 * np.maximum(np.abs(oq), 1.0)
+            if same.any():
+                dphi = max(dphi, float(np.max(np.abs(xr[same, :3] - xq[same, :3]) /
+                                              np.maximum(np.abs(xq[same, :3]), 1e-300))))
+                dPhi = max(dPhi, float(np.max(np.abs(xr[same, 3:] - xq[same, 3:]))))
+        plain_line = {"value": prec["value"], "unit": "solves/s", "ms_per_step": prec["total_ms"] / args.steps,
+                      "precision": "fp64", "seeds": grid["n_seeds"], "speedup": main_rec["value"] / prec["value"],
+                      "phase_misassignments": mis, "points_compared": both_n, "max_rel_dphi": dphi,
+                      "max_abs_dPhi": dPhi,
+                      "work_per_step": {k: v / args.steps for k, v in prec["kinds"].items()}}
 
-    # e2e: the host-pointer C-ABI call with pinned host buffers, copies inside the timed region
-    e2e_solved, e2e_s, h2d, d2h = 0, 0.0, 0, 0
-    for k in range(args.steps):
-        idx = chunks[k % args.chunks]
-        n = idx.size
-        Th = torch.from_numpy(T_all[idx]).pin_memory().numpy()
-        Mh = torch.from_numpy(mu_all[idx]).pin_memory().numpy()
-        Xh = torch.from_numpy(xi_all[idx]).pin_memory().numpy()
-        t0 = time.perf_counter()
-        r = eng.solve(Th, Mh, Xh, seed_table=table, seed_table_hot=hot, opts=opts)
-        e2e_s += time.perf_counter() - t0
-        e2e_solved += int(np.sum(r["converged"] & (r["residual_norm"] <= 1e-10)))
-        h2d = 5 * 8 * n  # T, mu_u, mu_d, mu_s, xi
-        d2h = sum(v.nbytes for v in r.values()) // 1
-    e2e = {"value": e2e_solved / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
-           "d2h_bytes_per_step": int(d2h)}
+    # e2e: the public host-array call (pnjl_solve_batch_learned / pnjl_solve_batch) with pinned
+    # host buffers; host<->device copies inside the timed region
+    e2e = None
+    if not args.no_e2e:
+        e2e_solved, e2e_s, h2d, d2h = 0, 0.0, 0, 0
+        for k in range(args.steps):
+            idx = chunks[k % args.chunks]
+            n = idx.size
+            Th = torch.from_numpy(T_all[idx]).pin_memory().numpy()
+            Mh = torch.from_numpy(mu_all[idx]).pin_memory().numpy()
+            Xh = torch.from_numpy(xi_all[idx]).pin_memory().numpy()
+            t0 = time.perf_counter()
+            if arm.learned:
+                r = ls.solve(Th, Mh, Xh, opts=arm.opts)
+            else:
+                r = eng.solve(Th, Mh, Xh, seed_table=table, seed_table_hot=hot, opts=arm.opts)
+            e2e_s += time.perf_counter() - t0
+            e2e_solved += int(np.sum(r["converged"] & (r["residual_norm"] <= 1e-10)))
+            h2d = 5 * 8 * n  # T, mu_u, mu_d, mu_s, xi
+            d2h = sum(v.nbytes for v in r.values())
+        e2e = {"value": e2e_solved / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h)}
 
     if rank != 0:
+        eng.close()
+        if dist is not None:
+            dist.destroy_process_group()
         return
     peak_fp64 = eng.probe_peak("fp64")
     peak_fp32 = eng.probe_peak("fp32")
-    avg_kernel_s = (sum(kernel_ms) / len(kernel_ms)) * 1e-3
-    ach64 = flops / args.steps / avg_kernel_s
-    ach32 = flops32 / args.steps / avg_kernel_s
-    kname = "solve_kernel<32>" if args.precision == "fp64" else "solve_kernel_mixed<32>"
+    avg_kernel_s = (sum(main_rec["kernel_ms"]) / len(main_rec["kernel_ms"])) * 1e-3
+    ach64 = main_rec["flops64"] / args.steps / avg_kernel_s
+    ach32 = main_rec["flops32"] / args.steps / avg_kernel_s
+    kname = "solve_kernel<32>" if precision == "fp64" else "solve_kernel_mixed<32>"
     roof = {"bound": "fp64", "kernel": kname, "achieved": ach64 / 1e12, "peak": peak_fp64 / 1e12,
             "unit": "TFLOP/s", "frac": ach64 / peak_fp64,
-            "peak_source": "measured in-run (pnjl_probe_peak, FMA chains on every lane of the GPU)",
+            "peak_source": "measured in-run (pnjl_probe_peak: FP64 FMA chains on every lane of the GPU); "
+                           "no HBM or tensor-core bound applies to this compute-bound path",
             "flop_per_node_flavour": {"newton_pass": FLOP_NEWTON, "thermo_pass": FLOP_THERMO,
                                       "residual_pass": FLOP_GRAD, "residual_thermo_pass": FLOP_GRAD_THERMO,
                                       "newton_pass_fp32": FLOP_NEWTON32},
-            "node_flavour_evals_per_launch": evals / args.steps, "traffic": None,
+            "node_flavour_evals_per_launch": main_rec["evals"] / args.steps, "kernel_ms": avg_kernel_s * 1e3,
+            "traffic": None,
             "fp32": {"achieved": ach32 / 1e12, "peak": peak_fp32 / 1e12, "frac": ach32 / peak_fp32}}
-    line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+    launches = main_rec["launches"]
+    line = {"metric": METRIC, "value": main_rec["value"], "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": main_rec["total_ms"] / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if precision == "fp64" else "f32+f64",
             "data": "synthetic", "config": config, "e2e": e2e, "gpu_launches": int(launches),
-            "roofline": roof, "clocks": clocks, "solved": solved,
-            "work_per_step": {k: v / args.steps for k, v in kinds.items()}}
+            "roofline": roof, "clocks": main_rec["clocks"], "solved": main_rec["solved"],
+            "work_per_step": {k: v / args.steps for k, v in main_rec["kinds"].items()}}
+    if train is not None:
+        line["surrogate"] = {"train": train,
+                             "fallback_rate": main_rec["kinds"].get("multiseed_fallbacks", 0) /
+                             max(1, config["points_per_step"] * args.steps),
+                             "verify": {"seeds": arm.opts.verify_seeds, "T_max_MeV": arm.opts.verify_T_max_MeV,
+                                        "max_step": arm.opts.verify_max_step}}
+    if plain_line is not None:
+        line["plain_fp64"] = plain_line
     if not args.no_cpu_baseline:
         class A:  # noqa: N801
             warmup, steps = 0, 1

@@ -244,6 +244,11 @@ int pnjl_mlp_set_params(pnjl_ctx *ctx, const float *in, int64_t count);
 int pnjl_solve_batch_learned_device(pnjl_ctx *ctx, int64_t n, const double *d_T, const double *d_mu_u,
                                     const double *d_mu_d, const double *d_mu_s, const double *d_xi,
                                     const pnjl_solve_opts *opts, pnjl_result_soa *d_out);
+/* Same with host pointers, synchronous (the end-to-end call: the host<->device copies of
+ * the inputs and results are part of it, like pnjl_solve_batch). */
+int pnjl_solve_batch_learned(pnjl_ctx *ctx, int64_t n, const double *T, const double *mu_u,
+                             const double *mu_d, const double *mu_s, const double *xi,
+                             const pnjl_solve_opts *opts, pnjl_result_soa *out);
 
 /* Largest batch of pnjl_solve_batch_noalloc, counted in tasks: n * n_seeds in
  * PNJL_SEEDS_TABLE mode, n in PNJL_SEEDS_PER_POINT mode (and n itself at most this). */

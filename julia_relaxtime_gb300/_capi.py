@@ -122,6 +122,8 @@ SIGNATURES = {
     "pnjl_mlp_set_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int64]),
     "pnjl_solve_batch_learned_device": (C.c_int, [C.c_void_p, C.c_int64, dp, dp, dp, dp, dp,
                                                   C.POINTER(pnjl_solve_opts), C.POINTER(pnjl_result_soa)]),
+    "pnjl_solve_batch_learned": (C.c_int, [C.c_void_p, C.c_int64, dp, dp, dp, dp, dp,
+                                           C.POINTER(pnjl_solve_opts), C.POINTER(pnjl_result_soa)]),
     "pnjl_solve_batch_noalloc": (C.c_int, [C.POINTER(pnjl_params), C.c_int32, C.c_int32, C.c_double, C.c_int64,
                                            dp, dp, dp, dp, dp, C.POINTER(pnjl_solve_opts),
                                            C.POINTER(pnjl_result_soa), C.c_void_p]),

@@ -721,18 +721,25 @@ int pnjl_solve_batch_learned_device(pnjl_ctx *ctx, int64_t n, const double *d_T,
     return pnjl_solve_batch_device(ctx, n, d_T, d_mu_u, d_mu_d, d_mu_s, d_xi, &o, d_out);
 }
 
-int pnjl_solve_batch(pnjl_ctx *ctx, int64_t n, const double *T, const double *mu_u, const double *mu_d,
-                     const double *mu_s, const double *xi, const pnjl_solve_opts *opts, pnjl_result_soa *out) {
+// Host-pointer solve: inputs to the workspace, the device solve (multi-seed/per-point, or
+// learned-seed), results back; synchronous.
+static int solve_batch_host(pnjl_ctx *ctx, int64_t n, const double *T, const double *mu_u, const double *mu_d,
+                            const double *mu_s, const double *xi, const pnjl_solve_opts *opts, pnjl_result_soa *out,
+                            bool learned) {
     if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
     if (ctx->p_num == 0) return fail(ctx, PNJL_ERR_NO_NODES, "call pnjl_set_nodes first");
     int rc = check_opts(ctx, opts);
     if (rc) return rc;
+    if (learned) {
+        rc = mlp_require(ctx, true);
+        if (rc) return rc;
+    }
     if (n < 0 || !out || (n > 0 && (!T || !mu_u || !mu_d || !mu_s || !xi)))
         return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "null array");
     if (n == 0) return PNJL_OK;
     cudaSetDevice(ctx->device);
     const size_t nn = (size_t)n;
-    const bool per_point = opts->seed_mode == PNJL_SEEDS_PER_POINT;
+    const bool per_point = !learned && opts->seed_mode == PNJL_SEEDS_PER_POINT;
     size_t bytes = 5 * carve_size(nn, 8) + (per_point ? carve_size(5 * nn, 8) : 0) + carve_size(5 * nn, 8) +
                    6 * carve_size(nn, 8) + 4 * carve_size(3 * nn, 8) + 3 * carve_size(nn, 4) + carve_size(nn, 1);
     rc = ensure_ws(ctx, bytes);
@@ -768,7 +775,8 @@ int pnjl_solve_batch(pnjl_ctx *ctx, int64_t n, const double *T, const double *mu
         PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dseeds, opts->point_seeds, 5 * nn * 8, cudaMemcpyHostToDevice, s));
         o2.point_seeds = dseeds;
     }
-    rc = pnjl_solve_batch_device(ctx, n, dT, du, dd, ds, dxi, &o2, &d);
+    rc = learned ? pnjl_solve_batch_learned_device(ctx, n, dT, du, dd, ds, dxi, &o2, &d)
+                 : pnjl_solve_batch_device(ctx, n, dT, du, dd, ds, dxi, &o2, &d);
     if (rc) return rc;
 #define PNJL_D2H(field, count, elem)                                                                              \
     if (out->field)                                                                                                \
@@ -791,6 +799,17 @@ int pnjl_solve_batch(pnjl_ctx *ctx, int64_t n, const double *T, const double *mu
 #undef PNJL_D2H
     PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(s));
     return pnjl_get_stats(ctx, &ctx->stats) == PNJL_OK ? PNJL_OK : PNJL_ERR_CUDA;
+}
+
+int pnjl_solve_batch(pnjl_ctx *ctx, int64_t n, const double *T, const double *mu_u, const double *mu_d,
+                     const double *mu_s, const double *xi, const pnjl_solve_opts *opts, pnjl_result_soa *out) {
+    return solve_batch_host(ctx, n, T, mu_u, mu_d, mu_s, xi, opts, out, false);
+}
+
+int pnjl_solve_batch_learned(pnjl_ctx *ctx, int64_t n, const double *T, const double *mu_u, const double *mu_d,
+                             const double *mu_s, const double *xi, const pnjl_solve_opts *opts,
+                             pnjl_result_soa *out) {
+    return solve_batch_host(ctx, n, T, mu_u, mu_d, mu_s, xi, opts, out, true);
 }
 
 void *pnjl_stream(pnjl_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }

@@ -305,7 +305,7 @@ struct Group {
     static constexpr double kFtol32 = 1e-8;   // FP32 residual that ends the FP32 phase
     static constexpr double kStall32 = 1e-6;  // ... or a relative step this small ...
     static constexpr double kLoose32 = 1e-3;  // ... with the FP32 residual below this
-    static constexpr int kMaxRefine = 6;
+    static constexpr int kMaxRefine = 8;
 
     __device__ __noinline__ void eval_newton32(const PointIn &pt, const double *x, double *F, double *J) {
         double M[3];
@@ -454,16 +454,17 @@ struct Group {
         return fr < kLoose32 ? 1 : 0;
     }
 
-    // FP64 refinement + certification of an FP32 solution; fills c.  Steps use the FP32
-    // Jacobian; when they stop contracting (residual not halved) or reach kMaxRefine, FP64
-    // Newton steps (FP64 Hessian passes) continue from the best state, so the mixed mode
-    // converges wherever the FP64 path does.  A certified candidate gets its thermo from an
-    // FP64 pass at its final x.
+    // FP64 refinement + certification of an FP32 solution; fills c.  Steps start from the
+    // FP32 Jacobian and improve it with Broyden's rank-one secant update after every FP64
+    // residual, B <- B + (dF - B dx) dx' / (dx' dx), so an inaccurate J32 (ill-conditioned
+    // roots) still converges superlinearly.  When the residual stops decreasing or kMaxRefine
+    // steps are spent, FP64 Newton steps (FP64 Hessian passes) continue from the best state,
+    // so the mixed mode converges wherever the FP64 path does.  A certified candidate gets its
+    // thermo from an FP64 pass at its final x.
     __device__ void refine64(const PointIn &pt, const SolveOpts &o, const double *J32, const double *x32, Candidate &c,
                              int &steps) {
-        double F[5], p[5], LU[25], xb[5];
-        int piv[5];
-        const bool factored = lu_factor5(J32, LU, piv);
+        double F[5], Fo[5], p[5], B[25], xb[5];
+        for (int i = 0; i < 25; ++i) B[i] = J32[i];
         for (int i = 0; i < 5; ++i) c.x[i] = xb[i] = x32[i];
         c.exception = false;
         c.phys = false;
@@ -481,7 +482,7 @@ struct Group {
                 for (int i = 0; i < 5; ++i) xb[i] = c.x[i];
                 fb = fn;
             }
-            if (bad || steps >= kMaxRefine || (steps > 0 && !(fn <= 0.5 * fprev))) {
+            if (bad || steps >= kMaxRefine || (steps > 0 && !(fn < fprev))) {
                 const int used = steps;
                 cnt.v[kStatRescue64] += 1;
                 newton(pt, xb, o, c);
@@ -489,17 +490,26 @@ struct Group {
                 return;
             }
             fprev = fn;
-            if (factored) {
-                lu_solve_factored5(LU, piv, F, p);
+            if (lu_solve5(B, F, p)) {
                 for (int i = 0; i < 5; ++i) p[i] = -p[i];
             } else {
-                levenberg_step(J32, F, p);
+                levenberg_step(B, F, p);
             }
             symmetrize_step(pt, c.x, p);
-            for (int i = 0; i < 5; ++i) c.x[i] += p[i];
+            for (int i = 0; i < 5; ++i) { c.x[i] += p[i]; Fo[i] = F[i]; }
             ++steps;
             eval_grad_thermo64(pt, o, c, F);
             thermo_at_x = true;
+            double pp = 0.0;
+            for (int i = 0; i < 5; ++i) pp += p[i] * p[i];
+            if (pp > 0.0) {
+                for (int i = 0; i < 5; ++i) {
+                    double r = F[i] - Fo[i];
+                    for (int j = 0; j < 5; ++j) r -= B[i * 5 + j] * p[j];
+                    r /= pp;
+                    for (int j = 0; j < 5; ++j) B[i * 5 + j] += r * p[j];
+                }
+            }
         }
         if (!thermo_at_x) eval_thermo(pt, o, c);
     }

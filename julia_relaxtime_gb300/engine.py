@@ -178,17 +178,19 @@ class GapEngine:
         return o
 
     def solve(self, T, mu, xi, *, seed_table=None, seed_table_hot=None, hot_T_MeV: float = 300.0,
-              point_seeds=None, opts: SolveOptions | None = None) -> BatchResult:
+              point_seeds=None, opts: SolveOptions | None = None, learned: bool = False) -> BatchResult:
         """Batched solve(::FixedMu) over host arrays (synchronous; includes the copies).
 
         seed_table [S,5]: MultiSeed candidates (min-Omega selection) and the fallback table.
         point_seeds [n,5]: one seed per point (ContinuitySeed-like); None selects table mode.
+        learned: the trained network's seed per point, computed on the device
+        (pnjl_solve_batch_learned); seed_table is then the fallback and verification table.
         """
         opts = opts or SolveOptions()
         n, T, mu_u, mu_d, mu_s, xi = self._point_arrays(T, mu, xi)
         st = None if seed_table is None else _f64(seed_table).reshape(-1, 5)
         sth = None if seed_table_hot is None else _f64(seed_table_hot).reshape(-1, 5)
-        ps = None if point_seeds is None else _f64(point_seeds, shape=(n, 5))
+        ps = None if point_seeds is None or learned else _f64(point_seeds, shape=(n, 5))
         o = self._opts_struct(opts, st, sth, hot_T_MeV, ps is not None, ps)
         out = BatchResult(
             x=np.zeros((n, 5)), omega=np.zeros(n), pressure=np.zeros(n), rho_norm=np.zeros(n), entropy=np.zeros(n),
@@ -199,28 +201,31 @@ class GapEngine:
         for k, v in out.items():
             ptr_t = api.i32p if v.dtype == np.int32 else (api.u8p if v.dtype == np.uint8 else api.dp)
             setattr(soa, k, v.ctypes.data_as(ptr_t))
-        rc = self._lib.pnjl_solve_batch(self._ctx, n, _dp(T), _dp(mu_u), _dp(mu_d), _dp(mu_s), _dp(xi),
-                                        C.byref(o), C.byref(soa))
-        self._check(rc, "pnjl_solve_batch")
+        fn = self._lib.pnjl_solve_batch_learned if learned else self._lib.pnjl_solve_batch
+        rc = fn(self._ctx, n, _dp(T), _dp(mu_u), _dp(mu_d), _dp(mu_s), _dp(xi), C.byref(o), C.byref(soa))
+        self._check(rc, "pnjl_solve_batch_learned" if learned else "pnjl_solve_batch")
         out["converged"] = out["converged"].astype(bool)
         return out
 
     def solve_device(self, n: int, d_T: int, d_mu_u: int, d_mu_d: int, d_mu_s: int, d_xi: int, d_out: dict, *,
                      seed_table=None, seed_table_hot=None, hot_T_MeV: float = 300.0, d_point_seeds: int = 0,
-                     opts: SolveOptions | None = None):
-        """Asynchronous solve on device pointers (integers); d_out maps result fields to device pointers."""
+                     opts: SolveOptions | None = None, learned: bool = False):
+        """Asynchronous solve on device pointers (integers); d_out maps result fields to device pointers.
+        learned: seeds from the trained network (pnjl_solve_batch_learned_device)."""
         opts = opts or SolveOptions()
         st = None if seed_table is None else _f64(seed_table).reshape(-1, 5)
         sth = None if seed_table_hot is None else _f64(seed_table_hot).reshape(-1, 5)
-        o = self._opts_struct(opts, st, sth, hot_T_MeV, bool(d_point_seeds), d_point_seeds or None)
+        ps = None if learned else (d_point_seeds or None)
+        o = self._opts_struct(opts, st, sth, hot_T_MeV, ps is not None, ps)
         soa = api.pnjl_result_soa()
         for k, v in d_out.items():
             ptr_t = dict(iterations=api.i32p, chosen_seed=api.i32p, status=api.i32p, converged=api.u8p).get(k, api.dp)
             setattr(soa, k, C.cast(C.c_void_p(v), ptr_t))
         cast = lambda p: C.cast(C.c_void_p(p), api.dp)  # noqa: E731
-        rc = self._lib.pnjl_solve_batch_device(self._ctx, n, cast(d_T), cast(d_mu_u), cast(d_mu_d), cast(d_mu_s),
-                                               cast(d_xi), C.byref(o), C.byref(soa))
-        self._check(rc, "pnjl_solve_batch_device")
+        fn = self._lib.pnjl_solve_batch_learned_device if learned else self._lib.pnjl_solve_batch_device
+        rc = fn(self._ctx, n, cast(d_T), cast(d_mu_u), cast(d_mu_d), cast(d_mu_s), cast(d_xi), C.byref(o),
+                C.byref(soa))
+        self._check(rc, "pnjl_solve_batch_learned_device" if learned else "pnjl_solve_batch_device")
         self._keep = (st, sth)  # seed tables are read by the async host->device copy
 
     # -- misc ------------------------------------------------------------------------------

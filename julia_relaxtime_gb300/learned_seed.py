@@ -136,14 +136,22 @@ class LearnedSeed(SeedStrategy):
         return self.seeds([theta[0]], [theta[1]], [xi])[0]
 
     def solve(self, T, mu, xi, *, opts: SolveOptions | None = None, multiseed: MultiSeed | None = None):
-        """Learned seed per point, MultiSeed fallback where it does not converge."""
-        opts = opts or SolveOptions(iterations=40)
+        """Learned seed per point (network evaluated on the device), then one Newton solve;
+        MultiSeed fallback where it does not converge, verification seeds where a second
+        phase can exist (opts.verify_*; default_learned_opts())."""
+        opts = opts or default_learned_opts()
         table, hot = (multiseed or MultiSeed()).tables()
         T_arr = np.atleast_1d(np.asarray(T, dtype=np.float64))
-        mu_arr = np.asarray(mu, dtype=np.float64)
-        mu1 = np.broadcast_to(mu_arr if mu_arr.ndim <= 1 else mu_arr[:, 0], T_arr.shape)
-        seeds = self.seeds(T_arr, mu1, np.broadcast_to(np.asarray(xi, dtype=np.float64), T_arr.shape))
-        return self.engine.solve(T_arr, mu, xi, seed_table=table, seed_table_hot=hot, point_seeds=seeds, opts=opts)
+        return self.engine.solve(T_arr, mu, xi, seed_table=table, seed_table_hot=hot, opts=opts, learned=True)
+
+
+def default_learned_opts(**kw) -> SolveOptions:
+    """Options of the learned-seed solve: mixed precision, 40 iterations, and verification by
+    the first two MultiSeed candidates below T = 170 MeV or where the root lies more than 0.3
+    (in fm^-3 / Polyakov units, inf-norm) from the learned seed."""
+    base = dict(iterations=40, precision="mixed", verify_seeds=2, verify_T_max_MeV=170.0, verify_max_step=0.3)
+    base.update(kw)
+    return SolveOptions(**base)
 
 
 def label_grid(engine: GapEngine, cfg: TrainConfig, opts: SolveOptions | None = None):
