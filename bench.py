@@ -246,7 +246,9 @@ def main():
         ls = train_learned_seed(eng, TrainConfig())
         train = {"seconds": time.perf_counter() - t0, "labels": "64 x 64 x 5 (T, mu, xi) grid, MultiSeed (6) mixed",
                  "epochs": TrainConfig().epochs}
-        arm = Arm("surrogate", eng, table, hot, default_learned_opts(ftol=1e-10, precision=precision), True)
+        arm = Arm("surrogate", eng, table, hot,
+                  default_learned_opts(ftol=1e-10, precision=precision, verify_map=ls.verify_map), True)
+        train["verify_map_cells_flagged"] = ls.verify_map.fraction()
     else:
         arm = Arm("multiseed", eng, table, hot, SolveOptions(iterations=40, ftol=1e-10, precision=precision), False)
     plain = Arm("plain_fp64", eng, table, hot, SolveOptions(iterations=40, ftol=1e-10, precision="fp64"), False)
@@ -342,22 +344,25 @@ def main():
     plain_line = None
     if args.mode == "surrogate" and not args.no_plain:
         prec = run_arm(plain, args.steps, 1, False)
-        mis, dphi, dPhi, both_n = 0, 0.0, 0.0, 0
+        mis, dphi, dphi_abs, dPhi, both_n, n_rel = 0, 0.0, 0.0, 0.0, 0, 0
         for r, q in zip(main_rec["results"], prec["results"]):
             both = r["converged"] & q["converged"]
             both_n += int(both.sum())
             om, oq = r["omega"][both], q["omega"][both]
-            mis += int(np.sum(np.abs(om - oq) > 1e-10 * np.maximum(np.abs(oq), 1.0)))
-            xr, xq = r["x"][both], q["x"][both]
             same = np.abs(om - oq) <= 1e-10 * np.maximum(np.abs(oq), 1.0)
-            if same.any():
-                dphi = max(dphi, float(np.max(np.abs(xr[same, :3] - xq[same, :3]) /
-                                              np.maximum(np.abs(xq[same, :3]), 1e-300))))
-                dPhi = max(dPhi, float(np.max(np.abs(xr[same, 3:] - xq[same, 3:]))))
+            mis += int(np.sum(~same))
+            xr, xq = r["x"][both][same], q["x"][both][same]
+            if xr.size:
+                d = np.abs(xr[:, :3] - xq[:, :3])
+                rel = d / np.maximum(np.abs(xq[:, :3]), 1e-300)
+                dphi = max(dphi, float(rel.max()))
+                dphi_abs = max(dphi_abs, float(d.max()))
+                n_rel += int(np.sum(rel.max(axis=1) > 1e-9))
+                dPhi = max(dPhi, float(np.max(np.abs(xr[:, 3:] - xq[:, 3:]))))
         plain_line = {"value": prec["value"], "unit": "solves/s", "ms_per_step": prec["total_ms"] / args.steps,
                       "precision": "fp64", "seeds": grid["n_seeds"], "speedup": main_rec["value"] / prec["value"],
                       "phase_misassignments": mis, "points_compared": both_n, "max_rel_dphi": dphi,
-                      "max_abs_dPhi": dPhi,
+                      "points_rel_dphi_above_1e-9": n_rel, "max_abs_dphi": dphi_abs, "max_abs_dPhi": dPhi,
                       "work_per_step": {k: v / args.steps for k, v in prec["kinds"].items()}}
 
     # e2e: the public host-array call (pnjl_solve_batch_learned / pnjl_solve_batch) with pinned
@@ -415,7 +420,10 @@ def main():
         line["surrogate"] = {"train": train,
                              "fallback_rate": main_rec["kinds"].get("multiseed_fallbacks", 0) /
                              max(1, config["points_per_step"] * args.steps),
-                             "verify": {"seeds": arm.opts.verify_seeds, "T_max_MeV": arm.opts.verify_T_max_MeV,
+                             "verify": {"seeds": grid["n_seeds"] if arm.opts.verify_seeds < 0 else arm.opts.verify_seeds,
+                                        "region": "verification map (flagged cells of the label grid)"
+                                        if arm.opts.verify_map is not None else
+                                        f"T < {arm.opts.verify_T_max_MeV} MeV",
                                         "max_step": arm.opts.verify_max_step}}
     if plain_line is not None:
         line["plain_fp64"] = plain_line

@@ -96,6 +96,16 @@ typedef struct pnjl_solve_opts {
     double verify_max_step;      /* ... and, at any T, when the converged state lies farther than
                                     this (infinity norm) from its per-point seed: the seed did not
                                     predict the branch it converged to.  <= 0 disables. */
+    const uint8_t *verify_map;   /* NULL, or host [dims[0]*dims[1]*dims[2]] flags over a uniform
+                                    (T, mu_u, xi) cell grid (T, mu in fm^-1, row-major, xi
+                                    fastest): when given, it replaces the verify_T_max_MeV rule --
+                                    a point is verified when its cell is flagged (points outside
+                                    the grid are always verified).  The learned-seed trainer flags
+                                    the cells where its labels show two coexisting phases or a
+                                    jump of the solution, grown by one cell. */
+    int32_t verify_map_dims[3];  /* cells along T, mu, xi (each >= 1)                          */
+    double verify_map_lo[3];     /* grid box: lower and upper edges along T, mu, xi            */
+    double verify_map_hi[3];
 } pnjl_solve_opts;
 
 /* Per-point results, SoA; any NULL pointer skips that output.  Fields follow SolverResult
@@ -138,6 +148,10 @@ typedef struct pnjl_stats {
     double last_kernel_ms;    /* device time of the last solve kernel (CUDA events)     */
     int64_t fp64_rescues;     /* mixed mode: FP32-Jacobian refinements that stopped
                                  contracting and were finished by FP64 Newton steps     */
+    int64_t node_evals_fp32_thermo; /* mixed mode: FP32 Omega passes at FP32 roots      */
+    int64_t pruned_candidates;/* mixed mode: FP32 roots whose Omega lies clearly above a
+                                 certified candidate of the same point (they cannot win
+                                 the min-Omega selection): no FP64 work spent on them   */
 } pnjl_stats;
 
 /* Default parameter set: config/pnjl/default.toml:1-21 through Constants_PNJL.jl:82-103. */
@@ -260,7 +274,7 @@ int pnjl_solve_batch_learned(pnjl_ctx *ctx, int64_t n, const double *T, const do
  * whose device memory belongs to another allocator's pool, services that reserve all memory
  * at start-up.  They pass device inputs and outputs (same layout and meaning as
  * pnjl_solve_batch_device; opts->seed_table stays a host pointer, opts->point_seeds is a
- * device pointer) and a stream; no context is used and the call makes no cudaMalloc,
+ * device pointer, opts->verify_map must be NULL) and a stream; no context is used and the call makes no cudaMalloc,
  * cudaFree or other allocating call.  The scratch it needs (candidate records, completion
  * counters, queue head, node and seed tables) is one static device array of about 6 MB that
  * every GPU loading this library holds until exit; batches beyond PNJL_NOALLOC_MAX_TASKS

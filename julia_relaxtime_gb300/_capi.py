@@ -68,6 +68,10 @@ class pnjl_solve_opts(C.Structure):
         ("verify_seeds", C.c_int32),
         ("verify_T_max_MeV", C.c_double),
         ("verify_max_step", C.c_double),
+        ("verify_map", u8p),
+        ("verify_map_dims", C.c_int32 * 3),
+        ("verify_map_lo", C.c_double * 3),
+        ("verify_map_hi", C.c_double * 3),
     ]
 
 
@@ -86,7 +90,7 @@ class pnjl_stats(C.Structure):
         ("node_evals_fp64_grad", C.c_int64), ("node_evals_fp64_grad_thermo", C.c_int64),
         ("node_evals_fp32", C.c_int64), ("seeds_run", C.c_int64), ("trust_region_runs", C.c_int64),
         ("multiseed_fallbacks", C.c_int64), ("kernel_launches", C.c_int64), ("last_kernel_ms", C.c_double),
-        ("fp64_rescues", C.c_int64),
+        ("fp64_rescues", C.c_int64), ("node_evals_fp32_thermo", C.c_int64), ("pruned_candidates", C.c_int64),
     ]
 
 

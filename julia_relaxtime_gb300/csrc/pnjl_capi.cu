@@ -32,6 +32,8 @@ struct pnjl_ctx {
     // control block: [0] queue head, [1..15] counters
     long long *d_ctrl = nullptr;
     double *d_seed_tables = nullptr; // 2 * 16 * 5
+    unsigned char *d_vmap = nullptr;  // device copy of the verification map
+    size_t vmap_cap = 0;
     // workspace for the host entry points
     unsigned char *d_ws = nullptr;
     size_t ws_cap = 0;
@@ -266,6 +268,7 @@ int pnjl_destroy(pnjl_ctx *ctx) {
     cudaFree(ctx->d_nodes_f);
     cudaFree(ctx->d_ctrl);
     cudaFree(ctx->d_seed_tables);
+    cudaFree(ctx->d_vmap);
     cudaFree(ctx->d_ws);
     cudaFree(ctx->d_scratch);
     cudaFree(ctx->mlp.params);
@@ -439,14 +442,36 @@ int pnjl_solve_batch_device(pnjl_ctx *ctx, int64_t n, const double *d_T, const d
     }
     pnjl::SolveArgs a{};
     const bool mixed = opts->precision == PNJL_PREC_MIXED;
+    const int S = has_table ? opts->n_seeds : 0;
+    auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
     if (opts->seed_mode == PNJL_SEEDS_TABLE && !mixed) {
         const size_t rec = (size_t)n * opts->n_seeds * sizeof(pnjl::CandRec);
-        const size_t cnt = ((size_t)n * sizeof(int) + 255) & ~size_t(255);
+        const size_t cnt = al((size_t)n * sizeof(int));
         int rc2 = ensure_scratch(ctx, cnt + rec);
         if (rc2) return rc2;
         a.done = (int *)ctx->d_scratch;
         a.cand = (pnjl::CandRec *)(ctx->d_scratch + cnt);
         PNJL_CUDA_TRY(ctx, cudaMemsetAsync(a.done, 0, (size_t)n * sizeof(int), s));
+    } else if (mixed && S > 0) {
+        // slots: every point (table mode) or the points the per-point kernel defers
+        const size_t nn = (size_t)n;
+        const size_t b_done = al(nn * sizeof(int)), b_flag = al(nn * S * sizeof(int));
+        const size_t b_cand = al(nn * (S + 1) * sizeof(pnjl::CandRec)), b_roots = al(nn * S * 5 * sizeof(double));
+        const size_t b_list = al(nn * sizeof(long long)), b_mode = al(nn * sizeof(int));
+        const size_t b_best = al(nn * sizeof(double));
+        int rc2 = ensure_scratch(ctx, b_done + b_flag + b_cand + b_roots + b_list + b_mode + b_best);
+        if (rc2) return rc2;
+        unsigned char *q = ctx->d_scratch;
+        a.done = (int *)q;
+        a.root_flag = (int *)(q + b_done);
+        a.cand = (pnjl::CandRec *)(q + b_done + b_flag);
+        a.roots = (double *)(q + b_done + b_flag + b_cand);
+        a.list = (long long *)(q + b_done + b_flag + b_cand + b_roots);
+        a.list_mode = (int *)(q + b_done + b_flag + b_cand + b_roots + b_list);
+        a.best_omega = (double *)(q + b_done + b_flag + b_cand + b_roots + b_list + b_mode);
+        // done and root_flag are adjacent: one memset clears both; best_omega starts as NaN
+        PNJL_CUDA_TRY(ctx, cudaMemsetAsync(q, 0, b_done + b_flag, s));
+        PNJL_CUDA_TRY(ctx, cudaMemsetAsync(a.best_omega, 0xff, nn * sizeof(double), s));
     }
     PNJL_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_ctrl, 0, 16 * sizeof(long long), s));
     a.P = ctx->dp;
@@ -461,26 +486,50 @@ int pnjl_solve_batch_device(pnjl_ctx *ctx, int64_t n, const double *d_T, const d
     a.hot_T_MeV = opts->hot_T_MeV;
     a.point_seeds = opts->point_seeds;
     pnjl::fill_solve_opts(opts, a.opts);
+    if (const int64_t cells = pnjl::verify_map_cells(opts)) {
+        if ((size_t)cells > ctx->vmap_cap) {
+            PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+            cudaFree(ctx->d_vmap);
+            ctx->d_vmap = nullptr;
+            ctx->vmap_cap = 0;
+            if (cudaMalloc(&ctx->d_vmap, (size_t)cells) != cudaSuccess)
+                return fail(ctx, PNJL_ERR_OUT_OF_MEMORY, "verification map allocation failed");
+            ctx->vmap_cap = (size_t)cells;
+        }
+        PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_vmap, opts->verify_map, (size_t)cells, cudaMemcpyHostToDevice, s));
+        a.opts.vmap = ctx->d_vmap;
+    }
     a.out = *d_out;
     a.queue = ctx->d_ctrl;
     a.stats = ctx->d_ctrl + 1;
+    a.list_count = ctx->d_ctrl + 1 + pnjl::kStatCount;
+    a.queue2 = ctx->d_ctrl + 2 + pnjl::kStatCount;
     const int group = ctx->group;
-    int grid = 0;
+    int grid = 0, grid_tasks = 0;
+    int launches = 1;
     if (mixed) {
-        int occ = pnjl::solve_mixed_occupancy(smem);
-        if (occ < 1) occ = 1;
-        if (ctx->blocks_per_sm > 0 && ctx->blocks_per_sm < occ) occ = ctx->blocks_per_sm;
-        const int64_t need = (n + pnjl::kSolveThreads / 32 - 1) / (pnjl::kSolveThreads / 32);
-        grid = (int)std::min<int64_t>((int64_t)ctx->sm_count * occ, need);
+        const int64_t wpb = pnjl::kSolveThreads / 32;
+        auto occ_of = [&](bool tasks) {
+            int occ = pnjl::solve_mixed_occupancy(tasks, smem);
+            if (occ < 1) occ = 1;
+            if (ctx->blocks_per_sm > 0 && ctx->blocks_per_sm < occ) occ = ctx->blocks_per_sm;
+            return (int64_t)occ;
+        };
+        const bool table = opts->seed_mode == PNJL_SEEDS_TABLE;
+        grid = (int)std::min<int64_t>((int64_t)ctx->sm_count * occ_of(false), (n + wpb - 1) / wpb);
+        const int64_t task_need = table ? (n * S + wpb - 1) / wpb : (int64_t)ctx->sm_count * occ_of(true);
+        grid_tasks = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->sm_count * occ_of(true), task_need));
+        launches = table ? 1 : (S > 0 ? 2 : 1);
     } else {
         const int64_t n_tasks = opts->seed_mode == PNJL_SEEDS_TABLE ? n * (int64_t)opts->n_seeds : n;
         grid = grid_for(ctx, group, smem, n_tasks);
     }
     PNJL_CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, s));
-    cudaError_t e = mixed ? pnjl::launch_solve_mixed(a, grid, smem, s) : pnjl::launch_solve(a, group, grid, smem, s);
+    cudaError_t e = mixed ? pnjl::launch_solve_mixed(a, grid, grid_tasks, smem, s)
+                          : pnjl::launch_solve(a, group, grid, smem, s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "solve kernel launch");
     PNJL_CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, s));
-    ctx->stats.kernel_launches += 1;
+    ctx->stats.kernel_launches += launches;
     ctx->stats.points = n;
     return PNJL_OK;
 }
@@ -841,6 +890,8 @@ int pnjl_get_stats(const pnjl_ctx *cctx, pnjl_stats *out) {
     st.passes_fp32 = c[pnjl::kStatPasses32];
     st.node_evals_fp32 = c[pnjl::kStatEvals32];
     st.fp64_rescues = c[pnjl::kStatRescue64];
+    st.node_evals_fp32_thermo = c[pnjl::kStatEvalsThermo32];
+    st.pruned_candidates = c[pnjl::kStatPruned];
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1) == cudaSuccess) st.last_kernel_ms = ms;
     *out = st;

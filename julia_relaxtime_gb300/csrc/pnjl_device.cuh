@@ -49,6 +49,9 @@ struct SolveOpts {
     int trust_region_fallback, auto_multiseed_fallback;
     int verify_seeds;
     double verify_T_max_MeV, verify_max_step;
+    const unsigned char *vmap;  // device copy of pnjl_solve_opts::verify_map, or null
+    int vn[3];
+    double vlo[3], vhi[3];
 };
 
 // The reference's POLYAKOV_EPS (Integrals.jl:151) and log(POLYAKOV_EPS)

@@ -321,6 +321,36 @@ struct Group {
         cnt.v[kStatPasses32] += 1;
     }
 
+    // Omega at x from an FP32 Kahan-compensated log pass (FP64 vacuum, chi and U terms):
+    // accurate to ~1e-6 absolute, used only to discard candidates that cannot win.
+    __device__ __noinline__ double eval_omega32(const PointIn &pt, const double *x) {
+        double M[3];
+        masses(P, x, M);
+        PassSums S;
+        node_pass<float, true, false, false, true, G>(nv, pt, x, M, gl, mask, S, cnt.v[kStatEvalsThermo32]);
+        Eval ev;
+        double V, V1[3], V2[3];
+        vacuum_terms<G>(P, M, gl, mask, leader(), V, V1, V2);
+        assemble<false, false, true>(P, pt, x, M, S, V, V1, V2, ev);
+        cnt.v[kStatPasses32] += 1;
+        return ev.omega;
+    }
+
+    // Whether the FP32 root x32 cannot win the min-Omega selection against a certified
+    // candidate of the same point with Omega `bound`: its FP32 Omega lies above bound by far
+    // more than the FP32 pass error.  (Candidates within the margin are refined and compared
+    // in FP64 as usual.)
+    static constexpr double kPruneRtol = 1e-5;
+    __device__ bool cannot_win(const PointIn &pt, const double *x32, double bound) {
+        if (!(bound == bound)) return false;
+        const double om = eval_omega32(pt, x32);
+        if (om > bound + kPruneRtol * fmax(fabs(bound), 1.0)) {
+            cnt.v[kStatPruned] += 1;
+            return true;
+        }
+        return false;
+    }
+
     __device__ __noinline__ void eval_grad64(const PointIn &pt, const double *x, double *F) {
         double M[3];
         masses(P, x, M);
@@ -514,11 +544,13 @@ struct Group {
         if (!thermo_at_x) eval_thermo(pt, o, c);
     }
 
-    // Mixed-precision counterpart of solve_seed.  `dup` is set when the FP32 solution equals
-    // one in seen[0..n_seen) (the same FP64 root, which a later seed cannot replace under the
-    // min-Omega tie rule); then no FP64 work is spent on it.
+    // Mixed-precision counterpart of solve_seed.  `dup` is set when the FP32 solution is a
+    // root that the dedup policy `dd` has already seen (the same FP64 root, which this seed
+    // cannot take from an earlier one under the min-Omega tie rule); then no FP64 work is
+    // spent on it.  D provides seen(x) and remember(x), uniform over the group.
+    template <class D>
     __device__ void mixed_solve_seed(const PointIn &pt, const double *x0, const SolveOpts &o, Candidate &out,
-                                     bool &converged, double *seen, int &n_seen, bool &dup) {
+                                     bool &converged, bool &dup, D &dd) {
         cnt.v[kStatSeeds] += 1;
         dup = false;
         double x32[5], J32[25];
@@ -531,8 +563,9 @@ struct Group {
         }
         out.exception = false;
         if (r > 0) {
-            if (is_seen(x32, seen, n_seen)) { dup = true; converged = false; return; }
-            remember(x32, seen, n_seen);
+            if (dd.seen(x32)) { dup = true; converged = false; return; }
+            dd.remember(x32);
+            if (cannot_win(pt, x32, dd.omega_bound())) { dup = true; converged = false; return; }
             int st = 0;
             refine64(pt, o, J32, x32, out, st);
             out.iterations = it32 + st;
@@ -548,8 +581,12 @@ struct Group {
             cnt.v[kStatTrRuns] += 1;
             double y32[5], K32[25];
             int itt = 0;
-            if (tr32(pt, x0, o, y32, K32, itt) > 0 && !is_seen(y32, seen, n_seen)) {
-                remember(y32, seen, n_seen);
+            if (tr32(pt, x0, o, y32, K32, itt) > 0 && !dd.seen(y32)) {
+                dd.remember(y32);
+                if (cannot_win(pt, y32, dd.omega_bound())) {  // the Newton result stays, unusable
+                    converged = false;
+                    return;
+                }
                 Candidate f;
                 int st = 0;
                 refine64(pt, o, K32, y32, f, st);
@@ -558,21 +595,7 @@ struct Group {
             }
         }
         converged = cand_good(out, o.residual_norm_max);
-    }
-
-    static constexpr int kMaxSeen = 34;
-    __device__ static bool is_seen(const double *x, const double *seen, int n_seen) {
-        for (int k = 0; k < n_seen; ++k) {
-            bool same = true;
-            for (int i = 0; i < 5; ++i) same = same && fabs(x[i] - seen[5 * k + i]) <= 1e-6 * (1.0 + fabs(x[i]));
-            if (same) return true;
-        }
-        return false;
-    }
-    __device__ static void remember(const double *x, double *seen, int &n_seen) {
-        if (n_seen >= kMaxSeen) return;
-        for (int i = 0; i < 5; ++i) seen[5 * n_seen + i] = x[i];
-        ++n_seen;
+        if (converged) dd.certified(out.omega);
     }
 
     // solve(::FixedMu) single-seed path without the MultiSeed fallback (ImplicitSolver.jl:261-304)
@@ -590,6 +613,100 @@ struct Group {
             if (!f.exception && choose_fallback(out, f, o.residual_norm_max)) out = f;
         }
         converged = cand_good(out, o.residual_norm_max);
+    }
+};
+
+// ---------------------------------------------------------------------------------------
+// Duplicate-root test of two FP32 solutions (both within the FP32 noise of one root).
+__device__ __forceinline__ bool same_root(const double *x, const double *y) {
+    bool same = true;
+    for (int i = 0; i < 5; ++i) same = same && fabs(x[i] - y[i]) <= 1e-6 * (1.0 + fabs(x[i]));
+    return same;
+}
+
+// Dedup policy of a single seed solved alone: its Newton root against its trust-region root.
+struct LocalRoots {
+    double r[2 * 5];
+    int n = 0;
+    __device__ bool seen(const double *x) const {
+        for (int k = 0; k < n; ++k)
+            if (same_root(x, r + 5 * k)) return true;
+        return false;
+    }
+    __device__ void remember(const double *x) {
+        if (n >= 2) return;
+        for (int i = 0; i < 5; ++i) r[5 * n + i] = x[i];
+        ++n;
+    }
+    __device__ double omega_bound() const { return __longlong_as_double(0x7ff8000000000000ll); }
+    __device__ void certified(double) {}
+};
+
+// Dedup policy of the task kernel: seed s of a slot compares its FP32 root with the roots that
+// seeds s' < s of the same slot have already published (and with `prior`, the certified root
+// of the slot's per-point seed, in verification mode), then publishes its own.  Only earlier
+// seeds can suppress a later one, so the selected candidate is the one the sequential
+// MultiSeed loop selects (an earlier seed still running is not waited for: both are refined
+// and the tie rule keeps the earlier).  The leader lane reads and writes; the answer is
+// broadcast to the group.
+struct PublishedRoots {
+    double *roots;        // [slots*S*5]
+    int *flag;            // [slots*S]
+    int64_t base;         // slot*S
+    int s;
+    const double *prior;  // or null
+    unsigned mask;
+    int leader, gl;
+    double *best;         // the slot's lowest certified Omega so far (NaN = none)
+    double prior_omega;   // Omega of `prior` (NaN when there is none)
+    LocalRoots own;
+    // lowest certified Omega of the slot known now: the per-point candidate's, or one that an
+    // earlier-finishing seed published (timing only decides how much work is saved: a pruned
+    // candidate lies above a certified one and would lose the selection anyway)
+    __device__ double omega_bound() const {
+        double b = prior_omega;
+        if (best) {
+            double v = 0.0;
+            if (gl == 0) v = __ldcg(best);
+            v = __shfl_sync(mask, v, leader);
+            if (v == v && !(b <= v)) b = v;
+        }
+        return b;
+    }
+    __device__ void certified(double om) {
+        if (!best || gl != 0 || !(om == om)) return;
+        unsigned long long *p = (unsigned long long *)best;
+        unsigned long long cur = __ldcg(p);
+        for (int k = 0; k < 64; ++k) {  // bounded CAS loop: one retry per competing writer
+            const double c = __longlong_as_double((long long)cur);
+            if (c == c && c <= om) return;
+            const unsigned long long prev = atomicCAS(p, cur, (unsigned long long)__double_as_longlong(om));
+            if (prev == cur) return;
+            cur = prev;
+        }
+    }
+    __device__ bool seen(const double *x) const {
+        if (own.seen(x)) return true;
+        int hit = 0;
+        if (gl == 0) {
+            if (prior && same_root(x, prior)) hit = 1;
+            for (int q = 0; q < s && !hit; ++q) {
+                if (*(volatile const int *)&flag[base + q] == 0) continue;
+                __threadfence();
+                double y[5];
+                for (int i = 0; i < 5; ++i) y[i] = __ldcg(&roots[5 * (base + q) + i]);
+                if (same_root(x, y)) hit = 1;
+            }
+        }
+        return __shfl_sync(mask, hit, leader) != 0;
+    }
+    __device__ void remember(const double *x) {
+        if (own.n == 0 && gl == 0) {
+            for (int i = 0; i < 5; ++i) __stcg(&roots[5 * (base + s) + i], x[i]);
+            __threadfence();
+            atomicExch(&flag[base + s], 1);
+        }
+        own.remember(x);
     }
 };
 
@@ -675,7 +792,20 @@ __device__ __forceinline__ const double *table_row(const SolveArgs &a, const Poi
 __device__ __forceinline__ bool needs_verification(const SolveOpts &o, const PointIn &pt, double hbarc,
                                                    const double *x0, const double *x) {
     if (o.verify_seeds <= 0) return false;
-    if (pt.T * hbarc < o.verify_T_max_MeV) return true;
+    if (o.vmap) {
+        // flagged cell of the (T, mu_u, xi) map; outside the map: always
+        const double v[3] = {pt.T, pt.mu[0], pt.xi};
+        int64_t idx = 0;
+        for (int k = 0; k < 3; ++k) {
+            const double f = (v[k] - o.vlo[k]) / (o.vhi[k] - o.vlo[k]) * o.vn[k];
+            if (!(f >= 0.0 && f <= (double)o.vn[k])) return true;
+            const int c = min((int)f, o.vn[k] - 1);
+            idx = idx * o.vn[k] + c;
+        }
+        if (o.vmap[idx]) return true;
+    } else if (pt.T * hbarc < o.verify_T_max_MeV) {
+        return true;
+    }
     if (o.verify_max_step > 0.0) {
         double d = 0.0;
         for (int k = 0; k < 5; ++k) d = fmax(d, fabs(x[k] - x0[k]));

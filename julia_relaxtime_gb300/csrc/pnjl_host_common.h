@@ -104,6 +104,17 @@ inline int validate_opts(const pnjl_solve_opts *o, const char **msg) {
         *msg = "verify_seeds must be 0..n_seeds (rows of the seed table)";
         return PNJL_ERR_INVALID_ARGUMENT;
     }
+    if (o->verify_map) {
+        int64_t cells = 1;
+        for (int k = 0; k < 3; ++k) {
+            if (o->verify_map_dims[k] < 1 || !(o->verify_map_hi[k] > o->verify_map_lo[k])) {
+                *msg = "verify_map: dims must be >= 1 and lo < hi";
+                return PNJL_ERR_INVALID_ARGUMENT;
+            }
+            cells *= o->verify_map_dims[k];
+        }
+        if (cells > (int64_t(1) << 24)) { *msg = "verify_map too large"; return PNJL_ERR_INVALID_ARGUMENT; }
+    }
     if (o->precision != PNJL_PREC_FP64 && o->precision != PNJL_PREC_MIXED) {
         *msg = "unknown precision";
         return PNJL_ERR_INVALID_ARGUMENT;
@@ -123,6 +134,16 @@ inline void fill_solve_opts(const pnjl_solve_opts *o, SolveOpts &d) {
     d.verify_seeds = o->seed_mode == PNJL_SEEDS_PER_POINT ? o->verify_seeds : 0;
     d.verify_T_max_MeV = o->verify_T_max_MeV;
     d.verify_max_step = o->verify_max_step;
+    d.vmap = nullptr;  // set by the caller to the device copy of o->verify_map
+    for (int k = 0; k < 3; ++k) {
+        d.vn[k] = o->verify_map ? o->verify_map_dims[k] : 0;
+        d.vlo[k] = o->verify_map_lo[k];
+        d.vhi[k] = o->verify_map_hi[k];
+    }
+}
+
+inline int64_t verify_map_cells(const pnjl_solve_opts *o) {
+    return o->verify_map ? (int64_t)o->verify_map_dims[0] * o->verify_map_dims[1] * o->verify_map_dims[2] : 0;
 }
 
 inline DevParams dev_params(const pnjl_params &p) {

@@ -30,7 +30,8 @@ struct CandRec {
 // Counter slots of SolveArgs::stats
 enum StatSlot {
     kStatPasses64 = 0, kStatEvalsNewton64, kStatEvalsThermo64, kStatSeeds, kStatTrRuns, kStatMsFallbacks,
-    kStatPasses32, kStatEvals32, kStatEvalsGrad64, kStatEvalsGradThermo64, kStatRescue64, kStatCount
+    kStatPasses32, kStatEvals32, kStatEvalsGrad64, kStatEvalsGradThermo64, kStatRescue64, kStatEvalsThermo32,
+    kStatPruned, kStatCount
 };
 
 struct SolveArgs {
@@ -45,11 +46,28 @@ struct SolveArgs {
     const double *point_seeds;    // device [n*5]
     SolveOpts opts;
     pnjl_result_soa out;          // device pointers
-    CandRec *cand;                // scratch [n*n_seeds] (MultiSeed mode)
+    CandRec *cand;                // scratch: FP64 kernel [n*n_seeds]; mixed kernels [n*(n_seeds+1)]
     int *done;                    // scratch [n], zeroed before the launch
     long long *queue;             // device work-queue head (zeroed before the launch)
     long long *stats;             // device counters [kStatCount]
+    // mixed-precision task kernel (zeroed before the launch where noted)
+    double *roots;                // [n*n_seeds*5] FP32 roots published per (slot, seed)
+    int *root_flag;               // [n*n_seeds] 1 once roots[slot, seed] is written (zeroed)
+    long long *list;              // [n] points deferred by the per-point kernel
+    int *list_mode;               // [n] kListVerify / kListFallback
+    long long *list_count;        // entries in list (zeroed)
+    long long *queue2;            // work-queue head of the task kernel (zeroed)
+    double *best_omega;           // [n] lowest certified Omega published per slot (NaN = none;
+                                  // set to all-ones bytes before the launch)
 };
+
+// Modes of a slot of the mixed task kernel: min-Omega over all seeds (MultiSeed table mode);
+// a converged per-point solution checked against the first verify_seeds seeds; a per-point
+// seed that failed, replaced by the MultiSeed solve (ImplicitSolver.jl:306-327).
+// the 16-slot control block of a context: queue head, counters, list length, task queue head
+static_assert(kStatCount + 3 <= 16, "control block too small");
+
+enum ListMode { kListFull = 0, kListVerify = 1, kListFallback = 2 };
 
 struct EvalArgs {
     DevParams P;
@@ -62,8 +80,10 @@ struct EvalArgs {
 
 size_t node_smem_bytes(int p_num, int t_num);
 cudaError_t launch_solve(const SolveArgs &a, int group, int grid, size_t smem, cudaStream_t s);
-cudaError_t launch_solve_mixed(const SolveArgs &a, int grid, size_t smem, cudaStream_t s);
-int solve_mixed_occupancy(size_t smem);
+// Mixed precision: per-point mode launches the per-point kernel (grid_points blocks) and then
+// the task kernel over the points it deferred; table mode launches the task kernel alone.
+cudaError_t launch_solve_mixed(const SolveArgs &a, int grid_points, int grid_tasks, size_t smem, cudaStream_t s);
+int solve_mixed_occupancy(bool tasks, size_t smem);
 cudaError_t launch_eval(const EvalArgs &a, bool fp32, int grid, size_t smem, cudaStream_t s);
 int solve_kernel_occupancy(int group, size_t smem);
 

@@ -89,6 +89,7 @@ extern "C" int pnjl_solve_batch_noalloc(const pnjl_params *params, int32_t p_num
     if (!params || !d_out) return PNJL_ERR_INVALID_ARGUMENT;
     const char *msg = "";
     if (pnjl::validate_opts(opts, &msg) != PNJL_OK) return PNJL_ERR_INVALID_ARGUMENT;
+    if (opts->verify_map) return PNJL_ERR_INVALID_ARGUMENT;  // no device copy without an allocation
     if (p_num < 1 || p_num > pnjl::kMaxPNodes || t_num < 1 || t_num > pnjl::kMaxTNodes || !(p_max > 0.0))
         return PNJL_ERR_INVALID_ARGUMENT;
     if (n < 0 || (n > 0 && (!d_T || !d_mu_u || !d_mu_d || !d_mu_s || !d_xi))) return PNJL_ERR_INVALID_ARGUMENT;

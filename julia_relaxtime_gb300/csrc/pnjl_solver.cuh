@@ -46,9 +46,12 @@ __device__ __forceinline__ void masses(const DevParams &P, const double *x, doub
 
 template <int G>
 __device__ __forceinline__ unsigned group_mask(int lane) {
-    if (G == 32) return 0xffffffffu;
-    const unsigned base = (unsigned)(lane & ~(G - 1));
-    return ((1u << G) - 1u) << base;
+    if constexpr (G == 32) {
+        return 0xffffffffu;
+    } else {
+        const unsigned base = (unsigned)(lane & ~(G - 1));
+        return ((1u << G) - 1u) << base;
+    }
 }
 
 // XOR butterfly: a + b == b + a bitwise, so every lane of the group ends with the

@@ -34,10 +34,29 @@ class SolveOptions:
     trust_region_fallback: bool = True
     auto_multiseed_fallback: bool = True
     precision: str = "fp64"
-    # per-point seeds only: also try the first `verify_seeds` table rows below this temperature
+    # per-point seeds only: also try the first `verify_seeds` table rows (-1: all) below this temperature
     verify_seeds: int = 0
     verify_T_max_MeV: float = 170.0
     verify_max_step: float = 0.0
+    # ... or, when given, in the flagged cells of this (T, mu_u, xi) map instead of below verify_T_max_MeV
+    verify_map: "VerifyMap | None" = None
+
+
+@dataclass
+class VerifyMap:
+    """Cells of a uniform (T, mu_u, xi) grid (T, mu in fm^-1) where per-point solutions are
+    verified by the MultiSeed candidates (pnjl_solve_opts::verify_map)."""
+    flags: np.ndarray  # uint8 [nT, nmu, nxi]
+    lo: tuple          # (T, mu, xi) lower edges
+    hi: tuple          # upper edges
+
+    def __post_init__(self):
+        self.flags = np.ascontiguousarray(np.asarray(self.flags, dtype=np.uint8))
+        if self.flags.ndim != 3:
+            raise ValueError("verify map flags must be 3-D (T, mu, xi)")
+
+    def fraction(self) -> float:
+        return float(self.flags.mean()) if self.flags.size else 0.0
 
 
 def _dp(a):
@@ -172,9 +191,16 @@ class GapEngine:
         o.trust_region_fallback = int(bool(opts.trust_region_fallback))
         o.auto_multiseed_fallback = int(bool(opts.auto_multiseed_fallback))
         o.precision = PRECISIONS[opts.precision]
-        o.verify_seeds = int(opts.verify_seeds)
+        o.verify_seeds = o.n_seeds if opts.verify_seeds < 0 else int(opts.verify_seeds)  # -1: every table row
         o.verify_T_max_MeV = float(opts.verify_T_max_MeV)
         o.verify_max_step = float(opts.verify_max_step)
+        vm = opts.verify_map
+        if vm is not None:
+            o.verify_map = vm.flags.ctypes.data_as(api.u8p)
+            for k in range(3):
+                o.verify_map_dims[k] = int(vm.flags.shape[k])
+                o.verify_map_lo[k] = float(vm.lo[k])
+                o.verify_map_hi[k] = float(vm.hi[k])
         return o
 
     def solve(self, T, mu, xi, *, seed_table=None, seed_table_hot=None, hot_T_MeV: float = 300.0,

@@ -11,13 +11,13 @@ only change how fast a point is solved, and the multi-seed result remains the ju
 from __future__ import annotations
 
 import ctypes as C
-from dataclasses import dataclass
+from dataclasses import dataclass, replace
 
 import numpy as np
 
 from . import _capi as api
 from .constants import HBARC_MEV_FM
-from .engine import GapEngine, SolveOptions, _dp
+from .engine import GapEngine, SolveOptions, VerifyMap, _dp
 from .pnjl import FixedMu, MultiSeed, SeedStrategy
 
 PARAM_COUNT = None
@@ -57,6 +57,7 @@ class LearnedSeed(SeedStrategy):
         self.trained = False
         self.last_loss = None
         self.scaling = None
+        self.verify_map: VerifyMap | None = None  # where the MultiSeed candidates verify a solution
 
     def _check(self, rc, what):
         api.check(self.engine._ctx, rc, what)
@@ -112,13 +113,19 @@ class LearnedSeed(SeedStrategy):
         self.trained = True
 
     def save(self, path: str):
+        extra = {}
+        if self.verify_map is not None:
+            extra = dict(vmap_flags=self.verify_map.flags, vmap_lo=np.array(self.verify_map.lo),
+                         vmap_hi=np.array(self.verify_map.hi))
         np.savez(path, params=self.params(), in_shift=self.scaling[0], in_scale=self.scaling[1],
-                 out_shift=self.scaling[2], out_scale=self.scaling[3])
+                 out_shift=self.scaling[2], out_scale=self.scaling[3], **extra)
 
     def load(self, path: str):
         d = np.load(path)
         self.set_scaling(d["in_shift"], d["in_scale"], d["out_shift"], d["out_scale"])
         self.set_params(d["params"])
+        if "vmap_flags" in d:
+            self.verify_map = VerifyMap(d["vmap_flags"], tuple(d["vmap_lo"]), tuple(d["vmap_hi"]))
 
     # -- inference -------------------------------------------------------------------------
     def seeds(self, T, mu, xi) -> np.ndarray:
@@ -140,6 +147,8 @@ class LearnedSeed(SeedStrategy):
         MultiSeed fallback where it does not converge, verification seeds where a second
         phase can exist (opts.verify_*; default_learned_opts())."""
         opts = opts or default_learned_opts()
+        if opts.verify_map is None and self.verify_map is not None:
+            opts = replace(opts, verify_map=self.verify_map)
         table, hot = (multiseed or MultiSeed()).tables()
         T_arr = np.atleast_1d(np.asarray(T, dtype=np.float64))
         return self.engine.solve(T_arr, mu, xi, seed_table=table, seed_table_hot=hot, opts=opts, learned=True)
@@ -147,9 +156,11 @@ class LearnedSeed(SeedStrategy):
 
 def default_learned_opts(**kw) -> SolveOptions:
     """Options of the learned-seed solve: mixed precision, 40 iterations, and verification by
-    the first two MultiSeed candidates below T = 170 MeV or where the root lies more than 0.3
-    (in fm^-3 / Polyakov units, inf-norm) from the learned seed."""
-    base = dict(iterations=40, precision="mixed", verify_seeds=2, verify_T_max_MeV=170.0, verify_max_step=0.3)
+    every MultiSeed candidate where a second, metastable phase can exist -- the cells of the
+    network's verification map (built from its labels, coexistence_map), or below T = 170 MeV
+    without a map -- and wherever the root lies more than 0.3 (fm^-3 / Polyakov units,
+    inf-norm) from the learned seed: there the multi-seed Newton judges the learned solution."""
+    base = dict(iterations=40, precision="mixed", verify_seeds=-1, verify_T_max_MeV=170.0, verify_max_step=0.3)
     base.update(kw)
     return SolveOptions(**base)
 
@@ -166,9 +177,82 @@ def label_grid(engine: GapEngine, cfg: TrainConfig, opts: SolveOptions | None = 
     return T[ok], mu[ok], xi[ok], res["x"][ok], res
 
 
+def candidate_roots(engine: GapEngine, cfg: TrainConfig):
+    """Root (NaN where not converged) and Omega of every MultiSeed candidate alone at every
+    label-grid point: [N, S, 5] and [N, S]."""
+    from .pnjl import multiseed_table
+
+    T, mu, xi = grid_points(cfg)
+    table, hot = multiseed_table(cfg.label_seeds)
+    opts = SolveOptions(iterations=40, ftol=1e-10, precision=cfg.label_precision)
+    roots, omegas = [], []
+    for s in range(table.shape[0]):  # each candidate alone: a one-row MultiSeed table
+        r = engine.solve(T, mu, xi, seed_table=table[s:s + 1], seed_table_hot=hot[s:s + 1], opts=opts)
+        roots.append(np.where(r["converged"][:, None], r["x"], np.nan))
+        omegas.append(np.where(r["converged"], r["omega"], np.nan))
+    return np.stack(roots, axis=1), np.stack(omegas, axis=1)
+
+
+def coexistence_map(engine: GapEngine, cfg: TrainConfig, labels, *, distinct: float = 0.05, gap_max: float = 1.0,
+                    jump: float = 0.25, grow: int = 1, roots=None) -> VerifyMap:
+    """Verification map on the label grid's cells.  A grid node is flagged where two MultiSeed
+    candidates converge to different physical roots (|dx|_inf > distinct) whose Omega both lie
+    within gap_max (fm^-4) of the minimum -- a second phase coexists; far-off roots such as the
+    deep chirally broken solution (phi_u ~ -5.3 fm^-3, Omega ~3.5 fm^-4 above the minimum at
+    low T) are not a competing phase -- or where the labelled solution jumps by more than
+    `jump` to a neighbour along T or mu (the first-order line or a steep crossover passes; the
+    xi step of the label grid is too coarse for this test).  A cell is flagged when any of its
+    8 corner nodes is, and the flagged cells grow by `grow` cells in every direction."""
+    T, mu, xi = grid_points(cfg)
+    nT, nm, nx = int(cfg.T_MeV[2]), int(cfg.mu_MeV[2]), int(cfg.xi[2])
+    R, Om = roots if roots is not None else candidate_roots(engine, cfg)
+    node = np.zeros(T.size, dtype=bool)
+    with np.errstate(invalid="ignore"):
+        omin = np.nanmin(np.where(np.isfinite(Om), Om, np.inf), axis=1)
+        for a in range(R.shape[1]):
+            for b in range(a + 1, R.shape[1]):
+                d = np.abs(R[:, a] - R[:, b]).max(axis=1)  # NaN (a seed failed) compares False
+                node |= (d > distinct) & (np.maximum(Om[:, a], Om[:, b]) - omin < gap_max)
+    X = labels["x"].reshape(nT, nm, nx, 5)
+    ok = labels["converged"].reshape(nT, nm, nx)
+    node = node.reshape(nT, nm, nx)
+    for ax in range(2):
+        d = np.abs(np.diff(X, axis=ax)).max(axis=-1)
+        both = np.logical_and(np.take(ok, range(0, X.shape[ax] - 1), axis=ax),
+                              np.take(ok, range(1, X.shape[ax]), axis=ax))
+        j = (d > jump) & both
+        pad = [(0, 0)] * 3
+        pad[ax] = (0, 1)
+        node |= np.pad(j, pad)
+        pad[ax] = (1, 0)
+        node |= np.pad(j, pad)
+    node |= ~ok  # unlabelled nodes: verify around them too
+    cells = np.zeros((max(nT - 1, 1), max(nm - 1, 1), max(nx - 1, 1)), dtype=bool)
+    for dT in (0, 1):
+        for dm in (0, 1):
+            for dx in (0, 1):
+                cells |= node[dT:dT + cells.shape[0], dm:dm + cells.shape[1], dx:dx + cells.shape[2]]
+    for _ in range(grow):
+        g = cells.copy()
+        for ax in range(3):
+            sl = [slice(None)] * 3
+            sl[ax] = slice(1, None)
+            sr = [slice(None)] * 3
+            sr[ax] = slice(None, -1)
+            g[tuple(sl)] |= cells[tuple(sr)]
+            g[tuple(sr)] |= cells[tuple(sl)]
+        cells = g
+    lo = (cfg.T_MeV[0] / HBARC_MEV_FM, cfg.mu_MeV[0] / HBARC_MEV_FM, cfg.xi[0])
+    hi = (cfg.T_MeV[1] / HBARC_MEV_FM, cfg.mu_MeV[1] / HBARC_MEV_FM, cfg.xi[1])
+    return VerifyMap(cells.astype(np.uint8), lo, hi)
+
+
 def train_learned_seed(engine: GapEngine, cfg: TrainConfig | None = None) -> LearnedSeed:
+    """Label the grid with the multi-seed solver, train the network on the labels and build its
+    verification map."""
     cfg = cfg or TrainConfig()
-    T, mu, xi, x, _ = label_grid(engine, cfg)
+    T, mu, xi, x, res = label_grid(engine, cfg)
     ls = LearnedSeed(engine, seed=cfg.seed)
     ls.fit(T, mu, xi, x, epochs=cfg.epochs, batch=cfg.batch, lr=cfg.lr, shuffle_seed=cfg.seed + 1)
+    ls.verify_map = coexistence_map(engine, cfg, res)
     return ls
