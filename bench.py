@@ -46,6 +46,9 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 HBARC = 197.327
+# DRAM bytes (read + write) per launch of the dominant kernel from one ncu capture, scaled to
+# the bench step by the points it processes; see profiles/ for the capture and the command
+TRAFFIC = {}
 METRIC = "gap solves/s at \u2016\u2202\u03a9\u2016\u22641e-10: surrogate-seeded vs plain FP64 Newton, 1 GB300"
 # Floating-point operations per node-flavour evaluation, counted from the source of
 # pnjl_device.cuh::node_flavour (FMA = 2, loop invariants hoisted, selects and compares not
@@ -56,18 +59,26 @@ METRIC = "gap solves/s at \u2016\u2202\u03a9\u2016\u22641e-10: surrogate-seeded 
 #   residual-only pass (mixed-precision refinement):  53 FLOP + 3 transcendentals
 #   residual + thermo pass (mixed refinement):        69 FLOP + 4 transcendentals
 #   FP32 Newton pass: 123 FLOP + 27 for the Kahan compensation of 9 sums = 150 FLOP
+#   FP32 Omega pass (candidate pruning): 58 FLOP + 6 for 2 compensated sums = 64 FLOP
+#   float-float residual pass: the 53 residual FLOP, float-float thermo pass: the 58 thermo
+#     FLOP, each a float-float operation of 6-20 FP32 instructions; reported as their own
+#     count, not added to the FP32 FLOP
 FLOP_NEWTON = 123
 FLOP_THERMO = 58
 FLOP_GRAD = 53
 FLOP_GRAD_THERMO = 69
 FLOP_NEWTON32 = 150
+FLOP_THERMO32 = 64
+FLOP_FF = 53
+FLOP_FF_THERMO = 58
 
 
 def pass_flops(st: dict):
-    """(FP64 FLOP, FP32 FLOP) of one solve from the library's node-evaluation counters."""
+    """(FP64 FLOP, FP32 FLOP, float-float FLOP) of one solve from the node-evaluation counters."""
     f64 = (st["node_evals_fp64_newton"] * FLOP_NEWTON + st["node_evals_fp64_thermo"] * FLOP_THERMO +
            st["node_evals_fp64_grad"] * FLOP_GRAD + st["node_evals_fp64_grad_thermo"] * FLOP_GRAD_THERMO)
-    return f64, st["node_evals_fp32"] * FLOP_NEWTON32
+    f32 = st["node_evals_fp32"] * FLOP_NEWTON32 + st["node_evals_fp32_thermo"] * FLOP_THERMO32
+    return f64, f32, st["node_evals_ff"] * FLOP_FF + st["node_evals_ff_thermo"] * FLOP_FF_THERMO
 
 
 def workload_grid(name: str):
@@ -231,7 +242,7 @@ def main():
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
     torch.cuda.set_device(local_rank)
-    from julia_relaxtime_gb300.engine import GapEngine, SolveOptions
+    from julia_relaxtime_gb300.engine import GapEngine, SolveOptions, shard_points
     from julia_relaxtime_gb300.learned_seed import TrainConfig, default_learned_opts, train_learned_seed
     from julia_relaxtime_gb300.pnjl import multiseed_table
 
@@ -254,7 +265,8 @@ def main():
     plain = Arm("plain_fp64", eng, table, hot, SolveOptions(iterations=40, ftol=1e-10, precision="fp64"), False)
 
     # this rank's share of the points: a strided shard (no data exchange between ranks)
-    T_all, mu_all, xi_all = grid["T"][rank::world], grid["mu"][rank::world], grid["xi"][rank::world]
+    mine = shard_points(grid["T"].size, rank, world)
+    T_all, mu_all, xi_all = grid["T"][mine], grid["mu"][mine], grid["xi"][mine]
     chunks = [np.arange(c, T_all.size, args.chunks) for c in range(args.chunks)]
     dev = torch.device("cuda", local_rank)
     stream = torch.cuda.ExternalStream(eng.stream(), device=dev)
@@ -287,8 +299,9 @@ def main():
             a.launch(n, d_in, ptrs)
             eng.synchronize()
         sampler = ClockSampler(local_rank) if sample_clocks else None
-        rec = {"step_ms": [], "kernel_ms": [], "solved": 0, "flops64": 0.0, "flops32": 0.0, "evals": 0, "kinds": {},
-               "results": []}
+        rec = {"step_ms": [], "kernel_ms": [], "solved": 0, "flops64": 0.0, "flops32": 0.0, "flops_ff": 0.0,
+               "evals": 0, "kinds": {}, "results": [], "k0_ms": [], "k1_ms": [], "k0_flops": [0.0, 0.0, 0.0],
+               "k0_evals": 0}
         launches0 = eng.stats()["kernel_launches"]
         if dist is not None:
             dist.barrier()
@@ -308,13 +321,24 @@ def main():
             rec["step_ms"].append(e0.elapsed_time(e1))
             st = eng.stats()
             rec["kernel_ms"].append(st["last_kernel_ms"])
-            rec["evals"] += st["node_evals_fp64"] + st["node_evals_fp32"]
-            f64_, f32_ = pass_flops(st)
+            rec["evals"] += st["node_evals_fp64"] + st["node_evals_fp32"] + st["node_evals_fp32_thermo"] + \
+                st["node_evals_ff"] + st["node_evals_ff_thermo"]
+            f64_, f32_, fff_ = pass_flops(st)
             rec["flops64"] += f64_
             rec["flops32"] += f32_
+            rec["flops_ff"] += fff_
+            # the first kernel alone (the per-point kernel of a learned / per-point solve)
+            s0, s1 = eng.stats(kernel=0), eng.stats(kernel=1)
+            rec["k0_ms"].append(s0["last_kernel_ms"])
+            rec["k1_ms"].append(s1["last_kernel_ms"])
+            for j, v in enumerate(pass_flops(s0)):
+                rec["k0_flops"][j] += v
+            rec["k0_evals"] += s0["node_evals_fp64"] + s0["node_evals_fp32"] + s0["node_evals_fp32_thermo"] + \
+                s0["node_evals_ff"] + s0["node_evals_ff_thermo"]
             for kk in ("node_evals_fp64_newton", "node_evals_fp64_thermo", "node_evals_fp64_grad",
-                       "node_evals_fp64_grad_thermo", "node_evals_fp32", "seeds_run", "trust_region_runs",
-                       "multiseed_fallbacks", "fp64_rescues"):
+                       "node_evals_fp64_grad_thermo", "node_evals_fp32", "node_evals_fp32_thermo", "node_evals_ff",
+                       "node_evals_ff_thermo",
+                       "seeds_run", "trust_region_runs", "multiseed_fallbacks", "fp64_rescues", "pruned_candidates"):
                 rec["kinds"][kk] = rec["kinds"].get(kk, 0) + st[kk]
             conv = d_out["converged"][:n].cpu().numpy().astype(bool)
             res = d_out["residual_norm"][:n].cpu().numpy()
@@ -395,20 +419,35 @@ def main():
         return
     peak_fp64 = eng.probe_peak("fp64")
     peak_fp32 = eng.probe_peak("fp32")
-    avg_kernel_s = (sum(main_rec["kernel_ms"]) / len(main_rec["kernel_ms"])) * 1e-3
-    ach64 = main_rec["flops64"] / args.steps / avg_kernel_s
-    ach32 = main_rec["flops32"] / args.steps / avg_kernel_s
-    kname = "solve_kernel<32>" if precision == "fp64" else "solve_kernel_mixed<32>"
+    K = args.steps
+    if precision == "fp64":
+        kname, k_ms, k_flops, k_evals = "solve_kernel<32>", main_rec["kernel_ms"], \
+            [main_rec["flops64"], main_rec["flops32"], main_rec["flops_ff"]], main_rec["evals"]
+    elif args.mode == "surrogate":
+        kname, k_ms, k_flops, k_evals = "mixed_points_kernel<32>", main_rec["k0_ms"], main_rec["k0_flops"], \
+            main_rec["k0_evals"]
+    else:
+        kname, k_ms, k_flops, k_evals = "mixed_tasks_kernel<32>", main_rec["kernel_ms"], \
+            [main_rec["flops64"], main_rec["flops32"], main_rec["flops_ff"]], main_rec["evals"]
+    avg_k_s = (sum(k_ms) / len(k_ms)) * 1e-3
+    ach64 = k_flops[0] / K / avg_k_s
+    ach32 = k_flops[1] / K / avg_k_s
+    step_kernels_ms = sum(main_rec["kernel_ms"]) / K
     roof = {"bound": "fp64", "kernel": kname, "achieved": ach64 / 1e12, "peak": peak_fp64 / 1e12,
             "unit": "TFLOP/s", "frac": ach64 / peak_fp64,
             "peak_source": "measured in-run (pnjl_probe_peak: FP64 FMA chains on every lane of the GPU); "
                            "no HBM or tensor-core bound applies to this compute-bound path",
             "flop_per_node_flavour": {"newton_pass": FLOP_NEWTON, "thermo_pass": FLOP_THERMO,
                                       "residual_pass": FLOP_GRAD, "residual_thermo_pass": FLOP_GRAD_THERMO,
-                                      "newton_pass_fp32": FLOP_NEWTON32},
-            "node_flavour_evals_per_launch": main_rec["evals"] / args.steps, "kernel_ms": avg_kernel_s * 1e3,
-            "traffic": None,
-            "fp32": {"achieved": ach32 / 1e12, "peak": peak_fp32 / 1e12, "frac": ach32 / peak_fp32}}
+                                      "newton_pass_fp32": FLOP_NEWTON32, "omega_pass_fp32": FLOP_THERMO32,
+                                      "residual_pass_float_float": FLOP_FF, "thermo_pass_float_float": FLOP_FF_THERMO},
+            "node_flavour_evals_per_launch": k_evals / K, "kernel_ms": avg_k_s * 1e3,
+            "kernel_share_of_step": avg_k_s * 1e3 / step_kernels_ms if step_kernels_ms > 0 else None,
+            "traffic": TRAFFIC.get(kname, {}).get("bytes_per_launch") if args.workload == "aniso_scan_256x256x9"
+            else None,
+            "traffic_source": TRAFFIC.get(kname, {}).get("source"),
+            "fp32": {"achieved": ach32 / 1e12, "peak": peak_fp32 / 1e12, "frac": ach32 / peak_fp32},
+            "float_float_flop_per_launch": k_flops[2] / K}
     launches = main_rec["launches"]
     line = {"metric": METRIC, "value": main_rec["value"], "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": main_rec["total_ms"] / args.steps, "higher_is_better": True,

@@ -48,6 +48,9 @@ extern "C" {
 #define PNJL_PREC_MIXED 1 /* Newton passes with an FP32 Kahan-compensated integrand; the
                              residual that decides convergence, Omega and the thermo output
                              come from FP64 passes                                          */
+#define PNJL_PREC_FF_RESIDUAL 2 /* pnjl_eval_batch only: the float-float residual pass the
+                             mixed solver steers its first FP64 correction step with
+                             (gradient only; omega and hess are NaN)                        */
 
 /* Model constants in fm units; src/Constants_PNJL.jl:82-103 (hbarc, N_color, rho0,
  * Lambda, G, K, m_ud0, m_s0, T0, a0, a1, a2, b3). */
@@ -152,6 +155,9 @@ typedef struct pnjl_stats {
     int64_t pruned_candidates;/* mixed mode: FP32 roots whose Omega lies clearly above a
                                  certified candidate of the same point (they cannot win
                                  the min-Omega selection): no FP64 work spent on them   */
+    int64_t node_evals_ff;    /* mixed mode: float-float residual passes (FP32 pipe)    */
+    int64_t node_evals_ff_thermo; /* mixed mode: float-float Omega / thermo passes at
+                                 certified states (FP32 pipe)                           */
 } pnjl_stats;
 
 /* Default parameter set: config/pnjl/default.toml:1-21 through Constants_PNJL.jl:82-103. */
@@ -173,8 +179,9 @@ int pnjl_get_nodes(const pnjl_ctx *ctx, double *p_mesh, double *c_mesh, double *
 
 /* Omega, grad_x Omega [5n] and Hessian_x Omega [25n, row-major] at given states:
  * calculate_omega (Thermodynamics.jl:181-195) and the ForwardDiff gradient/Jacobian of
- * gap_conditions (Conditions.jl:72-86; F = -grad_x Omega).  precision: PNJL_PREC_FP64 or
- * PNJL_PREC_MIXED (FP32-Kahan integrand, FP64 assembly).  Host pointers; NULL skips. */
+ * gap_conditions (Conditions.jl:72-86; F = -grad_x Omega).  precision: PNJL_PREC_FP64,
+ * PNJL_PREC_MIXED (FP32-Kahan integrand, FP64 assembly) or PNJL_PREC_FF_RESIDUAL (float-float
+ * gradient only).  Host pointers; NULL skips. */
 int pnjl_eval_batch(pnjl_ctx *ctx, int64_t n, const double *x, const double *T,
                     const double *mu_u, const double *mu_d, const double *mu_s,
                     const double *xi, int32_t precision,
@@ -206,6 +213,11 @@ int pnjl_solve_batch_device(pnjl_ctx *ctx, int64_t n, const double *d_T, const d
 void *pnjl_stream(pnjl_ctx *ctx);
 int pnjl_synchronize(pnjl_ctx *ctx);
 int pnjl_get_stats(const pnjl_ctx *ctx, pnjl_stats *out);
+/* The same for one kernel of the last solve: kernel 0 = the first kernel (the per-point kernel
+ * of a mixed per-point solve, else the only one), kernel 1 = the task kernel that follows it
+ * in a mixed per-point solve (all counters zero when there was none).  last_kernel_ms is that
+ * kernel's device time (CUDA events around it on the context stream). */
+int pnjl_get_kernel_stats(const pnjl_ctx *ctx, int32_t kernel, pnjl_stats *out);
 
 /* Number of streaming multiprocessors of the context's device. */
 int pnjl_device_sm_count(const pnjl_ctx *ctx);

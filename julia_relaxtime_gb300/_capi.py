@@ -33,6 +33,7 @@ PNJL_SEEDS_PER_POINT = 1
 
 PNJL_PREC_FP64 = 0
 PNJL_PREC_MIXED = 1
+PNJL_PREC_FF_RESIDUAL = 2  # pnjl_eval_batch only
 
 dp = C.POINTER(C.c_double)
 i32p = C.POINTER(C.c_int32)
@@ -91,6 +92,7 @@ class pnjl_stats(C.Structure):
         ("node_evals_fp32", C.c_int64), ("seeds_run", C.c_int64), ("trust_region_runs", C.c_int64),
         ("multiseed_fallbacks", C.c_int64), ("kernel_launches", C.c_int64), ("last_kernel_ms", C.c_double),
         ("fp64_rescues", C.c_int64), ("node_evals_fp32_thermo", C.c_int64), ("pruned_candidates", C.c_int64),
+        ("node_evals_ff", C.c_int64), ("node_evals_ff_thermo", C.c_int64),
     ]
 
 
@@ -111,6 +113,7 @@ SIGNATURES = {
     "pnjl_stream": (C.c_void_p, [C.c_void_p]),
     "pnjl_synchronize": (C.c_int, [C.c_void_p]),
     "pnjl_get_stats": (C.c_int, [C.c_void_p, C.POINTER(pnjl_stats)]),
+    "pnjl_get_kernel_stats": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(pnjl_stats)]),
     "pnjl_device_sm_count": (C.c_int, [C.c_void_p]),
     "pnjl_set_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "pnjl_probe_peak": (C.c_int, [C.c_void_p, C.c_int32, dp]),

@@ -20,7 +20,9 @@ struct pnjl_ctx {
     int device = 0;
     int sm_count = 0;
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_mid = nullptr;
+    long long *d_ctrl_snap = nullptr;  // counters after the first kernel of a two-kernel solve
+    bool split_last = false;           // the last solve ran two kernels (ev_mid, d_ctrl_snap valid)
     pnjl_params params{};
     pnjl::DevParams dp{};
     // nodes
@@ -29,7 +31,7 @@ struct pnjl_ctx {
     std::vector<double> p_mesh, c_mesh, coef;
     double *d_nodes = nullptr;  // p2[p] | A[p] | c2[t] | B[t]
     float *d_nodes_f = nullptr; // the same in FP32
-    // control block: [0] queue head, [1..15] counters
+    // control block (kCtrlSlots): [0] queue head, [1..kStatCount] counters, list length, task queue
     long long *d_ctrl = nullptr;
     double *d_seed_tables = nullptr; // 2 * 16 * 5
     unsigned char *d_vmap = nullptr;  // device copy of the verification map
@@ -125,6 +127,8 @@ pnjl::KernelNodes kernel_nodes(const pnjl_ctx *ctx) {
     kn.Af = ctx->d_nodes_f + np;
     kn.c2f = ctx->d_nodes_f + 2 * np;
     kn.Bf = ctx->d_nodes_f + 2 * np + nt;
+    kn.lo = ctx->d_nodes_f + 2 * (np + nt);
+    kn.expt = ctx->d_nodes_f + 4 * (np + nt);
     return kn;
 }
 
@@ -171,7 +175,7 @@ pnjl::MlpDev mlp_dev(pnjl_ctx *ctx) {
     m.grad = ctx->mlp.params + pnjl::kParamCount;
     m.adam_m = ctx->mlp.params + 2 * pnjl::kParamCount;
     m.adam_v = ctx->mlp.params + 3 * pnjl::kParamCount;
-    const int H = pnjl::mlp::H, IN = pnjl::mlp::IN, OUT = pnjl::mlp::OUT;
+    const int H = pnjl::mlp::H, IN = pnjl::mlp::IN;
     m.w1b = ctx->mlp.wb;
     m.w2b = ctx->mlp.wb + H * IN;
     m.w3b = m.w2b + H * H;
@@ -248,7 +252,9 @@ int pnjl_init(const pnjl_params *params, int device, pnjl_ctx **out) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
-    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_ctrl, 16 * sizeof(long long));
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_mid);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_ctrl, pnjl::kCtrlSlots * sizeof(long long));
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_ctrl_snap, pnjl::kCtrlSlots * sizeof(long long));
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_seed_tables, 2 * 16 * 5 * sizeof(double));
     if (e != cudaSuccess) {
         std::fprintf(stderr, "pnjl_init: %s\n", cudaGetErrorString(e));
@@ -281,6 +287,8 @@ int pnjl_destroy(pnjl_ctx *ctx) {
     cudaFree(ctx->mlp.seeds);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->ev_mid) cudaEventDestroy(ctx->ev_mid);
+    cudaFree(ctx->d_ctrl_snap);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return PNJL_OK;
@@ -309,19 +317,22 @@ int pnjl_set_nodes(pnjl_ctx *ctx, int32_t p_num, int32_t t_num, double p_max) {
             ctx->coef[k] = (wp[ip] * (wc[it] * 2.0)) * (xp[ip] * xp[ip]) / fourpi2;
         }
     // separable device tables: p2[p] | A[p] = w_p p^2/(2 pi)^2 | c2[t] | B[t] = 2 w_c
+    // FP32 device tables: hi parts | float-float lo parts | float-float exp tables
     const int m = 2 * (p_num + t_num);
     std::vector<double> h(m);
-    std::vector<float> hf(m);
-    pnjl::separable_tables(p_num, t_num, xp.data(), wp.data(), xc.data(), wc.data(), h.data(), hf.data());
+    std::vector<float> hf(2 * m + pnjl::kExpTableFloats);
+    pnjl::separable_tables(p_num, t_num, xp.data(), wp.data(), xc.data(), wc.data(), h.data(), hf.data(),
+                           hf.data() + m);
+    pnjl::ff_exp_tables(hf.data() + 2 * m);
     PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     cudaFree(ctx->d_nodes);
     cudaFree(ctx->d_nodes_f);
     ctx->d_nodes = nullptr;
     ctx->d_nodes_f = nullptr;
     PNJL_CUDA_TRY(ctx, cudaMalloc(&ctx->d_nodes, m * sizeof(double)));
-    PNJL_CUDA_TRY(ctx, cudaMalloc(&ctx->d_nodes_f, m * sizeof(float)));
+    PNJL_CUDA_TRY(ctx, cudaMalloc(&ctx->d_nodes_f, hf.size() * sizeof(float)));
     PNJL_CUDA_TRY(ctx, cudaMemcpy(ctx->d_nodes, h.data(), m * sizeof(double), cudaMemcpyHostToDevice));
-    PNJL_CUDA_TRY(ctx, cudaMemcpy(ctx->d_nodes_f, hf.data(), m * sizeof(float), cudaMemcpyHostToDevice));
+    PNJL_CUDA_TRY(ctx, cudaMemcpy(ctx->d_nodes_f, hf.data(), hf.size() * sizeof(float), cudaMemcpyHostToDevice));
     ctx->p_num = p_num;
     ctx->t_num = t_num;
     ctx->p_max = p_max;
@@ -345,8 +356,10 @@ static int eval_common(pnjl_ctx *ctx, int64_t n, const double *x, const double *
     if (ctx->p_num == 0) return fail(ctx, PNJL_ERR_NO_NODES, "call pnjl_set_nodes first");
     if (n < 0 || (n > 0 && (!x || !T || !mu_u || !mu_d || !mu_s || !xi)))
         return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "null input array");
-    if (precision != PNJL_PREC_FP64 && precision != PNJL_PREC_MIXED)
+    if (precision != PNJL_PREC_FP64 && precision != PNJL_PREC_MIXED && precision != PNJL_PREC_FF_RESIDUAL)
         return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "unknown precision");
+    if (precision == PNJL_PREC_FF_RESIDUAL && out)
+        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "the float-float pass gives the residual only");
     if (n == 0) return PNJL_OK;
     cudaSetDevice(ctx->device);
     const size_t nn = (size_t)n;
@@ -380,7 +393,7 @@ static int eval_common(pnjl_ctx *ctx, int64_t n, const double *x, const double *
     pnjl::EvalArgs a{};
     a.P = ctx->dp;
     a.nodes = kernel_nodes(ctx);
-    const bool fp32 = precision == PNJL_PREC_MIXED;
+    const int mode = precision;  // 0 FP64, 1 FP32-Kahan, 2 float-float residual
     const size_t smem = pnjl::node_smem_bytes(ctx->p_num, ctx->t_num);
     a.n = n;
     a.x = dx; a.T = dT; a.mu_u = du; a.mu_d = dd; a.mu_s = ds; a.xi = dxi;
@@ -388,7 +401,7 @@ static int eval_common(pnjl_ctx *ctx, int64_t n, const double *x, const double *
     a.out = dout;
     int64_t blocks = (n + 7) / 8;
     int grid = (int)std::min<int64_t>(blocks, (int64_t)ctx->sm_count * 8);
-    cudaError_t e = pnjl::launch_eval(a, fp32, grid, smem, s);
+    cudaError_t e = pnjl::launch_eval(a, mode, grid, smem, s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "eval_kernel launch");
     ctx->stats.kernel_launches += 1;
     if (omega) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(omega, dom, nn * 8, cudaMemcpyDeviceToHost, s));
@@ -473,7 +486,7 @@ int pnjl_solve_batch_device(pnjl_ctx *ctx, int64_t n, const double *d_T, const d
         PNJL_CUDA_TRY(ctx, cudaMemsetAsync(q, 0, b_done + b_flag, s));
         PNJL_CUDA_TRY(ctx, cudaMemsetAsync(a.best_omega, 0xff, nn * sizeof(double), s));
     }
-    PNJL_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_ctrl, 0, 16 * sizeof(long long), s));
+    PNJL_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_ctrl, 0, pnjl::kCtrlSlots * sizeof(long long), s));
     a.P = ctx->dp;
     a.nodes = kernel_nodes(ctx);
     const size_t smem = pnjl::node_smem_bytes(ctx->p_num, ctx->t_num);
@@ -525,8 +538,22 @@ int pnjl_solve_batch_device(pnjl_ctx *ctx, int64_t n, const double *d_T, const d
         grid = grid_for(ctx, group, smem, n_tasks);
     }
     PNJL_CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, s));
-    cudaError_t e = mixed ? pnjl::launch_solve_mixed(a, grid, grid_tasks, smem, s)
-                          : pnjl::launch_solve(a, group, grid, smem, s);
+    cudaError_t e = cudaSuccess;
+    ctx->split_last = mixed && launches == 2;
+    if (!mixed) {
+        e = pnjl::launch_solve(a, group, grid, smem, s);
+    } else if (opts->seed_mode == PNJL_SEEDS_TABLE) {
+        e = pnjl::launch_mixed_tasks(a, grid_tasks, smem, s);
+    } else {
+        e = pnjl::launch_mixed_points(a, grid, smem, s);
+        if (e == cudaSuccess && ctx->split_last) {
+            // the per-point kernel's own time and counters, then the task kernel
+            PNJL_CUDA_TRY(ctx, cudaEventRecord(ctx->ev_mid, s));
+            PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_ctrl_snap, ctx->d_ctrl, pnjl::kCtrlSlots * sizeof(long long),
+                                               cudaMemcpyDeviceToDevice, s));
+            e = pnjl::launch_mixed_tasks(a, grid_tasks, smem, s);
+        }
+    }
     if (e != cudaSuccess) return cuda_fail(ctx, e, "solve kernel launch");
     PNJL_CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, s));
     ctx->stats.kernel_launches += launches;
@@ -869,14 +896,7 @@ int pnjl_synchronize(pnjl_ctx *ctx) {
     return PNJL_OK;
 }
 
-int pnjl_get_stats(const pnjl_ctx *cctx, pnjl_stats *out) {
-    pnjl_ctx *ctx = const_cast<pnjl_ctx *>(cctx);
-    if (!ctx || !out) return PNJL_ERR_INVALID_ARGUMENT;
-    long long h[16];
-    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(h, ctx->d_ctrl, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
-    PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-    pnjl_stats st = ctx->stats;
-    const long long *c = h + 1;
+static void fill_counters(pnjl_stats &st, const long long *c) {
     st.passes_fp64 = c[pnjl::kStatPasses64];
     st.node_evals_fp64_newton = c[pnjl::kStatEvalsNewton64];
     st.node_evals_fp64_thermo = c[pnjl::kStatEvalsThermo64];
@@ -892,10 +912,53 @@ int pnjl_get_stats(const pnjl_ctx *cctx, pnjl_stats *out) {
     st.fp64_rescues = c[pnjl::kStatRescue64];
     st.node_evals_fp32_thermo = c[pnjl::kStatEvalsThermo32];
     st.pruned_candidates = c[pnjl::kStatPruned];
+    st.node_evals_ff = c[pnjl::kStatEvalsFF];
+    st.node_evals_ff_thermo = c[pnjl::kStatEvalsFFThermo];
+}
+
+int pnjl_get_stats(const pnjl_ctx *cctx, pnjl_stats *out) {
+    pnjl_ctx *ctx = const_cast<pnjl_ctx *>(cctx);
+    if (!ctx || !out) return PNJL_ERR_INVALID_ARGUMENT;
+    long long h[pnjl::kCtrlSlots];
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(h, ctx->d_ctrl, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+    PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    pnjl_stats st = ctx->stats;
+    fill_counters(st, h + 1);
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1) == cudaSuccess) st.last_kernel_ms = ms;
     *out = st;
     ctx->stats = st;
+    return PNJL_OK;
+}
+
+int pnjl_get_kernel_stats(const pnjl_ctx *cctx, int32_t kernel, pnjl_stats *out) {
+    pnjl_ctx *ctx = const_cast<pnjl_ctx *>(cctx);
+    if (!ctx || !out || (kernel != 0 && kernel != 1)) return PNJL_ERR_INVALID_ARGUMENT;
+    pnjl_stats total{};
+    int rc = pnjl_get_stats(ctx, &total);
+    if (rc) return rc;
+    pnjl_stats st = total;
+    if (!ctx->split_last) {
+        if (kernel == 1) {  // no second kernel: zero work
+            pnjl_stats z{};
+            z.points = total.points;
+            z.kernel_launches = total.kernel_launches;
+            *out = z;
+            return PNJL_OK;
+        }
+        *out = total;
+        return PNJL_OK;
+    }
+    long long h[pnjl::kCtrlSlots], t[pnjl::kCtrlSlots];
+    PNJL_CUDA_TRY(ctx, cudaMemcpy(h, ctx->d_ctrl_snap, sizeof h, cudaMemcpyDeviceToHost));
+    PNJL_CUDA_TRY(ctx, cudaMemcpy(t, ctx->d_ctrl, sizeof t, cudaMemcpyDeviceToHost));
+    if (kernel == 1)
+        for (int k = 0; k < pnjl::kCtrlSlots; ++k) h[k] = t[k] - h[k];
+    fill_counters(st, h + 1);
+    float ms = 0.f;
+    if (kernel == 0 && cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev_mid) == cudaSuccess) st.last_kernel_ms = ms;
+    if (kernel == 1 && cudaEventElapsedTime(&ms, ctx->ev_mid, ctx->ev1) == cudaSuccess) st.last_kernel_ms = ms;
+    *out = st;
     return PNJL_OK;
 }
 

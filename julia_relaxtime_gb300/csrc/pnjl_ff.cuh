@@ -1,0 +1,257 @@
+// pnjl_ff.cuh -- float-float ("double-single") residual pass of the mixed-precision solver.
+//
+// A float-float number is an unevaluated sum hi + lo of two FP32 values (|lo| <= ulp(hi)/2),
+// about 44-48 significant bits.  Its arithmetic runs on the FP32 pipe, which on this GPU has
+// 64x the FP64 rate, so one float-float pass over the nodes costs a small fraction of an FP64
+// pass.  The mixed solver uses it for exactly one thing: the residual F(x32) at the FP32 root,
+// accurate to ~1e-12, from which one FP64-Jacobian-free correction step lands within the FP64
+// certification radius.  Convergence is still certified by an FP64 residual pass (and the
+// thermodynamics come from that FP64 pass), so this pass only saves the FP64 residual pass
+// that used to precede the correction step.
+//
+// Error-free transformations (Knuth's TwoSum, Dekker's Fast2Sum, the FMA product), the
+// float-float add and multiply follow the published double-single / double-double algorithms
+// (Dekker 1971; Hida, Li and Bailey, "Library for double-double and quad-double arithmetic",
+// 2007).  exp is table-driven in the manner of Tang (ACM TOMS 15, 1989): e^x = e^n e^(j/16) e^g
+// with n integer, |g| <= 1/32 and a degree-7 Taylor polynomial.  Reciprocal and reciprocal
+// square root are one Newton step from the correctly rounded FP32 value.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace pnjl {
+
+struct ff {
+    float h, l;
+};
+
+// exp tables in shared memory: e^k (k = -kExpMaxN..kExpMaxN) and e^(j/16) (j = -8..8), as (h, l)
+constexpr int kExpMaxN = 88;
+constexpr int kExpIntN = 2 * kExpMaxN + 1;
+constexpr int kExpFracN = 17;
+constexpr int kExpTableFloats = 2 * (kExpIntN + kExpFracN);
+
+__device__ __forceinline__ ff ff_make(float h) { return ff{h, 0.0f}; }
+__device__ __forceinline__ ff ff_from_float_pair(float h, float l) { return ff{h, l}; }
+__device__ __forceinline__ ff ff_from_double(double d) {
+    const float h = __double2float_rn(d);
+    return ff{h, __double2float_rn(d - (double)h)};
+}
+__device__ __forceinline__ double ff_to_double(ff a) { return (double)a.h + (double)a.l; }
+
+__device__ __forceinline__ ff two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return ff{s, e};
+}
+__device__ __forceinline__ ff fast_two_sum(float a, float b) {  // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return ff{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ ff two_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    return ff{p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+    const ff s = two_sum(a.h, b.h);
+    const ff t = two_sum(a.l, b.l);
+    ff r = fast_two_sum(s.h, __fadd_rn(s.l, t.h));
+    return fast_two_sum(r.h, __fadd_rn(r.l, t.l));
+}
+__device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.h, -a.l}; }
+__device__ __forceinline__ ff ff_sub(ff a, ff b) { return ff_add(a, ff_neg(b)); }
+__device__ __forceinline__ ff ff_add_f(ff a, float b) {
+    const ff s = two_sum(a.h, b);
+    return fast_two_sum(s.h, __fadd_rn(s.l, a.l));
+}
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+    const ff p = two_prod(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.l, p.l);
+    e = __fmaf_rn(a.l, b.h, e);
+    return fast_two_sum(p.h, e);
+}
+__device__ __forceinline__ ff ff_mul_f(ff a, float b) {
+    const ff p = two_prod(a.h, b);
+    return fast_two_sum(p.h, __fmaf_rn(a.l, b, p.l));
+}
+__device__ __forceinline__ ff ff_sel(bool c, ff a, ff b) { return ff{c ? a.h : b.h, c ? a.l : b.l}; }
+
+// 1/b: one Newton step y = y0 + y0 (1 - b y0) from the correctly rounded FP32 reciprocal
+__device__ __forceinline__ ff ff_rcp(ff b) {
+    const float y0 = __frcp_rn(b.h);
+    const ff e = ff_sub(ff_make(1.0f), ff_mul_f(b, y0));
+    return ff_add_f(ff_mul_f(e, y0), y0);
+}
+
+// 1/sqrt(x): one Newton step y = y0 + y0 (1 - x y0^2) / 2 from the FP32 value
+__device__ __forceinline__ ff ff_rsqrt(ff x) {
+    const float y0 = __frsqrt_rn(x.h);
+    const ff r = ff_mul(x, two_prod(y0, y0));
+    const ff e = ff_sub(ff_make(1.0f), r);
+    return ff_add_f(ff_mul_f(e, 0.5f * y0), y0);
+}
+
+// e^x for |x| <= 88 (0 below, +inf above): x = n + f with n = rint(x), |f| <= 1/2; f = j/16 + g
+// with |g| <= 1/32; e^g by Taylor to degree 7 (remainder below 2e-17), the terms from g^4 on
+// in FP32.
+__device__ __forceinline__ ff ff_exp(ff x, const float *tab) {
+    if (!(x.h > -88.0f)) return ff{0.0f, 0.0f};
+    if (!(x.h < 88.0f)) return ff{__int_as_float(0x7f800000), 0.0f};
+    const float nf = rintf(x.h);
+    const int n = (int)nf;                           // -88..88
+    const ff f = two_sum(__fsub_rn(x.h, nf), x.l);  // x.h - nf is exact
+    const float jf = rintf(f.h * 16.0f);
+    const int j = (int)jf;  // -8..8
+    const ff g = fast_two_sum(__fsub_rn(f.h, jf * 0.0625f), f.l);
+    const float gh = g.h;
+    // q = 1/24 + g/120 + g^2/720 + g^3/5040
+    float q = __fmaf_rn(gh, 1.0f / 5040.0f, 1.0f / 720.0f);
+    q = __fmaf_rn(gh, q, 1.0f / 120.0f);
+    q = __fmaf_rn(gh, q, 1.0f / 24.0f);
+    // e^g = 1 + g + g^2 (1/2 + g (1/6 + g q))
+    const ff sixth{0.166666671633720398f, -4.96705388e-09f};  // 1/6 as float-float
+    ff u = ff_add(sixth, two_prod(gh, q));
+    u = ff_add_f(ff_mul(g, u), 0.5f);
+    u = ff_mul(ff_mul(g, g), u);
+    const ff eg = ff_add(ff_add_f(g, 1.0f), u);
+    const ff en{tab[2 * (n + kExpMaxN)], tab[2 * (n + kExpMaxN) + 1]};
+    const ff ej{tab[2 * (kExpIntN + j + 8)], tab[2 * (kExpIntN + j + 8) + 1]};
+    return ff_mul(ff_mul(en, ej), eg);
+}
+
+// ln x for x > 0: one Newton step y = y0 + x e^-y0 - 1 from the FP32 logarithm (its error
+// squares: ~1e-7 -> ~1e-14).
+__device__ __forceinline__ ff ff_log(ff x, const float *tab) {
+    const float y0 = logf(x.h);
+    const ff e = ff_mul(x, ff_exp(ff_make(-y0), tab));
+    return ff_add_f(ff_add_f(e, -1.0f), y0);
+}
+
+// Per-flavour constants of a float-float pass (the same branch-free form as FlavourConst).
+struct FlavourFF {
+    ff M, M2, mu, invT, C, C2;
+    ff Pq, Pa, Pq2, Pa2;
+    ff k1_0, k2_0, k1_1, k2_1;
+    ff e3_0, e2_0, e1_0, e2_1, e1_1, e0_1;
+};
+
+__device__ __forceinline__ FlavourFF make_flavour_ff(double M, double mu, double T, double Phi, double Phib,
+                                                     bool &swapped) {
+    FlavourFF fc;
+    swapped = mu < 0.0;
+    const double mua = swapped ? -mu : mu;
+    const double Pq = swapped ? Phib : Phi;
+    const double Pa = swapped ? Phi : Phib;
+    const double C = exp(-2.0 * mua / T);
+    fc.M = ff_from_double(M);
+    fc.M2 = ff_from_double(M * M);
+    fc.mu = ff_from_double(mua);
+    fc.invT = ff_from_double(1.0 / T);
+    fc.C = ff_from_double(C);
+    fc.C2 = ff_from_double(C * C);
+    fc.Pq = ff_from_double(Pq);
+    fc.Pa = ff_from_double(Pa);
+    fc.Pq2 = ff_from_double(2.0 * Pq);
+    fc.Pa2 = ff_from_double(2.0 * Pa);
+    fc.k1_0 = ff_from_double(3.0 * Pq);
+    fc.k2_0 = ff_from_double(3.0 * Pa);
+    fc.k1_1 = fc.k2_0;
+    fc.k2_1 = fc.k1_0;
+    fc.e3_0 = ff_from_double(C * C * C);
+    fc.e2_0 = ff_from_double(3.0 * Pq * C * C);
+    fc.e1_0 = ff_from_double(3.0 * Pa * C);
+    fc.e2_1 = fc.e1_0;
+    fc.e1_1 = fc.e2_0;
+    fc.e0_1 = fc.e3_0;
+    return fc;
+}
+
+// Per-flavour sums of a float-float pass: gradient terms dD/dM, dD/dPhi, dD/dPhibar (quark /
+// antiquark side) and thermo terms (number sums, a n+ + b n-, log term).
+struct FlavourAccFF {
+    ff DM, Sq, Sa, Nq, Na, SAN, SL;
+    __device__ __forceinline__ void zero() {
+        DM = Sq = Sa = Nq = Na = SAN = SL = ff{0.0f, 0.0f};
+    }
+};
+
+// One node-flavour evaluation (node_flavour<..., GRAD, THERMO> of pnjl_device.cuh in
+// float-float), with the reference's clamps max(f, 1e-16) decided on the leading parts.
+template <bool GRAD, bool THERMO>
+__device__ __forceinline__ void node_flavour_ff(const FlavourFF &fc, ff q2, ff w, const float *etab,
+                                                FlavourAccFF &acc) {
+    const ff E2 = ff_add(q2, fc.M2);
+    const ff rE = ff_rsqrt(E2);
+    const ff E = ff_mul(E2, rE);
+    const ff a = ff_mul(ff_sub(fc.mu, E), fc.invT);
+    const bool sig = a.h > 0.0f;
+    const ff t = ff_exp(sig ? ff_neg(a) : a, etab);
+    const ff t2 = ff_mul(t, t);
+    const ff t3 = ff_mul(t2, t);
+    const ff k1 = ff_sel(sig, fc.k1_1, fc.k1_0);
+    const ff k2 = ff_sel(sig, fc.k2_1, fc.k2_0);
+    const ff fp = ff_add_f(ff_mul(ff_add(ff_mul(ff_add(t, k2), t), k1), t), 1.0f);
+    const ff e3 = ff_sel(sig, ff_make(1.0f), fc.e3_0);
+    const ff e2 = ff_sel(sig, fc.e2_1, fc.e2_0);
+    const ff e1 = ff_sel(sig, fc.e1_1, fc.e1_0);
+    const ff e0 = ff_sel(sig, fc.e0_1, ff_make(1.0f));
+    const ff gm = ff_add(ff_mul(ff_add(ff_mul(ff_add(ff_mul(e3, t), e2), t), e1), t), e0);
+    const float alpha3 = sig ? t3.h : 1.0f;
+    const bool clP = fp.h < 1e-16f;
+    const bool clM = gm.h < 1e-16f * alpha3;
+    const ff fpc = clP ? ff_make(1.0f) : fp;
+    const ff gmc = clM ? ff_make(1.0f) : gm;
+    const ff prod = ff_mul(fpc, gmc);
+    const ff Rr = ff_rcp(prod);
+    const ff ip = clP ? ff_make(0.0f) : ff_mul(gmc, Rr);
+    const ff im = clM ? ff_make(0.0f) : ff_mul(fpc, Rr);
+    const ff u1 = ff_sel(sig, t2, t);
+    const ff u2 = ff_sel(sig, t, t2);
+    const ff u3 = ff_sel(sig, ff_make(1.0f), t3);
+    const ff r1 = ff_mul(u1, ip), r2 = ff_mul(u2, ip), r3 = ff_mul(u3, ip);
+    const ff Cim = ff_mul(fc.C, im);
+    const ff s1 = ff_mul(u1, Cim);
+    const ff s2 = ff_mul(fc.C, ff_mul(u2, Cim));
+    const ff s3 = ff_mul(fc.C2, ff_mul(u3, Cim));
+    const ff np = clP ? ff_make(sig ? 1.0f : 0.0f) : ff_add(ff_add(ff_mul(fc.Pq, r1), ff_mul(fc.Pa2, r2)), r3);
+    const ff nm = clM ? ff_make(0.0f) : ff_add(ff_add(ff_mul(fc.Pa, s1), ff_mul(fc.Pq2, s2)), s3);
+    if (GRAD) {
+        const ff mE = ff_mul(fc.M, rE);
+        const ff LE = ff_mul_f(ff_mul(ff_add(np, nm), fc.invT), -3.0f);
+        acc.DM = ff_add(acc.DM, ff_mul(w, ff_mul(LE, mE)));
+        acc.Sq = ff_add(acc.Sq, ff_mul_f(ff_mul(w, ff_add(r1, s2)), 3.0f));
+        acc.Sa = ff_add(acc.Sa, ff_mul_f(ff_mul(w, ff_add(r2, s1)), 3.0f));
+    }
+    if (THERMO) {
+        acc.Nq = ff_add(acc.Nq, ff_mul(w, np));
+        acc.Na = ff_add(acc.Na, ff_mul(w, nm));
+        const ff b = ff_sub(a, ff_mul_f(ff_mul(fc.mu, fc.invT), 2.0f));
+        acc.SAN = ff_add(acc.SAN, ff_mul(w, ff_add(ff_mul(a, np), ff_mul(b, nm))));
+        // ln f+ + ln f- = 6 max(a,0) + ln(fp gm); a clamped factor is replaced by the
+        // reference's constant (log(1e-16), plus 3a in its rescaled quark branch)
+        ff L = ff_log(prod, etab);
+        if (sig) L = ff_add(L, ff_mul_f(a, 6.0f));
+        if (clP) L = ff_add(L, ff_from_float_pair(-36.84136199951171875f, 5.11606970e-07f));
+        if (clM) {
+            L = ff_add(L, ff_from_float_pair(-36.84136199951171875f, 5.11606970e-07f));
+            if (sig) L = ff_sub(L, ff_mul_f(a, 3.0f));
+        }
+        acc.SL = ff_add(acc.SL, ff_mul(w, L));
+    }
+}
+
+// Butterfly sum of a float-float value over the lanes of a group (every lane ends with the
+// same bits: a + b and b + a are computed by the same operation order on both partners only
+// up to commutativity of TwoSum, which is exact, so the results are identical).
+template <int G>
+__device__ __forceinline__ ff group_sum_ffv(ff v, unsigned mask) {
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) {
+        const ff u{__shfl_xor_sync(mask, v.h, o), __shfl_xor_sync(mask, v.l, o)};
+        v = ff_add(v, u);
+    }
+    return v;
+}
+
+}  // namespace pnjl

@@ -24,6 +24,17 @@ __device__ __forceinline__ NodeView stage_nodes(const KernelNodes &kn, void *sme
     for (int i = threadIdx.x; i < nt; i += blockDim.x) { sf[2 * np + i] = kn.c2f[i]; sf[2 * np + nt + i] = kn.Bf[i]; }
     nv.p2 = sd; nv.A = sd + np; nv.c2 = sd + 2 * np; nv.B = sd + 2 * np + nt;
     nv.p2f = sf; nv.Af = sf + np; nv.c2f = sf + 2 * np; nv.Bf = sf + 2 * np + nt;
+    nv.p2l = nv.Al = nv.c2l = nv.Bl = nullptr;
+    nv.expt = nullptr;
+    if (kn.lo && kn.expt) {
+        const int m = 2 * (np + nt);
+        float *sl = sf + m;
+        for (int i = threadIdx.x; i < m; i += blockDim.x) sl[i] = kn.lo[i];
+        float *se = sl + m;
+        for (int i = threadIdx.x; i < kExpTableFloats; i += blockDim.x) se[i] = kn.expt[i];
+        nv.p2l = sl; nv.Al = sl + np; nv.c2l = sl + 2 * np; nv.Bl = sl + 2 * np + nt;
+        nv.expt = se;
+    }
     return nv;
 }
 
@@ -351,6 +362,44 @@ struct Group {
         return false;
     }
 
+    // Residual at x from the float-float pass (FP32 pipe, ~1e-12 accurate); false when the
+    // float-float tables are not staged or a sum is not finite (FP32 range exceeded).
+    __device__ __noinline__ bool eval_grad_ff(const PointIn &pt, const double *x, double *F) {
+        if (!nv.p2l) return false;
+        double M[3];
+        masses(P, x, M);
+        PassSums S;
+        node_pass_ff<G, true, false>(nv, pt, x, M, gl, mask, S, cnt.v[kStatEvalsFF]);
+        Eval ev;
+        double V, V1[3], V2[3];
+        vacuum_terms<G>(P, M, gl, mask, leader(), V, V1, V2);
+        assemble<true, false, false>(P, pt, x, M, S, V, V1, V2, ev);
+        for (int i = 0; i < 5; ++i) F[i] = ev.F[i];
+        cnt.v[kStatPasses32] += 1;
+        return all_finite5(F);
+    }
+
+    // Omega, entropy, rho_f and number densities at c.x from the float-float pass (the
+    // outputs of a certified candidate, ~1e-13 relative); false when not available or not
+    // finite (the caller then uses the FP64 thermo pass).
+    __device__ __noinline__ bool eval_thermo_ff(const PointIn &pt, const SolveOpts &o, Candidate &c) {
+        if (!nv.p2l) return false;
+        double M[3];
+        masses(P, c.x, M);
+        PassSums S;
+        node_pass_ff<G, false, true>(nv, pt, c.x, M, gl, mask, S, cnt.v[kStatEvalsFFThermo]);
+        Eval ev;
+        double V, V1[3], V2[3];
+        vacuum_terms<G>(P, M, gl, mask, leader(), V, V1, V2);
+        assemble<false, false, true>(P, pt, c.x, M, S, V, V1, V2, ev);
+        cnt.v[kStatPasses32] += 1;
+        bool ok = ev.omega == ev.omega && fabs(ev.omega) < 1e300 && ev.dOdT == ev.dOdT;
+        for (int f = 0; f < 3; ++f) ok = ok && ev.rho[f] == ev.rho[f] && ev.nq[f] == ev.nq[f] && ev.naq[f] == ev.naq[f];
+        if (!ok) return false;
+        postprocess(P, pt, o, ev, c);
+        return true;
+    }
+
     __device__ __noinline__ void eval_grad64(const PointIn &pt, const double *x, double *F) {
         double M[3];
         masses(P, x, M);
@@ -364,26 +413,6 @@ struct Group {
         cnt.v[kStatPasses64] += 1;
     }
 
-    __device__ __noinline__ void eval_grad_thermo64(const PointIn &pt, const SolveOpts &o, Candidate &c, double *F) {
-        double M[3];
-        masses(P, c.x, M);
-        PassSums S;
-        node_pass<double, false, true, false, true, G>(nv, pt, c.x, M, gl, mask, S, cnt.v[kStatEvalsGradThermo64]);
-        Eval ev;
-        double V, V1[3], V2[3];
-        vacuum_terms<G>(P, M, gl, mask, leader(), V, V1, V2);
-        assemble<true, false, true>(P, pt, c.x, M, S, V, V1, V2, ev);
-        for (int i = 0; i < 5; ++i) F[i] = ev.F[i];
-        cnt.v[kStatPasses64] += 1;
-        postprocess(P, pt, o, ev, c);
-    }
-
-    // 1: reached the FP32 floor, 0: did not converge, -1: residual at x0 not finite.
-    // The FP32 phase ends at the first of: a tiny residual; a Newton step at the FP32
-    // resolution (relative kStall32) with a small residual; a small residual that stopped
-    // halving for two steps (the FP32 noise floor, or the linear convergence of a nearly
-    // singular Jacobian, which the FP64 phase then finishes); the iteration limit with a
-    // small residual.
     __device__ int newton32(const PointIn &pt, const double *x0, const SolveOpts &o, double *x, double *J, int &iters) {
         double F[5], p[5];
         for (int i = 0; i < 5; ++i) x[i] = x0[i];
@@ -499,15 +528,20 @@ struct Group {
         c.exception = false;
         c.phys = false;
         c.omega = c.entropy = qnan();
-        eval_grad64(pt, c.x, F);
+        // the first residual, at the FP32 root, from the float-float pass (it only steers the
+        // first correction step; every certifying residual is FP64)
+        bool certifiable = false;
+        if (!eval_grad_ff(pt, c.x, F)) {
+            eval_grad64(pt, c.x, F);
+            certifiable = true;
+        }
         steps = 0;
-        bool thermo_at_x = false;
         double fb = 0.0, fprev = 0.0;
         for (;;) {
             const double fn = norm_inf5(F);
             c.residual_norm = fn;
             const bool bad = !(fn == fn) || any_nan5(c.x);
-            if (!bad && fn < o.ftol) { c.f_converged = true; break; }
+            if (!bad && certifiable && fn < o.ftol) { c.f_converged = true; break; }
             if (!bad && (steps == 0 || fn < fb)) {
                 for (int i = 0; i < 5; ++i) xb[i] = c.x[i];
                 fb = fn;
@@ -528,8 +562,8 @@ struct Group {
             symmetrize_step(pt, c.x, p);
             for (int i = 0; i < 5; ++i) { c.x[i] += p[i]; Fo[i] = F[i]; }
             ++steps;
-            eval_grad_thermo64(pt, o, c, F);
-            thermo_at_x = true;
+            eval_grad64(pt, c.x, F);
+            certifiable = true;
             double pp = 0.0;
             for (int i = 0; i < 5; ++i) pp += p[i] * p[i];
             if (pp > 0.0) {
@@ -541,7 +575,8 @@ struct Group {
                 }
             }
         }
-        if (!thermo_at_x) eval_thermo(pt, o, c);
+        // the outputs at the certified state: float-float thermo pass (FP64 pass if unavailable)
+        if (!eval_thermo_ff(pt, o, c)) eval_thermo(pt, o, c);
     }
 
     // Mixed-precision counterpart of solve_seed.  `dup` is set when the FP32 solution is a

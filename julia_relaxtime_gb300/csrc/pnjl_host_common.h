@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdint>
 
+#include "pnjl_ff.cuh"
 #include "pnjl_kernels.h"
 
 namespace pnjl {
@@ -63,7 +64,7 @@ static constexpr int kMaxTNodes = 64;
 // Separable device tables p2[p] | A[p] = w_p p^2/(2 pi)^2 | c2[t] | B[t] = 2 w_c
 // (2 (p + t) values) from the p rule on [0, p_max] and the cos(theta) rule on [0, 1].
 inline void separable_tables(int p_num, int t_num, const double *xp, const double *wp, const double *xc,
-                             const double *wc, double *h, float *hf) {
+                             const double *wc, double *h, float *hf, float *hl = nullptr) {
     const double fourpi2 = (2.0 * M_PI) * (2.0 * M_PI);
     for (int ip = 0; ip < p_num; ++ip) {
         h[ip] = xp[ip] * xp[ip];
@@ -75,6 +76,25 @@ inline void separable_tables(int p_num, int t_num, const double *xp, const doubl
     }
     const int m = 2 * (p_num + t_num);
     for (int i = 0; i < m; ++i) hf[i] = (float)h[i];
+    if (hl)  // float-float low parts: h = hf + hl to ~2^-48
+        for (int i = 0; i < m; ++i) hl[i] = (float)(h[i] - (double)hf[i]);
+}
+
+// Float-float tables of the float-float exp (pnjl_ff.cuh): e^k for k = -kExpMaxN..kExpMaxN, then
+// e^(j/16) for j = -8..8, each as (hi, lo) floats, from long-double exp.
+inline void ff_exp_tables(float *out) {
+    for (int k = -kExpMaxN; k <= kExpMaxN; ++k) {
+        const long double v = expl((long double)k);
+        const float h = (float)v;
+        out[2 * (k + kExpMaxN)] = h;
+        out[2 * (k + kExpMaxN) + 1] = (float)(v - (long double)h);
+    }
+    for (int j = -8; j <= 8; ++j) {
+        const long double v = expl((long double)j / 16.0L);
+        const float h = (float)v;
+        out[2 * (kExpIntN + j + 8)] = h;
+        out[2 * (kExpIntN + j + 8) + 1] = (float)(v - (long double)h);
+    }
 }
 
 // Checks of pnjl_solve_opts; returns PNJL_OK or PNJL_ERR_INVALID_ARGUMENT and a message.

@@ -15,7 +15,10 @@
 
 namespace pnjl {
 
-size_t node_smem_bytes(int p_num, int t_num) { return (size_t)(p_num + t_num) * 2 * (sizeof(double) + sizeof(float)) + 16; }
+size_t node_smem_bytes(int p_num, int t_num) {
+    // FP64 tables, FP32 tables, float-float low parts, float-float exp tables
+    return (size_t)(p_num + t_num) * 2 * (sizeof(double) + 2 * sizeof(float)) + kExpTableFloats * sizeof(float) + 16;
+}
 
 template <int G>
 __global__ void __launch_bounds__(kSolveThreads, 2) solve_kernel(SolveArgs a) {
@@ -144,8 +147,9 @@ __global__ void __launch_bounds__(kSolveThreads, 2) solve_kernel(SolveArgs a) {
             if (cnt.v[k]) atomicAdd((unsigned long long *)&a.stats[k], (unsigned long long)cnt.v[k]);
 }
 
-// One full pass + assembly per state: Omega, grad_x Omega, Hessian_x Omega and thermo.
-template <int G, bool FP32>
+// One full pass + assembly per state: Omega, grad_x Omega, Hessian_x Omega and thermo
+// (MODE 0 FP64, 1 FP32-Kahan); MODE 2: the float-float residual pass alone.
+template <int G, int MODE>
 __global__ void __launch_bounds__(kSolveThreads) eval_kernel(EvalArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const NodeView nv = stage_nodes(a.nodes, smem_raw);
@@ -169,10 +173,23 @@ __global__ void __launch_bounds__(kSolveThreads) eval_kernel(EvalArgs a) {
         double M[3];
         masses(a.P, x, M);
         PassSums S;
-        if (FP32) node_pass<float, true, true, true, true, G>(nv, pt, x, M, gl, mask, S, evals);
-        else node_pass<double, false, true, true, true, G>(nv, pt, x, M, gl, mask, S, evals);
         Eval ev;
         double V, V1[3], V2[3];
+        if constexpr (MODE == 2) {
+            node_pass_ff<G, true, false>(nv, pt, x, M, gl, mask, S, evals);
+            vacuum_terms<G>(a.P, M, gl, mask, lane & ~(G - 1), V, V1, V2);
+            assemble<true, false, false>(a.P, pt, x, M, S, V, V1, V2, ev);
+            if (gl == 0) {
+                if (a.omega) a.omega[i] = qnan();
+                if (a.grad) for (int k = 0; k < 5; ++k) a.grad[5 * i + k] = -ev.F[k];
+                if (a.hess) for (int k = 0; k < 25; ++k) a.hess[25 * i + k] = qnan();
+            }
+            continue;
+        } else if constexpr (MODE == 1) {
+            node_pass<float, true, true, true, true, G>(nv, pt, x, M, gl, mask, S, evals);
+        } else {
+            node_pass<double, false, true, true, true, G>(nv, pt, x, M, gl, mask, S, evals);
+        }
         vacuum_terms<G>(a.P, M, gl, mask, lane & ~(G - 1), V, V1, V2);
         assemble<true, true, true>(a.P, pt, x, M, S, V, V1, V2, ev);
         if (gl == 0) {
@@ -213,14 +230,19 @@ cudaError_t launch_solve(const SolveArgs &a, int group, int grid, size_t smem, c
     }
 }
 
-template <int G, bool FP32>
+template <int G, int MODE>
 static cudaError_t launch_eval_g(const EvalArgs &a, int grid, size_t smem, cudaStream_t s) {
-    eval_kernel<G, FP32><<<grid, kSolveThreads, smem, s>>>(a);
+    eval_kernel<G, MODE><<<grid, kSolveThreads, smem, s>>>(a);
     return cudaGetLastError();
 }
 
-cudaError_t launch_eval(const EvalArgs &a, bool fp32, int grid, size_t smem, cudaStream_t s) {
-    return fp32 ? launch_eval_g<32, true>(a, grid, smem, s) : launch_eval_g<32, false>(a, grid, smem, s);
+cudaError_t launch_eval(const EvalArgs &a, int mode, int grid, size_t smem, cudaStream_t s) {
+    switch (mode) {
+        case 0: return launch_eval_g<32, 0>(a, grid, smem, s);
+        case 1: return launch_eval_g<32, 1>(a, grid, smem, s);
+        case 2: return launch_eval_g<32, 2>(a, grid, smem, s);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 int solve_kernel_occupancy(int group, size_t smem) {

@@ -16,6 +16,9 @@ static constexpr int kSolveThreads = 256;
 struct KernelNodes {
     const double *p2, *A, *c2, *B;
     const float *p2f, *Af, *c2f, *Bf;
+    // float-float low parts of the FP32 tables (same layout) and the float-float exp tables
+    // (kExpTableFloats); null where a kernel has no float-float pass
+    const float *lo, *expt;
     int p_num, t_num;
 };
 
@@ -31,7 +34,7 @@ struct CandRec {
 enum StatSlot {
     kStatPasses64 = 0, kStatEvalsNewton64, kStatEvalsThermo64, kStatSeeds, kStatTrRuns, kStatMsFallbacks,
     kStatPasses32, kStatEvals32, kStatEvalsGrad64, kStatEvalsGradThermo64, kStatRescue64, kStatEvalsThermo32,
-    kStatPruned, kStatCount
+    kStatPruned, kStatEvalsFF, kStatEvalsFFThermo, kStatCount
 };
 
 struct SolveArgs {
@@ -64,8 +67,9 @@ struct SolveArgs {
 // Modes of a slot of the mixed task kernel: min-Omega over all seeds (MultiSeed table mode);
 // a converged per-point solution checked against the first verify_seeds seeds; a per-point
 // seed that failed, replaced by the MultiSeed solve (ImplicitSolver.jl:306-327).
-// the 16-slot control block of a context: queue head, counters, list length, task queue head
-static_assert(kStatCount + 3 <= 16, "control block too small");
+// the control block of a context: queue head, counters, list length, task queue head
+constexpr int kCtrlSlots = 32;
+static_assert(kStatCount + 3 <= kCtrlSlots, "control block too small");
 
 enum ListMode { kListFull = 0, kListVerify = 1, kListFallback = 2 };
 
@@ -80,11 +84,12 @@ struct EvalArgs {
 
 size_t node_smem_bytes(int p_num, int t_num);
 cudaError_t launch_solve(const SolveArgs &a, int group, int grid, size_t smem, cudaStream_t s);
-// Mixed precision: per-point mode launches the per-point kernel (grid_points blocks) and then
-// the task kernel over the points it deferred; table mode launches the task kernel alone.
-cudaError_t launch_solve_mixed(const SolveArgs &a, int grid_points, int grid_tasks, size_t smem, cudaStream_t s);
+// Mixed precision: per-point mode launches the per-point kernel and then the task kernel
+// over the points it deferred; table mode launches the task kernel alone.
+cudaError_t launch_mixed_points(const SolveArgs &a, int grid, size_t smem, cudaStream_t s);
+cudaError_t launch_mixed_tasks(const SolveArgs &a, int grid, size_t smem, cudaStream_t s);
 int solve_mixed_occupancy(bool tasks, size_t smem);
-cudaError_t launch_eval(const EvalArgs &a, bool fp32, int grid, size_t smem, cudaStream_t s);
+cudaError_t launch_eval(const EvalArgs &a, int mode, int grid, size_t smem, cudaStream_t s);  // 0 FP64, 1 FP32, 2 ff
 int solve_kernel_occupancy(int group, size_t smem);
 
 }  // namespace pnjl

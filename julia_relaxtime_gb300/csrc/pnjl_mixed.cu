@@ -190,14 +190,13 @@ __global__ void __launch_bounds__(kSolveThreads, 2) mixed_tasks_kernel(SolveArgs
             if (cnt.v[k]) atomicAdd((unsigned long long *)&a.stats[k], (unsigned long long)cnt.v[k]);
 }
 
-cudaError_t launch_solve_mixed(const SolveArgs &a, int grid_points, int grid_tasks, size_t smem, cudaStream_t s) {
-    if (a.seed_mode != PNJL_SEEDS_TABLE) {
-        mixed_points_kernel<32><<<grid_points, kSolveThreads, smem, s>>>(a);
-        const cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) return e;
-        if (a.n_seeds == 0) return cudaSuccess;
-    }
-    mixed_tasks_kernel<32><<<grid_tasks, kSolveThreads, smem, s>>>(a);
+cudaError_t launch_mixed_points(const SolveArgs &a, int grid, size_t smem, cudaStream_t s) {
+    mixed_points_kernel<32><<<grid, kSolveThreads, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mixed_tasks(const SolveArgs &a, int grid, size_t smem, cudaStream_t s) {
+    mixed_tasks_kernel<32><<<grid, kSolveThreads, smem, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -27,8 +27,8 @@ constexpr size_t kAlign = 256;
 constexpr size_t round_up(size_t b) { return (b + kAlign - 1) & ~(kAlign - 1); }
 
 // byte offsets inside the static array
-constexpr size_t kCtrlOff = 0;                                                  // 16 x int64: queue head + counters
-constexpr size_t kDoneOff = kCtrlOff + round_up(16 * sizeof(long long));        // kMaxTasks x int
+constexpr size_t kCtrlOff = 0;  // kCtrlSlots x int64: queue head + counters
+constexpr size_t kDoneOff = kCtrlOff + round_up(pnjl::kCtrlSlots * sizeof(long long));        // kMaxTasks x int
 constexpr size_t kCandOff = kDoneOff + round_up(kMaxTasks * sizeof(int));       // kMaxTasks x CandRec
 constexpr size_t kNodesOff = kCandOff + round_up(kMaxTasks * sizeof(pnjl::CandRec));
 constexpr size_t kNodesF64 = 2 * (pnjl::kMaxPNodes + pnjl::kMaxTNodes);         // doubles
@@ -128,7 +128,7 @@ extern "C" int pnjl_solve_batch_noalloc(const pnjl_params *params, int32_t p_num
                             cudaMemcpyHostToDevice, s) != cudaSuccess)
             return PNJL_ERR_CUDA;
     }
-    if (cudaMemsetAsync(d_ctrl, 0, 16 * sizeof(long long), s) != cudaSuccess) return PNJL_ERR_CUDA;
+    if (cudaMemsetAsync(d_ctrl, 0, pnjl::kCtrlSlots * sizeof(long long), s) != cudaSuccess) return PNJL_ERR_CUDA;
     if (table_mode && cudaMemsetAsync(d_done, 0, (size_t)n * sizeof(int), s) != cudaSuccess) return PNJL_ERR_CUDA;
 
     pnjl::SolveArgs a{};

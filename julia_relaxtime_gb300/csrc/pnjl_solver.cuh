@@ -14,6 +14,7 @@
 #pragma once
 
 #include "pnjl_device.cuh"
+#include "pnjl_ff.cuh"
 
 namespace pnjl {
 
@@ -35,6 +36,8 @@ struct Eval {
 struct NodeView {
     const double *p2, *A, *c2, *B;
     const float *p2f, *Af, *c2f, *Bf;
+    const float *p2l, *Al, *c2l, *Bl;  // float-float low parts (null when not staged)
+    const float *expt;                 // float-float exp tables (null when not staged)
     int p_num, t_num;
 };
 
@@ -209,6 +212,76 @@ __device__ void node_pass(const NodeView &nv, const PointIn &pt, const double *x
     }
     S.SL = acc[18]; S.SP = acc[19]; S.SPb = acc[20]; S.SPP = acc[21]; S.SPPb = acc[22]; S.SPbPb = acc[23];
     S.SAN = acc[24];
+}
+
+// Float-float pass: the sums of node_pass<..., GRAD, THERMO> (S.DM, S.SP, S.SPb; S.Nq, S.Na,
+// S.SAN, S.SL) computed in float-float arithmetic on the FP32 pipe (pnjl_ff.cuh); requires the
+// staged float-float tables (nv.p2l != null).  Non-finite sums are returned as such.
+template <int G, bool GRAD, bool THERMO>
+__device__ void node_pass_ff(const NodeView &nv, const PointIn &pt, const double *x, const double *M, int gl,
+                             unsigned mask, PassSums &S, int64_t &evals) {
+    const bool dedup = (M[1] == M[0]) && (pt.mu[1] == pt.mu[0]);
+    const int pn = nv.p_num, n = nv.p_num * nv.t_num;
+    const ff xi = ff_from_double(pt.xi);
+    const ff z{0.0f, 0.0f};
+    ff DM[3] = {z, z, z}, Nq[3] = {z, z, z}, Na[3] = {z, z, z};
+    ff SP = z, SPb = z, SAN = z, SL = z;
+#pragma unroll 1
+    for (int f = 0; f < 3; ++f) {
+        if (f == 1 && dedup) continue;
+        bool sw;
+        const FlavourFF fc = make_flavour_ff(M[f], pt.mu[f], pt.T, x[3], x[4], sw);
+        FlavourAccFF fa;
+        fa.zero();
+        int ip = gl, it = 0;
+        while (ip >= pn) { ip -= pn; ++it; }
+        ff sxi = ff_make(1.f), bw = z;
+        if (it < nv.t_num) {
+            sxi = ff_add_f(ff_mul(xi, ff{nv.c2f[it], nv.c2l[it]}), 1.0f);
+            bw = ff{nv.Bf[it], nv.Bl[it]};
+        }
+#pragma unroll 1
+        for (int k = gl; k < n; k += G) {
+            const ff q2 = ff_mul(ff{nv.p2f[ip], nv.p2l[ip]}, sxi);
+            const ff w = ff_mul(ff{nv.Af[ip], nv.Al[ip]}, bw);
+            node_flavour_ff<GRAD, THERMO>(fc, q2, w, nv.expt, fa);
+            ip += G;
+            if (ip >= pn) {
+                do { ip -= pn; ++it; } while (ip >= pn);
+                if (it < nv.t_num) {
+                    sxi = ff_add_f(ff_mul(xi, ff{nv.c2f[it], nv.c2l[it]}), 1.0f);
+                    bw = ff{nv.Bf[it], nv.Bl[it]};
+                }
+            }
+        }
+        const bool two = (f == 0 && dedup);
+        auto dbl = [two](ff v) { return two ? ff_mul_f(v, 2.0f) : v; };
+        if (GRAD) {
+            DM[f] = fa.DM;
+            if (two) DM[1] = fa.DM;
+            SP = ff_add(SP, dbl(sw ? fa.Sa : fa.Sq));
+            SPb = ff_add(SPb, dbl(sw ? fa.Sq : fa.Sa));
+        }
+        if (THERMO) {
+            Nq[f] = sw ? fa.Na : fa.Nq;
+            Na[f] = sw ? fa.Nq : fa.Na;
+            if (two) { Nq[1] = Nq[0]; Na[1] = Na[0]; }
+            SAN = ff_add(SAN, dbl(fa.SAN));
+            SL = ff_add(SL, dbl(fa.SL));
+        }
+        if (gl == 0) evals += (int64_t)n;
+    }
+    for (int f = 0; f < 3; ++f) {
+        S.DM[f] = GRAD ? ff_to_double(group_sum_ffv<G>(DM[f], mask)) : 0.0;
+        S.Nq[f] = THERMO ? ff_to_double(group_sum_ffv<G>(Nq[f], mask)) : 0.0;
+        S.Na[f] = THERMO ? ff_to_double(group_sum_ffv<G>(Na[f], mask)) : 0.0;
+        S.DMM[f] = S.DMP[f] = S.DMPb[f] = 0.0;
+    }
+    S.SP = GRAD ? ff_to_double(group_sum_ffv<G>(SP, mask)) : 0.0;
+    S.SPb = GRAD ? ff_to_double(group_sum_ffv<G>(SPb, mask)) : 0.0;
+    S.SAN = THERMO ? ff_to_double(group_sum_ffv<G>(SAN, mask)) : 0.0;
+    S.SL = THERMO ? ff_to_double(group_sum_ffv<G>(SL, mask)) : 0.0;
+    S.SPP = S.SPPb = S.SPbPb = 0.0;
 }
 
 // FP64 assembly of Omega, grad, Hessian and thermo from the pass sums and the vacuum terms.

@@ -14,6 +14,7 @@ from . import _capi as api
 from .constants import PNJLParams
 
 PRECISIONS = {"fp64": api.PNJL_PREC_FP64, "mixed": api.PNJL_PREC_MIXED}
+EVAL_PRECISIONS = dict(PRECISIONS, ff_residual=api.PNJL_PREC_FF_RESIDUAL)
 
 
 @dataclass
@@ -57,6 +58,15 @@ class VerifyMap:
 
     def fraction(self) -> float:
         return float(self.flags.mean()) if self.flags.size else 0.0
+
+
+def shard_points(n: int, rank: int, world: int) -> np.ndarray:
+    """Indices of the points rank `rank` of `world` solves: a strided shard (points are
+    independent, so ranks exchange no data; every point belongs to exactly one rank and
+    every rank's share spans the whole (T, mu, xi) box)."""
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError("need 0 <= rank < world")
+    return np.arange(rank, n, world, dtype=np.int64)
 
 
 def _dp(a):
@@ -148,12 +158,13 @@ class GapEngine:
         return n, T, mu_u, mu_d, mu_s, xi
 
     def evaluate(self, x, T, mu, xi, precision: str = "fp64"):
-        """Omega, grad_x Omega [n,5], Hessian_x Omega [n,5,5] at given states."""
+        """Omega, grad_x Omega [n,5], Hessian_x Omega [n,5,5] at given states.  precision
+        "ff_residual": the gradient from the float-float pass alone (Omega, Hessian NaN)."""
         n, T, mu_u, mu_d, mu_s, xi = self._point_arrays(T, mu, xi)
         x = _f64(x, shape=(n, 5))
         om, g, h = np.zeros(n), np.zeros((n, 5)), np.zeros((n, 5, 5))
         rc = self._lib.pnjl_eval_batch(self._ctx, n, _dp(x), _dp(T), _dp(mu_u), _dp(mu_d), _dp(mu_s), _dp(xi),
-                                       PRECISIONS[precision], _dp(om), _dp(g), _dp(h))
+                                       EVAL_PRECISIONS[precision], _dp(om), _dp(g), _dp(h))
         self._check(rc, "pnjl_eval_batch")
         return om, g, h
 
@@ -261,9 +272,14 @@ class GapEngine:
     def synchronize(self):
         self._check(self._lib.pnjl_synchronize(self._ctx), "pnjl_synchronize")
 
-    def stats(self) -> dict:
+    def stats(self, kernel: int | None = None) -> dict:
+        """Counters of the last solve; kernel 0 / 1: the per-point / task kernel of a mixed
+        per-point solve alone (pnjl_get_kernel_stats)."""
         st = api.pnjl_stats()
-        self._check(self._lib.pnjl_get_stats(self._ctx, C.byref(st)), "pnjl_get_stats")
+        if kernel is None:
+            self._check(self._lib.pnjl_get_stats(self._ctx, C.byref(st)), "pnjl_get_stats")
+        else:
+            self._check(self._lib.pnjl_get_kernel_stats(self._ctx, int(kernel), C.byref(st)), "pnjl_get_kernel_stats")
         return {k: getattr(st, k) for k, _ in api.pnjl_stats._fields_}
 
     def sm_count(self) -> int:

@@ -291,3 +291,222 @@ def main(argv: Sequence[str] | None = None):
 
 if __name__ == "__main__":
     main()
+
+
+# ---------------------------------------------------------------------------------------
+# TmuScan (src/pnjl/scans/TmuScan.jl): T-mu scan with phase-aware continuation along mu.
+
+TMU_HEADER = ["T_MeV", "mu_MeV", "xi", "pressure_fm4", "rho", "entropy_fm3", "energy_fm4", "phi_u", "phi_d",
+              "phi_s", "Phi1", "Phi2", "M_u_MeV", "M_d_MeV", "M_s_MeV", "iterations", "residual_norm", "converged",
+              "message"]  # TmuScan.jl:62-82
+TMU_ACCEPTABLE_RESIDUAL = 1e-4  # TmuScan.jl:60
+
+
+def _fmt6(x) -> str:
+    """@sprintf("%.6f", x) as Julia prints it (NaN, Inf, -Inf spelled as Julia does)."""
+    x = float(x)
+    if math.isnan(x):
+        return "NaN"
+    if math.isinf(x):
+        return "Inf" if x > 0 else "-Inf"
+    return "%.6f" % x
+
+
+def _tmu_key(T, mu, xi):
+    return (round(float(T), 6), round(float(mu), 6), round(float(xi), 6))
+
+
+def _tmu_load_completed(path: str) -> set:
+    """TmuScan.jl:243-264: keys of the rows already in the file."""
+    done: set = set()
+    if not os.path.isfile(path):
+        return done
+    with open(path) as fh:
+        next(fh, None)
+        for line in fh:
+            cols = line.strip().split(",")
+            if len(cols) < 3:
+                continue
+            try:
+                done.add(_tmu_key(float(cols[0]), float(cols[1]), float(cols[2])))
+            except ValueError:
+                continue
+    return done
+
+
+def _tmu_success(r) -> bool:
+    """TmuScan.jl:428-436: converged, or a finite residual <= 1e-4."""
+    if r is None:
+        return False
+    return bool(r["converged"]) or (math.isfinite(r["residual_norm"]) and r["residual_norm"] <= TMU_ACCEPTABLE_RESIDUAL)
+
+
+def _tmu_failure(label: str, msg: str, r) -> str:
+    """TmuScan.jl:521-534."""
+    base = f"seed[{label}] failed"
+    if r is not None:
+        base += f" (iterations={r['iterations']}, residual={_fmt6(r['residual_norm'])}, converged=false)"
+    return base if not msg else f"{base}: {msg}"
+
+
+def _tmu_pick(res, j) -> dict | None:
+    """One point of a batch result as the fields TmuScan reads; None where the reference's
+    solve raised (its _solve_point catches the exception, TmuScan.jl:380-400)."""
+    if int(res["status"][j]) == api.PNJL_POINT_EXCEPTION:
+        return None
+    return {"x": np.array(res["x"][j], dtype=np.float64), "converged": bool(res["converged"][j]),
+            "residual_norm": float(res["residual_norm"][j]), "iterations": int(res["iterations"][j]),
+            "pressure": float(res["pressure"][j]), "rho_norm": float(res["rho_norm"][j]),
+            "entropy": float(res["entropy"][j]), "energy": float(res["energy"][j]),
+            "masses": np.array(res["masses"][j], dtype=np.float64)}
+
+
+def _tmu_seed_candidates(tracker, cache: dict, T, mu, xi, T_fm, mu_fm):
+    """_build_seed_candidates_v2 (TmuScan.jl:267-301)."""
+    from .pnjl import HADRON_SEED_5, QUARK_SEED_5
+
+    cands = []
+    if tracker is not None:
+        label = "phase_aware_default" if tracker.previous_solution is None else "phase_aware_continuity"
+        cands.append((label, np.array(tracker.get_seed([T_fm, mu_fm], FixedMu()), dtype=np.float64)))
+    key = (round(float(T), 6), round(float(xi), 6))
+    if key in cache:
+        cands.append(("continuation", cache[key].copy()))
+    quark, hadron = ("quark", np.array(QUARK_SEED_5)), ("hadron", np.array(HADRON_SEED_5))
+    cands.extend([quark, hadron] if (T > 150 or mu > 300) else [hadron, quark])
+    return cands
+
+
+def tmu_scan_rows(T_values, mu_values, xi_values, solver: PointSolver, *, use_phase_aware: bool = True,
+                  max_iter: int = 1000, boundary_path: str | None = None, cep_path: str | None = None,
+                  skip: set | None = None):
+    """The scan of run_tmu_scan (TmuScan.jl:120-234) as batched solves: every (xi, T) row walks mu
+    with its own tracker (the reference resets one tracker per T), so all rows advance together --
+    step k solves the k-th mu of every row, trying the rows' k-th seed candidates in one launch per
+    candidate rank.  Returns the rows in the reference's order (xi, T, mu) and the statistics."""
+    skip = skip or set()
+    rows_idx = [(float(xi), float(T)) for xi in xi_values for T in T_values]
+    trackers = {}
+    for xi, T in rows_idx:
+        if not use_phase_aware:
+            trackers[(xi, T)] = None
+            continue
+        try:
+            trackers[(xi, T)] = PhaseAwareContinuitySeed(xi, boundary_path=boundary_path, cep_path=cep_path)
+        except (OSError, ValueError, KeyError):
+            trackers[(xi, T)] = PhaseAwareContinuitySeed()  # no boundary data: plain continuation
+    cache: dict = {}
+    out = {key: [None] * len(mu_values) for key in rows_idx}
+    stats = {"total": 0, "success": 0, "failure": 0, "skipped": 0}
+    for m, mu in enumerate(mu_values):
+        mu = float(mu)
+        active = []
+        for key in rows_idx:
+            stats["total"] += 1
+            if _tmu_key(key[1], mu, key[0]) in skip:
+                stats["skipped"] += 1
+                continue
+            active.append(key)
+        if not active:
+            continue
+        cands = {}
+        for xi, T in active:
+            cands[(xi, T)] = _tmu_seed_candidates(trackers[(xi, T)], cache, T, mu, xi, T / HBARC_MEV_FM,
+                                                  mu / HBARC_MEV_FM)
+        msgs = {key: [] for key in active}
+        final = {}
+        pending = list(active)
+        rank = 0
+        while pending:
+            batch = [key for key in pending if rank < len(cands[key])]
+            for key in pending:
+                if rank >= len(cands[key]):
+                    final[key] = (None, " | ".join(x for x in msgs[key] if x))
+            if not batch:
+                break
+            T_arr = np.array([k[1] / HBARC_MEV_FM for k in batch])
+            res = solver(T_arr, np.full(len(batch), mu / HBARC_MEV_FM), np.array([k[0] for k in batch]),
+                         np.array([cands[k][rank][1] for k in batch]), max_iter)
+            nxt = []
+            for j, key in enumerate(batch):
+                r = _tmu_pick(res, j)
+                msg = "" if r is not None else "solver exception"
+                if _tmu_success(r):
+                    final[key] = (r, msg)
+                else:
+                    msgs[key].append(_tmu_failure(cands[key][rank][0], msg, r))
+                    nxt.append(key)
+            pending = nxt
+            rank += 1
+        # _refine_result (TmuScan.jl:406-425): near-converged successes are solved again from
+        # their own solution
+        near = [k for k, (r, _) in final.items() if r is not None and not r["converged"]]
+        refine_msg = {}
+        if near:
+            res = solver(np.array([k[1] / HBARC_MEV_FM for k in near]), np.full(len(near), mu / HBARC_MEV_FM),
+                         np.array([k[0] for k in near]), np.array([final[k][0]["x"] for k in near]), max_iter)
+            for j, key in enumerate(near):
+                r2 = _tmu_pick(res, j)
+                if r2 is not None and r2["converged"]:
+                    final[key] = (r2, final[key][1])
+                    refine_msg[key] = "refined from near-converged seed"
+                else:
+                    refine_msg[key] = "" if r2 is not None else "solver exception"
+        for key in active:
+            r, msg = final[key]
+            parts = list(msgs[key])
+            if r is not None:
+                promote = ""
+                if not r["converged"]:  # _promote_success (TmuScan.jl:439-468)
+                    r = dict(r, converged=True)
+                    promote = f"force-marked converged (residual {_fmt6(r['residual_norm'])})"
+                parts += [msg, promote, refine_msg.get(key, "")]
+                xi, T = key
+                if trackers[key] is not None:
+                    trackers[key].update(r["x"], T, mu)
+                cache[(round(T, 6), round(xi, 6))] = r["x"].copy()
+                stats["success"] += 1
+            else:
+                parts = [msg] if msg else parts
+                stats["failure"] += 1
+            out[key][m] = (key[1], mu, key[0], r, " | ".join(p for p in parts if p))
+    rows = [out[key][m] for key in rows_idx for m in range(len(mu_values)) if out[key][m] is not None]
+    return rows, stats
+
+
+def format_tmu_row(T, mu, xi, r, message: str) -> str:
+    """_write_row (TmuScan.jl:471-515)."""
+    q = f'"{message}"' if message else ""
+    if r is None:
+        vals = [_fmt6(T), _fmt6(mu), _fmt6(xi)] + ["NaN"] * 12 + ["-1", "NaN", "false", q]
+        return ",".join(vals)
+    x, M = r["x"], r["masses"] * HBARC_MEV_FM
+    vals = [_fmt6(T), _fmt6(mu), _fmt6(xi), _fmt6(r["pressure"]), _fmt6(r["rho_norm"]), _fmt6(r["entropy"]),
+            _fmt6(r["energy"]), _fmt6(x[0]), _fmt6(x[1]), _fmt6(x[2]), _fmt6(x[3]), _fmt6(x[4]),
+            _fmt6(M[0]), _fmt6(M[1]), _fmt6(M[2]), str(int(r["iterations"])), _fmt6(r["residual_norm"]),
+            "true" if r["converged"] else "false", q]
+    return ",".join(vals)
+
+
+def run_tmu_scan(*, T_values=None, mu_values=None, xi_values=(0.0,),
+                 output_path: str = os.path.join("data", "outputs", "results", "pnjl", "tmu_scan.csv"),
+                 overwrite: bool = False, resume: bool = True, use_phase_aware: bool = True, p_num: int = 24,
+                 t_num: int = 8, max_iter: int = 1000, precision: str = "fp64", solver: PointSolver | None = None,
+                 boundary_path: str | None = None, cep_path: str | None = None) -> dict:
+    """run_tmu_scan (TmuScan.jl:120-234): same keyword arguments, CSV, resume and statistics."""
+    T_values = list(np.arange(50.0, 200.0 + 1e-9, 10.0)) if T_values is None else list(T_values)
+    mu_values = list(np.arange(0.0, 400.0 + 1e-9, 10.0)) if mu_values is None else list(mu_values)
+    solver = solver or gpu_point_solver(p_num, t_num, precision)
+    d = os.path.dirname(output_path)
+    if d:
+        os.makedirs(d, exist_ok=True)
+    completed = _tmu_load_completed(output_path) if (resume and not overwrite and os.path.isfile(output_path)) else set()
+    mode = "w" if (overwrite or not os.path.isfile(output_path)) else "a"
+    rows, stats = tmu_scan_rows(T_values, mu_values, xi_values, solver, use_phase_aware=use_phase_aware,
+                                max_iter=max_iter, boundary_path=boundary_path, cep_path=cep_path, skip=completed)
+    with open(output_path, mode) as fh:
+        if mode == "w":
+            fh.write(",".join(TMU_HEADER) + "\n")
+        for T, mu, xi, r, msg in rows:
+            fh.write(format_tmu_row(T, mu, xi, r, msg) + "\n")
+    return dict(stats, output=output_path)

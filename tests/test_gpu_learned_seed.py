@@ -53,17 +53,23 @@ def test_mlp_loss_and_gradient_match_cpu_oracle(engine_factory, n):
 
 def test_learned_seed_trains_and_beats_multiseed(engine_factory):
     """Train on a solver-labelled (T, mu, xi) grid, then solve held-out points: same roots and
-    phases as the multi-seed method (its fallback), at a fraction of the node evaluations."""
-    from julia_relaxtime_gb300.learned_seed import LearnedSeed, TrainConfig, label_grid
+    phases as the multi-seed method (its fallback and judge), at a fraction of the node
+    evaluations.  Without verification the learned seed alone lands on a metastable branch
+    near the first-order line at a few points; with the verification map built from the
+    labels, the phases are identical."""
+    from julia_relaxtime_gb300.learned_seed import (LearnedSeed, TrainConfig, coexistence_map,
+                                                    default_learned_opts, label_grid)
 
     eng = engine_factory(32, 8)
     cfg = TrainConfig(T_MeV=(50.0, 300.0, 24), mu_MeV=(0.0, 400.0, 24), xi=(-0.5, 0.5, 3), epochs=300, batch=256)
-    T, mu, xi, x, _ = label_grid(eng, cfg)
+    T, mu, xi, x, lres = label_grid(eng, cfg)
     assert T.size > 0.95 * 24 * 24 * 3
     ls = LearnedSeed(eng, seed=3)
     loss0, _ = (ls.default_scaling(x), ls.loss_grad(T, mu, xi, x))[1]
     loss = ls.fit(T, mu, xi, x, epochs=cfg.epochs, batch=cfg.batch, lr=cfg.lr)
     assert loss < 0.05 * loss0, (loss0, loss)
+    ls.verify_map = coexistence_map(eng, cfg, lres)
+    assert 0.0 < ls.verify_map.fraction() < 0.6
     rng = np.random.default_rng(99)
     m = 400
     Tt = rng.uniform(50, 300, m) / HBARC
@@ -73,12 +79,38 @@ def test_learned_seed_trains_and_beats_multiseed(engine_factory):
     opts = SolveOptions(iterations=40, ftol=1e-10, precision="mixed")
     ref = eng.solve(Tt, mt, xt, seed_table=table, seed_table_hot=hot, opts=opts)
     st_ref = eng.stats()
-    got = ls.solve(Tt, mt, xt, opts=opts)
+    # the learned seed alone (no verification)
+    alone = ls.solve(Tt, mt, xt, opts=default_learned_opts(ftol=1e-10, verify_seeds=0, verify_max_step=0.0))
+    both = ref["converged"] & alone["converged"]
+    assert both.mean() > 0.98
+    same = np.abs(alone["omega"] - ref["omega"]) <= 1e-10 * np.abs(ref["omega"])
+    assert same[both].mean() >= 0.97, np.sum(~same[both])
+    # the default learned solve: verification inside the map, MultiSeed fallback
+    got = ls.solve(Tt, mt, xt, opts=default_learned_opts(ftol=1e-10))
     st = eng.stats()
     both = ref["converged"] & got["converged"]
     assert both.mean() > 0.98
-    same_phase = np.abs(got["omega"] - ref["omega"]) <= 1e-10 * np.abs(ref["omega"])
-    assert same_phase[both].mean() >= 0.98, np.sum(~same_phase[both])
+    same = np.abs(got["omega"] - ref["omega"]) <= 1e-10 * np.abs(ref["omega"])
+    assert same[both].all(), np.sum(~same[both])
     work_ref = st_ref["node_evals_fp32"] + 64 * st_ref["node_evals_fp64"]
-    work = st["node_evals_fp32"] + 64 * st["node_evals_fp64"]
+    work = st["node_evals_fp32"] + st["node_evals_fp32_thermo"] + 64 * st["node_evals_fp64"]
     assert work < 0.5 * work_ref, (work, work_ref)
+    assert st["multiseed_fallbacks"] <= 0.02 * m
+    # the host-array entry point and the device entry point give identical results
+    import torch
+
+    dev = torch.device("cuda", 0)
+    d_in = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in (("T", Tt), ("mu", mt), ("xi", xt))}
+    d_out = {"x": torch.empty(5 * m, dtype=torch.float64, device=dev),
+             "omega": torch.empty(m, dtype=torch.float64, device=dev),
+             "converged": torch.empty(m, dtype=torch.uint8, device=dev),
+             "chosen_seed": torch.empty(m, dtype=torch.int32, device=dev)}
+    torch.cuda.synchronize()
+    mptr = d_in["mu"].data_ptr()
+    eng.solve_device(m, d_in["T"].data_ptr(), mptr, mptr, mptr, d_in["xi"].data_ptr(),
+                     {k: v.data_ptr() for k, v in d_out.items()}, seed_table=table, seed_table_hot=hot,
+                     opts=default_learned_opts(ftol=1e-10, verify_map=ls.verify_map), learned=True)
+    eng.synchronize()
+    np.testing.assert_array_equal(d_out["x"].cpu().numpy().reshape(m, 5), got["x"])
+    np.testing.assert_array_equal(d_out["omega"].cpu().numpy(), got["omega"])
+    np.testing.assert_array_equal(d_out["chosen_seed"].cpu().numpy(), got["chosen_seed"])

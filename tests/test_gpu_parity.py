@@ -75,6 +75,22 @@ def test_eval_mixed_fp32_pass_close_to_fp64(engine_factory):
     assert np.abs(h32 - h).max() <= 1e-4 * max(1.0, np.abs(h).max())
 
 
+@pytest.mark.parametrize("p_num,t_num,mu_neg,asym", [(64, 8, False, False), (128, 32, True, True)])
+def test_eval_ff_residual_matches_oracle(engine_factory, P, p_num, t_num, mu_neg, asym):
+    """The float-float residual pass (FP32 pipe) that steers the mixed solver's first FP64
+    correction: the gradient to ~1e-12 of its scale, against the FP64 jet oracle (states with
+    mu/T moderate enough that no FP32 exponent range is exceeded)."""
+    eng = engine_factory(p_num, t_num)
+    nd = orc.Nodes(p_num, t_num)
+    x, T, mu, xi = random_states(48, 3 + p_num, mu_neg, asym)
+    T = np.maximum(T, 45.0 / HBARC)
+    _, g, _ = eng.evaluate(x, T, mu, xi, precision="ff_residual")
+    for i in range(len(T)):
+        _, g_ref, _ = orc.evaluate(P, nd, x[i], mu[i], T[i], xi[i])
+        sg = max(1.0, np.abs(g_ref).max())
+        assert np.abs(g[i] - g_ref).max() <= 1e-11 * sg, (i, g[i] - g_ref, sg)
+
+
 def test_thermo_matches_oracle(engine_factory, P):
     eng = engine_factory(64, 8)
     nd = orc.Nodes(64, 8)
@@ -279,3 +295,28 @@ def test_mixed_per_point_seed_and_fallback(engine_factory, P):
         if ref["converged"]:
             assert abs(res["omega"][i] - ref["omega"]) <= 1e-12 * abs(ref["omega"]), i
             assert np.all(np.abs(res["x"][i][3:] - ref["x"][3:]) <= 1e-10), i
+
+
+def test_tmu_scan_gpu_matches_oracle(engine_factory):
+    """run_tmu_scan (TmuScan.jl:120-234) through the GPU point solver: the same rows, branches,
+    candidate messages and iteration counts as the same driver over the oracle."""
+    import os
+
+    from julia_relaxtime_gb300 import scan
+    from oracle_adapter import GOLDEN, oracle_point_solver
+
+    eng = engine_factory(24, 8)
+    kw = dict(boundary_path=os.path.join(GOLDEN, "boundary.csv"), cep_path=os.path.join(GOLDEN, "cep.csv"))
+    Ts, mus = [50.0, 130.0, 200.0], np.arange(0.0, 401.0, 10.0)
+    rows_g, st_g = scan.tmu_scan_rows(Ts, mus, [0.0, 0.2], scan.gpu_point_solver(24, 8, engine=eng), **kw)
+    rows_o, st_o = scan.tmu_scan_rows(Ts, mus, [0.0, 0.2], oracle_point_solver(24, 8), **kw)
+    assert st_g == st_o
+    for (T, mu, xi, r, msg), (T2, mu2, xi2, r2, msg2) in zip(rows_g, rows_o):
+        assert (T, mu, xi) == (T2, mu2, xi2)
+        assert msg == msg2
+        assert r["converged"] == r2["converged"] and r["iterations"] == r2["iterations"], (T, mu, xi)
+        np.testing.assert_allclose(r["x"], r2["x"], rtol=1e-9, atol=1e-11)
+        assert r["pressure"] == pytest.approx(r2["pressure"], rel=1e-12, abs=1e-13)
+        a = [float(v) for v in scan.format_tmu_row(T, mu, xi, r, msg).split(",")[:15]]
+        b = [float(v) for v in scan.format_tmu_row(T2, mu2, xi2, r2, msg2).split(",")[:15]]
+        assert np.allclose(a, b, rtol=0, atol=1.01e-6), (a, b)  # 6-decimal columns, last digit

@@ -178,3 +178,145 @@ def test_scan_resume_skips_existing_rows(tmp_path):
     run_gap_transport_scan(opts, solver=oracle_point_solver(12, 6))
     lines = [ln for ln in out.read_text().splitlines() if not ln.startswith("#")]
     assert len(lines) == 5 and lines[-1].startswith("150.0,")
+
+
+# ---- TmuScan driver (TmuScan.jl) with the oracle as the point solver --------------------
+def _tmu_rows(Ts, solver):
+    from julia_relaxtime_gb300 import scan
+
+    return scan.tmu_scan_rows(Ts, np.arange(0.0, 401.0, 10.0), [0.0], solver,
+                              boundary_path=os.path.join(GOLDEN, "boundary.csv"),
+                              cep_path=os.path.join(GOLDEN, "cep.csv"))
+
+
+def test_tmu_scan_oracle_matches_golden_rows():
+    """run_tmu_scan's candidate order, continuation and phase-aware switch (TmuScan.jl:120-301)
+    reproduce the stored tmu_scan.csv (p24/t8) at its 6 decimals.  The stored file predates the
+    phase-aware tracker: where it stays on the metastable branch past mu_c, the scan here
+    switches to the stable one (higher pressure) -- allowed, and checked to be the stable one."""
+    from julia_relaxtime_gb300 import scan
+    from oracle_adapter import oracle_point_solver
+
+    Ts = [50.0, 100.0, 130.0, 150.0, 200.0]
+    rows, stats = _tmu_rows(Ts, oracle_point_solver(24, 8))
+    assert stats == {"total": 205, "success": 205, "failure": 0, "skipped": 0}
+    g = {(float(r["T_MeV"]), float(r["mu_MeV"])): r for r in read_csv("tmu_scan.csv")}
+    switched = 0
+    for T, mu, xi, r, msg in rows:
+        gr = g[(T, mu)]
+        d = max(abs(float(scan._fmt6(r["x"][k])) - float(gr[c]))
+                for k, c in enumerate(("phi_u", "phi_d", "phi_s", "Phi1", "Phi2")))
+        dp = float(scan._fmt6(r["pressure"])) - float(gr["pressure_fm4"])
+        if d <= 2e-6 and abs(dp) <= 2e-6:
+            continue
+        assert dp > 1e-4, (T, mu, d, dp)  # a different branch only if it is the stable one
+        switched += 1
+    assert switched <= 2
+
+
+def test_tmu_csv_format_and_resume(tmp_path):
+    from julia_relaxtime_gb300 import scan
+    from oracle_adapter import oracle_point_solver
+
+    out = tmp_path / "tmu.csv"
+    solver = oracle_point_solver(12, 4)
+    st = scan.run_tmu_scan(T_values=[60.0, 180.0], mu_values=[0.0, 10.0, 20.0], output_path=str(out),
+                           p_num=12, t_num=4, solver=solver, use_phase_aware=False)
+    assert st["total"] == 6 and st["success"] == 6
+    lines = out.read_text().splitlines()
+    assert lines[0].split(",") == scan.TMU_HEADER and len(scan.TMU_HEADER) == 19
+    first = lines[1].split(",")
+    assert first[:3] == ["60.000000", "0.000000", "0.000000"] and first[17] == "true"
+    assert all(len(c.split(".")[1]) == 6 for c in first[3:15])
+    # resume: a second call with one more mu solves only the new points
+    st2 = scan.run_tmu_scan(T_values=[60.0, 180.0], mu_values=[0.0, 10.0, 20.0, 30.0], output_path=str(out),
+                            p_num=12, t_num=4, solver=solver, use_phase_aware=False)
+    assert st2["skipped"] == 6 and st2["success"] == 2
+    assert len(out.read_text().splitlines()) == 1 + 8
+    # a failed point (the reference's `nothing` result) is written with NaNs and the messages
+    row = scan.format_tmu_row(50.0, 10.0, 0.0, None, "seed[hadron] failed")
+    c = row.split(",")
+    assert c[3] == "NaN" and c[15] == "-1" and c[17] == "false" and c[18] == '"seed[hadron] failed"'
+    assert scan._fmt6(float("nan")) == "NaN" and scan._fmt6(-1e-9) == "-0.000000"
+
+
+# ---- learned-seed verification map (host logic) -----------------------------------------
+def test_coexistence_map_flags_coexistence_and_jumps():
+    from julia_relaxtime_gb300.learned_seed import TrainConfig, coexistence_map
+
+    cfg = TrainConfig(T_MeV=(50.0, 300.0, 6), mu_MeV=(0.0, 400.0, 6), xi=(-0.5, 0.5, 3))
+    nT, nm, nx = 6, 6, 3
+    N = nT * nm * nx
+    base = np.tile(np.array([-1.8, -1.8, -2.2, 0.01, 0.01]), (N, 1))
+    R = np.repeat(base[:, None, :], 6, axis=1).copy()
+    Om = np.full((N, 6), -21.0)
+    idx = lambda i, j, k: (i * nm + j) * nx + k  # noqa: E731
+    # node (1, 4, 0): a second phase 0.01 above the minimum -> flagged
+    R[idx(1, 4, 0), 2] = [-0.2, -0.2, -2.0, 0.05, 0.06]
+    Om[idx(1, 4, 0), 2] = -20.99
+    # node (4, 1, 2): a far-off root 3.5 above the minimum -> not a competing phase
+    R[idx(4, 1, 2), 3] = [-5.3, -5.3, -2.3, 0.0, 0.0]
+    Om[idx(4, 1, 2), 3] = -17.5
+    lab = {"x": base.copy(), "converged": np.ones(N, bool)}
+    vm = coexistence_map(None, cfg, lab, roots=(R, Om), grow=0)
+    assert vm.flags.shape == (5, 5, 2)
+    assert vm.flags[0:2, 3:5, 0].all() and vm.flags.sum() == 4  # the 4 cells around node (1, 4, 0)
+    # a jump of the labelled solution along mu between nodes (3, 2, *) and (3, 3, *)
+    lab2 = {"x": base.copy(), "converged": np.ones(N, bool)}
+    for k in range(nx):
+        lab2["x"][idx(3, 3, k), 0] = -0.2
+    R2 = np.repeat(lab2["x"][:, None, :], 6, axis=1)
+    vm2 = coexistence_map(None, cfg, lab2, roots=(R2, np.full((N, 6), -21.0)), grow=0)
+    assert vm2.flags[2:4, 1:4, :].all()
+    vm3 = coexistence_map(None, cfg, lab2, roots=(R2, np.full((N, 6), -21.0)), grow=1)
+    assert vm3.flags.sum() > vm2.flags.sum()
+    assert vm.lo[0] == pytest.approx(50.0 / HBARC) and vm.hi[2] == 0.5
+
+
+# ---- sharding of the bench over ranks (gloo, world size 2) ---------------------------------
+def _shard_worker(rank, world, port, n, q):
+    import torch
+    import torch.distributed as dist
+
+    from julia_relaxtime_gb300.engine import shard_points
+
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
+    mine = shard_points(n, rank, world)
+    counts = [torch.zeros(1, dtype=torch.int64) for _ in range(world)]
+    dist.all_gather(counts, torch.tensor([mine.size], dtype=torch.int64))
+    total = torch.tensor([int(mine.sum())], dtype=torch.int64)
+    dist.all_reduce(total)
+    t = torch.tensor([float(10 + rank)])
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    q.put((rank, [int(c.item()) for c in counts], int(total.item()), float(t.item())))
+    dist.destroy_process_group()
+
+
+def test_shard_points_two_ranks_gloo():
+    """The bench's sharding: every point on exactly one rank, max-over-ranks timing (gloo)."""
+    import multiprocessing as mp
+    import socket
+
+    from julia_relaxtime_gb300.engine import shard_points
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    n = 589_824 + 3
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    ps = [ctx.Process(target=_shard_worker, args=(r, 2, port, n, q)) for r in range(2)]
+    for p in ps:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in ps)
+    for p in ps:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for rank, counts, total, tmax in res:
+        assert sum(counts) == n and abs(counts[0] - counts[1]) <= 1
+        assert total == n * (n - 1) // 2  # disjoint and complete
+        assert tmax == 11.0
+    a, b = shard_points(10, 0, 2), shard_points(10, 1, 2)
+    assert set(a) | set(b) == set(range(10)) and not set(a) & set(b)
+    with pytest.raises(ValueError):
+        shard_points(10, 2, 2)
