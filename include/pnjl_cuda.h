@@ -48,9 +48,8 @@ extern "C" {
 #define PNJL_PREC_MIXED 1 /* Newton passes with an FP32 Kahan-compensated integrand; the
                              residual that decides convergence, Omega and the thermo output
                              come from FP64 passes                                          */
-#define PNJL_PREC_FF_RESIDUAL 2 /* pnjl_eval_batch only: the float-float residual pass the
-                             mixed solver steers its first FP64 correction step with
-                             (gradient only; omega and hess are NaN)                        */
+#define PNJL_PREC_FF_RESIDUAL 2 /* pnjl_eval_batch only: the float-float passes the mixed
+                             solver refines with (gradient and Hessian; omega is NaN)       */
 
 /* Model constants in fm units; src/Constants_PNJL.jl:82-103 (hbarc, N_color, rho0,
  * Lambda, G, K, m_ud0, m_s0, T0, a0, a1, a2, b3). */
@@ -181,7 +180,7 @@ int pnjl_get_nodes(const pnjl_ctx *ctx, double *p_mesh, double *c_mesh, double *
  * calculate_omega (Thermodynamics.jl:181-195) and the ForwardDiff gradient/Jacobian of
  * gap_conditions (Conditions.jl:72-86; F = -grad_x Omega).  precision: PNJL_PREC_FP64,
  * PNJL_PREC_MIXED (FP32-Kahan integrand, FP64 assembly) or PNJL_PREC_FF_RESIDUAL (float-float
- * gradient only).  Host pointers; NULL skips. */
+ * gradient and Hessian).  Host pointers; NULL skips. */
 int pnjl_eval_batch(pnjl_ctx *ctx, int64_t n, const double *x, const double *T,
                     const double *mu_u, const double *mu_d, const double *mu_s,
                     const double *xi, int32_t precision,
@@ -225,6 +224,31 @@ int pnjl_device_sm_count(const pnjl_ctx *ctx);
 /* Launch shape of the solve kernel: lanes per task (32: one warp) and resident blocks
  * per SM (0 = occupancy maximum).  Chosen by the autotuner; results do not depend on it. */
 int pnjl_set_tuning(pnjl_ctx *ctx, int32_t lanes_per_point, int32_t blocks_per_sm);
+/* Mixed-precision per-point solves (learned / continuation seeds) are cut into `chunks` pieces
+ * over two streams: the per-point kernel of piece c+1 overlaps the task kernel (verification,
+ * MultiSeed fallback) of piece c.  0 = automatic, 1 = no pipeline, at most 16.  Results do
+ * not depend on it.  pnjl_get_tuning reads the current launch shape. */
+int pnjl_set_pipeline(pnjl_ctx *ctx, int32_t chunks);
+int pnjl_get_tuning(const pnjl_ctx *ctx, int32_t *lanes_per_point, int32_t *blocks_per_sm, int32_t *chunks);
+
+/* One launch shape and its measured solve time (device time of the solve kernels, CUDA events). */
+typedef struct pnjl_tuning {
+    int32_t lanes_per_point;
+    int32_t blocks_per_sm;
+    int32_t pipeline_chunks;
+    double ms;
+} pnjl_tuning;
+
+/* Autotuner (no counterpart in the reference): solves the given representative batch (device
+ * pointers, as pnjl_solve_batch_device, or pnjl_solve_batch_learned_device when `learned`) with
+ * every candidate launch shape -- resident blocks per SM from the occupancy maximum down to 1,
+ * and for mixed per-point solves the chunk pipeline 1, 2, 3, 4, 6, 8 -- `reps` times each, keeps
+ * the fastest (minimum over repetitions) and sets it on the context.  `tried` (optional) receives
+ * up to max_tried candidates with their times; d_out receives the last solve's results. */
+int pnjl_autotune(pnjl_ctx *ctx, int64_t n, const double *d_T, const double *d_mu_u, const double *d_mu_d,
+                  const double *d_mu_s, const double *d_xi, const pnjl_solve_opts *opts, pnjl_result_soa *d_out,
+                  int32_t learned, int32_t reps, pnjl_tuning *best, pnjl_tuning *tried, int32_t max_tried,
+                  int32_t *n_tried);
 
 /* Measured pipe throughput of the context's device, the denominators of the kernels'
  * rooflines (no counterpart in the reference, which has no GPU): kind 0 = FP64 FMA

@@ -45,6 +45,10 @@ struct pnjl_ctx {
     // tuning
     int group = 32;
     int blocks_per_sm = 0;  // 0 = occupancy maximum
+    int pipeline_chunks = 0;  // mixed per-point solves: chunks over two streams (0 = automatic)
+    cudaStream_t stream2 = nullptr;  // second stream of the chunk pipeline
+    cudaEvent_t ev_chunk[pnjl::kMaxPipelineChunks] = {};
+    cudaEvent_t ev_join = nullptr;
     pnjl_stats stats{};
     std::string err;
     // learned seed
@@ -253,6 +257,10 @@ int pnjl_init(const pnjl_params *params, int device, pnjl_ctx **out) {
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_mid);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking);
+    for (int k = 0; k < pnjl::kMaxPipelineChunks && e == cudaSuccess; ++k)
+        e = cudaEventCreateWithFlags(&ctx->ev_chunk[k], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_ctrl, pnjl::kCtrlSlots * sizeof(long long));
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_ctrl_snap, pnjl::kCtrlSlots * sizeof(long long));
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_seed_tables, 2 * 16 * 5 * sizeof(double));
@@ -288,6 +296,10 @@ int pnjl_destroy(pnjl_ctx *ctx) {
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->ev_mid) cudaEventDestroy(ctx->ev_mid);
+    for (int k = 0; k < pnjl::kMaxPipelineChunks; ++k)
+        if (ctx->ev_chunk[k]) cudaEventDestroy(ctx->ev_chunk[k]);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+    if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
     cudaFree(ctx->d_ctrl_snap);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -433,6 +445,55 @@ int pnjl_thermo_batch(pnjl_ctx *ctx, int64_t n, const double *x, const double *T
     return eval_common(ctx, n, x, T, mu_u, mu_d, mu_s, xi, PNJL_PREC_FP64, nullptr, nullptr, nullptr, out);
 }
 
+// Chunks of the mixed per-point pipeline for n points: the tuned value, or automatic -- one
+// chunk per ~2 points for every resident warp (sm_count x 16 warps x 2), at most 4.
+static int pipeline_chunks(const pnjl_ctx *ctx, int64_t n) {
+    int C = ctx->pipeline_chunks;
+    if (C <= 0) {
+        const int64_t per = (int64_t)ctx->sm_count * 16 * 2;
+        C = (int)std::min<int64_t>(4, std::max<int64_t>(1, n / std::max<int64_t>(per, 1)));
+    }
+    C = std::min<int>(C, pnjl::kMaxPipelineChunks);
+    return (int)std::max<int64_t>(1, std::min<int64_t>(C, n / 64 > 0 ? n / 64 : 1));
+}
+
+// The arguments of the mixed solve restricted to points [lo, hi): inputs, per-point seeds,
+// outputs and every per-slot scratch array offset by lo (slots are chunk-local point
+// indices), and the chunk's own queue heads and list length in the control block.
+static pnjl::SolveArgs chunk_args(const pnjl::SolveArgs &a, int64_t lo, int64_t hi, long long *ctrl3) {
+    pnjl::SolveArgs c = a;
+    const int S = a.n_seeds;
+    c.n = hi - lo;
+    c.T = a.T + lo; c.mu_u = a.mu_u + lo; c.mu_d = a.mu_d + lo; c.mu_s = a.mu_s + lo; c.xi = a.xi + lo;
+    if (a.point_seeds) c.point_seeds = a.point_seeds + 5 * lo;
+    auto sh = [lo](auto *p, int64_t k) { return p ? p + k * lo : p; };
+    c.out.x = sh(a.out.x, 5);
+    c.out.omega = sh(a.out.omega, 1);
+    c.out.pressure = sh(a.out.pressure, 1);
+    c.out.rho_norm = sh(a.out.rho_norm, 1);
+    c.out.entropy = sh(a.out.entropy, 1);
+    c.out.energy = sh(a.out.energy, 1);
+    c.out.masses = sh(a.out.masses, 3);
+    c.out.rho = sh(a.out.rho, 3);
+    c.out.n_q = sh(a.out.n_q, 3);
+    c.out.n_aq = sh(a.out.n_aq, 3);
+    c.out.residual_norm = sh(a.out.residual_norm, 1);
+    c.out.iterations = sh(a.out.iterations, 1);
+    c.out.chosen_seed = sh(a.out.chosen_seed, 1);
+    c.out.status = sh(a.out.status, 1);
+    c.out.converged = sh(a.out.converged, 1);
+    c.cand = sh(a.cand, S + 1);
+    c.done = sh(a.done, 1);
+    c.roots = sh(a.roots, 5 * S);
+    c.root_flag = sh(a.root_flag, S);
+    c.list = sh(a.list, 1);
+    c.list_mode = sh(a.list_mode, 1);
+    c.queue = ctrl3;
+    c.list_count = ctrl3 + 1;
+    c.queue2 = ctrl3 + 2;
+    return c;
+}
+
 int pnjl_solve_batch_device(pnjl_ctx *ctx, int64_t n, const double *d_T, const double *d_mu_u, const double *d_mu_d,
                             const double *d_mu_s, const double *d_xi, const pnjl_solve_opts *opts,
                             pnjl_result_soa *d_out) {
@@ -471,8 +532,7 @@ int pnjl_solve_batch_device(pnjl_ctx *ctx, int64_t n, const double *d_T, const d
         const size_t b_done = al(nn * sizeof(int)), b_flag = al(nn * S * sizeof(int));
         const size_t b_cand = al(nn * (S + 1) * sizeof(pnjl::CandRec)), b_roots = al(nn * S * 5 * sizeof(double));
         const size_t b_list = al(nn * sizeof(long long)), b_mode = al(nn * sizeof(int));
-        const size_t b_best = al(nn * sizeof(double));
-        int rc2 = ensure_scratch(ctx, b_done + b_flag + b_cand + b_roots + b_list + b_mode + b_best);
+        int rc2 = ensure_scratch(ctx, b_done + b_flag + b_cand + b_roots + b_list + b_mode);
         if (rc2) return rc2;
         unsigned char *q = ctx->d_scratch;
         a.done = (int *)q;
@@ -481,10 +541,8 @@ int pnjl_solve_batch_device(pnjl_ctx *ctx, int64_t n, const double *d_T, const d
         a.roots = (double *)(q + b_done + b_flag + b_cand);
         a.list = (long long *)(q + b_done + b_flag + b_cand + b_roots);
         a.list_mode = (int *)(q + b_done + b_flag + b_cand + b_roots + b_list);
-        a.best_omega = (double *)(q + b_done + b_flag + b_cand + b_roots + b_list + b_mode);
-        // done and root_flag are adjacent: one memset clears both; best_omega starts as NaN
+        // done and root_flag are adjacent: one memset clears both
         PNJL_CUDA_TRY(ctx, cudaMemsetAsync(q, 0, b_done + b_flag, s));
-        PNJL_CUDA_TRY(ctx, cudaMemsetAsync(a.best_omega, 0xff, nn * sizeof(double), s));
     }
     PNJL_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_ctrl, 0, pnjl::kCtrlSlots * sizeof(long long), s));
     a.P = ctx->dp;
@@ -544,6 +602,27 @@ int pnjl_solve_batch_device(pnjl_ctx *ctx, int64_t n, const double *d_T, const d
         e = pnjl::launch_solve(a, group, grid, smem, s);
     } else if (opts->seed_mode == PNJL_SEEDS_TABLE) {
         e = pnjl::launch_mixed_tasks(a, grid_tasks, smem, s);
+    } else if (ctx->split_last && pipeline_chunks(ctx, n) > 1) {
+        // chunk pipeline: the per-point kernel of chunk c+1 (stream 1) runs while the task
+        // kernel of chunk c (stream 2) works through the points chunk c deferred; each fills
+        // the other's tail.  The chunks' queue heads and list lengths are separate slots.
+        ctx->split_last = false;
+        const int C = pipeline_chunks(ctx, n);
+        for (int c = 0; c < C && e == cudaSuccess; ++c) {
+            const int64_t lo = n * c / C, hi = n * (c + 1) / C;
+            const pnjl::SolveArgs ac = chunk_args(a, lo, hi, ctx->d_ctrl + pnjl::kChunkCtrlBase + 3 * c);
+            const int g1 = (int)std::max<int64_t>(1, std::min<int64_t>(grid, (hi - lo + 7) / 8));
+            e = pnjl::launch_mixed_points(ac, g1, smem, s);
+            if (e != cudaSuccess) break;
+            PNJL_CUDA_TRY(ctx, cudaEventRecord(ctx->ev_chunk[c], s));
+            PNJL_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream2, ctx->ev_chunk[c], 0));
+            e = pnjl::launch_mixed_tasks(ac, grid_tasks, smem, ctx->stream2);
+        }
+        if (e == cudaSuccess) {
+            PNJL_CUDA_TRY(ctx, cudaEventRecord(ctx->ev_join, ctx->stream2));
+            PNJL_CUDA_TRY(ctx, cudaStreamWaitEvent(s, ctx->ev_join, 0));
+        }
+        launches = 2 * C;
     } else {
         e = pnjl::launch_mixed_points(a, grid, smem, s);
         if (e == cudaSuccess && ctx->split_last) {
@@ -971,6 +1050,70 @@ int pnjl_probe_peak(pnjl_ctx *ctx, int32_t kind, double *ops_per_s) {
     PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     int rc = pnjl_probe_peak_impl(ctx->device, kind, ops_per_s);
     if (rc) return fail(ctx, rc, "peak probe failed");
+    return PNJL_OK;
+}
+
+int pnjl_set_pipeline(pnjl_ctx *ctx, int32_t chunks) {
+    if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
+    if (chunks < 0 || chunks > pnjl::kMaxPipelineChunks)
+        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "pipeline chunks out of range (0..16)");
+    ctx->pipeline_chunks = chunks;
+    return PNJL_OK;
+}
+
+int pnjl_get_tuning(const pnjl_ctx *ctx, int32_t *lanes_per_point, int32_t *blocks_per_sm, int32_t *chunks) {
+    if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
+    if (lanes_per_point) *lanes_per_point = ctx->group;
+    if (blocks_per_sm) *blocks_per_sm = ctx->blocks_per_sm;
+    if (chunks) *chunks = ctx->pipeline_chunks;
+    return PNJL_OK;
+}
+
+int pnjl_autotune(pnjl_ctx *ctx, int64_t n, const double *d_T, const double *d_mu_u, const double *d_mu_d,
+                  const double *d_mu_s, const double *d_xi, const pnjl_solve_opts *opts, pnjl_result_soa *d_out,
+                  int32_t learned, int32_t reps, pnjl_tuning *best, pnjl_tuning *tried, int32_t max_tried,
+                  int32_t *n_tried) {
+    if (!ctx || !opts || !d_out || !best || n <= 0 || reps < 1) return PNJL_ERR_INVALID_ARGUMENT;
+    int rc = check_opts(ctx, opts);
+    if (rc) return rc;
+    const bool mixed = opts->precision == PNJL_PREC_MIXED;
+    const bool per_point = learned || opts->seed_mode == PNJL_SEEDS_PER_POINT;
+    int occ_max = mixed ? std::max(pnjl::solve_mixed_occupancy(false, pnjl::node_smem_bytes(ctx->p_num, ctx->t_num)), 1)
+                        : std::max(pnjl::solve_kernel_occupancy(32, pnjl::node_smem_bytes(ctx->p_num, ctx->t_num)), 1);
+    const int chunk_list[] = {1, 2, 3, 4, 6, 8};
+    const int n_chunk = (mixed && per_point) ? 6 : 1;
+    const int old_bps = ctx->blocks_per_sm, old_c = ctx->pipeline_chunks;
+    pnjl_tuning b{};
+    b.ms = 1e300;
+    int count = 0;
+    for (int bps = occ_max; bps >= 1; --bps) {
+        for (int ci = 0; ci < n_chunk; ++ci) {
+            ctx->blocks_per_sm = bps;
+            ctx->pipeline_chunks = chunk_list[ci];
+            double t_min = 1e300;
+            for (int r = 0; r < reps; ++r) {
+                rc = learned ? pnjl_solve_batch_learned_device(ctx, n, d_T, d_mu_u, d_mu_d, d_mu_s, d_xi, opts, d_out)
+                             : pnjl_solve_batch_device(ctx, n, d_T, d_mu_u, d_mu_d, d_mu_s, d_xi, opts, d_out);
+                if (rc) {
+                    ctx->blocks_per_sm = old_bps;
+                    ctx->pipeline_chunks = old_c;
+                    return rc;
+                }
+                PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+                float ms = 0.f;
+                PNJL_CUDA_TRY(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+                t_min = std::min(t_min, (double)ms);
+            }
+            pnjl_tuning t{32, bps, chunk_list[ci], t_min};
+            if (tried && count < max_tried) tried[count] = t;
+            ++count;
+            if (t_min < b.ms) b = t;
+        }
+    }
+    if (n_tried) *n_tried = count;
+    ctx->blocks_per_sm = b.blocks_per_sm;
+    ctx->pipeline_chunks = b.pipeline_chunks;
+    *best = b;
     return PNJL_OK;
 }
 

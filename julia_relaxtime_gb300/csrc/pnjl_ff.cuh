@@ -171,14 +171,16 @@ __device__ __forceinline__ FlavourFF make_flavour_ff(double M, double mu, double
 // antiquark side) and thermo terms (number sums, a n+ + b n-, log term).
 struct FlavourAccFF {
     ff DM, Sq, Sa, Nq, Na, SAN, SL;
+    ff DMM, DMq, DMa, Sqq, Sqa, Saa;  // second derivatives (Newton passes)
     __device__ __forceinline__ void zero() {
         DM = Sq = Sa = Nq = Na = SAN = SL = ff{0.0f, 0.0f};
+        DMM = DMq = DMa = Sqq = Sqa = Saa = ff{0.0f, 0.0f};
     }
 };
 
-// One node-flavour evaluation (node_flavour<..., GRAD, THERMO> of pnjl_device.cuh in
+// One node-flavour evaluation (node_flavour<..., GRAD, HESS, THERMO> of pnjl_device.cuh in
 // float-float), with the reference's clamps max(f, 1e-16) decided on the leading parts.
-template <bool GRAD, bool THERMO>
+template <bool GRAD, bool THERMO, bool HESS = false>
 __device__ __forceinline__ void node_flavour_ff(const FlavourFF &fc, ff q2, ff w, const float *etab,
                                                 FlavourAccFF &acc) {
     const ff E2 = ff_add(q2, fc.M2);
@@ -216,12 +218,40 @@ __device__ __forceinline__ void node_flavour_ff(const FlavourFF &fc, ff q2, ff w
     const ff s3 = ff_mul(fc.C2, ff_mul(u3, Cim));
     const ff np = clP ? ff_make(sig ? 1.0f : 0.0f) : ff_add(ff_add(ff_mul(fc.Pq, r1), ff_mul(fc.Pa2, r2)), r3);
     const ff nm = clM ? ff_make(0.0f) : ff_add(ff_add(ff_mul(fc.Pa, s1), ff_mul(fc.Pq2, s2)), s3);
-    if (GRAD) {
+    if (GRAD || HESS) {
         const ff mE = ff_mul(fc.M, rE);
         const ff LE = ff_mul_f(ff_mul(ff_add(np, nm), fc.invT), -3.0f);
-        acc.DM = ff_add(acc.DM, ff_mul(w, ff_mul(LE, mE)));
-        acc.Sq = ff_add(acc.Sq, ff_mul_f(ff_mul(w, ff_add(r1, s2)), 3.0f));
-        acc.Sa = ff_add(acc.Sa, ff_mul_f(ff_mul(w, ff_add(r2, s1)), 3.0f));
+        if (GRAD) {
+            acc.DM = ff_add(acc.DM, ff_mul(w, ff_mul(LE, mE)));
+            acc.Sq = ff_add(acc.Sq, ff_mul_f(ff_mul(w, ff_add(r1, s2)), 3.0f));
+            acc.Sa = ff_add(acc.Sa, ff_mul_f(ff_mul(w, ff_add(r2, s1)), 3.0f));
+        }
+        if (HESS) {
+            const ff one = ff_make(1.0f);
+            const ff Laa = clP ? ff_make(0.0f)
+                               : ff_sub(ff_add(ff_add(ff_mul_f(ff_mul(fc.Pq, r1), 3.0f), ff_mul_f(ff_mul(fc.Pa, r2), 12.0f)),
+                                               ff_mul_f(r3, 9.0f)),
+                                        ff_mul_f(ff_mul(np, np), 9.0f));
+            const ff Lbb = clM ? ff_make(0.0f)
+                               : ff_sub(ff_add(ff_add(ff_mul_f(ff_mul(fc.Pa, s1), 3.0f), ff_mul_f(ff_mul(fc.Pq, s2), 12.0f)),
+                                               ff_mul_f(s3, 9.0f)),
+                                        ff_mul_f(ff_mul(nm, nm), 9.0f));
+            const ff iT2 = ff_mul(fc.invT, fc.invT);
+            const ff LEE = ff_mul(ff_add(Laa, Lbb), iT2);
+            const ff mE2 = ff_mul(mE, mE);
+            const ff LMM = ff_add(ff_mul(LEE, mE2), ff_mul(ff_mul(LE, ff_sub(one, mE2)), rE));
+            const ff np3 = ff_mul_f(np, 3.0f), nm3 = ff_mul_f(nm, 3.0f);
+            const ff LEq = ff_neg(ff_mul(fc.invT, ff_mul_f(ff_add(ff_mul(r1, ff_sub(one, np3)),
+                                                                 ff_mul(s2, ff_sub(ff_make(2.0f), nm3))), 3.0f)));
+            const ff LEa = ff_neg(ff_mul(fc.invT, ff_mul_f(ff_add(ff_mul(r2, ff_sub(ff_make(2.0f), np3)),
+                                                                 ff_mul(s1, ff_sub(one, nm3))), 3.0f)));
+            acc.DMM = ff_add(acc.DMM, ff_mul(w, LMM));
+            acc.DMq = ff_add(acc.DMq, ff_mul(w, ff_mul(LEq, mE)));
+            acc.DMa = ff_add(acc.DMa, ff_mul(w, ff_mul(LEa, mE)));
+            acc.Sqq = ff_add(acc.Sqq, ff_mul_f(ff_mul(w, ff_add(ff_mul(r1, r1), ff_mul(s2, s2))), -9.0f));
+            acc.Sqa = ff_add(acc.Sqa, ff_mul_f(ff_mul(w, ff_add(ff_mul(r1, r2), ff_mul(s1, s2))), -9.0f));
+            acc.Saa = ff_add(acc.Saa, ff_mul_f(ff_mul(w, ff_add(ff_mul(r2, r2), ff_mul(s1, s1))), -9.0f));
+        }
     }
     if (THERMO) {
         acc.Nq = ff_add(acc.Nq, ff_mul(w, np));

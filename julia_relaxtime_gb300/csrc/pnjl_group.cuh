@@ -96,7 +96,8 @@ struct Group {
     }
 
     // NLsolve :newton (static line search) from x0
-    __device__ void newton(const PointIn &pt, const double *x0, const SolveOpts &o, Candidate &c) {
+    __device__ void newton(const PointIn &pt, const double *x0, const SolveOpts &o, Candidate &c, int max_iter = -1) {
+        if (max_iter < 0) max_iter = o.max_iter;
         double x[5], xold[5], p[5], F[5], J[25];
 #pragma unroll
         for (int i = 0; i < 5; ++i) { x[i] = x0[i]; xold[i] = qnan(); }
@@ -114,7 +115,7 @@ struct Group {
         bool xconv = false, fconv = norm_inf5(F) < o.ftol;
         bool stopped = any_nan5(x) || any_nan5(F);
         bool converged = fconv;
-        while (!stopped && !converged && it < o.max_iter) {
+        while (!stopped && !converged && it < max_iter) {
             ++it;
             if (lu_solve5(J, F, p)) {
 #pragma unroll
@@ -315,8 +316,8 @@ struct Group {
     // ||grad_x Omega||_inf is below ftol; Omega and the thermo output come from FP64 passes.
     static constexpr double kFtol32 = 1e-8;   // FP32 residual that ends the FP32 phase
     static constexpr double kStall32 = 1e-6;  // ... or a relative step this small ...
-    static constexpr double kLoose32 = 1e-3;  // ... with the FP32 residual below this
-    static constexpr int kMaxRefine = 8;
+    static constexpr double kNoise32 = 1e-5;  // ... with the FP32 residual near its noise floor
+    static constexpr double kLoose32 = 1e-3;  // residual at the iteration limit still handed on
 
     __device__ __noinline__ void eval_newton32(const PointIn &pt, const double *x, double *F, double *J) {
         double M[3];
@@ -332,34 +333,38 @@ struct Group {
         cnt.v[kStatPasses32] += 1;
     }
 
-    // Omega at x from an FP32 Kahan-compensated log pass (FP64 vacuum, chi and U terms):
-    // accurate to ~1e-6 absolute, used only to discard candidates that cannot win.
-    __device__ __noinline__ double eval_omega32(const PointIn &pt, const double *x) {
+    // Omega and the residual norm at x from one FP32 Kahan-compensated pass (FP64 vacuum, chi
+    // and U terms): Omega accurate to ~1e-6 absolute, used only to discard candidates that
+    // cannot win.
+    __device__ __noinline__ double eval_omega32(const PointIn &pt, const double *x, double &fres) {
         double M[3];
         masses(P, x, M);
         PassSums S;
-        node_pass<float, true, false, false, true, G>(nv, pt, x, M, gl, mask, S, cnt.v[kStatEvalsThermo32]);
+        node_pass<float, true, true, false, true, G>(nv, pt, x, M, gl, mask, S, cnt.v[kStatEvalsThermo32]);
         Eval ev;
         double V, V1[3], V2[3];
         vacuum_terms<G>(P, M, gl, mask, leader(), V, V1, V2);
-        assemble<false, false, true>(P, pt, x, M, S, V, V1, V2, ev);
+        assemble<true, false, true>(P, pt, x, M, S, V, V1, V2, ev);
         cnt.v[kStatPasses32] += 1;
+        fres = norm_inf5(ev.F);
         return ev.omega;
     }
 
     // Whether the FP32 root x32 cannot win the min-Omega selection against a certified
-    // candidate of the same point with Omega `bound`: its FP32 Omega lies above bound by far
-    // more than the FP32 pass error.  (Candidates within the margin are refined and compared
-    // in FP64 as usual.)
-    static constexpr double kPruneRtol = 1e-5;
+    // candidate of the same point with Omega `bound`.  The FP32 Omega pass is accurate to
+    // ~1e-5 |Omega| (Kahan sums of FP32 terms).  A tight FP32 root (residual <= 1e-6) lies so
+    // close to its FP64 root that their Omega differ by far less, so it is discarded when its
+    // FP32 Omega exceeds bound by 1e-4 |bound|.  Loose end points of the FP32 phase (slow
+    // convergence) are never discarded: refinement can still carry them far.  Anything not
+    // discarded is refined and compared in FP64 as usual.
+    static constexpr double kPruneTight = 1e-6, kPruneTightRtol = 1e-4;
     __device__ bool cannot_win(const PointIn &pt, const double *x32, double bound) {
         if (!(bound == bound)) return false;
-        const double om = eval_omega32(pt, x32);
-        if (om > bound + kPruneRtol * fmax(fabs(bound), 1.0)) {
-            cnt.v[kStatPruned] += 1;
-            return true;
-        }
-        return false;
+        double fres = 0.0;
+        const double om = eval_omega32(pt, x32, fres);
+        const bool out = fres <= kPruneTight && om > bound + kPruneTightRtol * fmax(fabs(bound), 1.0);
+        if (out) cnt.v[kStatPruned] += 1;
+        return out;
     }
 
     // Residual at x from the float-float pass (FP32 pipe, ~1e-12 accurate); false when the
@@ -377,6 +382,26 @@ struct Group {
         for (int i = 0; i < 5; ++i) F[i] = ev.F[i];
         cnt.v[kStatPasses32] += 1;
         return all_finite5(F);
+    }
+
+    // Residual and Jacobian at x from the float-float Newton pass (~1e-12 accurate, FP32
+    // pipe); false when the tables are not staged or a value is not finite.
+    __device__ __noinline__ bool eval_newton_ff(const PointIn &pt, const double *x, double *F, double *J) {
+        if (!nv.p2l) return false;
+        double M[3];
+        masses(P, x, M);
+        PassSums S;
+        node_pass_ff<G, true, false, true>(nv, pt, x, M, gl, mask, S, cnt.v[kStatEvalsFF]);
+        Eval ev;
+        double V, V1[3], V2[3];
+        vacuum_terms<G>(P, M, gl, mask, leader(), V, V1, V2);
+        assemble<true, true, false>(P, pt, x, M, S, V, V1, V2, ev);
+        bool ok = all_finite5(ev.F);
+        for (int i = 0; i < 25; ++i) ok = ok && ev.J[i] == ev.J[i] && fabs(ev.J[i]) < 1e300;
+        for (int i = 0; i < 5; ++i) F[i] = ev.F[i];
+        for (int i = 0; i < 25; ++i) J[i] = ev.J[i];
+        cnt.v[kStatPasses32] += 1;
+        return ok;
     }
 
     // Omega, entropy, rho_f and number densities at c.x from the float-float pass (the
@@ -413,6 +438,14 @@ struct Group {
         cnt.v[kStatPasses64] += 1;
     }
 
+    // FP32-pass Newton from x0.  1: reached the FP32 floor, 0: did not converge, -1: residual
+    // at x0 not finite.  The phase ends at the first of: a tiny residual; near the FP32 noise
+    // floor (residual below kNoise32), a Newton step at the FP32 resolution (relative
+    // kStall32) or a residual that stopped halving for two steps (the floor itself, or the
+    // linear convergence of a nearly singular Jacobian, which the refinement then finishes);
+    // the iteration limit, handed on only with a small residual.  Far from the floor the FP32
+    // iteration goes on as the reference's FP64 Newton iteration would, within the same
+    // iteration budget.
     __device__ int newton32(const PointIn &pt, const double *x0, const SolveOpts &o, double *x, double *J, int &iters) {
         double F[5], p[5];
         for (int i = 0; i < 5; ++i) x[i] = x0[i];
@@ -436,16 +469,18 @@ struct Group {
             eval_newton32(pt, x, F, J);
             if (any_nan5(x) || any_nan5(F)) return 0;
             const double fnew = norm_inf5(F);
-            if (fnew < kLoose32) {
+            if (fnew < kNoise32) {
                 if (pn <= kStall32 * (1.0 + xn)) return 1;
                 slow = fnew > 0.5 * fn ? slow + 1 : 0;
                 if (slow >= 2) return 1;
+            } else {
+                slow = 0;
             }
         }
     }
 
     // NLsolve-style dogleg trust region on FP32 passes; same return codes and stop rules as
-    // newton32, plus a trust radius collapsed to the FP32 resolution with a small residual.
+    // newton32, plus a trust radius collapsed to the FP32 resolution near the noise floor.
     __device__ int tr32(const PointIn &pt, const double *x0, const SolveOpts &o, double *x, double *Jacc, int &iters) {
         double d[5], p[5], r[5], F[5], J[25], xt[5];
         for (int i = 0; i < 5; ++i) x[i] = x0[i];
@@ -497,61 +532,100 @@ struct Group {
                 const double fn = norm_inf5(r);
                 if (any_nan5(x) || !(fn == fn)) return 0;
                 if (fn < kFtol32) return 1;
-                if (fn < kLoose32) {
+                if (fn < kNoise32) {
                     if (norm_inf5(p) <= kStall32 * (1.0 + xn)) return 1;
                     slow = fn > 0.5 * fr ? slow + 1 : 0;
                     if (slow >= 2) return 1;
+                } else {
+                    slow = 0;
                 }
                 fr = fn;
             }
             if (rho < 0.1) delta = delta / 2.0;
             else if (rho >= 0.9) delta = 2.0 * wp;
             else if (rho >= 0.5) delta = fmax(delta, 2.0 * wp);
-            if (fr < kLoose32 && delta <= kStall32 * (1.0 + xn)) return 1;
+            if (fr < kNoise32 && delta <= kStall32 * (1.0 + xn)) return 1;
             if (!(delta > 0.0)) return 0;
         }
         return fr < kLoose32 ? 1 : 0;
     }
 
-    // FP64 refinement + certification of an FP32 solution; fills c.  Steps start from the
-    // FP32 Jacobian and improve it with Broyden's rank-one secant update after every FP64
-    // residual, B <- B + (dF - B dx) dx' / (dx' dx), so an inaccurate J32 (ill-conditioned
-    // roots) still converges superlinearly.  When the residual stops decreasing or kMaxRefine
-    // steps are spent, FP64 Newton steps (FP64 Hessian passes) continue from the best state,
-    // so the mixed mode converges wherever the FP64 path does.  A certified candidate gets its
-    // thermo from an FP64 pass at its final x.
+    // Refinement and FP64 certification of an FP32 solution; fills c.
+    // Steps x <- x - B^-1 F run on the FP32 pipe: F is the float-float residual (~1e-12
+    // accurate), B starts as the FP32 Jacobian, gets Broyden's rank-one secant update
+    // B <- B + (dF - B dx) dx' / (dx' dx) after every step, and is replaced by the float-float
+    // Jacobian at x when the steps stop contracting (a slowly converging, nearly singular
+    // root: Newton steps in float-float arithmetic, as accurate as FP64 Newton).  An FP64 residual pass is spent only
+    // to certify: once the float-float residual is below ftol/10 (or has stopped decreasing
+    // below ftol), and the root is accepted only when the FP64 residual ||grad_x Omega||_inf <
+    // ftol.  Omega, entropy, rho_f and n_f at the certified state come from a float-float pass.
+    // Without the float-float tables, or when their residuals are not finite, every residual is
+    // FP64.  The seed's iteration budget (max_iter less the FP32 phase's iterations, as the
+    // reference's NLsolve counts one budget per seed) bounds the steps; a seed that spends it
+    // is not converged.  Steps that stop contracting even with fresh FP32 Jacobians hand the
+    // rest of the budget to FP64 Newton steps (FP64 Hessian passes) from the best state.
+    static constexpr int kMaxRefreshJ = 12;
     __device__ void refine64(const PointIn &pt, const SolveOpts &o, const double *J32, const double *x32, Candidate &c,
-                             int &steps) {
-        double F[5], Fo[5], p[5], B[25], xb[5];
+                             int &steps, int budget) {
+        double F[5], Fo[5], p[5], B[25], xb[5], Jn[25];
         for (int i = 0; i < 25; ++i) B[i] = J32[i];
         for (int i = 0; i < 5; ++i) c.x[i] = xb[i] = x32[i];
         c.exception = false;
         c.phys = false;
         c.omega = c.entropy = qnan();
-        // the first residual, at the FP32 root, from the float-float pass (it only steers the
-        // first correction step; every certifying residual is FP64)
-        bool certifiable = false;
-        if (!eval_grad_ff(pt, c.x, F)) {
-            eval_grad64(pt, c.x, F);
-            certifiable = true;
-        }
+        bool use_ff = eval_grad_ff(pt, c.x, F);
+        if (!use_ff) eval_grad64(pt, c.x, F);
+        bool is64 = !use_ff;  // F is an FP64 residual
         steps = 0;
-        double fb = 0.0, fprev = 0.0;
+        int refresh = 0;
+        if (budget < 2) budget = 2;  // at least one correction and its certification
+        double fb = 1e300, fprev = 1e300;
         for (;;) {
             const double fn = norm_inf5(F);
             c.residual_norm = fn;
             const bool bad = !(fn == fn) || any_nan5(c.x);
-            if (!bad && certifiable && fn < o.ftol) { c.f_converged = true; break; }
-            if (!bad && (steps == 0 || fn < fb)) {
+            if (bad && !is64) {  // float-float residual not usable here: FP64 from now on
+                use_ff = false;
+                eval_grad64(pt, c.x, F);
+                is64 = true;
+                continue;
+            }
+            if (!bad && is64 && fn < o.ftol) { c.f_converged = true; break; }
+            if (!bad && fn < fb) {
                 for (int i = 0; i < 5; ++i) xb[i] = c.x[i];
                 fb = fn;
             }
-            if (bad || steps >= kMaxRefine || (steps > 0 && !(fn < fprev))) {
+            if (!bad && !is64 && (fn < 0.1 * o.ftol || (fn < o.ftol && !(fn < 0.5 * fprev)))) {
+                eval_grad64(pt, c.x, F);  // certification attempt at the current state
+                is64 = true;
+                if (norm_inf5(F) < o.ftol) continue;
+                use_ff = false;  // float-float and FP64 disagree here: continue in FP64
+                continue;
+            }
+            const bool stalled = steps > 0 && !(fn < 0.5 * fprev);
+            if (steps >= budget) {  // the seed's iteration budget is spent: not converged
+                c.f_converged = false;
+                if (!is64) { eval_grad64(pt, c.x, F); c.residual_norm = norm_inf5(F); }
+                break;
+            }
+            if (bad || (stalled && refresh >= kMaxRefreshJ)) {
                 const int used = steps;
                 cnt.v[kStatRescue64] += 1;
-                newton(pt, xb, o, c);
+                newton(pt, xb, o, c, budget - used);
                 steps = used + c.iterations;
                 return;
+            }
+            if (stalled) {
+                // a Newton step with the float-float Jacobian at x (its residual replaces F:
+                // same accuracy); without float-float, a fresh FP32 Jacobian
+                double Fn[5];
+                if (use_ff && eval_newton_ff(pt, c.x, Fn, Jn)) {
+                    for (int i = 0; i < 5; ++i) F[i] = Fn[i];
+                } else {
+                    eval_newton32(pt, c.x, Fn, Jn);
+                }
+                for (int i = 0; i < 25; ++i) B[i] = Jn[i];
+                ++refresh;
             }
             fprev = fn;
             if (lu_solve5(B, F, p)) {
@@ -562,8 +636,13 @@ struct Group {
             symmetrize_step(pt, c.x, p);
             for (int i = 0; i < 5; ++i) { c.x[i] += p[i]; Fo[i] = F[i]; }
             ++steps;
-            eval_grad64(pt, c.x, F);
-            certifiable = true;
+            if (use_ff && eval_grad_ff(pt, c.x, F)) {
+                is64 = false;
+            } else {
+                use_ff = false;
+                eval_grad64(pt, c.x, F);
+                is64 = true;
+            }
             double pp = 0.0;
             for (int i = 0; i < 5; ++i) pp += p[i] * p[i];
             if (pp > 0.0) {
@@ -575,7 +654,7 @@ struct Group {
                 }
             }
         }
-        // the outputs at the certified state: float-float thermo pass (FP64 pass if unavailable)
+        // the outputs at the final state: float-float thermo pass (FP64 pass if unavailable)
         if (!eval_thermo_ff(pt, o, c)) eval_thermo(pt, o, c);
     }
 
@@ -602,7 +681,7 @@ struct Group {
             dd.remember(x32);
             if (cannot_win(pt, x32, dd.omega_bound())) { dup = true; converged = false; return; }
             int st = 0;
-            refine64(pt, o, J32, x32, out, st);
+            refine64(pt, o, J32, x32, out, st, o.max_iter - it32);
             out.iterations = it32 + st;
         } else {
             for (int i = 0; i < 5; ++i) out.x[i] = x32[i];
@@ -624,13 +703,12 @@ struct Group {
                 }
                 Candidate f;
                 int st = 0;
-                refine64(pt, o, K32, y32, f, st);
+                refine64(pt, o, K32, y32, f, st, o.max_iter - itt);
                 f.iterations = itt + st;
                 if (choose_fallback(out, f, o.residual_norm_max)) out = f;
             }
         }
         converged = cand_good(out, o.residual_norm_max);
-        if (converged) dd.certified(out.omega);
     }
 
     // solve(::FixedMu) single-seed path without the MultiSeed fallback (ImplicitSolver.jl:261-304)
@@ -674,16 +752,18 @@ struct LocalRoots {
         ++n;
     }
     __device__ double omega_bound() const { return __longlong_as_double(0x7ff8000000000000ll); }
-    __device__ void certified(double) {}
 };
 
-// Dedup policy of the task kernel: seed s of a slot compares its FP32 root with the roots that
-// seeds s' < s of the same slot have already published (and with `prior`, the certified root
-// of the slot's per-point seed, in verification mode), then publishes its own.  Only earlier
-// seeds can suppress a later one, so the selected candidate is the one the sequential
-// MultiSeed loop selects (an earlier seed still running is not waited for: both are refined
-// and the tie rule keeps the earlier).  The leader lane reads and writes; the answer is
-// broadcast to the group.
+// Dedup policy of the task kernel.  Seed s of a slot skips its FP64 work when its FP32 root
+// equals one that an earlier seed s' < s of the same slot has already produced (published as
+// soon as that seed's FP32 phase ends), or `prior`, the certified root of the slot's
+// per-point seed in verification mode.  Only earlier seeds suppress a later one, and a
+// suppressed seed would reach the same FP64 root and lose the min-Omega tie to the earlier
+// seed; an earlier seed still running is not waited for (both are refined, the tie rule
+// keeps the earlier).  omega_bound() is the per-point candidate's Omega (verification mode)
+// -- a bound fixed before the task kernel starts, so which candidates are discarded as unable
+// to win does not depend on timing; in MultiSeed table mode there is none.  The leader lane
+// reads and writes; answers are broadcast.
 struct PublishedRoots {
     double *roots;        // [slots*S*5]
     int *flag;            // [slots*S]
@@ -692,34 +772,9 @@ struct PublishedRoots {
     const double *prior;  // or null
     unsigned mask;
     int leader, gl;
-    double *best;         // the slot's lowest certified Omega so far (NaN = none)
     double prior_omega;   // Omega of `prior` (NaN when there is none)
     LocalRoots own;
-    // lowest certified Omega of the slot known now: the per-point candidate's, or one that an
-    // earlier-finishing seed published (timing only decides how much work is saved: a pruned
-    // candidate lies above a certified one and would lose the selection anyway)
-    __device__ double omega_bound() const {
-        double b = prior_omega;
-        if (best) {
-            double v = 0.0;
-            if (gl == 0) v = __ldcg(best);
-            v = __shfl_sync(mask, v, leader);
-            if (v == v && !(b <= v)) b = v;
-        }
-        return b;
-    }
-    __device__ void certified(double om) {
-        if (!best || gl != 0 || !(om == om)) return;
-        unsigned long long *p = (unsigned long long *)best;
-        unsigned long long cur = __ldcg(p);
-        for (int k = 0; k < 64; ++k) {  // bounded CAS loop: one retry per competing writer
-            const double c = __longlong_as_double((long long)cur);
-            if (c == c && c <= om) return;
-            const unsigned long long prev = atomicCAS(p, cur, (unsigned long long)__double_as_longlong(om));
-            if (prev == cur) return;
-            cur = prev;
-        }
-    }
+    __device__ double omega_bound() const { return prior_omega; }
     __device__ bool seen(const double *x) const {
         if (own.seen(x)) return true;
         int hit = 0;

@@ -176,13 +176,13 @@ __global__ void __launch_bounds__(kSolveThreads) eval_kernel(EvalArgs a) {
         Eval ev;
         double V, V1[3], V2[3];
         if constexpr (MODE == 2) {
-            node_pass_ff<G, true, false>(nv, pt, x, M, gl, mask, S, evals);
+            node_pass_ff<G, true, false, true>(nv, pt, x, M, gl, mask, S, evals);
             vacuum_terms<G>(a.P, M, gl, mask, lane & ~(G - 1), V, V1, V2);
-            assemble<true, false, false>(a.P, pt, x, M, S, V, V1, V2, ev);
+            assemble<true, true, false>(a.P, pt, x, M, S, V, V1, V2, ev);
             if (gl == 0) {
                 if (a.omega) a.omega[i] = qnan();
                 if (a.grad) for (int k = 0; k < 5; ++k) a.grad[5 * i + k] = -ev.F[k];
-                if (a.hess) for (int k = 0; k < 25; ++k) a.hess[25 * i + k] = qnan();
+                if (a.hess) for (int k = 0; k < 25; ++k) a.hess[25 * i + k] = -ev.J[k];
             }
             continue;
         } else if constexpr (MODE == 1) {

@@ -60,16 +60,18 @@ struct SolveArgs {
     int *list_mode;               // [n] kListVerify / kListFallback
     long long *list_count;        // entries in list (zeroed)
     long long *queue2;            // work-queue head of the task kernel (zeroed)
-    double *best_omega;           // [n] lowest certified Omega published per slot (NaN = none;
-                                  // set to all-ones bytes before the launch)
 };
 
 // Modes of a slot of the mixed task kernel: min-Omega over all seeds (MultiSeed table mode);
 // a converged per-point solution checked against the first verify_seeds seeds; a per-point
 // seed that failed, replaced by the MultiSeed solve (ImplicitSolver.jl:306-327).
 // the control block of a context: queue head, counters, list length, task queue head
-constexpr int kCtrlSlots = 32;
+constexpr int kCtrlSlots = 80;
+// per-chunk queue heads of the pipelined mixed per-point solve: queue, list length, task queue
+constexpr int kMaxPipelineChunks = 16;
+constexpr int kChunkCtrlBase = 1 + 16;  // after the queue head and up to 16 counters
 static_assert(kStatCount + 3 <= kCtrlSlots, "control block too small");
+static_assert(kStatCount <= 16 && kChunkCtrlBase + 3 * kMaxPipelineChunks <= kCtrlSlots, "chunk control slots");
 
 enum ListMode { kListFull = 0, kListVerify = 1, kListFallback = 2 };
 

@@ -138,8 +138,8 @@ __global__ void __launch_bounds__(kSolveThreads, 2) mixed_tasks_kernel(SolveArgs
             for (int k = 0; k < 5; ++k) prior[k] = __ldcg(&rec[S].x[k]);
             prior_omega = __ldcg(&rec[S].omega);
         }
-        PublishedRoots dd{a.roots,  a.root_flag, slot * S,         s, mode == kListVerify ? prior : nullptr,
-                          mask,     leader,      gl,               a.best_omega + slot, prior_omega};
+        PublishedRoots dd{a.roots, a.root_flag, slot * S, s, mode == kListVerify ? prior : nullptr, mask, leader, gl,
+                          prior_omega};
         Candidate c;
         bool conv, dup;
         grp.mixed_solve_seed(pt, x0, o, c, conv, dup, dd);

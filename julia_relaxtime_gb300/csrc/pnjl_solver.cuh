@@ -217,7 +217,7 @@ __device__ void node_pass(const NodeView &nv, const PointIn &pt, const double *x
 // Float-float pass: the sums of node_pass<..., GRAD, THERMO> (S.DM, S.SP, S.SPb; S.Nq, S.Na,
 // S.SAN, S.SL) computed in float-float arithmetic on the FP32 pipe (pnjl_ff.cuh); requires the
 // staged float-float tables (nv.p2l != null).  Non-finite sums are returned as such.
-template <int G, bool GRAD, bool THERMO>
+template <int G, bool GRAD, bool THERMO, bool HESS = false>
 __device__ void node_pass_ff(const NodeView &nv, const PointIn &pt, const double *x, const double *M, int gl,
                              unsigned mask, PassSums &S, int64_t &evals) {
     const bool dedup = (M[1] == M[0]) && (pt.mu[1] == pt.mu[0]);
@@ -225,7 +225,8 @@ __device__ void node_pass_ff(const NodeView &nv, const PointIn &pt, const double
     const ff xi = ff_from_double(pt.xi);
     const ff z{0.0f, 0.0f};
     ff DM[3] = {z, z, z}, Nq[3] = {z, z, z}, Na[3] = {z, z, z};
-    ff SP = z, SPb = z, SAN = z, SL = z;
+    ff DMM[3] = {z, z, z}, DMP[3] = {z, z, z}, DMPb[3] = {z, z, z};
+    ff SP = z, SPb = z, SAN = z, SL = z, SPP = z, SPPb = z, SPbPb = z;
 #pragma unroll 1
     for (int f = 0; f < 3; ++f) {
         if (f == 1 && dedup) continue;
@@ -244,7 +245,7 @@ __device__ void node_pass_ff(const NodeView &nv, const PointIn &pt, const double
         for (int k = gl; k < n; k += G) {
             const ff q2 = ff_mul(ff{nv.p2f[ip], nv.p2l[ip]}, sxi);
             const ff w = ff_mul(ff{nv.Af[ip], nv.Al[ip]}, bw);
-            node_flavour_ff<GRAD, THERMO>(fc, q2, w, nv.expt, fa);
+            node_flavour_ff<GRAD, THERMO, HESS>(fc, q2, w, nv.expt, fa);
             ip += G;
             if (ip >= pn) {
                 do { ip -= pn; ++it; } while (ip >= pn);
@@ -262,6 +263,15 @@ __device__ void node_pass_ff(const NodeView &nv, const PointIn &pt, const double
             SP = ff_add(SP, dbl(sw ? fa.Sa : fa.Sq));
             SPb = ff_add(SPb, dbl(sw ? fa.Sq : fa.Sa));
         }
+        if (HESS) {
+            DMM[f] = fa.DMM;
+            DMP[f] = sw ? fa.DMa : fa.DMq;
+            DMPb[f] = sw ? fa.DMq : fa.DMa;
+            if (two) { DMM[1] = DMM[0]; DMP[1] = DMP[0]; DMPb[1] = DMPb[0]; }
+            SPP = ff_add(SPP, dbl(sw ? fa.Saa : fa.Sqq));
+            SPPb = ff_add(SPPb, dbl(fa.Sqa));
+            SPbPb = ff_add(SPbPb, dbl(sw ? fa.Sqq : fa.Saa));
+        }
         if (THERMO) {
             Nq[f] = sw ? fa.Na : fa.Nq;
             Na[f] = sw ? fa.Nq : fa.Na;
@@ -275,13 +285,17 @@ __device__ void node_pass_ff(const NodeView &nv, const PointIn &pt, const double
         S.DM[f] = GRAD ? ff_to_double(group_sum_ffv<G>(DM[f], mask)) : 0.0;
         S.Nq[f] = THERMO ? ff_to_double(group_sum_ffv<G>(Nq[f], mask)) : 0.0;
         S.Na[f] = THERMO ? ff_to_double(group_sum_ffv<G>(Na[f], mask)) : 0.0;
-        S.DMM[f] = S.DMP[f] = S.DMPb[f] = 0.0;
+        S.DMM[f] = HESS ? ff_to_double(group_sum_ffv<G>(DMM[f], mask)) : 0.0;
+        S.DMP[f] = HESS ? ff_to_double(group_sum_ffv<G>(DMP[f], mask)) : 0.0;
+        S.DMPb[f] = HESS ? ff_to_double(group_sum_ffv<G>(DMPb[f], mask)) : 0.0;
     }
     S.SP = GRAD ? ff_to_double(group_sum_ffv<G>(SP, mask)) : 0.0;
     S.SPb = GRAD ? ff_to_double(group_sum_ffv<G>(SPb, mask)) : 0.0;
     S.SAN = THERMO ? ff_to_double(group_sum_ffv<G>(SAN, mask)) : 0.0;
     S.SL = THERMO ? ff_to_double(group_sum_ffv<G>(SL, mask)) : 0.0;
-    S.SPP = S.SPPb = S.SPbPb = 0.0;
+    S.SPP = HESS ? ff_to_double(group_sum_ffv<G>(SPP, mask)) : 0.0;
+    S.SPPb = HESS ? ff_to_double(group_sum_ffv<G>(SPPb, mask)) : 0.0;
+    S.SPbPb = HESS ? ff_to_double(group_sum_ffv<G>(SPbPb, mask)) : 0.0;
 }
 
 // FP64 assembly of Omega, grad, Hessian and thermo from the pass sums and the vacuum terms.

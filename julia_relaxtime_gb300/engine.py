@@ -292,6 +292,37 @@ class GapEngine:
         self._check(self._lib.pnjl_probe_peak(self._ctx, k, C.byref(v)), "pnjl_probe_peak")
         return float(v.value)
 
-    def set_tuning(self, lanes_per_point: int, blocks_per_sm: int = 0):
+    def set_tuning(self, lanes_per_point: int, blocks_per_sm: int = 0, pipeline_chunks: int | None = None):
         self._check(self._lib.pnjl_set_tuning(self._ctx, int(lanes_per_point), int(blocks_per_sm)),
                     "pnjl_set_tuning")
+        if pipeline_chunks is not None:
+            self._check(self._lib.pnjl_set_pipeline(self._ctx, int(pipeline_chunks)), "pnjl_set_pipeline")
+
+    def tuning(self) -> dict:
+        a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
+        self._check(self._lib.pnjl_get_tuning(self._ctx, C.byref(a), C.byref(b), C.byref(c)), "pnjl_get_tuning")
+        return {"lanes_per_point": a.value, "blocks_per_sm": b.value, "pipeline_chunks": c.value}
+
+    def autotune(self, n: int, d_T: int, d_mu_u: int, d_mu_d: int, d_mu_s: int, d_xi: int, d_out: dict, *,
+                 seed_table=None, seed_table_hot=None, hot_T_MeV: float = 300.0, opts: SolveOptions | None = None,
+                 learned: bool = False, reps: int = 2):
+        """pnjl_autotune on a representative device batch: tries the launch shapes, keeps the
+        fastest on this context; returns (best, [all tried]) as dicts."""
+        opts = opts or SolveOptions()
+        st = None if seed_table is None else _f64(seed_table).reshape(-1, 5)
+        sth = None if seed_table_hot is None else _f64(seed_table_hot).reshape(-1, 5)
+        o = self._opts_struct(opts, st, sth, hot_T_MeV, False, None)
+        soa = api.pnjl_result_soa()
+        for k, v in d_out.items():
+            ptr_t = dict(iterations=api.i32p, chosen_seed=api.i32p, status=api.i32p, converged=api.u8p).get(k, api.dp)
+            setattr(soa, k, C.cast(C.c_void_p(v), ptr_t))
+        cast = lambda p: C.cast(C.c_void_p(p), api.dp)  # noqa: E731
+        best = api.pnjl_tuning()
+        tried = (api.pnjl_tuning * 64)()
+        nt = C.c_int32()
+        rc = self._lib.pnjl_autotune(self._ctx, n, cast(d_T), cast(d_mu_u), cast(d_mu_d), cast(d_mu_s), cast(d_xi),
+                                     C.byref(o), C.byref(soa), int(learned), int(reps), C.byref(best), tried, 64,
+                                     C.byref(nt))
+        self._check(rc, "pnjl_autotune")
+        as_dict = lambda t: {k: getattr(t, k) for k, _ in api.pnjl_tuning._fields_}  # noqa: E731
+        return as_dict(best), [as_dict(tried[i]) for i in range(min(nt.value, 64))]

@@ -77,18 +77,20 @@ def test_eval_mixed_fp32_pass_close_to_fp64(engine_factory):
 
 @pytest.mark.parametrize("p_num,t_num,mu_neg,asym", [(64, 8, False, False), (128, 32, True, True)])
 def test_eval_ff_residual_matches_oracle(engine_factory, P, p_num, t_num, mu_neg, asym):
-    """The float-float residual pass (FP32 pipe) that steers the mixed solver's first FP64
-    correction: the gradient to ~1e-12 of its scale, against the FP64 jet oracle (states with
-    mu/T moderate enough that no FP32 exponent range is exceeded)."""
+    """The float-float passes (FP32 pipe) the mixed solver refines with: gradient to ~1e-12 and
+    Hessian to ~1e-11 of their scale, against the FP64 jet oracle (states with mu/T moderate
+    enough that no FP32 exponent range is exceeded)."""
     eng = engine_factory(p_num, t_num)
     nd = orc.Nodes(p_num, t_num)
     x, T, mu, xi = random_states(48, 3 + p_num, mu_neg, asym)
     T = np.maximum(T, 45.0 / HBARC)
-    _, g, _ = eng.evaluate(x, T, mu, xi, precision="ff_residual")
+    _, g, h = eng.evaluate(x, T, mu, xi, precision="ff_residual")
     for i in range(len(T)):
-        _, g_ref, _ = orc.evaluate(P, nd, x[i], mu[i], T[i], xi[i])
+        _, g_ref, h_ref = orc.evaluate(P, nd, x[i], mu[i], T[i], xi[i])
         sg = max(1.0, np.abs(g_ref).max())
         assert np.abs(g[i] - g_ref).max() <= 1e-11 * sg, (i, g[i] - g_ref, sg)
+        sh = max(1.0, np.abs(h_ref).max())
+        assert np.abs(h[i] - h_ref).max() <= 1e-10 * sh, (i, h[i] - h_ref, sh)
 
 
 def test_thermo_matches_oracle(engine_factory, P):
@@ -320,3 +322,48 @@ def test_tmu_scan_gpu_matches_oracle(engine_factory):
         a = [float(v) for v in scan.format_tmu_row(T, mu, xi, r, msg).split(",")[:15]]
         b = [float(v) for v in scan.format_tmu_row(T2, mu2, xi2, r2, msg2).split(",")[:15]]
         assert np.allclose(a, b, rtol=0, atol=1.01e-6), (a, b)  # 6-decimal columns, last digit
+
+
+def test_mixed_pipeline_chunks_and_autotune(engine_factory):
+    """The chunk pipeline of mixed per-point solves (two streams) and the autotuner change
+    launch shapes only: bit-identical results for every shape."""
+    import torch
+
+    eng = engine_factory(32, 8)
+    rng = np.random.default_rng(77)
+    n = 3000
+    T = rng.uniform(50, 300, n) / HBARC
+    mu = rng.uniform(0, 400, n) / HBARC
+    xi = rng.uniform(-0.4, 0.4, n)
+    seeds = np.where((T * HBARC < 160)[:, None], np.array(pnjl.HADRON_SEED_5), np.array(pnjl.QUARK_SEED_5))
+    table, hot = pnjl.multiseed_table(4)
+    opts = SolveOptions(iterations=40, ftol=1e-10, precision="mixed", verify_seeds=-1, verify_T_max_MeV=170.0,
+                        verify_max_step=0.3)
+    outs = []
+    for chunks in (1, 3, 7):
+        eng.set_tuning(32, 0, pipeline_chunks=chunks)
+        outs.append(eng.solve(T, mu, xi, seed_table=table, seed_table_hot=hot, point_seeds=seeds, opts=opts))
+        st = eng.stats()
+        assert st["kernel_launches"] > 0
+    for r in outs[1:]:
+        for k in ("x", "omega", "entropy", "n_q", "status", "chosen_seed", "iterations", "converged"):
+            np.testing.assert_array_equal(r[k], outs[0][k], err_msg=k)
+    assert outs[0]["converged"].mean() > 0.99
+    # autotuner over the table-mode mixed solve of the same points (device arrays)
+    dev = torch.device("cuda", 0)
+    d = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in (("T", T), ("mu", mu), ("xi", xi))}
+    d_out = {"x": torch.empty(5 * n, dtype=torch.float64, device=dev),
+             "omega": torch.empty(n, dtype=torch.float64, device=dev),
+             "converged": torch.empty(n, dtype=torch.uint8, device=dev)}
+    torch.cuda.synchronize()
+    m = d["mu"].data_ptr()
+    best, tried = eng.autotune(n, d["T"].data_ptr(), m, m, m, d["xi"].data_ptr(),
+                               {k: v.data_ptr() for k, v in d_out.items()}, seed_table=table, seed_table_hot=hot,
+                               opts=SolveOptions(iterations=40, ftol=1e-10, precision="mixed"), reps=1)
+    assert len(tried) >= 1 and best["ms"] == min(t["ms"] for t in tried) and best["ms"] > 0
+    tu = eng.tuning()
+    assert tu["blocks_per_sm"] == best["blocks_per_sm"] and tu["pipeline_chunks"] == best["pipeline_chunks"]
+    ref = eng.solve(T, mu, xi, seed_table=table, seed_table_hot=hot,
+                    opts=SolveOptions(iterations=40, ftol=1e-10, precision="mixed"))
+    np.testing.assert_array_equal(d_out["omega"].cpu().numpy(), ref["omega"])
+    eng.set_tuning(32, 0, pipeline_chunks=0)
