@@ -46,9 +46,13 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 HBARC = 197.327
-# DRAM bytes (read + write) per launch of the dominant kernel from one ncu capture, scaled to
-# the bench step by the points it processes; see profiles/ for the capture and the command
-TRAFFIC = {}
+# DRAM bytes (read + write) per launch of the dominant kernel from one ncu capture of a
+# 9,216-point launch (0.279 GB + 0.778 GB), scaled by points to the 18,432-point step; it is
+# local-memory (stack) write-back, not data (inputs and outputs are 240 B per point)
+TRAFFIC = {"mixed_points_kernel<32>": {
+    "bytes_per_launch": 2 * (0.279048448e9 + 0.778367e9),
+    "source": "ncu --set full of one 9,216-point launch (profiles/mixed_points_and_tasks_kernels_surrogate_aniso_"
+              "9216pt.md), scaled by points; local-memory write-back"}}
 METRIC = "gap solves/s at \u2016\u2202\u03a9\u2016\u22641e-10: surrogate-seeded vs plain FP64 Newton, 1 GB300"
 # Floating-point operations per node-flavour evaluation, counted from the source of
 # pnjl_device.cuh::node_flavour (FMA = 2, loop invariants hoisted, selects and compares not
@@ -206,6 +210,7 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=48, help="points per step of the CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the library's default launch shape")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -361,7 +366,25 @@ def main():
         rec["value"] = solved / (total_ms * 1e-3)
         return rec
 
+    # launch shape from the library's autotuner on the first slice (untimed set-up)
+    tuning = None
+    if not args.no_autotune:
+        n0 = load_chunk(0)
+        m0 = d_in["mu"].data_ptr()
+        best, tried = eng.autotune(n0, d_in["T"].data_ptr(), m0, m0, m0, d_in["xi"].data_ptr(), ptrs,
+                                   seed_table=table, seed_table_hot=hot, opts=arm.opts, learned=arm.learned, reps=2)
+        eng.synchronize()
+        tuning = {"chosen": best, "candidates": len(tried)}
     main_rec = run_arm(arm, args.steps, args.warmup, True)
+
+    # the dominant kernel's own launches, for the roofline: the same slices with the chunk
+    # pipeline off, so that the per-point kernel runs alone between its CUDA events
+    roof_rec = main_rec
+    if args.mode == "surrogate" and precision == "mixed":
+        tu = eng.tuning()
+        eng.set_tuning(32, tu["blocks_per_sm"], pipeline_chunks=1)
+        roof_rec = run_arm(arm, args.steps, 0, False)
+        eng.set_tuning(32, tu["blocks_per_sm"], pipeline_chunks=tu["pipeline_chunks"])
 
     # the plain FP64 multi-seed Newton on the same chunks: the denominator of the speed-up and
     # the FP64 judge of the surrogate's phase selection
@@ -424,15 +447,15 @@ def main():
         kname, k_ms, k_flops, k_evals = "solve_kernel<32>", main_rec["kernel_ms"], \
             [main_rec["flops64"], main_rec["flops32"], main_rec["flops_ff"]], main_rec["evals"]
     elif args.mode == "surrogate":
-        kname, k_ms, k_flops, k_evals = "mixed_points_kernel<32>", main_rec["k0_ms"], main_rec["k0_flops"], \
-            main_rec["k0_evals"]
+        kname, k_ms, k_flops, k_evals = "mixed_points_kernel<32>", roof_rec["k0_ms"], roof_rec["k0_flops"], \
+            roof_rec["k0_evals"]
     else:
         kname, k_ms, k_flops, k_evals = "mixed_tasks_kernel<32>", main_rec["kernel_ms"], \
             [main_rec["flops64"], main_rec["flops32"], main_rec["flops_ff"]], main_rec["evals"]
     avg_k_s = (sum(k_ms) / len(k_ms)) * 1e-3
     ach64 = k_flops[0] / K / avg_k_s
     ach32 = k_flops[1] / K / avg_k_s
-    step_kernels_ms = sum(main_rec["kernel_ms"]) / K
+    step_kernels_ms = sum(roof_rec["kernel_ms"]) / K
     roof = {"bound": "fp64", "kernel": kname, "achieved": ach64 / 1e12, "peak": peak_fp64 / 1e12,
             "unit": "TFLOP/s", "frac": ach64 / peak_fp64,
             "peak_source": "measured in-run (pnjl_probe_peak: FP64 FMA chains on every lane of the GPU); "
@@ -453,7 +476,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": main_rec["total_ms"] / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if precision == "fp64" else "f32+f64",
             "data": "synthetic", "config": config, "e2e": e2e, "gpu_launches": int(launches),
-            "roofline": roof, "clocks": main_rec["clocks"], "solved": main_rec["solved"],
+            "roofline": roof, "clocks": main_rec["clocks"], "solved": main_rec["solved"], "tuning": tuning,
             "work_per_step": {k: v / args.steps for k, v in main_rec["kinds"].items()}}
     if train is not None:
         line["surrogate"] = {"train": train,
