@@ -300,6 +300,27 @@ int pnjl_solve_batch_learned(pnjl_ctx *ctx, int64_t n, const double *T, const do
                              const double *mu_d, const double *mu_s, const double *xi,
                              const pnjl_solve_opts *opts, pnjl_result_soa *out);
 
+/* ---- plans: several batched solves in one CUDA graph ---------------------------------------
+ * A plan holds segments -- batched solves, each with its own quadrature order (p_num x t_num
+ * on [0, p_max]), device inputs and outputs, options and seed mode (learned: the network's
+ * seed per point, as pnjl_solve_batch_learned_device) -- captured once into one CUDA graph
+ * with one branch per segment, then replayed by pnjl_plan_launch on the context stream.  No
+ * counterpart in the reference (one point at a time, one quadrature per call).  pnjl_plan_add
+ * copies the node tables, seed tables and verification map and allocates the segment's
+ * scratch, so launches allocate and copy nothing.  Segments write only their own outputs;
+ * replays re-read the inputs and (for learned segments) the network weights at launch time.
+ * pnjl_plan_stats sums the counters of one segment (or all: segment = -1); last_kernel_ms is
+ * the last launch's device time. */
+typedef struct pnjl_plan pnjl_plan;
+int pnjl_plan_create(pnjl_ctx *ctx, pnjl_plan **out);
+int pnjl_plan_add(pnjl_plan *plan, int32_t p_num, int32_t t_num, double p_max, int64_t n, const double *d_T,
+                  const double *d_mu_u, const double *d_mu_d, const double *d_mu_s, const double *d_xi,
+                  const pnjl_solve_opts *opts, int32_t learned, pnjl_result_soa *d_out);
+int pnjl_plan_finalize(pnjl_plan *plan);
+int pnjl_plan_launch(pnjl_plan *plan);
+int pnjl_plan_stats(pnjl_plan *plan, int32_t segment, pnjl_stats *out);
+int pnjl_plan_destroy(pnjl_plan *plan);
+
 /* Largest batch of pnjl_solve_batch_noalloc, counted in tasks: n * n_seeds in
  * PNJL_SEEDS_TABLE mode, n in PNJL_SEEDS_PER_POINT mode (and n itself at most this). */
 #define PNJL_NOALLOC_MAX_TASKS 32768

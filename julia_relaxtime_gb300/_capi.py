@@ -141,6 +141,13 @@ SIGNATURES = {
                                                   C.POINTER(pnjl_solve_opts), C.POINTER(pnjl_result_soa)]),
     "pnjl_solve_batch_learned": (C.c_int, [C.c_void_p, C.c_int64, dp, dp, dp, dp, dp,
                                            C.POINTER(pnjl_solve_opts), C.POINTER(pnjl_result_soa)]),
+    "pnjl_plan_create": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "pnjl_plan_add": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_double, C.c_int64, dp, dp, dp, dp, dp,
+                                C.POINTER(pnjl_solve_opts), C.c_int32, C.POINTER(pnjl_result_soa)]),
+    "pnjl_plan_finalize": (C.c_int, [C.c_void_p]),
+    "pnjl_plan_launch": (C.c_int, [C.c_void_p]),
+    "pnjl_plan_stats": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(pnjl_stats)]),
+    "pnjl_plan_destroy": (C.c_int, [C.c_void_p]),
     "pnjl_solve_batch_noalloc": (C.c_int, [C.POINTER(pnjl_params), C.c_int32, C.c_int32, C.c_double, C.c_int64,
                                            dp, dp, dp, dp, dp, C.POINTER(pnjl_solve_opts),
                                            C.POINTER(pnjl_result_soa), C.c_void_p]),

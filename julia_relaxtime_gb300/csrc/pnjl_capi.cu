@@ -160,7 +160,7 @@ int check_opts(pnjl_ctx *ctx, const pnjl_solve_opts *o) {
     return rc ? fail(ctx, rc, msg) : PNJL_OK;
 }
 
-int grid_for(pnjl_ctx *ctx, int group, size_t smem, int64_t n) {
+int grid_for(const pnjl_ctx *ctx, int group, size_t smem, int64_t n) {
     int occ = pnjl::solve_kernel_occupancy(group, smem);
     if (occ < 1) occ = 1;
     int bps = ctx->blocks_per_sm > 0 ? std::min(ctx->blocks_per_sm, occ) : occ;
@@ -307,6 +307,31 @@ int pnjl_destroy(pnjl_ctx *ctx) {
 }
 
 const char *pnjl_last_error(const pnjl_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+// Device node tables of one quadrature (p_num x t_num, p in [0, p_max]): FP64 separable
+// tables and the FP32 hi | float-float lo | float-float exp tables.
+static void node_tables_host(int p_num, int t_num, double p_max, std::vector<double> &h, std::vector<float> &hf) {
+    std::vector<double> xp, wp, xc, wc;
+    gauss_legendre(p_num, 0.0, p_max, xp, wp);
+    gauss_legendre(t_num, 0.0, 1.0, xc, wc);
+    const int m = 2 * (p_num + t_num);
+    h.assign(m, 0.0);
+    hf.assign(2 * m + pnjl::kExpTableFloats, 0.0f);
+    pnjl::separable_tables(p_num, t_num, xp.data(), wp.data(), xc.data(), wc.data(), h.data(), hf.data(),
+                           hf.data() + m);
+    pnjl::ff_exp_tables(hf.data() + 2 * m);
+}
+
+static pnjl::KernelNodes kernel_nodes_of(const double *d, const float *f, int np, int nt) {
+    pnjl::KernelNodes kn;
+    kn.p_num = np;
+    kn.t_num = nt;
+    kn.p2 = d; kn.A = d + np; kn.c2 = d + 2 * np; kn.B = d + 2 * np + nt;
+    kn.p2f = f; kn.Af = f + np; kn.c2f = f + 2 * np; kn.Bf = f + 2 * np + nt;
+    kn.lo = f + 2 * (np + nt);
+    kn.expt = f + 4 * (np + nt);
+    return kn;
+}
 
 int pnjl_set_nodes(pnjl_ctx *ctx, int32_t p_num, int32_t t_num, double p_max) {
     if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
@@ -494,47 +519,59 @@ static pnjl::SolveArgs chunk_args(const pnjl::SolveArgs &a, int64_t lo, int64_t 
     return c;
 }
 
-int pnjl_solve_batch_device(pnjl_ctx *ctx, int64_t n, const double *d_T, const double *d_mu_u, const double *d_mu_d,
-                            const double *d_mu_s, const double *d_xi, const pnjl_solve_opts *opts,
-                            pnjl_result_soa *d_out) {
-    if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
-    if (ctx->p_num == 0) return fail(ctx, PNJL_ERR_NO_NODES, "call pnjl_set_nodes first");
-    int rc = check_opts(ctx, opts);
-    if (rc) return rc;
-    if (n < 0 || !d_out || (n > 0 && (!d_T || !d_mu_u || !d_mu_d || !d_mu_s || !d_xi)))
-        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "null array");
-    if (n == 0) return PNJL_OK;
-    cudaSetDevice(ctx->device);
-    cudaStream_t s = ctx->stream;
+// Device-side resources one batched solve writes to: the context's own, or a plan segment's.
+struct SolveRes {
+    long long *ctrl;               // kCtrlSlots counters and queue heads (zeroed by the enqueue)
+    unsigned char *scratch;        // at least solve_scratch_bytes(n, opts)
+    const double *seed_tables;     // device copy of the seed tables (cold | hot, 16 rows each)
+    const unsigned char *vmap;     // device copy of the verification map, or null
+    cudaStream_t s, s2;            // s2: second stream of the chunk pipeline
+    const cudaEvent_t *ev_chunk;   // kMaxPipelineChunks events (no timing)
+    cudaEvent_t ev_join;
+    cudaEvent_t ev_mid;            // optional: end of the first kernel (timed split) ...
+    long long *ctrl_snap;          // ... and the counters at that moment
+};
+
+static size_t al256(size_t b) { return (b + 255) & ~size_t(255); }
+
+// Scratch bytes of one batched solve of n points.
+static size_t solve_scratch_bytes(int64_t n, const pnjl_solve_opts *o) {
+    const bool mixed = o->precision == PNJL_PREC_MIXED;
+    const int S = (o->n_seeds > 0 && o->seed_table) ? o->n_seeds : 0;
+    const size_t nn = (size_t)n;
+    if (o->seed_mode == PNJL_SEEDS_TABLE && !mixed)
+        return al256(nn * sizeof(int)) + nn * o->n_seeds * sizeof(pnjl::CandRec);
+    if (mixed && S > 0)
+        return al256(nn * sizeof(int)) + al256(nn * S * sizeof(int)) + al256(nn * (S + 1) * sizeof(pnjl::CandRec)) +
+               al256(nn * S * 5 * sizeof(double)) + al256(nn * sizeof(long long)) + al256(nn * sizeof(int));
+    return 0;
+}
+
+// Enqueue one batched solve (memsets and kernels only: no host copies, no allocation, no
+// host synchronisation -- so it can also be captured into a CUDA graph).  `launches` receives
+// the kernel count; `split` whether ev_mid / ctrl_snap were recorded.
+static cudaError_t solve_enqueue(const pnjl_ctx *ctx, const pnjl::KernelNodes &nodes, int64_t n, const double *d_T,
+                                 const double *d_mu_u, const double *d_mu_d, const double *d_mu_s, const double *d_xi,
+                                 const pnjl_solve_opts *opts, const pnjl_result_soa &d_out, const SolveRes &r,
+                                 int *launches, bool *split) {
+    cudaStream_t s = r.s;
     const bool has_table = opts->n_seeds > 0 && opts->seed_table;
-    if (has_table) {
-        PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_seed_tables, opts->seed_table, opts->n_seeds * 5 * sizeof(double),
-                                           cudaMemcpyHostToDevice, s));
-        if (opts->seed_table_hot)
-            PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_seed_tables + 80, opts->seed_table_hot,
-                                               opts->n_seeds * 5 * sizeof(double), cudaMemcpyHostToDevice, s));
-    }
     pnjl::SolveArgs a{};
     const bool mixed = opts->precision == PNJL_PREC_MIXED;
     const int S = has_table ? opts->n_seeds : 0;
-    auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+    cudaError_t e = cudaSuccess;
     if (opts->seed_mode == PNJL_SEEDS_TABLE && !mixed) {
-        const size_t rec = (size_t)n * opts->n_seeds * sizeof(pnjl::CandRec);
-        const size_t cnt = al((size_t)n * sizeof(int));
-        int rc2 = ensure_scratch(ctx, cnt + rec);
-        if (rc2) return rc2;
-        a.done = (int *)ctx->d_scratch;
-        a.cand = (pnjl::CandRec *)(ctx->d_scratch + cnt);
-        PNJL_CUDA_TRY(ctx, cudaMemsetAsync(a.done, 0, (size_t)n * sizeof(int), s));
+        const size_t cnt = al256((size_t)n * sizeof(int));
+        a.done = (int *)r.scratch;
+        a.cand = (pnjl::CandRec *)(r.scratch + cnt);
+        if ((e = cudaMemsetAsync(a.done, 0, (size_t)n * sizeof(int), s)) != cudaSuccess) return e;
     } else if (mixed && S > 0) {
         // slots: every point (table mode) or the points the per-point kernel defers
         const size_t nn = (size_t)n;
-        const size_t b_done = al(nn * sizeof(int)), b_flag = al(nn * S * sizeof(int));
-        const size_t b_cand = al(nn * (S + 1) * sizeof(pnjl::CandRec)), b_roots = al(nn * S * 5 * sizeof(double));
-        const size_t b_list = al(nn * sizeof(long long)), b_mode = al(nn * sizeof(int));
-        int rc2 = ensure_scratch(ctx, b_done + b_flag + b_cand + b_roots + b_list + b_mode);
-        if (rc2) return rc2;
-        unsigned char *q = ctx->d_scratch;
+        const size_t b_done = al256(nn * sizeof(int)), b_flag = al256(nn * S * sizeof(int));
+        const size_t b_cand = al256(nn * (S + 1) * sizeof(pnjl::CandRec)), b_roots = al256(nn * S * 5 * sizeof(double));
+        const size_t b_list = al256(nn * sizeof(long long));
+        unsigned char *q = r.scratch;
         a.done = (int *)q;
         a.root_flag = (int *)(q + b_done);
         a.cand = (pnjl::CandRec *)(q + b_done + b_flag);
@@ -542,42 +579,30 @@ int pnjl_solve_batch_device(pnjl_ctx *ctx, int64_t n, const double *d_T, const d
         a.list = (long long *)(q + b_done + b_flag + b_cand + b_roots);
         a.list_mode = (int *)(q + b_done + b_flag + b_cand + b_roots + b_list);
         // done and root_flag are adjacent: one memset clears both
-        PNJL_CUDA_TRY(ctx, cudaMemsetAsync(q, 0, b_done + b_flag, s));
+        if ((e = cudaMemsetAsync(q, 0, b_done + b_flag, s)) != cudaSuccess) return e;
     }
-    PNJL_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_ctrl, 0, pnjl::kCtrlSlots * sizeof(long long), s));
+    if ((e = cudaMemsetAsync(r.ctrl, 0, pnjl::kCtrlSlots * sizeof(long long), s)) != cudaSuccess) return e;
     a.P = ctx->dp;
-    a.nodes = kernel_nodes(ctx);
-    const size_t smem = pnjl::node_smem_bytes(ctx->p_num, ctx->t_num);
+    a.nodes = nodes;
+    const size_t smem = pnjl::node_smem_bytes(nodes.p_num, nodes.t_num);
     a.n = n;
     a.T = d_T; a.mu_u = d_mu_u; a.mu_d = d_mu_d; a.mu_s = d_mu_s; a.xi = d_xi;
     a.seed_mode = opts->seed_mode;
-    a.n_seeds = has_table ? opts->n_seeds : 0;
-    a.seed_table = ctx->d_seed_tables;
-    a.seed_table_hot = (has_table && opts->seed_table_hot) ? ctx->d_seed_tables + 80 : nullptr;
+    a.n_seeds = S;
+    a.seed_table = r.seed_tables;
+    a.seed_table_hot = (has_table && opts->seed_table_hot) ? r.seed_tables + 80 : nullptr;
     a.hot_T_MeV = opts->hot_T_MeV;
     a.point_seeds = opts->point_seeds;
     pnjl::fill_solve_opts(opts, a.opts);
-    if (const int64_t cells = pnjl::verify_map_cells(opts)) {
-        if ((size_t)cells > ctx->vmap_cap) {
-            PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(s));
-            cudaFree(ctx->d_vmap);
-            ctx->d_vmap = nullptr;
-            ctx->vmap_cap = 0;
-            if (cudaMalloc(&ctx->d_vmap, (size_t)cells) != cudaSuccess)
-                return fail(ctx, PNJL_ERR_OUT_OF_MEMORY, "verification map allocation failed");
-            ctx->vmap_cap = (size_t)cells;
-        }
-        PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_vmap, opts->verify_map, (size_t)cells, cudaMemcpyHostToDevice, s));
-        a.opts.vmap = ctx->d_vmap;
-    }
-    a.out = *d_out;
-    a.queue = ctx->d_ctrl;
-    a.stats = ctx->d_ctrl + 1;
-    a.list_count = ctx->d_ctrl + 1 + pnjl::kStatCount;
-    a.queue2 = ctx->d_ctrl + 2 + pnjl::kStatCount;
+    if (pnjl::verify_map_cells(opts)) a.opts.vmap = r.vmap;
+    a.out = d_out;
+    a.queue = r.ctrl;
+    a.stats = r.ctrl + 1;
+    a.list_count = r.ctrl + 1 + pnjl::kStatCount;
+    a.queue2 = r.ctrl + 2 + pnjl::kStatCount;
     const int group = ctx->group;
     int grid = 0, grid_tasks = 0;
-    int launches = 1;
+    *launches = 1;
     if (mixed) {
         const int64_t wpb = pnjl::kSolveThreads / 32;
         auto occ_of = [&](bool tasks) {
@@ -590,50 +615,95 @@ int pnjl_solve_batch_device(pnjl_ctx *ctx, int64_t n, const double *d_T, const d
         grid = (int)std::min<int64_t>((int64_t)ctx->sm_count * occ_of(false), (n + wpb - 1) / wpb);
         const int64_t task_need = table ? (n * S + wpb - 1) / wpb : (int64_t)ctx->sm_count * occ_of(true);
         grid_tasks = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->sm_count * occ_of(true), task_need));
-        launches = table ? 1 : (S > 0 ? 2 : 1);
+        *launches = table ? 1 : (S > 0 ? 2 : 1);
     } else {
         const int64_t n_tasks = opts->seed_mode == PNJL_SEEDS_TABLE ? n * (int64_t)opts->n_seeds : n;
         grid = grid_for(ctx, group, smem, n_tasks);
     }
-    PNJL_CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, s));
-    cudaError_t e = cudaSuccess;
-    ctx->split_last = mixed && launches == 2;
+    *split = false;
+    const bool two = mixed && *launches == 2;
     if (!mixed) {
         e = pnjl::launch_solve(a, group, grid, smem, s);
     } else if (opts->seed_mode == PNJL_SEEDS_TABLE) {
         e = pnjl::launch_mixed_tasks(a, grid_tasks, smem, s);
-    } else if (ctx->split_last && pipeline_chunks(ctx, n) > 1) {
-        // chunk pipeline: the per-point kernel of chunk c+1 (stream 1) runs while the task
-        // kernel of chunk c (stream 2) works through the points chunk c deferred; each fills
+    } else if (two && pipeline_chunks(ctx, n) > 1) {
+        // chunk pipeline: the per-point kernel of chunk c+1 (stream s) runs while the task
+        // kernel of chunk c (stream s2) works through the points chunk c deferred; each fills
         // the other's tail.  The chunks' queue heads and list lengths are separate slots.
-        ctx->split_last = false;
         const int C = pipeline_chunks(ctx, n);
         for (int c = 0; c < C && e == cudaSuccess; ++c) {
             const int64_t lo = n * c / C, hi = n * (c + 1) / C;
-            const pnjl::SolveArgs ac = chunk_args(a, lo, hi, ctx->d_ctrl + pnjl::kChunkCtrlBase + 3 * c);
+            const pnjl::SolveArgs ac = chunk_args(a, lo, hi, r.ctrl + pnjl::kChunkCtrlBase + 3 * c);
             const int g1 = (int)std::max<int64_t>(1, std::min<int64_t>(grid, (hi - lo + 7) / 8));
-            e = pnjl::launch_mixed_points(ac, g1, smem, s);
-            if (e != cudaSuccess) break;
-            PNJL_CUDA_TRY(ctx, cudaEventRecord(ctx->ev_chunk[c], s));
-            PNJL_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream2, ctx->ev_chunk[c], 0));
-            e = pnjl::launch_mixed_tasks(ac, grid_tasks, smem, ctx->stream2);
+            if ((e = pnjl::launch_mixed_points(ac, g1, smem, s)) != cudaSuccess) break;
+            if ((e = cudaEventRecord(r.ev_chunk[c], s)) != cudaSuccess) break;
+            if ((e = cudaStreamWaitEvent(r.s2, r.ev_chunk[c], 0)) != cudaSuccess) break;
+            e = pnjl::launch_mixed_tasks(ac, grid_tasks, smem, r.s2);
         }
-        if (e == cudaSuccess) {
-            PNJL_CUDA_TRY(ctx, cudaEventRecord(ctx->ev_join, ctx->stream2));
-            PNJL_CUDA_TRY(ctx, cudaStreamWaitEvent(s, ctx->ev_join, 0));
-        }
-        launches = 2 * C;
+        if (e == cudaSuccess && (e = cudaEventRecord(r.ev_join, r.s2)) == cudaSuccess)
+            e = cudaStreamWaitEvent(s, r.ev_join, 0);
+        *launches = 2 * C;
     } else {
         e = pnjl::launch_mixed_points(a, grid, smem, s);
-        if (e == cudaSuccess && ctx->split_last) {
-            // the per-point kernel's own time and counters, then the task kernel
-            PNJL_CUDA_TRY(ctx, cudaEventRecord(ctx->ev_mid, s));
-            PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_ctrl_snap, ctx->d_ctrl, pnjl::kCtrlSlots * sizeof(long long),
-                                               cudaMemcpyDeviceToDevice, s));
+        if (e == cudaSuccess && two) {
+            if (r.ev_mid && r.ctrl_snap) {
+                // the per-point kernel's own time and counters, then the task kernel
+                if ((e = cudaEventRecord(r.ev_mid, s)) != cudaSuccess) return e;
+                if ((e = cudaMemcpyAsync(r.ctrl_snap, r.ctrl, pnjl::kCtrlSlots * sizeof(long long),
+                                         cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
+                    return e;
+                *split = true;
+            }
             e = pnjl::launch_mixed_tasks(a, grid_tasks, smem, s);
         }
     }
+    return e;
+}
+
+int pnjl_solve_batch_device(pnjl_ctx *ctx, int64_t n, const double *d_T, const double *d_mu_u, const double *d_mu_d,
+                            const double *d_mu_s, const double *d_xi, const pnjl_solve_opts *opts,
+                            pnjl_result_soa *d_out) {
+    if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
+    if (ctx->p_num == 0) return fail(ctx, PNJL_ERR_NO_NODES, "call pnjl_set_nodes first");
+    int rc = check_opts(ctx, opts);
+    if (rc) return rc;
+    if (n < 0 || !d_out || (n > 0 && (!d_T || !d_mu_u || !d_mu_d || !d_mu_s || !d_xi)))
+        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "null array");
+    if (n == 0) return PNJL_OK;
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = ctx->stream;
+    if (opts->n_seeds > 0 && opts->seed_table) {
+        PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_seed_tables, opts->seed_table, opts->n_seeds * 5 * sizeof(double),
+                                           cudaMemcpyHostToDevice, s));
+        if (opts->seed_table_hot)
+            PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_seed_tables + 80, opts->seed_table_hot,
+                                               opts->n_seeds * 5 * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    if (const int64_t cells = pnjl::verify_map_cells(opts)) {
+        if ((size_t)cells > ctx->vmap_cap) {
+            PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+            cudaFree(ctx->d_vmap);
+            ctx->d_vmap = nullptr;
+            ctx->vmap_cap = 0;
+            if (cudaMalloc(&ctx->d_vmap, (size_t)cells) != cudaSuccess)
+                return fail(ctx, PNJL_ERR_OUT_OF_MEMORY, "verification map allocation failed");
+            ctx->vmap_cap = (size_t)cells;
+        }
+        PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_vmap, opts->verify_map, (size_t)cells, cudaMemcpyHostToDevice, s));
+    }
+    if (const size_t bytes = solve_scratch_bytes(n, opts)) {
+        rc = ensure_scratch(ctx, bytes);
+        if (rc) return rc;
+    }
+    SolveRes r{ctx->d_ctrl, ctx->d_scratch, ctx->d_seed_tables, ctx->d_vmap, s, ctx->stream2, ctx->ev_chunk,
+               ctx->ev_join, ctx->ev_mid, ctx->d_ctrl_snap};
+    PNJL_CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, s));
+    int launches = 0;
+    bool split = false;
+    const cudaError_t e = solve_enqueue(ctx, kernel_nodes(ctx), n, d_T, d_mu_u, d_mu_d, d_mu_s, d_xi, opts, *d_out,
+                                        r, &launches, &split);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "solve kernel launch");
+    ctx->split_last = split;
     PNJL_CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, s));
     ctx->stats.kernel_launches += launches;
     ctx->stats.points = n;
@@ -1124,6 +1194,231 @@ int pnjl_set_tuning(pnjl_ctx *ctx, int32_t lanes_per_point, int32_t blocks_per_s
     if (blocks_per_sm < 0 || blocks_per_sm > 32) return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "blocks_per_sm out of range");
     ctx->group = lanes_per_point;
     ctx->blocks_per_sm = blocks_per_sm;
+    return PNJL_OK;
+}
+
+
+// ---------------------------------------------------------------------------------------
+// Plans: several batched solves -- each with its own quadrature order, inputs, outputs and
+// options -- captured once into one CUDA graph and replayed with one launch.
+
+struct PlanSeg {
+    int p_num = 0, t_num = 0;
+    double *d_nodes = nullptr;
+    float *d_nodes_f = nullptr;
+    int64_t n = 0;
+    const double *T = nullptr, *mu_u = nullptr, *mu_d = nullptr, *mu_s = nullptr, *xi = nullptr;
+    pnjl_solve_opts opts{};
+    double *d_seeds = nullptr;         // seed tables (cold | hot)
+    unsigned char *d_vmap = nullptr;
+    double *d_point_seeds = nullptr;   // learned segments: the network's seeds
+    bool learned = false;
+    pnjl_result_soa out{};
+    long long *ctrl = nullptr;
+    unsigned char *scratch = nullptr;
+    cudaStream_t s = nullptr, s2 = nullptr;
+    cudaEvent_t ev_chunk[pnjl::kMaxPipelineChunks] = {};
+    cudaEvent_t ev_join = nullptr, ev_done = nullptr;
+};
+
+struct pnjl_plan {
+    pnjl_ctx *ctx = nullptr;
+    std::vector<PlanSeg> segs;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t ev_fork = nullptr;
+    int launches = 0;
+};
+
+static void plan_free(pnjl_plan *pl) {
+    if (!pl) return;
+    if (pl->ctx) cudaSetDevice(pl->ctx->device);
+    if (pl->exec) cudaGraphExecDestroy(pl->exec);
+    if (pl->graph) cudaGraphDestroy(pl->graph);
+    if (pl->ev_fork) cudaEventDestroy(pl->ev_fork);
+    for (auto &g : pl->segs) {
+        cudaFree(g.d_nodes); cudaFree(g.d_nodes_f); cudaFree(g.d_seeds); cudaFree(g.d_vmap);
+        cudaFree(g.d_point_seeds); cudaFree(g.ctrl); cudaFree(g.scratch);
+        for (auto &ev : g.ev_chunk) if (ev) cudaEventDestroy(ev);
+        if (g.ev_join) cudaEventDestroy(g.ev_join);
+        if (g.ev_done) cudaEventDestroy(g.ev_done);
+        if (g.s) cudaStreamDestroy(g.s);
+        if (g.s2) cudaStreamDestroy(g.s2);
+    }
+    delete pl;
+}
+
+int pnjl_plan_create(pnjl_ctx *ctx, pnjl_plan **out) {
+    if (!ctx || !out) return PNJL_ERR_INVALID_ARGUMENT;
+    pnjl_plan *pl = new (std::nothrow) pnjl_plan();
+    if (!pl) return PNJL_ERR_OUT_OF_MEMORY;
+    pl->ctx = ctx;
+    *out = pl;
+    return PNJL_OK;
+}
+
+int pnjl_plan_add(pnjl_plan *pl, int32_t p_num, int32_t t_num, double p_max, int64_t n, const double *d_T,
+                  const double *d_mu_u, const double *d_mu_d, const double *d_mu_s, const double *d_xi,
+                  const pnjl_solve_opts *opts, int32_t learned, pnjl_result_soa *d_out) {
+    if (!pl || !pl->ctx) return PNJL_ERR_INVALID_ARGUMENT;
+    pnjl_ctx *ctx = pl->ctx;
+    if (pl->exec) return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "plan already finalised");
+    int rc = check_opts(ctx, opts);
+    if (rc) return rc;
+    if (p_num < 1 || p_num > pnjl::kMaxPNodes || t_num < 1 || t_num > pnjl::kMaxTNodes || !(p_max > 0.0))
+        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "node counts out of range (1..512 x 1..64, p_max > 0)");
+    if (n <= 0 || !d_out || !d_T || !d_mu_u || !d_mu_d || !d_mu_s || !d_xi)
+        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "segment needs n > 0 points and device arrays");
+    if (learned) {
+        rc = mlp_require(ctx, true);
+        if (rc) return rc;
+    }
+    cudaSetDevice(ctx->device);
+    PlanSeg g;
+    g.p_num = p_num;
+    g.t_num = t_num;
+    g.n = n;
+    g.T = d_T; g.mu_u = d_mu_u; g.mu_d = d_mu_d; g.mu_s = d_mu_s; g.xi = d_xi;
+    g.opts = *opts;
+    g.out = *d_out;
+    g.learned = learned != 0;
+    std::vector<double> h;
+    std::vector<float> hf;
+    node_tables_host(p_num, t_num, p_max, h, hf);
+    bool ok = cudaMalloc(&g.d_nodes, h.size() * sizeof(double)) == cudaSuccess &&
+              cudaMalloc(&g.d_nodes_f, hf.size() * sizeof(float)) == cudaSuccess &&
+              cudaMemcpy(g.d_nodes, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemcpy(g.d_nodes_f, hf.data(), hf.size() * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
+    // the seed tables and the verification map are copied now: the graph reads device copies
+    ok = ok && cudaMalloc(&g.d_seeds, 2 * 16 * 5 * sizeof(double)) == cudaSuccess &&
+         cudaMemset(g.d_seeds, 0, 2 * 16 * 5 * sizeof(double)) == cudaSuccess;
+    if (ok && opts->n_seeds > 0 && opts->seed_table) {
+        ok = cudaMemcpy(g.d_seeds, opts->seed_table, opts->n_seeds * 5 * sizeof(double), cudaMemcpyHostToDevice) ==
+             cudaSuccess;
+        if (ok && opts->seed_table_hot)
+            ok = cudaMemcpy(g.d_seeds + 80, opts->seed_table_hot, opts->n_seeds * 5 * sizeof(double),
+                            cudaMemcpyHostToDevice) == cudaSuccess;
+    }
+    if (ok && pnjl::verify_map_cells(opts)) {
+        const size_t cells = (size_t)pnjl::verify_map_cells(opts);
+        ok = cudaMalloc(&g.d_vmap, cells) == cudaSuccess &&
+             cudaMemcpy(g.d_vmap, opts->verify_map, cells, cudaMemcpyHostToDevice) == cudaSuccess;
+    }
+    if (ok && g.learned) {
+        ok = cudaMalloc(&g.d_point_seeds, (size_t)n * 5 * sizeof(double)) == cudaSuccess;
+        g.opts.seed_mode = PNJL_SEEDS_PER_POINT;
+        g.opts.point_seeds = g.d_point_seeds;
+    }
+    if (ok) {
+        const size_t bytes = solve_scratch_bytes(n, &g.opts);
+        ok = cudaMalloc(&g.ctrl, pnjl::kCtrlSlots * sizeof(long long)) == cudaSuccess &&
+             cudaMemset(g.ctrl, 0, pnjl::kCtrlSlots * sizeof(long long)) == cudaSuccess &&
+             (bytes == 0 || cudaMalloc(&g.scratch, bytes) == cudaSuccess);
+    }
+    ok = ok && cudaStreamCreateWithFlags(&g.s, cudaStreamNonBlocking) == cudaSuccess &&
+         cudaStreamCreateWithFlags(&g.s2, cudaStreamNonBlocking) == cudaSuccess &&
+         cudaEventCreateWithFlags(&g.ev_join, cudaEventDisableTiming) == cudaSuccess &&
+         cudaEventCreateWithFlags(&g.ev_done, cudaEventDisableTiming) == cudaSuccess;
+    for (int k = 0; ok && k < pnjl::kMaxPipelineChunks; ++k)
+        ok = cudaEventCreateWithFlags(&g.ev_chunk[k], cudaEventDisableTiming) == cudaSuccess;
+    // host pointers of the options are not read after this call
+    g.opts.seed_table = opts->n_seeds > 0 && opts->seed_table ? g.d_seeds : nullptr;
+    g.opts.seed_table_hot = opts->n_seeds > 0 && opts->seed_table_hot ? g.d_seeds + 80 : nullptr;
+    g.opts.verify_map = g.d_vmap;
+    if (!ok) {
+        pnjl_plan *tmp = new (std::nothrow) pnjl_plan();
+        if (tmp) {  // free this segment's resources through the plan destructor
+            tmp->ctx = ctx;
+            tmp->segs.push_back(g);
+            plan_free(tmp);
+        }
+        return fail(ctx, PNJL_ERR_OUT_OF_MEMORY, "plan segment allocation failed");
+    }
+    pl->segs.push_back(g);
+    return PNJL_OK;
+}
+
+int pnjl_plan_finalize(pnjl_plan *pl) {
+    if (!pl || !pl->ctx) return PNJL_ERR_INVALID_ARGUMENT;
+    pnjl_ctx *ctx = pl->ctx;
+    if (pl->exec) return PNJL_OK;
+    if (pl->segs.empty()) return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "plan has no segments");
+    cudaSetDevice(ctx->device);
+    PNJL_CUDA_TRY(ctx, cudaEventCreateWithFlags(&pl->ev_fork, cudaEventDisableTiming));
+    PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    // every segment runs on its own stream pair: the graph gets one branch per segment
+    cudaStream_t s = ctx->stream;
+    PNJL_CUDA_TRY(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaEventRecord(pl->ev_fork, s);
+    int launches = 0;
+    for (auto &g : pl->segs) {
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(g.s, pl->ev_fork, 0);
+        if (e == cudaSuccess && g.learned) {
+            e = pnjl::mlp_launch_infer(mlp_dev(ctx), ctx->mlp.sc, g.n, g.T, g.mu_u, g.xi, g.d_point_seeds,
+                                       ctx->sm_count, g.s);
+            ++launches;
+        }
+        if (e == cudaSuccess) {
+            SolveRes r{g.ctrl, g.scratch, g.d_seeds, g.d_vmap, g.s, g.s2, g.ev_chunk, g.ev_join, nullptr, nullptr};
+            int l = 0;
+            bool split = false;
+            e = solve_enqueue(ctx, kernel_nodes_of(g.d_nodes, g.d_nodes_f, g.p_num, g.t_num), g.n, g.T, g.mu_u,
+                              g.mu_d, g.mu_s, g.xi, &g.opts, g.out, r, &l, &split);
+            launches += l;
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(g.ev_done, g.s);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, g.ev_done, 0);
+    }
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(s, &graph);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return cuda_fail(ctx, e != cudaSuccess ? e : e2, "plan capture");
+    }
+    pl->graph = graph;
+    PNJL_CUDA_TRY(ctx, cudaGraphInstantiate(&pl->exec, graph, 0));
+    pl->launches = launches;
+    return PNJL_OK;
+}
+
+int pnjl_plan_launch(pnjl_plan *pl) {
+    if (!pl || !pl->ctx) return PNJL_ERR_INVALID_ARGUMENT;
+    pnjl_ctx *ctx = pl->ctx;
+    if (!pl->exec) return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "plan not finalised");
+    cudaSetDevice(ctx->device);
+    PNJL_CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+    PNJL_CUDA_TRY(ctx, cudaGraphLaunch(pl->exec, ctx->stream));
+    PNJL_CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+    ctx->split_last = false;
+    ctx->stats.kernel_launches += pl->launches;
+    return PNJL_OK;
+}
+
+int pnjl_plan_stats(pnjl_plan *pl, int32_t segment, pnjl_stats *out) {
+    if (!pl || !pl->ctx || !out) return PNJL_ERR_INVALID_ARGUMENT;
+    pnjl_ctx *ctx = pl->ctx;
+    if (segment < -1 || segment >= (int32_t)pl->segs.size()) return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "no such segment");
+    cudaSetDevice(ctx->device);
+    PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    pnjl_stats st{};
+    long long sum[pnjl::kCtrlSlots] = {};
+    for (int k = 0; k < (int)pl->segs.size(); ++k) {
+        if (segment >= 0 && k != segment) continue;
+        long long h[pnjl::kCtrlSlots];
+        PNJL_CUDA_TRY(ctx, cudaMemcpy(h, pl->segs[k].ctrl, sizeof h, cudaMemcpyDeviceToHost));
+        for (int j = 0; j < pnjl::kCtrlSlots; ++j) sum[j] += h[j];
+        st.points += pl->segs[k].n;
+    }
+    fill_counters(st, sum + 1);
+    st.kernel_launches = pl->launches;
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1) == cudaSuccess) st.last_kernel_ms = ms;
+    *out = st;
+    return PNJL_OK;
+}
+
+int pnjl_plan_destroy(pnjl_plan *pl) {
+    plan_free(pl);
     return PNJL_OK;
 }
 

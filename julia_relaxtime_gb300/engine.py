@@ -326,3 +326,65 @@ class GapEngine:
         self._check(rc, "pnjl_autotune")
         as_dict = lambda t: {k: getattr(t, k) for k, _ in api.pnjl_tuning._fields_}  # noqa: E731
         return as_dict(best), [as_dict(tried[i]) for i in range(min(nt.value, 64))]
+
+
+class SolvePlan:
+    """Several batched solves -- each with its own quadrature order, device inputs, outputs and
+    options -- captured into one CUDA graph and replayed with one launch (pnjl_plan_*).
+
+    Typical use: the same (T, mu, xi) grid at p = 64, 128 and 256 nodes (a quadrature
+    convergence study), or slices of a scan with different orders, in one launch."""
+
+    def __init__(self, engine: GapEngine):
+        self.engine = engine
+        self._lib = engine._lib
+        h = C.c_void_p()
+        engine._check(self._lib.pnjl_plan_create(engine._ctx, C.byref(h)), "pnjl_plan_create")
+        self._h = h
+        self.segments = 0
+
+    def add(self, p_num: int, t_num: int, n: int, d_T: int, d_mu_u: int, d_mu_d: int, d_mu_s: int, d_xi: int,
+            d_out: dict, *, seed_table=None, seed_table_hot=None, hot_T_MeV: float = 300.0,
+            opts: SolveOptions | None = None, learned: bool = False, p_max: float = 10.0, d_point_seeds: int = 0):
+        """Add a segment (device pointers as integers; d_out maps result fields to device pointers).
+        Host tables are copied now."""
+        opts = opts or SolveOptions()
+        st = None if seed_table is None else _f64(seed_table).reshape(-1, 5)
+        sth = None if seed_table_hot is None else _f64(seed_table_hot).reshape(-1, 5)
+        ps = None if learned else (d_point_seeds or None)
+        o = GapEngine._opts_struct(opts, st, sth, hot_T_MeV, ps is not None, ps)
+        soa = api.pnjl_result_soa()
+        for k, v in d_out.items():
+            ptr_t = dict(iterations=api.i32p, chosen_seed=api.i32p, status=api.i32p, converged=api.u8p).get(k, api.dp)
+            setattr(soa, k, C.cast(C.c_void_p(v), ptr_t))
+        cast = lambda p: C.cast(C.c_void_p(p), api.dp)  # noqa: E731
+        rc = self._lib.pnjl_plan_add(self._h, int(p_num), int(t_num), float(p_max), int(n), cast(d_T), cast(d_mu_u),
+                                     cast(d_mu_d), cast(d_mu_s), cast(d_xi), C.byref(o), int(bool(learned)),
+                                     C.byref(soa))
+        self.engine._check(rc, "pnjl_plan_add")
+        self.segments += 1
+        return self.segments - 1
+
+    def finalize(self):
+        self.engine._check(self._lib.pnjl_plan_finalize(self._h), "pnjl_plan_finalize")
+
+    def launch(self):
+        """One graph launch on the engine's stream (asynchronous)."""
+        self.engine._check(self._lib.pnjl_plan_launch(self._h), "pnjl_plan_launch")
+
+    def stats(self, segment: int = -1) -> dict:
+        st = api.pnjl_stats()
+        self.engine._check(self._lib.pnjl_plan_stats(self._h, int(segment), C.byref(st)), "pnjl_plan_stats")
+        return {k: getattr(st, k) for k, _ in api.pnjl_stats._fields_}
+
+    def close(self):
+        if self._h:
+            self._lib.pnjl_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001 -- interpreter shutdown
+            pass
+

@@ -367,3 +367,78 @@ def test_mixed_pipeline_chunks_and_autotune(engine_factory):
                     opts=SolveOptions(iterations=40, ftol=1e-10, precision="mixed"))
     np.testing.assert_array_equal(d_out["omega"].cpu().numpy(), ref["omega"])
     eng.set_tuning(32, 0, pipeline_chunks=0)
+
+
+def test_plan_mixed_orders_one_graph(engine_factory):
+    """Config-3 shape: the same T x mu grid at p = 64, 128 and 256 momentum nodes (plus an FP64
+    per-point segment and a learned-seed segment) captured into one CUDA graph and replayed:
+    every segment equals the same solve launched on its own, on every replay."""
+    import torch
+
+    from julia_relaxtime_gb300.engine import SolvePlan
+    from julia_relaxtime_gb300.learned_seed import LearnedSeed
+
+    eng = engine_factory(64, 8)
+    dev = torch.device("cuda", 0)
+    Tg, mg = np.meshgrid(np.linspace(50, 300, 12), np.linspace(0, 400, 12), indexing="ij")
+    T = Tg.ravel() / HBARC
+    mu = mg.ravel() / HBARC
+    n = T.size
+    xi = np.zeros(n)
+    d = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in (("T", T), ("mu", mu), ("xi", xi))}
+    table, hot = pnjl.multiseed_table(6)
+    seeds = np.tile(np.array(pnjl.HADRON_SEED_5), (n, 1))
+    d_seeds = torch.from_numpy(seeds.ravel().copy()).to(dev)
+    ls = LearnedSeed(eng, seed=5)
+    ls.default_scaling(np.tile(np.array(pnjl.HADRON_SEED_5), (4, 1)) + np.arange(4)[:, None] * 0.1)
+    mixed = SolveOptions(iterations=40, ftol=1e-10, precision="mixed")
+    fp64 = SolveOptions(iterations=40, ftol=1e-10, precision="fp64")
+    segs = [(64, mixed, 0, False), (128, mixed, 0, False), (256, mixed, 0, False),
+            (32, fp64, d_seeds.data_ptr(), False), (64, mixed, 0, True)]
+
+    def outputs():
+        return {"x": torch.empty(5 * n, dtype=torch.float64, device=dev),
+                "omega": torch.empty(n, dtype=torch.float64, device=dev),
+                "status": torch.empty(n, dtype=torch.int32, device=dev),
+                "converged": torch.empty(n, dtype=torch.uint8, device=dev)}
+
+    m = d["mu"].data_ptr()
+    plan = SolvePlan(eng)
+    outs = []
+    for p_num, o, ps, learned in segs:
+        out = outputs()
+        outs.append(out)
+        plan.add(p_num, 8, n, d["T"].data_ptr(), m, m, m, d["xi"].data_ptr(), {k: v.data_ptr() for k, v in out.items()},
+                 seed_table=table, seed_table_hot=hot, opts=o, learned=learned, d_point_seeds=ps)
+    torch.cuda.synchronize()
+    plan.finalize()
+    first = None
+    for rep in range(2):
+        for out in outs:
+            out["omega"].fill_(0.0)
+        plan.launch()
+        eng.synchronize()
+        got = [{k: v.cpu().numpy().copy() for k, v in out.items()} for out in outs]
+        if first is None:
+            first = got
+        else:
+            for a, b in zip(got, first):
+                for k in a:
+                    np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    st = plan.stats()
+    assert st["points"] == 5 * n and st["kernel_launches"] >= 5 and st["last_kernel_ms"] > 0
+    # each segment alone, through the context with its own node tables
+    for (p_num, o, ps, learned), g in zip(segs, first):
+        eng.set_nodes(p_num, 8)
+        ref = outputs()
+        eng.solve_device(n, d["T"].data_ptr(), m, m, m, d["xi"].data_ptr(), {k: v.data_ptr() for k, v in ref.items()},
+                         seed_table=table, seed_table_hot=hot, opts=o, learned=learned, d_point_seeds=ps)
+        eng.synchronize()
+        for k, v in ref.items():
+            np.testing.assert_array_equal(v.cpu().numpy(), g[k], err_msg=f"p{p_num} {k}")
+        assert g["converged"].mean() > 0.95
+    # higher orders move the solution by the quadrature error only
+    d64, d256 = first[0]["x"].reshape(n, 5), first[2]["x"].reshape(n, 5)
+    both = first[0]["converged"].astype(bool) & first[2]["converged"].astype(bool)
+    assert np.median(np.abs(d64[both] - d256[both])) < 1e-2
+    plan.close()
