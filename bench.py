@@ -194,6 +194,88 @@ class Arm:
                               seed_table_hot=self.hot, opts=self.opts, learned=self.learned)
 
 
+def run_orders(args):
+    """Mixed quadrature orders in one graph launch: the 32 x 32 (T 50-300 MeV, mu 0-400 MeV, xi = 0)
+    grid solved with MultiSeed (6 candidates, min-Omega) in mixed precision at p = 64, 128 and 256
+    momentum nodes (t = 8), the three segments captured into one CUDA graph (pnjl_plan_*).  Per-point
+    errors against the FP64 solve of the same kernel at the same order."""
+    import torch
+
+    from julia_relaxtime_gb300.engine import GapEngine, SolveOptions, SolvePlan
+    from julia_relaxtime_gb300.pnjl import multiseed_table
+
+    grid = workload_grid("iso_scan_32x32")
+    T, mu, xi = grid["T"], grid["mu"], grid["xi"]
+    n = T.size
+    orders = (64, 128, 256)
+    eng = GapEngine(p_num=64, t_num=8)
+    dev = torch.device("cuda", 0)
+    d = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in (("T", T), ("mu", mu), ("xi", xi))}
+    table, hot = multiseed_table(6)
+    mixed = SolveOptions(iterations=40, ftol=1e-10, precision="mixed")
+    f64 = lambda *sh: torch.empty(*sh, dtype=torch.float64, device=dev)  # noqa: E731
+    outs = [{"x": f64(5 * n), "omega": f64(n), "residual_norm": f64(n),
+             "converged": torch.empty(n, dtype=torch.uint8, device=dev)} for _ in orders]
+    m = d["mu"].data_ptr()
+    plan = SolvePlan(eng)
+    for p_num, out in zip(orders, outs):
+        plan.add(p_num, 8, n, d["T"].data_ptr(), m, m, m, d["xi"].data_ptr(), {k: v.data_ptr() for k, v in out.items()},
+                 seed_table=table, seed_table_hot=hot, opts=mixed)
+    torch.cuda.synchronize()
+    plan.finalize()
+    stream = torch.cuda.ExternalStream(eng.stream(), device=dev)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    for _ in range(args.warmup):
+        plan.launch()
+    eng.synchronize()
+    ms, solved = [], 0
+    sampler = ClockSampler(0)
+    sampler.start()
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 0xFF)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        plan.launch()
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+        for out in outs:
+            solved += int(((out["converged"] == 1) & (out["residual_norm"] <= 1e-10)).sum().item())
+    clocks = sampler.stop()
+    st = plan.stats()
+    # errors against the FP64 solve of the same kernel at each order
+    errs = {}
+    for p_num, out in zip(orders, outs):
+        eng.set_nodes(p_num, 8)
+        ref = eng.solve(T, mu, xi, seed_table=table, seed_table_hot=hot,
+                        opts=SolveOptions(iterations=40, ftol=1e-10, precision="fp64"))
+        x = out["x"].cpu().numpy().reshape(n, 5)
+        om = out["omega"].cpu().numpy()
+        conv = out["converged"].cpu().numpy().astype(bool) & ref["converged"]
+        same = conv & (np.abs(om - ref["omega"]) <= 1e-10 * np.maximum(np.abs(ref["omega"]), 1.0))
+        errs[f"p{p_num}"] = {
+            "points": int(conv.sum()), "phase_misassignments": int(np.sum(conv & ~same)),
+            "max_abs_dphi": float(np.abs(x[same, :3] - ref["x"][same, :3]).max()),
+            "max_rel_dphi": float((np.abs(x[same, :3] - ref["x"][same, :3]) / np.abs(ref["x"][same, :3])).max()),
+            "max_abs_dPhi": float(np.abs(x[same, 3:] - ref["x"][same, 3:]).max()),
+            "max_rel_domega": float((np.abs(om[same] - ref["omega"][same]) / np.abs(ref["omega"][same])).max())}
+    total = sum(ms)
+    line = {"metric": METRIC, "value": solved / (total * 1e-3), "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": "iso_orders_32x32_p64_128_256", "grid": grid["desc"].replace("p64 x t8, ", ""),
+                       "segments": "p = 64, 128, 256 x t = 8, one CUDA graph launch per step", "points_per_step":
+                       len(orders) * n, "ftol": 1e-10, "max_iter": 40, "precision": "mixed",
+                       "l2": "256 MiB device buffer written before every timed step"},
+            "gpu_launches": st["kernel_launches"] * args.steps, "clocks": clocks,
+            "errors_vs_fp64": errs, "e2e": None}
+    print(json.dumps(line))
+    plan.close()
+    eng.close()
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__)
     ap.add_argument("--gpus", type=int, default=1)
@@ -201,8 +283,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=("gpu", "reference"))
     ap.add_argument("--workload", default="aniso_scan_256x256x9")
-    ap.add_argument("--mode", default="surrogate", choices=("surrogate", "multiseed"),
-                    help="surrogate: learned seed + mixed precision (headline); multiseed: the MultiSeed table")
+    ap.add_argument("--mode", default="surrogate", choices=("surrogate", "multiseed", "orders"),
+                    help="surrogate: learned seed + mixed precision (headline); multiseed: the MultiSeed table; "
+                         "orders: the 32 x 32 isotropic grid at p = 64, 128, 256 in one CUDA graph (mixed "
+                         "precision, errors against the FP64 solve of the same kernel)")
     ap.add_argument("--precision", default=None, choices=("fp64", "mixed"),
                     help="precision of the timed arm (default: mixed for surrogate, fp64 for multiseed)")
     ap.add_argument("--chunks", type=int, default=32, help="the grid is solved in this many strided slices")
@@ -240,6 +324,10 @@ def main():
         return
 
     import torch
+
+    if args.mode == "orders":
+        run_orders(args)
+        return
 
     dist = None
     if world > 1:
