@@ -1,12 +1,12 @@
 """LearnedSeed: an MLP initial guess for the gap equations, trained on the GPU solver's own
-solutions (the north-star "learned seed"; the reference's seed interface is
+solutions (a learned seed; the reference's seed interface is
 src/pnjl/solver/SeedStrategies.jl:118).
 
 The network (3 -> 128 -> 128 -> 128 -> 5, SiLU, BF16 weights, FP32 accumulation) lives in
 the libpnjl_cuda context and is trained and evaluated by its kernels.  As a SeedStrategy it
 returns one seed per point; in batches it feeds the per-point-seed solve, whose fallback is
 the plain MultiSeed solve (the reference's auto_multiseed_fallback) -- so the learned seed can
-only change how fast a point is solved, and the multi-seed result remains the judge.
+only change how fast a point is solved, and the multi-seed result remains the arbiter.
 """
 from __future__ import annotations
 
@@ -29,7 +29,7 @@ def param_count() -> int:
 
 @dataclass
 class TrainConfig:
-    """Config 4 of the scan: a 64 x 64 x 5 solver-labelled (T, mu, xi) grid."""
+    """The training set: a 64 x 64 x 5 solver-labelled (T 50-300 MeV, mu 0-400 MeV, xi -0.5..0.5) grid."""
     T_MeV: tuple = (50.0, 300.0, 64)
     mu_MeV: tuple = (0.0, 400.0, 64)
     xi: tuple = (-0.5, 0.5, 5)

@@ -2,7 +2,7 @@
 
 Tolerances: FP64 kernel vs the jet-AD oracle -- Omega 1e-13 relative, gradient and Hessian
 1e-11 relative (different but exact derivative formulas, rounding only); solved states --
-|dphi|/|phi| <= 1e-9 and |dPhi| <= 1e-10 (the benchmark spec's bound), Omega 1e-12 relative.
+|dphi|/|phi| <= 1e-9 and |dPhi| <= 1e-10 (the required bound), Omega 1e-12 relative.
 """
 import os
 
@@ -121,7 +121,7 @@ def assert_solution_parity(res, i, ref, msg=""):
 
 
 def test_multiseed_solve_matches_oracle(engine_factory, P):
-    """Config-1 shape (T x mu grid, xi = 0, p64/t8, MultiSeed) on a coarse 6 x 6 sub-grid."""
+    """The isotropic T x mu scan shape (xi = 0, p64/t8, MultiSeed) on a coarse 6 x 6 sub-grid."""
     eng = engine_factory(64, 8)
     nd = orc.Nodes(64, 8)
     Tg, mg = np.meshgrid(np.linspace(50, 300, 6), np.linspace(0, 400, 6), indexing="ij")
@@ -140,7 +140,7 @@ def test_multiseed_solve_matches_oracle(engine_factory, P):
 
 
 def test_anisotropic_asymmetric_solve_matches_oracle(engine_factory, P):
-    """Config-2/5 shapes: xi != 0, 4 seeds, flavour-asymmetric mu_s = mu/2, p32/t8."""
+    """Anisotropic and flavour-asymmetric shapes: xi != 0, 4 seeds, mu_s = mu/2, p32/t8."""
     eng = engine_factory(32, 8)
     nd = orc.Nodes(32, 8)
     rng = np.random.default_rng(5)
@@ -248,7 +248,7 @@ def test_solve_api_mirrors_reference(engine_factory):
 @pytest.mark.parametrize("p_num,t_num,asym", [(64, 8, False), (32, 8, True)])
 def test_mixed_precision_matches_fp64_oracle(engine_factory, P, p_num, t_num, asym):
     """PNJL_PREC_MIXED: FP32 Kahan-compensated Newton passes, FP64 refinement and certification.
-    The certified roots and the selected phase must match the FP64 oracle (spec bound
+    The certified roots and the selected phase must match the FP64 oracle (required bound
     |dphi|/|phi| <= 1e-9, |dPhi| <= 1e-10; Omega 1e-12 relative); iteration counts differ by
     construction and are not compared."""
     eng = engine_factory(p_num, t_num)
@@ -370,7 +370,7 @@ def test_mixed_pipeline_chunks_and_autotune(engine_factory):
 
 
 def test_plan_mixed_orders_one_graph(engine_factory):
-    """Config-3 shape: the same T x mu grid at p = 64, 128 and 256 momentum nodes (plus an FP64
+    """Mixed quadrature orders: the same T x mu grid at p = 64, 128 and 256 momentum nodes (plus an FP64
     per-point segment and a learned-seed segment) captured into one CUDA graph and replayed:
     every segment equals the same solve launched on its own, on every replay."""
     import torch
