@@ -82,7 +82,8 @@ def pass_flops(st: dict):
     f64 = (st["node_evals_fp64_newton"] * FLOP_NEWTON + st["node_evals_fp64_thermo"] * FLOP_THERMO +
            st["node_evals_fp64_grad"] * FLOP_GRAD + st["node_evals_fp64_grad_thermo"] * FLOP_GRAD_THERMO)
     f32 = st["node_evals_fp32"] * FLOP_NEWTON32 + st["node_evals_fp32_thermo"] * FLOP_THERMO32
-    return f64, f32, st["node_evals_ff"] * FLOP_FF + st["node_evals_ff_thermo"] * FLOP_FF_THERMO
+    return f64, f32, (st["node_evals_ff"] * FLOP_FF + st["node_evals_ff_thermo"] * FLOP_FF_THERMO +
+                      st["node_evals_ff_grad_thermo"] * FLOP_GRAD_THERMO)
 
 
 def workload_grid(name: str):
@@ -415,7 +416,7 @@ def main():
             st = eng.stats()
             rec["kernel_ms"].append(st["last_kernel_ms"])
             rec["evals"] += st["node_evals_fp64"] + st["node_evals_fp32"] + st["node_evals_fp32_thermo"] + \
-                st["node_evals_ff"] + st["node_evals_ff_thermo"]
+                st["node_evals_ff"] + st["node_evals_ff_thermo"] + st["node_evals_ff_grad_thermo"]
             f64_, f32_, fff_ = pass_flops(st)
             rec["flops64"] += f64_
             rec["flops32"] += f32_
@@ -427,10 +428,10 @@ def main():
             for j, v in enumerate(pass_flops(s0)):
                 rec["k0_flops"][j] += v
             rec["k0_evals"] += s0["node_evals_fp64"] + s0["node_evals_fp32"] + s0["node_evals_fp32_thermo"] + \
-                s0["node_evals_ff"] + s0["node_evals_ff_thermo"]
+                s0["node_evals_ff"] + s0["node_evals_ff_thermo"] + s0["node_evals_ff_grad_thermo"]
             for kk in ("node_evals_fp64_newton", "node_evals_fp64_thermo", "node_evals_fp64_grad",
                        "node_evals_fp64_grad_thermo", "node_evals_fp32", "node_evals_fp32_thermo", "node_evals_ff",
-                       "node_evals_ff_thermo",
+                       "node_evals_ff_thermo", "node_evals_ff_grad_thermo",
                        "seeds_run", "trust_region_runs", "multiseed_fallbacks", "fp64_rescues", "pruned_candidates"):
                 rec["kinds"][kk] = rec["kinds"].get(kk, 0) + st[kk]
             conv = d_out["converged"][:n].cpu().numpy().astype(bool)
@@ -465,10 +466,10 @@ def main():
         tuning = {"chosen": best, "candidates": len(tried)}
     main_rec = run_arm(arm, args.steps, args.warmup, True)
 
-    # the dominant kernel's own launches, for the roofline: the same slices with the chunk
-    # pipeline off, so that the per-point kernel runs alone between its CUDA events
+    # the dominant kernel's own launches, for the roofline: the fused kernel (one launch per
+    # step) alone between its CUDA events -- the timed run itself when the tuner chose it
     roof_rec = main_rec
-    if args.mode == "surrogate" and precision == "mixed":
+    if args.mode == "surrogate" and precision == "mixed" and eng.tuning()["pipeline_chunks"] not in (0, 1):
         tu = eng.tuning()
         eng.set_tuning(32, tu["blocks_per_sm"], pipeline_chunks=1)
         roof_rec = run_arm(arm, args.steps, 0, False)
@@ -535,7 +536,7 @@ def main():
         kname, k_ms, k_flops, k_evals = "solve_kernel<32>", main_rec["kernel_ms"], \
             [main_rec["flops64"], main_rec["flops32"], main_rec["flops_ff"]], main_rec["evals"]
     elif args.mode == "surrogate":
-        kname, k_ms, k_flops, k_evals = "mixed_points_kernel<32>", roof_rec["k0_ms"], roof_rec["k0_flops"], \
+        kname, k_ms, k_flops, k_evals = "mixed_fused_kernel<32>", roof_rec["k0_ms"], roof_rec["k0_flops"], \
             roof_rec["k0_evals"]
     else:
         kname, k_ms, k_flops, k_evals = "mixed_tasks_kernel<32>", main_rec["kernel_ms"], \
@@ -551,7 +552,8 @@ def main():
             "flop_per_node_flavour": {"newton_pass": FLOP_NEWTON, "thermo_pass": FLOP_THERMO,
                                       "residual_pass": FLOP_GRAD, "residual_thermo_pass": FLOP_GRAD_THERMO,
                                       "newton_pass_fp32": FLOP_NEWTON32, "omega_pass_fp32": FLOP_THERMO32,
-                                      "residual_pass_float_float": FLOP_FF, "thermo_pass_float_float": FLOP_FF_THERMO},
+                                      "residual_pass_float_float": FLOP_FF, "thermo_pass_float_float": FLOP_FF_THERMO,
+                                      "residual_thermo_pass_float_float": FLOP_GRAD_THERMO},
             "node_flavour_evals_per_launch": k_evals / K, "kernel_ms": avg_k_s * 1e3,
             "kernel_share_of_step": avg_k_s * 1e3 / step_kernels_ms if step_kernels_ms > 0 else None,
             "traffic": TRAFFIC.get(kname, {}).get("bytes_per_launch") if args.workload == "aniso_scan_256x256x9"

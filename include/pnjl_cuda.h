@@ -157,6 +157,11 @@ typedef struct pnjl_stats {
     int64_t node_evals_ff;    /* mixed mode: float-float residual passes (FP32 pipe)    */
     int64_t node_evals_ff_thermo; /* mixed mode: float-float Omega / thermo passes at
                                  certified states (FP32 pipe)                           */
+    int64_t device_wait_timeouts; /* mixed mode: tasks that gave up waiting (bounded) on a
+                                 listed point still being written; always 0 in practice.
+                                 pnjl_solve_batch returns PNJL_ERR_CUDA when it is not. */
+    int64_t node_evals_ff_grad_thermo; /* mixed mode: float-float passes giving both the
+                                 residual and the outputs (after a correction step)     */
 } pnjl_stats;
 
 /* Default parameter set: config/pnjl/default.toml:1-21 through Constants_PNJL.jl:82-103. */
@@ -213,8 +218,8 @@ void *pnjl_stream(pnjl_ctx *ctx);
 int pnjl_synchronize(pnjl_ctx *ctx);
 int pnjl_get_stats(const pnjl_ctx *ctx, pnjl_stats *out);
 /* The same for one kernel of the last solve: kernel 0 = the first kernel (the per-point kernel
- * of a mixed per-point solve, else the only one), kernel 1 = the task kernel that follows it
- * in a mixed per-point solve (all counters zero when there was none).  last_kernel_ms is that
+ * of a mixed per-point solve run as two kernels, else the only one), kernel 1 = the task
+ * kernel that follows it (all counters zero when there was none).  last_kernel_ms is that
  * kernel's device time (CUDA events around it on the context stream). */
 int pnjl_get_kernel_stats(const pnjl_ctx *ctx, int32_t kernel, pnjl_stats *out);
 
@@ -224,10 +229,13 @@ int pnjl_device_sm_count(const pnjl_ctx *ctx);
 /* Launch shape of the solve kernel: lanes per task (32: one warp) and resident blocks
  * per SM (0 = occupancy maximum).  Chosen by the autotuner; results do not depend on it. */
 int pnjl_set_tuning(pnjl_ctx *ctx, int32_t lanes_per_point, int32_t blocks_per_sm);
-/* Mixed-precision per-point solves (learned / continuation seeds) are cut into `chunks` pieces
- * over two streams: the per-point kernel of piece c+1 overlaps the task kernel (verification,
- * MultiSeed fallback) of piece c.  0 = automatic, 1 = no pipeline, at most 16.  Results do
- * not depend on it.  pnjl_get_tuning reads the current launch shape. */
+/* How a mixed-precision per-point solve (learned / continuation seeds) with a MultiSeed table
+ * is launched.  1 (and 0, automatic): one fused kernel, in which the verification and
+ * MultiSeed-fallback tasks of listed points run beside the remaining points.  -1: the per-point
+ * kernel, then the task kernel (pnjl_get_kernel_stats splits their counters and times).
+ * 2..16: the points are cut into that many pieces over two streams, and the task kernel of
+ * piece c overlaps the per-point kernel of piece c+1.  Results do not depend on it.
+ * pnjl_get_tuning reads the current launch shape. */
 int pnjl_set_pipeline(pnjl_ctx *ctx, int32_t chunks);
 int pnjl_get_tuning(const pnjl_ctx *ctx, int32_t *lanes_per_point, int32_t *blocks_per_sm, int32_t *chunks);
 
@@ -242,7 +250,7 @@ typedef struct pnjl_tuning {
 /* Autotuner (no counterpart in the reference): solves the given representative batch (device
  * pointers, as pnjl_solve_batch_device, or pnjl_solve_batch_learned_device when `learned`) with
  * every candidate launch shape -- resident blocks per SM from the occupancy maximum down to 1,
- * and for mixed per-point solves the chunk pipeline 1, 2, 3, 4, 6, 8 -- `reps` times each, keeps
+ * and for mixed per-point solves the launch forms 1, -1, 2, 4 of pnjl_set_pipeline -- `reps` times each, keeps
  * the fastest (minimum over repetitions) and sets it on the context.  `tried` (optional) receives
  * up to max_tried candidates with their times; d_out receives the last solve's results. */
 int pnjl_autotune(pnjl_ctx *ctx, int64_t n, const double *d_T, const double *d_mu_u, const double *d_mu_d,

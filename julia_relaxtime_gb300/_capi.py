@@ -92,7 +92,8 @@ class pnjl_stats(C.Structure):
         ("node_evals_fp32", C.c_int64), ("seeds_run", C.c_int64), ("trust_region_runs", C.c_int64),
         ("multiseed_fallbacks", C.c_int64), ("kernel_launches", C.c_int64), ("last_kernel_ms", C.c_double),
         ("fp64_rescues", C.c_int64), ("node_evals_fp32_thermo", C.c_int64), ("pruned_candidates", C.c_int64),
-        ("node_evals_ff", C.c_int64), ("node_evals_ff_thermo", C.c_int64),
+        ("node_evals_ff", C.c_int64), ("node_evals_ff_thermo", C.c_int64), ("device_wait_timeouts", C.c_int64),
+        ("node_evals_ff_grad_thermo", C.c_int64),
     ]
 
 

@@ -474,10 +474,8 @@ int pnjl_thermo_batch(pnjl_ctx *ctx, int64_t n, const double *x, const double *T
 // chunk per ~2 points for every resident warp (sm_count x 16 warps x 2), at most 4.
 static int pipeline_chunks(const pnjl_ctx *ctx, int64_t n) {
     int C = ctx->pipeline_chunks;
-    if (C <= 0) {
-        const int64_t per = (int64_t)ctx->sm_count * 16 * 2;
-        C = (int)std::min<int64_t>(4, std::max<int64_t>(1, n / std::max<int64_t>(per, 1)));
-    }
+    if (C < 0) return -1;  // the two kernels one after the other
+    if (C == 0) return 1;  // automatic: the fused kernel
     C = std::min<int>(C, pnjl::kMaxPipelineChunks);
     return (int)std::max<int64_t>(1, std::min<int64_t>(C, n / 64 > 0 ? n / 64 : 1));
 }
@@ -516,6 +514,7 @@ static pnjl::SolveArgs chunk_args(const pnjl::SolveArgs &a, int64_t lo, int64_t 
     c.queue = ctrl3;
     c.list_count = ctrl3 + 1;
     c.queue2 = ctrl3 + 2;
+    c.points_done = nullptr;
     return c;
 }
 
@@ -542,8 +541,9 @@ static size_t solve_scratch_bytes(int64_t n, const pnjl_solve_opts *o) {
     if (o->seed_mode == PNJL_SEEDS_TABLE && !mixed)
         return al256(nn * sizeof(int)) + nn * o->n_seeds * sizeof(pnjl::CandRec);
     if (mixed && S > 0)
-        return al256(nn * sizeof(int)) + al256(nn * S * sizeof(int)) + al256(nn * (S + 1) * sizeof(pnjl::CandRec)) +
-               al256(nn * S * 5 * sizeof(double)) + al256(nn * sizeof(long long)) + al256(nn * sizeof(int));
+        return al256(nn * sizeof(int)) + al256(nn * S * sizeof(int)) + al256(nn * sizeof(int)) +
+               al256(nn * (S + 1) * sizeof(pnjl::CandRec)) + al256(nn * S * 5 * sizeof(double)) +
+               al256(nn * sizeof(long long));
     return 0;
 }
 
@@ -569,17 +569,17 @@ static cudaError_t solve_enqueue(const pnjl_ctx *ctx, const pnjl::KernelNodes &n
         // slots: every point (table mode) or the points the per-point kernel defers
         const size_t nn = (size_t)n;
         const size_t b_done = al256(nn * sizeof(int)), b_flag = al256(nn * S * sizeof(int));
+        const size_t b_mode = al256(nn * sizeof(int));
         const size_t b_cand = al256(nn * (S + 1) * sizeof(pnjl::CandRec)), b_roots = al256(nn * S * 5 * sizeof(double));
-        const size_t b_list = al256(nn * sizeof(long long));
         unsigned char *q = r.scratch;
         a.done = (int *)q;
         a.root_flag = (int *)(q + b_done);
-        a.cand = (pnjl::CandRec *)(q + b_done + b_flag);
-        a.roots = (double *)(q + b_done + b_flag + b_cand);
-        a.list = (long long *)(q + b_done + b_flag + b_cand + b_roots);
-        a.list_mode = (int *)(q + b_done + b_flag + b_cand + b_roots + b_list);
-        // done and root_flag are adjacent: one memset clears both
-        if ((e = cudaMemsetAsync(q, 0, b_done + b_flag, s)) != cudaSuccess) return e;
+        a.list_mode = (int *)(q + b_done + b_flag);
+        a.cand = (pnjl::CandRec *)(q + b_done + b_flag + b_mode);
+        a.roots = (double *)(q + b_done + b_flag + b_mode + b_cand);
+        a.list = (long long *)(q + b_done + b_flag + b_mode + b_cand + b_roots);
+        // done, root_flag and list_mode are adjacent: one memset clears them
+        if ((e = cudaMemsetAsync(q, 0, b_done + b_flag + b_mode, s)) != cudaSuccess) return e;
     }
     if ((e = cudaMemsetAsync(r.ctrl, 0, pnjl::kCtrlSlots * sizeof(long long), s)) != cudaSuccess) return e;
     a.P = ctx->dp;
@@ -600,21 +600,25 @@ static cudaError_t solve_enqueue(const pnjl_ctx *ctx, const pnjl::KernelNodes &n
     a.stats = r.ctrl + 1;
     a.list_count = r.ctrl + 1 + pnjl::kStatCount;
     a.queue2 = r.ctrl + 2 + pnjl::kStatCount;
+    a.points_done = r.ctrl + 3 + pnjl::kStatCount;
     const int group = ctx->group;
-    int grid = 0, grid_tasks = 0;
+    int grid = 0, grid_tasks = 0, grid_fused = 0;
     *launches = 1;
     if (mixed) {
         const int64_t wpb = pnjl::kSolveThreads / 32;
-        auto occ_of = [&](bool tasks) {
-            int occ = pnjl::solve_mixed_occupancy(tasks, smem);
+        auto occ_of = [&](int kernel) {
+            int occ = pnjl::solve_mixed_occupancy(kernel, smem);
             if (occ < 1) occ = 1;
             if (ctx->blocks_per_sm > 0 && ctx->blocks_per_sm < occ) occ = ctx->blocks_per_sm;
             return (int64_t)occ;
         };
         const bool table = opts->seed_mode == PNJL_SEEDS_TABLE;
-        grid = (int)std::min<int64_t>((int64_t)ctx->sm_count * occ_of(false), (n + wpb - 1) / wpb);
-        const int64_t task_need = table ? (n * S + wpb - 1) / wpb : (int64_t)ctx->sm_count * occ_of(true);
-        grid_tasks = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->sm_count * occ_of(true), task_need));
+        grid = (int)std::min<int64_t>((int64_t)ctx->sm_count * occ_of(pnjl::kMixedPoints), (n + wpb - 1) / wpb);
+        const int64_t task_need = table ? (n * S + wpb - 1) / wpb : (int64_t)ctx->sm_count * occ_of(pnjl::kMixedTasks);
+        grid_tasks = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->sm_count * occ_of(pnjl::kMixedTasks),
+                                                                 task_need));
+        grid_fused = (int)std::max<int64_t>(
+            1, std::min<int64_t>((int64_t)ctx->sm_count * occ_of(pnjl::kMixedFused), (n * (S + 1) + wpb - 1) / wpb));
         *launches = table ? 1 : (S > 0 ? 2 : 1);
     } else {
         const int64_t n_tasks = opts->seed_mode == PNJL_SEEDS_TABLE ? n * (int64_t)opts->n_seeds : n;
@@ -626,6 +630,11 @@ static cudaError_t solve_enqueue(const pnjl_ctx *ctx, const pnjl::KernelNodes &n
         e = pnjl::launch_solve(a, group, grid, smem, s);
     } else if (opts->seed_mode == PNJL_SEEDS_TABLE) {
         e = pnjl::launch_mixed_tasks(a, grid_tasks, smem, s);
+    } else if (two && pipeline_chunks(ctx, n) == 1) {
+        // one launch: the per-point seeds and the tasks they defer (verification, MultiSeed
+        // fallback) share the persistent grid
+        e = pnjl::launch_mixed_fused(a, grid_fused, smem, s);
+        *launches = 1;
     } else if (two && pipeline_chunks(ctx, n) > 1) {
         // chunk pipeline: the per-point kernel of chunk c+1 (stream s) runs while the task
         // kernel of chunk c (stream s2) works through the points chunk c deferred; each fills
@@ -1023,7 +1032,10 @@ static int solve_batch_host(pnjl_ctx *ctx, int64_t n, const double *T, const dou
     PNJL_D2H(converged, nn, 1)
 #undef PNJL_D2H
     PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(s));
-    return pnjl_get_stats(ctx, &ctx->stats) == PNJL_OK ? PNJL_OK : PNJL_ERR_CUDA;
+    if (pnjl_get_stats(ctx, &ctx->stats) != PNJL_OK) return PNJL_ERR_CUDA;
+    if (ctx->stats.device_wait_timeouts)
+        return fail(ctx, PNJL_ERR_CUDA, "a solve kernel gave up waiting on a listed point (results incomplete)");
+    return PNJL_OK;
 }
 
 int pnjl_solve_batch(pnjl_ctx *ctx, int64_t n, const double *T, const double *mu_u, const double *mu_d,
@@ -1063,6 +1075,8 @@ static void fill_counters(pnjl_stats &st, const long long *c) {
     st.pruned_candidates = c[pnjl::kStatPruned];
     st.node_evals_ff = c[pnjl::kStatEvalsFF];
     st.node_evals_ff_thermo = c[pnjl::kStatEvalsFFThermo];
+    st.device_wait_timeouts = c[pnjl::kStatWaitTimeouts];
+    st.node_evals_ff_grad_thermo = c[pnjl::kStatEvalsFFGradThermo];
 }
 
 int pnjl_get_stats(const pnjl_ctx *cctx, pnjl_stats *out) {
@@ -1125,8 +1139,8 @@ int pnjl_probe_peak(pnjl_ctx *ctx, int32_t kind, double *ops_per_s) {
 
 int pnjl_set_pipeline(pnjl_ctx *ctx, int32_t chunks) {
     if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
-    if (chunks < 0 || chunks > pnjl::kMaxPipelineChunks)
-        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "pipeline chunks out of range (0..16)");
+    if (chunks < -1 || chunks > pnjl::kMaxPipelineChunks)
+        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "pipeline chunks out of range (-1..16)");
     ctx->pipeline_chunks = chunks;
     return PNJL_OK;
 }
@@ -1148,10 +1162,11 @@ int pnjl_autotune(pnjl_ctx *ctx, int64_t n, const double *d_T, const double *d_m
     if (rc) return rc;
     const bool mixed = opts->precision == PNJL_PREC_MIXED;
     const bool per_point = learned || opts->seed_mode == PNJL_SEEDS_PER_POINT;
-    int occ_max = mixed ? std::max(pnjl::solve_mixed_occupancy(false, pnjl::node_smem_bytes(ctx->p_num, ctx->t_num)), 1)
+    int occ_max = mixed ? std::max(pnjl::solve_mixed_occupancy(pnjl::kMixedFused,
+                                                               pnjl::node_smem_bytes(ctx->p_num, ctx->t_num)), 1)
                         : std::max(pnjl::solve_kernel_occupancy(32, pnjl::node_smem_bytes(ctx->p_num, ctx->t_num)), 1);
-    const int chunk_list[] = {1, 2, 3, 4, 6, 8};
-    const int n_chunk = (mixed && per_point) ? 6 : 1;
+    const int chunk_list[] = {1, -1, 2, 4};
+    const int n_chunk = (mixed && per_point) ? 4 : 1;
     const int old_bps = ctx->blocks_per_sm, old_c = ctx->pipeline_chunks;
     pnjl_tuning b{};
     b.ms = 1e300;

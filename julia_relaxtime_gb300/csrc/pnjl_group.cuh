@@ -404,6 +404,32 @@ struct Group {
         return ok;
     }
 
+    // Residual at c.x and, from the same float-float pass, Omega, entropy, rho_f and the
+    // number densities at c.x (the outputs should c.x be certified: the quantities the two
+    // need per node -- E, the exponential, the Polyakov factors, n+ and n- -- are computed
+    // once).  Bit 0 of the result: F finite; bit 1: the thermo fields of c were set (finite).
+    __device__ __noinline__ int eval_grad_thermo_ff(const PointIn &pt, const SolveOpts &o, Candidate &c, double *F) {
+        if (!nv.p2l) return 0;
+        double M[3];
+        masses(P, c.x, M);
+        PassSums S;
+        node_pass_ff<G, true, true>(nv, pt, c.x, M, gl, mask, S, cnt.v[kStatEvalsFFGradThermo]);
+        Eval ev;
+        double V, V1[3], V2[3];
+        vacuum_terms<G>(P, M, gl, mask, leader(), V, V1, V2);
+        assemble<true, false, true>(P, pt, c.x, M, S, V, V1, V2, ev);
+        cnt.v[kStatPasses32] += 1;
+        for (int i = 0; i < 5; ++i) F[i] = ev.F[i];
+        int r = all_finite5(F) ? 1 : 0;
+        bool ok = ev.omega == ev.omega && fabs(ev.omega) < 1e300 && ev.dOdT == ev.dOdT;
+        for (int f = 0; f < 3; ++f) ok = ok && ev.rho[f] == ev.rho[f] && ev.nq[f] == ev.nq[f] && ev.naq[f] == ev.naq[f];
+        if (ok) {
+            postprocess(P, pt, o, ev, c);
+            r |= 2;
+        }
+        return r;
+    }
+
     // Omega, entropy, rho_f and number densities at c.x from the float-float pass (the
     // outputs of a certified candidate, ~1e-13 relative); false when not available or not
     // finite (the caller then uses the FP64 thermo pass).
@@ -576,6 +602,7 @@ struct Group {
         bool use_ff = eval_grad_ff(pt, c.x, F);
         if (!use_ff) eval_grad64(pt, c.x, F);
         bool is64 = !use_ff;  // F is an FP64 residual
+        bool th_valid = false;  // c's thermo fields are those of the current c.x
         steps = 0;
         int refresh = 0;
         if (budget < 2) budget = 2;  // at least one correction and its certification
@@ -636,7 +663,11 @@ struct Group {
             symmetrize_step(pt, c.x, p);
             for (int i = 0; i < 5; ++i) { c.x[i] += p[i]; Fo[i] = F[i]; }
             ++steps;
-            if (use_ff && eval_grad_ff(pt, c.x, F)) {
+            // after a correction step the state is usually final: the float-float pass also
+            // returns the outputs at it
+            const int ffr = use_ff ? eval_grad_thermo_ff(pt, o, c, F) : 0;
+            th_valid = (ffr & 2) != 0;
+            if (ffr & 1) {
                 is64 = false;
             } else {
                 use_ff = false;
@@ -654,8 +685,9 @@ struct Group {
                 }
             }
         }
-        // the outputs at the final state: float-float thermo pass (FP64 pass if unavailable)
-        if (!eval_thermo_ff(pt, o, c)) eval_thermo(pt, o, c);
+        // the outputs at the final state: from its float-float residual pass when that was
+        // the last one, else a float-float thermo pass (FP64 pass if unavailable)
+        if (!th_valid && !eval_thermo_ff(pt, o, c)) eval_thermo(pt, o, c);
     }
 
     // Mixed-precision counterpart of solve_seed.  `dup` is set when the FP32 solution is a
@@ -663,7 +695,7 @@ struct Group {
     // cannot take from an earlier one under the min-Omega tie rule); then no FP64 work is
     // spent on it.  D provides seen(x) and remember(x), uniform over the group.
     template <class D>
-    __device__ void mixed_solve_seed(const PointIn &pt, const double *x0, const SolveOpts &o, Candidate &out,
+    __device__ __noinline__ void mixed_solve_seed(const PointIn &pt, const double *x0, const SolveOpts &o, Candidate &out,
                                      bool &converged, bool &dup, D &dd) {
         cnt.v[kStatSeeds] += 1;
         dup = false;
@@ -761,9 +793,10 @@ struct LocalRoots {
 // suppressed seed would reach the same FP64 root and lose the min-Omega tie to the earlier
 // seed; an earlier seed still running is not waited for (both are refined, the tie rule
 // keeps the earlier).  omega_bound() is the per-point candidate's Omega (verification mode)
-// -- a bound fixed before the task kernel starts, so which candidates are discarded as unable
-// to win does not depend on timing; in MultiSeed table mode there is none.  The leader lane
-// reads and writes; answers are broadcast.
+// -- a bound fixed before any task of the slot starts, so which candidates are discarded as
+// unable to win does not depend on timing; in MultiSeed table mode there is none.  The leader
+// lane reads and writes; answers are broadcast.  With roots = null (a per-point seed, which
+// has no slot) it is LocalRoots alone.
 struct PublishedRoots {
     double *roots;        // [slots*S*5]
     int *flag;            // [slots*S]
@@ -791,7 +824,7 @@ struct PublishedRoots {
         return __shfl_sync(mask, hit, leader) != 0;
     }
     __device__ void remember(const double *x) {
-        if (own.n == 0 && gl == 0) {
+        if (own.n == 0 && gl == 0 && roots) {
             for (int i = 0; i < 5; ++i) __stcg(&roots[5 * (base + s) + i], x[i]);
             __threadfence();
             atomicExch(&flag[base + s], 1);

@@ -34,7 +34,7 @@ struct CandRec {
 enum StatSlot {
     kStatPasses64 = 0, kStatEvalsNewton64, kStatEvalsThermo64, kStatSeeds, kStatTrRuns, kStatMsFallbacks,
     kStatPasses32, kStatEvals32, kStatEvalsGrad64, kStatEvalsGradThermo64, kStatRescue64, kStatEvalsThermo32,
-    kStatPruned, kStatEvalsFF, kStatEvalsFFThermo, kStatCount
+    kStatPruned, kStatEvalsFF, kStatEvalsFFThermo, kStatWaitTimeouts, kStatEvalsFFGradThermo, kStatCount
 };
 
 struct SolveArgs {
@@ -57,21 +57,24 @@ struct SolveArgs {
     double *roots;                // [n*n_seeds*5] FP32 roots published per (slot, seed)
     int *root_flag;               // [n*n_seeds] 1 once roots[slot, seed] is written (zeroed)
     long long *list;              // [n] points deferred by the per-point kernel
-    int *list_mode;               // [n] kListVerify / kListFallback
+    int *list_mode;               // [n] kListVerify / kListFallback, stored + 1 once the slot's
+                                  // point and record are written (zeroed: 0 = not yet)
     long long *list_count;        // entries in list (zeroed)
     long long *queue2;            // work-queue head of the task kernel (zeroed)
+    long long *points_done;       // fused kernel: points whose own seed is finished (zeroed)
 };
 
 // Modes of a slot of the mixed task kernel: min-Omega over all seeds (MultiSeed table mode);
 // a converged per-point solution checked against the first verify_seeds seeds; a per-point
 // seed that failed, replaced by the MultiSeed solve (ImplicitSolver.jl:306-327).
-// the control block of a context: queue head, counters, list length, task queue head
+// the control block of a context: queue head, counters, list length, task queue head,
+// finished points of the fused kernel
 constexpr int kCtrlSlots = 80;
 // per-chunk queue heads of the pipelined mixed per-point solve: queue, list length, task queue
 constexpr int kMaxPipelineChunks = 16;
-constexpr int kChunkCtrlBase = 1 + 16;  // after the queue head and up to 16 counters
-static_assert(kStatCount + 3 <= kCtrlSlots, "control block too small");
-static_assert(kStatCount <= 16 && kChunkCtrlBase + 3 * kMaxPipelineChunks <= kCtrlSlots, "chunk control slots");
+constexpr int kChunkCtrlBase = 24;
+static_assert(1 + kStatCount + 3 <= kChunkCtrlBase, "control block too small");
+static_assert(kChunkCtrlBase + 3 * kMaxPipelineChunks <= kCtrlSlots, "chunk control slots");
 
 enum ListMode { kListFull = 0, kListVerify = 1, kListFallback = 2 };
 
@@ -86,11 +89,14 @@ struct EvalArgs {
 
 size_t node_smem_bytes(int p_num, int t_num);
 cudaError_t launch_solve(const SolveArgs &a, int group, int grid, size_t smem, cudaStream_t s);
-// Mixed precision: per-point mode launches the per-point kernel and then the task kernel
-// over the points it deferred; table mode launches the task kernel alone.
+// Mixed precision: per-point mode launches the fused kernel (points and the tasks they defer
+// in one launch), or the per-point kernel and then the task kernel over the points it
+// deferred; table mode launches the task kernel alone.
 cudaError_t launch_mixed_points(const SolveArgs &a, int grid, size_t smem, cudaStream_t s);
 cudaError_t launch_mixed_tasks(const SolveArgs &a, int grid, size_t smem, cudaStream_t s);
-int solve_mixed_occupancy(bool tasks, size_t smem);
+cudaError_t launch_mixed_fused(const SolveArgs &a, int grid, size_t smem, cudaStream_t s);
+enum MixedKernel { kMixedPoints = 0, kMixedTasks = 1, kMixedFused = 2 };
+int solve_mixed_occupancy(int kernel, size_t smem);
 cudaError_t launch_eval(const EvalArgs &a, int mode, int grid, size_t smem, cudaStream_t s);  // 0 FP64, 1 FP32, 2 ff
 int solve_kernel_occupancy(int group, size_t smem);
 

@@ -325,7 +325,8 @@ def test_tmu_scan_gpu_matches_oracle(engine_factory):
 
 
 def test_mixed_pipeline_chunks_and_autotune(engine_factory):
-    """The chunk pipeline of mixed per-point solves (two streams) and the autotuner change
+    """The launch forms of mixed per-point solves (one fused kernel; the per-point and task
+    kernels one after the other; the two-stream chunk pipeline) and the autotuner change
     launch shapes only: bit-identical results for every shape."""
     import torch
 
@@ -340,11 +341,11 @@ def test_mixed_pipeline_chunks_and_autotune(engine_factory):
     opts = SolveOptions(iterations=40, ftol=1e-10, precision="mixed", verify_seeds=-1, verify_T_max_MeV=170.0,
                         verify_max_step=0.3)
     outs = []
-    for chunks in (1, 3, 7):
+    for chunks in (1, -1, 3, 7):
         eng.set_tuning(32, 0, pipeline_chunks=chunks)
         outs.append(eng.solve(T, mu, xi, seed_table=table, seed_table_hot=hot, point_seeds=seeds, opts=opts))
         st = eng.stats()
-        assert st["kernel_launches"] > 0
+        assert st["kernel_launches"] > 0 and st["device_wait_timeouts"] == 0
     for r in outs[1:]:
         for k in ("x", "omega", "entropy", "n_q", "status", "chosen_seed", "iterations", "converged"):
             np.testing.assert_array_equal(r[k], outs[0][k], err_msg=k)
