@@ -50,6 +50,8 @@ extern "C" {
                              come from FP64 passes                                          */
 #define PNJL_PREC_FF_RESIDUAL 2 /* pnjl_eval_batch only: the float-float passes the mixed
                              solver refines with (gradient and Hessian; omega is NaN)       */
+#define PNJL_PREC_FP64_CERT 3 /* pnjl_eval_batch only: the FP64 residual pass that certifies
+                             the mixed solver's roots (gradient; omega, Hessian NaN)        */
 
 /* Model constants in fm units; src/Constants_PNJL.jl:82-103 (hbarc, N_color, rho0,
  * Lambda, G, K, m_ud0, m_s0, T0, a0, a1, a2, b3). */
@@ -184,8 +186,9 @@ int pnjl_get_nodes(const pnjl_ctx *ctx, double *p_mesh, double *c_mesh, double *
 /* Omega, grad_x Omega [5n] and Hessian_x Omega [25n, row-major] at given states:
  * calculate_omega (Thermodynamics.jl:181-195) and the ForwardDiff gradient/Jacobian of
  * gap_conditions (Conditions.jl:72-86; F = -grad_x Omega).  precision: PNJL_PREC_FP64,
- * PNJL_PREC_MIXED (FP32-Kahan integrand, FP64 assembly) or PNJL_PREC_FF_RESIDUAL (float-float
- * gradient and Hessian).  Host pointers; NULL skips. */
+ * PNJL_PREC_MIXED (FP32-Kahan integrand, FP64 assembly), PNJL_PREC_FF_RESIDUAL (float-float
+ * gradient and Hessian) or PNJL_PREC_FP64_CERT (gradient from the certification pass).  Host
+ * pointers; NULL skips. */
 int pnjl_eval_batch(pnjl_ctx *ctx, int64_t n, const double *x, const double *T,
                     const double *mu_u, const double *mu_d, const double *mu_s,
                     const double *xi, int32_t precision,
@@ -263,6 +266,13 @@ int pnjl_autotune(pnjl_ctx *ctx, int64_t n, const double *d_T, const double *d_m
  * (FLOP/s, FMA = 2), 1 = FP32 FMA (FLOP/s), 2 = SFU ex2.approx.f32 (operations/s), 3 = FP64 FMA
  * issued by one lane per warp (FLOP/s of the active lanes). */
 int pnjl_probe_peak(pnjl_ctx *ctx, int32_t kind, double *ops_per_s);
+
+/* Element-wise FP64 functions of the mixed solver's certification pass, for checking them
+ * against the library functions (no counterpart in the reference): y[i] = f(x[i]) on the
+ * device, host arrays of n.  fn 0: e^x by the table method (for -700 <= x <= 0; other x take
+ * the library exp), 1: 1/x from the hardware approximation and a Newton correction, 2:
+ * 1/sqrt(x) likewise; 3, 4, 5: the library exp, division and rsqrt. */
+int pnjl_f64_math(pnjl_ctx *ctx, int32_t fn, int64_t n, const double *x, double *y);
 
 /* ---- learned seed: MLP (T, mu, xi) -> (phi_u, phi_d, phi_s, Phi, Phibar) ----------------
  * 3 -> 128 -> 128 -> 128 -> 5, SiLU, BF16 weights, FP32 accumulation, trained with Adam by

@@ -34,6 +34,7 @@ PNJL_SEEDS_PER_POINT = 1
 PNJL_PREC_FP64 = 0
 PNJL_PREC_MIXED = 1
 PNJL_PREC_FF_RESIDUAL = 2  # pnjl_eval_batch only
+PNJL_PREC_FP64_CERT = 3  # pnjl_eval_batch only
 
 dp = C.POINTER(C.c_double)
 i32p = C.POINTER(C.c_int32)
@@ -128,6 +129,7 @@ SIGNATURES = {
                                 C.POINTER(pnjl_tuning), C.c_int32, C.POINTER(C.c_int32)]),
     "pnjl_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "pnjl_probe_peak": (C.c_int, [C.c_void_p, C.c_int32, dp]),
+    "pnjl_f64_math": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64, dp, dp]),
     "pnjl_mlp_param_count": (C.c_int, []),
     "pnjl_mlp_init": (C.c_int, [C.c_void_p, C.c_uint64]),
     "pnjl_mlp_set_scaling": (C.c_int, [C.c_void_p, dp, dp, dp, dp]),

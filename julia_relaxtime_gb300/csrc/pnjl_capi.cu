@@ -393,10 +393,11 @@ static int eval_common(pnjl_ctx *ctx, int64_t n, const double *x, const double *
     if (ctx->p_num == 0) return fail(ctx, PNJL_ERR_NO_NODES, "call pnjl_set_nodes first");
     if (n < 0 || (n > 0 && (!x || !T || !mu_u || !mu_d || !mu_s || !xi)))
         return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "null input array");
-    if (precision != PNJL_PREC_FP64 && precision != PNJL_PREC_MIXED && precision != PNJL_PREC_FF_RESIDUAL)
+    if (precision != PNJL_PREC_FP64 && precision != PNJL_PREC_MIXED && precision != PNJL_PREC_FF_RESIDUAL &&
+        precision != PNJL_PREC_FP64_CERT)
         return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "unknown precision");
-    if (precision == PNJL_PREC_FF_RESIDUAL && out)
-        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "the float-float pass gives the residual only");
+    if ((precision == PNJL_PREC_FF_RESIDUAL || precision == PNJL_PREC_FP64_CERT) && out)
+        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "this pass gives the residual only");
     if (n == 0) return PNJL_OK;
     cudaSetDevice(ctx->device);
     const size_t nn = (size_t)n;
@@ -430,7 +431,7 @@ static int eval_common(pnjl_ctx *ctx, int64_t n, const double *x, const double *
     pnjl::EvalArgs a{};
     a.P = ctx->dp;
     a.nodes = kernel_nodes(ctx);
-    const int mode = precision;  // 0 FP64, 1 FP32-Kahan, 2 float-float residual
+    const int mode = precision;  // 0 FP64, 1 FP32-Kahan, 2 float-float residual, 3 FP64 certification
     const size_t smem = pnjl::node_smem_bytes(ctx->p_num, ctx->t_num);
     a.n = n;
     a.x = dx; a.T = dT; a.mu_u = du; a.mu_d = dd; a.mu_s = ds; a.xi = dxi;
@@ -1128,6 +1129,14 @@ int pnjl_get_kernel_stats(const pnjl_ctx *cctx, int32_t kernel, pnjl_stats *out)
 int pnjl_device_sm_count(const pnjl_ctx *ctx) { return ctx ? ctx->sm_count : 0; }
 
 extern "C" int pnjl_probe_peak_impl(int device, int kind, double *ops_per_s);
+extern "C" int pnjl_f64_math_impl(int device, int fn, int64_t n, const double *x, double *y);
+
+int pnjl_f64_math(pnjl_ctx *ctx, int32_t fn, int64_t n, const double *x, double *y) {
+    if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
+    const int rc = pnjl_f64_math_impl(ctx->device, fn, n, x, y);
+    if (rc == PNJL_ERR_INVALID_ARGUMENT) return fail(ctx, rc, "pnjl_f64_math: bad arguments");
+    return rc;
+}
 
 int pnjl_probe_peak(pnjl_ctx *ctx, int32_t kind, double *ops_per_s) {
     if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;

@@ -58,6 +58,13 @@ struct SolveOpts {
 static constexpr double kPolyakovEps = 1e-16;
 static constexpr double kLogPolyakovEps = -36.841361487904734;
 
+// FP64 passes: in the rescaled branch (a > 0) t = exp(-min(a, kRescaleCapA)).  The antiquark
+// variable C/t = exp(-(E + mu)/T) never exceeds t, so beyond the cap (t < 1.3e-100) every
+// antiquark term is negligible against 1 in FP64, while t^3 (the rescaling of f-) stays a
+// normal number: without the cap, t and C both underflow at T -> 0 and 0 * inf appears.
+// The log term keeps the exact offset: ln f+ + ln f- = 3a + 3 min(a, cap) + ln(f+' f-').
+static constexpr double kRescaleCapA = 230.0;
+
 // Per-flavour constants of a pass.
 template <typename R>
 struct FlavourConst {
@@ -162,7 +169,10 @@ __device__ __forceinline__ void node_flavour(const FlavourConst<R> &fc, R q2, R 
     const R mE = fc.M * rE;  // dE/dM
     const R a = (fc.mu - E) * fc.invT;
     const bool sig = a > R(0);
-    const R t = fast_exp(sig ? -a : a);
+    // rescaling exponent of the a > 0 branch (capped in FP64, see kRescaleCapA)
+    R ac = a;
+    if constexpr (sizeof(R) == 8) ac = fmin(a, kRescaleCapA);
+    const R t = fast_exp(sig ? -ac : a);
     const R t2 = t * t;
     const R t3 = t2 * t;
     const R k1 = sig ? fc.k1_1 : fc.k1_0;
@@ -207,9 +217,9 @@ __device__ __forceinline__ void node_flavour(const FlavourConst<R> &fc, R q2, R 
         acc.SAN.add(w * (a * np + b * nm));
         // ln f+ + ln f- = 6 max(a,0) + ln(fp gm); a clamped factor is replaced by the
         // reference's constant (log(1e-16), plus 3a in its rescaled quark branch)
-        R L = (sig ? R(6) * a : R(0)) + fast_log(prod);
+        R L = (sig ? R(3) * (a + ac) : R(0)) + fast_log(prod);
         if (clP) L += R(kLogPolyakovEps);
-        if (clM) L += R(kLogPolyakovEps) - (sig ? R(3) * a : R(0));
+        if (clM) L += R(kLogPolyakovEps) - (sig ? R(3) * ac : R(0));
         acc.SL.add(w * L);
     }
     if (HESS) {

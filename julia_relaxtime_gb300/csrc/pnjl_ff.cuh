@@ -26,10 +26,14 @@ struct ff {
 };
 
 // exp tables in shared memory: e^k (k = -kExpMaxN..kExpMaxN) and e^(j/16) (j = -8..8), as (h, l)
+// float pairs, then (from float kExp64Offset, 8-byte aligned) the kExp64N doubles 2^(j/64) of
+// the FP64 exponential (pnjl_f64.cuh)
 constexpr int kExpMaxN = 88;
 constexpr int kExpIntN = 2 * kExpMaxN + 1;
 constexpr int kExpFracN = 17;
-constexpr int kExpTableFloats = 2 * (kExpIntN + kExpFracN);
+constexpr int kExp64Offset = 2 * (kExpIntN + kExpFracN);
+constexpr int kExpTableFloats = kExp64Offset + 2 * 64;
+static_assert(kExp64Offset % 2 == 0, "FP64 table alignment");
 
 __device__ __forceinline__ ff ff_make(float h) { return ff{h, 0.0f}; }
 __device__ __forceinline__ ff ff_from_float_pair(float h, float l) { return ff{h, l}; }
@@ -53,11 +57,21 @@ __device__ __forceinline__ ff two_prod(float a, float b) {
     const float p = __fmul_rn(a, b);
     return ff{p, __fmaf_rn(a, b, -p)};
 }
-__device__ __forceinline__ ff ff_add(ff a, ff b) {
+// a + b with relative error ~2^-47 of the result (two TwoSums; 20 FP32 additions): for the
+// lane reductions of the pass sums
+__device__ __forceinline__ ff ff_add_acc(ff a, ff b) {
     const ff s = two_sum(a.h, b.h);
     const ff t = two_sum(a.l, b.l);
     ff r = fast_two_sum(s.h, __fadd_rn(s.l, t.h));
     return fast_two_sum(r.h, __fadd_rn(r.l, t.l));
+}
+// a + b with absolute error ~2^-47 (|a| + |b|) (one TwoSum on the high parts; 11 FP32
+// additions).  In the node integrand every operand already carries a relative error of that
+// size from its own float-float rounding, so the cheaper form loses nothing there: where a
+// and b cancel, their own errors dominate either way.
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+    const ff s = two_sum(a.h, b.h);
+    return fast_two_sum(s.h, __fadd_rn(__fadd_rn(s.l, a.l), b.l));
 }
 __device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.h, -a.l}; }
 __device__ __forceinline__ ff ff_sub(ff a, ff b) { return ff_add(a, ff_neg(b)); }
@@ -279,7 +293,7 @@ __device__ __forceinline__ ff group_sum_ffv(ff v, unsigned mask) {
 #pragma unroll
     for (int o = G / 2; o > 0; o >>= 1) {
         const ff u{__shfl_xor_sync(mask, v.h, o), __shfl_xor_sync(mask, v.l, o)};
-        v = ff_add(v, u);
+        v = ff_add_acc(v, u);
     }
     return v;
 }

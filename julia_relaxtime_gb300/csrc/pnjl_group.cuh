@@ -26,6 +26,7 @@ __device__ __forceinline__ NodeView stage_nodes(const KernelNodes &kn, void *sme
     nv.p2f = sf; nv.Af = sf + np; nv.c2f = sf + 2 * np; nv.Bf = sf + 2 * np + nt;
     nv.p2l = nv.Al = nv.c2l = nv.Bl = nullptr;
     nv.expt = nullptr;
+    nv.exp64 = nullptr;
     if (kn.lo && kn.expt) {
         const int m = 2 * (np + nt);
         float *sl = sf + m;
@@ -34,6 +35,7 @@ __device__ __forceinline__ NodeView stage_nodes(const KernelNodes &kn, void *sme
         for (int i = threadIdx.x; i < kExpTableFloats; i += blockDim.x) se[i] = kn.expt[i];
         nv.p2l = sl; nv.Al = sl + np; nv.c2l = sl + 2 * np; nv.Bl = sl + 2 * np + nt;
         nv.expt = se;
+        nv.exp64 = (const double *)(se + kExp64Offset);
     }
     return nv;
 }
@@ -451,11 +453,13 @@ struct Group {
         return true;
     }
 
+    // FP64 residual at x: the certification pass (node_pass_cert) where its table is staged.
     __device__ __noinline__ void eval_grad64(const PointIn &pt, const double *x, double *F) {
         double M[3];
         masses(P, x, M);
         PassSums S;
-        node_pass<double, false, true, false, false, G>(nv, pt, x, M, gl, mask, S, cnt.v[kStatEvalsGrad64]);
+        if (nv.exp64) node_pass_cert<G>(nv, pt, x, M, gl, mask, S, cnt.v[kStatEvalsGrad64]);
+        else node_pass<double, false, true, false, false, G>(nv, pt, x, M, gl, mask, S, cnt.v[kStatEvalsGrad64]);
         Eval ev;
         double V, V1[3], V2[3];
         vacuum_terms<G>(P, M, gl, mask, leader(), V, V1, V2);

@@ -5,7 +5,9 @@
 
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 
+#include "pnjl_f64.cuh"
 #include "pnjl_ff.cuh"
 #include "pnjl_kernels.h"
 
@@ -80,9 +82,14 @@ inline void separable_tables(int p_num, int t_num, const double *xp, const doubl
         for (int i = 0; i < m; ++i) hl[i] = (float)(h[i] - (double)hf[i]);
 }
 
-// Float-float tables of the float-float exp (pnjl_ff.cuh): e^k for k = -kExpMaxN..kExpMaxN, then
-// e^(j/16) for j = -8..8, each as (hi, lo) floats, from long-double exp.
+// exp tables (pnjl_ff.cuh, pnjl_f64.cuh): e^k for k = -kExpMaxN..kExpMaxN, then e^(j/16) for
+// j = -8..8, each as (hi, lo) floats, from long-double exp; then 2^(j/64), j = 0..63, as
+// doubles rounded from long-double exp2.
 inline void ff_exp_tables(float *out) {
+    for (int j = 0; j < kExp64N; ++j) {
+        const double v = (double)exp2l((long double)j / 64.0L);
+        std::memcpy(out + kExp64Offset + 2 * j, &v, sizeof v);
+    }
     for (int k = -kExpMaxN; k <= kExpMaxN; ++k) {
         const long double v = expl((long double)k);
         const float h = (float)v;

@@ -6,9 +6,16 @@
 // seeded from the thread index and written back so the compiler cannot drop them.
 // kind 3: FP64 FMA chains on lane 0 of every warp only (the other lanes are predicated off),
 // reported per active lane -- whether the FP64 pipe skips inactive lanes.
+//
+// Also the element-wise check of the FP64 functions of the certification pass
+// (pnjl_f64.cuh) against the library functions, for the tests.
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "../../include/pnjl_cuda.h"
+#include "pnjl_f64.cuh"
+#include "pnjl_host_common.h"
 
 namespace pnjl {
 
@@ -46,7 +53,51 @@ __global__ void __launch_bounds__(256) ex2_probe(float *out, int iters) {
     out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// y[i] = f(x[i]): fn 0 exp_nonpos, 1 rcp_normal, 2 rsqrt_normal, 3 exp, 4 1/x, 5 rsqrt
+__global__ void __launch_bounds__(256) f64_math_kernel(int fn, int64_t n, const double *x, double *y,
+                                                       const double *tab_global) {
+    __shared__ double tab[kExp64N];
+    for (int i = threadIdx.x; i < kExp64N; i += blockDim.x) tab[i] = tab_global[i];
+    __syncthreads();
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double v = x[i];
+        double r;
+        switch (fn) {
+            case 0: r = exp_nonpos(v, tab); break;
+            case 1: r = rcp_normal(v); break;
+            case 2: r = rsqrt_normal(v); break;
+            case 3: r = exp(v); break;
+            case 4: r = 1.0 / v; break;
+            default: r = rsqrt(v); break;
+        }
+        y[i] = r;
+    }
+}
+
 }  // namespace pnjl
+
+extern "C" int pnjl_f64_math_impl(int device, int fn, int64_t n, const double *x, double *y) {
+    if (fn < 0 || fn > 5 || n < 0 || (n > 0 && (!x || !y))) return PNJL_ERR_INVALID_ARGUMENT;
+    if (n == 0) return PNJL_OK;
+    if (cudaSetDevice(device) != cudaSuccess) return PNJL_ERR_CUDA;
+    std::vector<float> tabs(pnjl::kExpTableFloats);
+    pnjl::ff_exp_tables(tabs.data());
+    double *d = nullptr;
+    const size_t bytes = (size_t)n * sizeof(double);
+    if (cudaMalloc(&d, 2 * bytes + pnjl::kExp64N * sizeof(double)) != cudaSuccess) return PNJL_ERR_OUT_OF_MEMORY;
+    double *dx = d, *dy = d + n, *dt = d + 2 * n;
+    cudaError_t e = cudaMemcpy(dx, x, bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(dt, tabs.data() + pnjl::kExp64Offset, pnjl::kExp64N * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        const int64_t blocks = std::min<int64_t>((n + 255) / 256, 4096);
+        pnjl::f64_math_kernel<<<(int)blocks, 256>>>(fn, n, dx, dy, dt);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(y, dy, bytes, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return e == cudaSuccess ? PNJL_OK : PNJL_ERR_CUDA;
+}
 
 extern "C" int pnjl_probe_peak_impl(int device, int kind, double *ops_per_s) {
     if (!ops_per_s || kind < 0 || kind > 3) return PNJL_ERR_INVALID_ARGUMENT;

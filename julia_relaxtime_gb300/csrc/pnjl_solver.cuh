@@ -14,6 +14,7 @@
 #pragma once
 
 #include "pnjl_device.cuh"
+#include "pnjl_f64.cuh"
 #include "pnjl_ff.cuh"
 
 namespace pnjl {
@@ -38,6 +39,7 @@ struct NodeView {
     const float *p2f, *Af, *c2f, *Bf;
     const float *p2l, *Al, *c2l, *Bl;  // float-float low parts (null when not staged)
     const float *expt;                 // float-float exp tables (null when not staged)
+    const double *exp64;               // 2^(j/64) table of exp_nonpos (null when not staged)
     int p_num, t_num;
 };
 
@@ -212,6 +214,89 @@ __device__ void node_pass(const NodeView &nv, const PointIn &pt, const double *x
     }
     S.SL = acc[18]; S.SP = acc[19]; S.SPb = acc[20]; S.SPP = acc[21]; S.SPPb = acc[22]; S.SPbPb = acc[23];
     S.SAN = acc[24];
+}
+
+// FP64 residual pass of the mixed solve's certification: the sums S.DM, S.SP, S.SPb of
+// node_pass<double, GRAD only> from the same integrand in FP64, arranged for the FP64 pipe
+// (56 FP64 instructions per node-flavour): exp, 1/x and 1/sqrt from pnjl_f64.cuh, Horner
+// forms in FMAs, and the per-flavour factors -3/T (dOmega/dM) and 3 (dOmega/dPhi) applied
+// once to the lane sums instead of per node.  With r_k = u_k / f+ and s_k = C^(k-1) u_k / f-
+// (u = (t, t^2, t^3) for a <= 0, (t^2, t, 1) for a > 0) the Polyakov distributions are
+//   n+ = (Phi u1 + 2 Phibar u2 + u3) / f+,   n- = C (Phibar u1 + 2 Phi C u2 + C^2 u3) / f-
+// and the Phi / Phibar derivatives take r1 + s2 and r2 + s1 (quark / antiquark sides
+// swapped for mu < 0).  Requires the staged FP64 exp table (nv.exp64).
+template <int G>
+__device__ void node_pass_cert(const NodeView &nv, const PointIn &pt, const double *x, const double *M, int gl,
+                               unsigned mask, PassSums &S, int64_t &evals) {
+    const bool dedup = (M[1] == M[0]) && (pt.mu[1] == pt.mu[0]);
+    const double *p2 = nv.p2, *A = nv.A, *c2 = nv.c2, *B = nv.B, *tab = nv.exp64;
+    const int pn = nv.p_num, n = nv.p_num * nv.t_num;
+    const double xi = pt.xi;
+    double DM[3] = {0.0, 0.0, 0.0}, SP = 0.0, SPb = 0.0;
+#pragma unroll 1
+    for (int f = 0; f < 3; ++f) {
+        if (f == 1 && dedup) continue;
+        bool sw;
+        const FlavourConst<double> fc = make_flavour<double>(M[f], pt.mu[f], pt.T, x[3], x[4], sw);
+        const double Mf = fc.M, M2 = fc.M2, invT = fc.invT, muT = fc.mu * fc.invT, C = fc.C, C2 = fc.C2;
+        const double Pq = fc.Pq, Pa = fc.Pa, Pa2 = 2.0 * fc.Pa, Pq2C = 2.0 * fc.Pq * fc.C;
+        double dm = 0.0, sq = 0.0, sa = 0.0;
+        int ip = gl, it = 0;
+        while (ip >= pn) { ip -= pn; ++it; }
+        double sxi = 1.0, bw = 0.0;
+        if (it < nv.t_num) { sxi = fma(xi, c2[it], 1.0); bw = B[it]; }
+#pragma unroll 1
+        for (int k = gl; k < n; k += G) {
+            const double q2 = p2[ip] * sxi, w = A[ip] * bw;
+            const double E2 = q2 + M2;
+            const double rE = rsqrt_normal(E2);
+            const double E = E2 * rE, mE = Mf * rE;
+            const double a = fma(-E, invT, muT);  // (mu - E)/T
+            // a > 0, and -min(a, kRescaleCapA) or a, from the bit patterns (integer pipe):
+            // among negative doubles the larger pattern is the larger magnitude
+            const long long ab = __double_as_longlong(a);
+            const bool sig = ab > 0;
+            const unsigned long long nb = (unsigned long long)ab | 0x8000000000000000ull;
+            const unsigned long long cap = (unsigned long long)__double_as_longlong(-kRescaleCapA);
+            const double t = exp_nonpos(__longlong_as_double((long long)(sig && nb > cap ? cap : nb)), tab);
+            const double t2 = t * t, t3 = t2 * t;
+            const double fp = fma(fma(t + (sig ? fc.k2_1 : fc.k2_0), t, sig ? fc.k1_1 : fc.k1_0), t, 1.0);
+            const double gm = fma(fma(fma(sig ? 1.0 : fc.e3_0, t, sig ? fc.e2_1 : fc.e2_0), t, sig ? fc.e1_1 : fc.e1_0),
+                                  t, sig ? fc.e0_1 : 1.0);
+            // the reference's max(f, 1e-16) clamps (NaN is not clamped)
+            const bool clP = fp < kPolyakovEps;
+            const bool clM = gm < kPolyakovEps * (sig ? t3 : 1.0);
+            const double fpc = clP ? 1.0 : fp, gmc = clM ? 1.0 : gm;
+            const double Rr = rcp_normal(fpc * gmc);
+            const double ipv = clP ? 0.0 : gmc * Rr;  // 1/f+
+            const double im = clM ? 0.0 : fpc * Rr;   // 1/f-
+            const double u1 = sig ? t2 : t, u2 = sig ? t : t2, u3 = sig ? 1.0 : t3;
+            const double Cim = C * im, CCim = C * Cim;
+            const double np = clP ? (sig ? 1.0 : 0.0) : ipv * fma(Pq, u1, fma(Pa2, u2, u3));
+            const double nm = clM ? 0.0 : Cim * fma(Pa, u1, fma(Pq2C, u2, C2 * u3));
+            dm = fma(w, (np + nm) * mE, dm);
+            sq = fma(w, fma(ipv, u1, CCim * u2), sq);
+            sa = fma(w, fma(ipv, u2, Cim * u1), sa);
+            ip += G;
+            if (ip >= pn) {
+                do { ip -= pn; ++it; } while (ip >= pn);
+                if (it < nv.t_num) { sxi = fma(xi, c2[it], 1.0); bw = B[it]; }
+            }
+        }
+        const double mult = (f == 0 && dedup) ? 2.0 : 1.0;
+        DM[f] = -3.0 * invT * dm;
+        if (f == 0 && dedup) DM[1] = DM[0];
+        SP += mult * 3.0 * (sw ? sa : sq);
+        SPb += mult * 3.0 * (sw ? sq : sa);
+        if (gl == 0) evals += (int64_t)n;
+    }
+    for (int f = 0; f < 3; ++f) {
+        S.DM[f] = group_sum<G>(DM[f], mask);
+        S.DMM[f] = S.DMP[f] = S.DMPb[f] = S.Nq[f] = S.Na[f] = 0.0;
+    }
+    S.SP = group_sum<G>(SP, mask);
+    S.SPb = group_sum<G>(SPb, mask);
+    S.SL = S.SAN = S.SPP = S.SPPb = S.SPbPb = 0.0;
 }
 
 // Float-float pass: the sums of node_pass<..., GRAD, THERMO> (S.DM, S.SP, S.SPb; S.Nq, S.Na,

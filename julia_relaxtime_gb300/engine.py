@@ -14,7 +14,7 @@ from . import _capi as api
 from .constants import PNJLParams
 
 PRECISIONS = {"fp64": api.PNJL_PREC_FP64, "mixed": api.PNJL_PREC_MIXED}
-EVAL_PRECISIONS = dict(PRECISIONS, ff_residual=api.PNJL_PREC_FF_RESIDUAL)
+EVAL_PRECISIONS = dict(PRECISIONS, ff_residual=api.PNJL_PREC_FF_RESIDUAL, fp64_cert=api.PNJL_PREC_FP64_CERT)
 
 
 @dataclass
@@ -291,6 +291,17 @@ class GapEngine:
         k = {"fp64": 0, "fp32": 1, "sfu": 2, "fp64_one_lane": 3}[kind]
         self._check(self._lib.pnjl_probe_peak(self._ctx, k, C.byref(v)), "pnjl_probe_peak")
         return float(v.value)
+
+    def f64_math(self, fn: str, x) -> np.ndarray:
+        """Element-wise FP64 function of the certification pass on the device (pnjl_f64_math):
+        "exp", "rcp", "rsqrt" (the pass's own) or "exp_lib", "rcp_lib", "rsqrt_lib"."""
+        k = {"exp": 0, "rcp": 1, "rsqrt": 2, "exp_lib": 3, "rcp_lib": 4, "rsqrt_lib": 5}[fn]
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.empty_like(x)
+        dp = C.POINTER(C.c_double)
+        self._check(self._lib.pnjl_f64_math(self._ctx, k, x.size, x.ctypes.data_as(dp), y.ctypes.data_as(dp)),
+                    "pnjl_f64_math")
+        return y
 
     def set_tuning(self, lanes_per_point: int, blocks_per_sm: int = 0, pipeline_chunks: int | None = None):
         self._check(self._lib.pnjl_set_tuning(self._ctx, int(lanes_per_point), int(blocks_per_sm)),

@@ -55,6 +55,7 @@ def test_eval_fp64_matches_oracle(engine_factory, P, p_num, t_num, mu_neg, asym)
     eng = engine_factory(p_num, t_num)
     nd = orc.Nodes(p_num, t_num)
     x, T, mu, xi = random_states(48, p_num + t_num, mu_neg, asym)
+    T[:3] = 0.5 / HBARC  # (mu - E)/T beyond the rescaling cap of the FP64 passes
     om, g, h = eng.evaluate(x, T, mu, xi)
     for i in range(len(T)):
         o_ref, g_ref, h_ref = orc.evaluate(P, nd, x[i], mu[i], T[i], xi[i])
@@ -91,6 +92,59 @@ def test_eval_ff_residual_matches_oracle(engine_factory, P, p_num, t_num, mu_neg
         assert np.abs(g[i] - g_ref).max() <= 1e-11 * sg, (i, g[i] - g_ref, sg)
         sh = max(1.0, np.abs(h_ref).max())
         assert np.abs(h[i] - h_ref).max() <= 1e-10 * sh, (i, h[i] - h_ref, sh)
+
+
+@pytest.mark.parametrize("p_num,t_num,mu_neg,asym", [(64, 8, False, False), (128, 32, True, True)])
+def test_eval_fp64_cert_matches_oracle(engine_factory, P, p_num, t_num, mu_neg, asym):
+    """The FP64 residual pass that certifies the mixed solver's roots (table exp, hardware
+    rcp / rsqrt approximations with Newton corrections): gradient to 1e-12 of its scale
+    against the FP64 jet oracle and to 2e-14 against the library-function FP64 pass; states
+    at T = 0.5 MeV (exponent arguments below -700: the library exp) included."""
+    eng = engine_factory(p_num, t_num)
+    nd = orc.Nodes(p_num, t_num)
+    x, T, mu, xi = random_states(40, 5 + p_num, mu_neg, asym)
+    T[:4] = 0.5 / HBARC
+    _, g, _ = eng.evaluate(x, T, mu, xi, precision="fp64_cert")
+    _, g64, _ = eng.evaluate(x, T, mu, xi)
+    for i in range(len(T)):
+        _, g_ref, _ = orc.evaluate(P, nd, x[i], mu[i], T[i], xi[i])
+        sg = max(1.0, np.abs(g_ref).max())
+        assert np.abs(g[i] - g_ref).max() <= 1e-12 * sg, (i, g[i] - g_ref, sg)
+        assert np.abs(g[i] - g64[i]).max() <= 2e-14 * sg, (i, g[i] - g64[i], sg)
+
+
+def test_f64_math_functions_within_ulps(engine_factory):
+    """exp / 1/x / 1/sqrt of the certification pass against correctly rounded references
+    (long-double numpy) and the library functions: within 2, 1 and 2 ulp on their fast
+    ranges; the arguments outside them give the library function's value."""
+    eng = engine_factory(12, 6)
+    rng = np.random.default_rng(3)
+    ld = np.longdouble
+
+    def ulps(y, ref):
+        ref = np.asarray(ref, dtype=np.float64)
+        return np.abs(y - ref) / np.spacing(np.abs(ref))
+
+    x = np.concatenate([-rng.uniform(0, 700, 20000), -np.exp(rng.uniform(-40, 6, 20000)),
+                        [-0.0, -700.0, -699.999, -5e-324, -1e-310, -1e-16]])
+    y = eng.f64_math("exp", x)
+    assert ulps(y, np.exp(x.astype(ld))).max() <= 2.0
+    assert ulps(y, eng.f64_math("exp_lib", x)).max() <= 2.0
+    edge = np.array([-700.5, -1000.0, -np.inf, np.nan, 0.0, 1.0, 3.5])
+    np.testing.assert_array_equal(eng.f64_math("exp", edge), eng.f64_math("exp_lib", edge))
+
+    x = np.concatenate([np.exp(rng.uniform(-700, 700, 20000)), -np.exp(rng.uniform(-700, 700, 5000)),
+                        [1.0, 2.0, 3.0, 0.1, 1e-16]])
+    y = eng.f64_math("rcp", x)
+    assert ulps(y, ld(1) / x.astype(ld)).max() <= 1.0
+    edge = np.array([0.0, -0.0, 1e-310, 5e-324, 1e308, -1e308, np.inf, np.nan])
+    np.testing.assert_array_equal(eng.f64_math("rcp", edge), eng.f64_math("rcp_lib", edge))
+
+    x = np.concatenate([np.exp(rng.uniform(-700, 700, 20000)), [1.0, 4.0, 2.0, 0.5, 9.869604401089358]])
+    y = eng.f64_math("rsqrt", x)
+    assert ulps(y, ld(1) / np.sqrt(x.astype(ld))).max() <= 2.0
+    edge = np.array([0.0, 1e-310, 1e308, -1.0, np.inf, np.nan])
+    np.testing.assert_array_equal(eng.f64_math("rsqrt", edge), eng.f64_math("rsqrt_lib", edge))
 
 
 def test_thermo_matches_oracle(engine_factory, P):
