@@ -91,19 +91,25 @@ __device__ __forceinline__ ff ff_mul_f(ff a, float b) {
 }
 __device__ __forceinline__ ff ff_sel(bool c, ff a, ff b) { return ff{c ? a.h : b.h, c ? a.l : b.l}; }
 
-// 1/b: one Newton step y = y0 + y0 (1 - b y0) from the correctly rounded FP32 reciprocal
+// 1/b: one Newton step y = y0 + y0 e, e = 1 - b y0, from the correctly rounded FP32
+// reciprocal y0.  1 - b.h y0 is exactly representable (|e| < 2^-23 with bits down to
+// 2^-48), so one FMA gives it; the b.l term is small.  Relative error ~e^2 + 2^-48.
 __device__ __forceinline__ ff ff_rcp(ff b) {
     const float y0 = __frcp_rn(b.h);
-    const ff e = ff_sub(ff_make(1.0f), ff_mul_f(b, y0));
-    return ff_add_f(ff_mul_f(e, y0), y0);
+    float e = __fmaf_rn(-b.h, y0, 1.0f);
+    e = __fmaf_rn(-b.l, y0, e);
+    return fast_two_sum(y0, __fmul_rn(y0, e));
 }
 
-// 1/sqrt(x): one Newton step y = y0 + y0 (1 - x y0^2) / 2 from the FP32 value
+// 1/sqrt(x): y = y0 (1 + e/2 + 3e^2/8), e = 1 - x y0^2, from the correctly rounded FP32 value
+// y0 (y0^2 exact as a pair; 1 - x.h y0^2 is again exact in one FMA).
 __device__ __forceinline__ ff ff_rsqrt(ff x) {
     const float y0 = __frsqrt_rn(x.h);
-    const ff r = ff_mul(x, two_prod(y0, y0));
-    const ff e = ff_sub(ff_make(1.0f), r);
-    return ff_add_f(ff_mul_f(e, 0.5f * y0), y0);
+    const ff p = two_prod(y0, y0);
+    float e = __fmaf_rn(-x.h, p.h, 1.0f);
+    e = __fmaf_rn(-x.h, p.l, e);
+    e = __fmaf_rn(-x.l, p.h, e);
+    return fast_two_sum(y0, __fmul_rn(__fmul_rn(y0, e), __fmaf_rn(e, 0.375f, 0.5f)));
 }
 
 // e^x for |x| <= 88 (0 below, +inf above): x = n + f with n = rint(x), |f| <= 1/2; f = j/16 + g
@@ -218,10 +224,8 @@ __device__ __forceinline__ void node_flavour_ff(const FlavourFF &fc, ff q2, ff w
     const bool clM = gm.h < 1e-16f * alpha3;
     const ff fpc = clP ? ff_make(1.0f) : fp;
     const ff gmc = clM ? ff_make(1.0f) : gm;
-    const ff prod = ff_mul(fpc, gmc);
-    const ff Rr = ff_rcp(prod);
-    const ff ip = clP ? ff_make(0.0f) : ff_mul(gmc, Rr);
-    const ff im = clM ? ff_make(0.0f) : ff_mul(fpc, Rr);
+    const ff ip = clP ? ff_make(0.0f) : ff_rcp(fpc);
+    const ff im = clM ? ff_make(0.0f) : ff_rcp(gmc);
     const ff u1 = ff_sel(sig, t2, t);
     const ff u2 = ff_sel(sig, t, t2);
     const ff u3 = ff_sel(sig, ff_make(1.0f), t3);
@@ -274,7 +278,7 @@ __device__ __forceinline__ void node_flavour_ff(const FlavourFF &fc, ff q2, ff w
         acc.SAN = ff_add(acc.SAN, ff_mul(w, ff_add(ff_mul(a, np), ff_mul(b, nm))));
         // ln f+ + ln f- = 6 max(a,0) + ln(fp gm); a clamped factor is replaced by the
         // reference's constant (log(1e-16), plus 3a in its rescaled quark branch)
-        ff L = ff_log(prod, etab);
+        ff L = ff_log(ff_mul(fpc, gmc), etab);
         if (sig) L = ff_add(L, ff_mul_f(a, 6.0f));
         if (clP) L = ff_add(L, ff_from_float_pair(-36.84136199951171875f, 5.11606970e-07f));
         if (clM) {
