@@ -487,7 +487,7 @@ struct Group {
             const double fn = norm_inf5(F);
             if (fn < kFtol32) return 1;
             if (iters >= o.max_iter) return fn < kLoose32 ? 1 : 0;
-            if (lu_solve5(J, F, p)) {
+            if (lu_solve5<true>(J, F, p)) {
                 for (int i = 0; i < 5; ++i) p[i] = -p[i];
             } else {
                 levenberg_step(J, F, p);
@@ -659,7 +659,7 @@ struct Group {
                 ++refresh;
             }
             fprev = fn;
-            if (lu_solve5(B, F, p)) {
+            if (lu_solve5<true>(B, F, p)) {
                 for (int i = 0; i < 5; ++i) p[i] = -p[i];
             } else {
                 levenberg_step(B, F, p);

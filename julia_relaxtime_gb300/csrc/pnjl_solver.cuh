@@ -123,6 +123,50 @@ __device__ __forceinline__ void vacuum_terms(const DevParams &P, const double *M
     }
 }
 
+// Per-pass sums of node_pass, per lane before the group reduction.  FP64 passes keep
+// doubles.  FP32 (Kahan) passes keep each sum as a float pair (h, l) -- a flavour's Kahan
+// accumulator (s, c) enters as (s, -c) -- and reduce the pairs over the lanes by TwoSum
+// butterflies, so that only the final value of each sum is converted to FP64: the FP64 pipe,
+// the scarcest on the GB300, sees 3 instructions per sum instead of about 10.
+template <typename R, bool KAHAN>
+struct PassAcc {
+    double v[25];
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int i = 0; i < 25; ++i) v[i] = 0.0;
+    }
+    __device__ __forceinline__ void set(int i, const Acc<R, KAHAN> &a) { v[i] = a.value(); }
+    __device__ __forceinline__ void add(int i, bool twice, const Acc<R, KAHAN> &a) {
+        v[i] += (twice ? 2.0 : 1.0) * a.value();
+    }
+    template <int G>
+    __device__ __forceinline__ double reduce(int i, unsigned mask) { return group_sum<G>(v[i], mask); }
+};
+template <>
+struct PassAcc<float, true> {
+    float h[25], l[25];
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int i = 0; i < 25; ++i) h[i] = l[i] = 0.0f;
+    }
+    __device__ __forceinline__ void set(int i, const Acc<float, true> &a) { h[i] = a.s; l[i] = -a.c; }
+    __device__ __forceinline__ void add(int i, bool twice, const Acc<float, true> &a) {
+        const float m = twice ? 2.0f : 1.0f;  // exact scaling
+        const float bh = m * a.s, bl = -m * a.c;
+        const float sum = __fadd_rn(h[i], bh);
+        const float hp = __fsub_rn(sum, bh);
+        const float err = __fadd_rn(__fsub_rn(h[i], hp), __fsub_rn(bh, __fsub_rn(sum, hp)));
+        l[i] = __fadd_rn(__fadd_rn(l[i], bl), err);
+        h[i] = sum;
+    }
+    template <int G>
+    __device__ __forceinline__ double reduce(int i, unsigned mask) {
+        float hh = h[i], ll = l[i];
+        group_sum_ff<G>(hh, ll, mask);
+        return (double)hh + (double)ll;
+    }
+};
+
 // One pass over the node-flavour mesh at state x; lane `gl` of a group of G lanes takes
 // the flattened nodes k = gl, gl+G, ... (k = ip + p_num*it).  Returns the group-reduced
 // sums (identical in every lane of the group); entries a pass does not compute are 0.
@@ -130,9 +174,8 @@ template <typename R, bool KAHAN, bool GRAD, bool HESS, bool THERMO, int G>
 __device__ void node_pass(const NodeView &nv, const PointIn &pt, const double *x, const double *M, int gl,
                           unsigned mask, PassSums &S, int64_t &evals) {
     constexpr int NS = 25;
-    double acc[NS];
-#pragma unroll
-    for (int i = 0; i < NS; ++i) acc[i] = 0.0;
+    PassAcc<R, KAHAN> acc;
+    acc.zero();
     const bool dedup = (M[1] == M[0]) && (pt.mu[1] == pt.mu[0]);
     const R *p2, *A, *c2, *B;
     if constexpr (sizeof(R) == 8) { p2 = (const R *)nv.p2; A = (const R *)nv.A; c2 = (const R *)nv.c2; B = (const R *)nv.B; }
@@ -161,59 +204,49 @@ __device__ void node_pass(const NodeView &nv, const PointIn &pt, const double *x
             }
         }
         const bool two = (f == 0 && dedup);
-        const double mult = two ? 2.0 : 1.0;
 #pragma unroll
         for (int j = 0; j < 2; ++j) {
             if (j == 1 && !two) break;
             const int ff = j == 0 ? f : 1;
-            if (GRAD) acc[0 + ff] = fa.DM.value();
+            if (GRAD) acc.set(0 + ff, fa.DM);
             if (HESS) {
-                acc[3 + ff] = fa.DMM.value();
-                acc[6 + ff] = sw ? fa.DMa.value() : fa.DMq.value();
-                acc[9 + ff] = sw ? fa.DMq.value() : fa.DMa.value();
+                acc.set(3 + ff, fa.DMM);
+                acc.set(6 + ff, sw ? fa.DMa : fa.DMq);
+                acc.set(9 + ff, sw ? fa.DMq : fa.DMa);
             }
             if (THERMO) {
-                acc[12 + ff] = sw ? fa.Na.value() : fa.Nq.value();
-                acc[15 + ff] = sw ? fa.Nq.value() : fa.Na.value();
+                acc.set(12 + ff, sw ? fa.Na : fa.Nq);
+                acc.set(15 + ff, sw ? fa.Nq : fa.Na);
             }
         }
         if (GRAD) {
-            acc[19] += mult * (sw ? fa.Sa.value() : fa.Sq.value());
-            acc[20] += mult * (sw ? fa.Sq.value() : fa.Sa.value());
+            acc.add(19, two, sw ? fa.Sa : fa.Sq);
+            acc.add(20, two, sw ? fa.Sq : fa.Sa);
         }
         if (HESS) {
-            acc[21] += mult * (sw ? fa.Saa.value() : fa.Sqq.value());
-            acc[22] += mult * fa.Sqa.value();
-            acc[23] += mult * (sw ? fa.Sqq.value() : fa.Saa.value());
+            acc.add(21, two, sw ? fa.Saa : fa.Sqq);
+            acc.add(22, two, fa.Sqa);
+            acc.add(23, two, sw ? fa.Sqq : fa.Saa);
         }
         if (THERMO) {
-            acc[18] += mult * fa.SL.value();
-            acc[24] += mult * fa.SAN.value();
+            acc.add(18, two, fa.SL);
+            acc.add(24, two, fa.SAN);
         }
         if (gl == 0) evals += (int64_t)n;
     }
+    double r[NS];
 #pragma unroll
     for (int i = 0; i < NS; ++i) {
         const bool used = (i < 3 || i == 19 || i == 20) ? GRAD
                           : (i < 12 || (i >= 21 && i <= 23)) ? HESS : THERMO;
-        if (!used) continue;
-        if constexpr (sizeof(R) == 4) {
-            // FP32 pass: reduce the compensated sums as float pairs (exact TwoSum on the
-            // high parts), so the lane reduction costs no FP64 instructions
-            float h = (float)acc[i];
-            float l = (float)(acc[i] - (double)h);
-            group_sum_ff<G>(h, l, mask);
-            acc[i] = (double)h + (double)l;
-        } else {
-            acc[i] = group_sum<G>(acc[i], mask);
-        }
+        r[i] = used ? acc.template reduce<G>(i, mask) : 0.0;
     }
     for (int f = 0; f < 3; ++f) {
-        S.DM[f] = acc[0 + f]; S.DMM[f] = acc[3 + f]; S.DMP[f] = acc[6 + f]; S.DMPb[f] = acc[9 + f];
-        S.Nq[f] = acc[12 + f]; S.Na[f] = acc[15 + f];
+        S.DM[f] = r[0 + f]; S.DMM[f] = r[3 + f]; S.DMP[f] = r[6 + f]; S.DMPb[f] = r[9 + f];
+        S.Nq[f] = r[12 + f]; S.Na[f] = r[15 + f];
     }
-    S.SL = acc[18]; S.SP = acc[19]; S.SPb = acc[20]; S.SPP = acc[21]; S.SPPb = acc[22]; S.SPbPb = acc[23];
-    S.SAN = acc[24];
+    S.SL = r[18]; S.SP = r[19]; S.SPb = r[20]; S.SPP = r[21]; S.SPPb = r[22]; S.SPbPb = r[23];
+    S.SAN = r[24];
 }
 
 // FP64 residual pass of the mixed solve's certification: the sums S.DM, S.SP, S.SPb of
@@ -476,9 +509,13 @@ __device__ void assemble(const DevParams &P, const PointIn &pt, const double *x,
 
 // ---------------------------------------------------------------------------------------
 // 5x5 dense LU with partial pivoting (first maximal pivot, as LAPACK getrf); returns
-// false when a pivot is exactly zero (Julia's SingularException).
+// false when a pivot is exactly zero (Julia's SingularException).  FAST (the mixed solver's
+// FP32-phase steps): each pivot's reciprocal is taken once, by rcp_normal, and multiplied in
+// -- LAPACK's dgetf2 scales the column by the pivot's reciprocal the same way -- instead of
+// 15 IEEE divisions.
+template <bool FAST = false>
 __device__ __forceinline__ bool lu_solve5(const double *Ain, const double *b, double *x) {
-    double A[25], y[5];
+    double A[25], y[5], inv[5];
 #pragma unroll
     for (int i = 0; i < 25; ++i) A[i] = Ain[i];
 #pragma unroll
@@ -504,9 +541,10 @@ __device__ __forceinline__ bool lu_solve5(const double *Ain, const double *b, do
             y[k] = y[p];
             y[p] = t;
         }
+        if (FAST) inv[k] = rcp_normal(A[k * 5 + k]);
 #pragma unroll
         for (int i = k + 1; i < 5; ++i) {
-            const double l = A[i * 5 + k] / A[k * 5 + k];
+            const double l = FAST ? A[i * 5 + k] * inv[k] : A[i * 5 + k] / A[k * 5 + k];
             A[i * 5 + k] = l;
 #pragma unroll
             for (int j = k + 1; j < 5; ++j) A[i * 5 + j] -= l * A[k * 5 + j];
@@ -518,7 +556,7 @@ __device__ __forceinline__ bool lu_solve5(const double *Ain, const double *b, do
         double s = y[i];
 #pragma unroll
         for (int j = i + 1; j < 5; ++j) s -= A[i * 5 + j] * y[j];
-        y[i] = s / A[i * 5 + i];
+        y[i] = FAST ? s * inv[i] : s / A[i * 5 + i];
     }
 #pragma unroll
     for (int i = 0; i < 5; ++i) x[i] = y[i];
