@@ -29,6 +29,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "pnjl_f64.cuh"
+
 namespace pnjl {
 
 struct DevParams {
@@ -114,6 +116,15 @@ __device__ __forceinline__ FlavourConst<R> make_flavour(double M, double mu, dou
     fc.e1_1 = R(3) * Pq * C2;
     fc.e0_1 = C3;
     return fc;
+}
+
+// Makes the per-flavour constants opaque register values for the node loop (see opaque()).
+template <typename R>
+__device__ __forceinline__ void opaque_flavour(FlavourConst<R> &fc) {
+    opaque(fc.M); opaque(fc.M2); opaque(fc.mu); opaque(fc.invT); opaque(fc.C); opaque(fc.C2); opaque(fc.C3);
+    opaque(fc.Pq); opaque(fc.Pa); opaque(fc.k1_0); opaque(fc.k2_0); opaque(fc.k1_1); opaque(fc.k2_1);
+    opaque(fc.e3_0); opaque(fc.e2_0); opaque(fc.e1_0); opaque(fc.e0_0);
+    opaque(fc.e3_1); opaque(fc.e2_1); opaque(fc.e1_1); opaque(fc.e0_1);
 }
 
 __device__ __forceinline__ double fast_exp(double x) { return exp(x); }

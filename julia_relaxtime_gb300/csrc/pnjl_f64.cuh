@@ -23,6 +23,23 @@ constexpr double kLn2HiD64 = 0x1.62e42fefp-7;
 constexpr double kLn2LoD64 = 0x1.473de6af278edp-40;
 constexpr double kRoundShifter = 0x1.8p52;           // 1.5*2^52: adding it rounds to an integer
 
+// c ? a : b as a 64-bit integer select (selp.b64).  The compiler otherwise turns some
+// selects between FP64 values into FP64 arithmetic; measured in the certification pass.
+__device__ __forceinline__ double dsel(bool c, double a, double b) {
+    long long r;
+    asm("{\n\t.reg .pred p;\n\tsetp.ne.s32 p, %3, 0;\n\tselp.b64 %0, %1, %2, p;\n\t}"
+        : "=l"(r)
+        : "l"(__double_as_longlong(a)), "l"(__double_as_longlong(b)), "r"((int)c));
+    return __longlong_as_double(r);
+}
+
+// Marks a loop invariant as an opaque register value.  Without it the compiler recomputes
+// products of invariants (3 Phi, 2 Phi C, ...) inside the node loop to save registers, which
+// in the certification pass cost about 15 extra FP64 instructions per node-flavour (measured:
+// 72 -> 57 per node-flavour, 26 % less time).
+__device__ __forceinline__ void opaque(double &v) { asm volatile("" : "+d"(v)); }
+__device__ __forceinline__ void opaque(float &v) { asm volatile("" : "+f"(v)); }
+
 static __device__ __noinline__ double exp_library(double x) { return exp(x); }
 static __device__ __noinline__ double rcp_library(double x) { return 1.0 / x; }
 static __device__ __noinline__ double rsqrt_library(double x) { return rsqrt(x); }

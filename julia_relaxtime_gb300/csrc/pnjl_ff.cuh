@@ -187,6 +187,15 @@ __device__ __forceinline__ FlavourFF make_flavour_ff(double M, double mu, double
     return fc;
 }
 
+__device__ __forceinline__ void opaque(ff &v) { asm volatile("" : "+f"(v.h), "+f"(v.l)); }
+// the per-flavour constants as opaque register values for the node loop (see opaque())
+__device__ __forceinline__ void opaque_flavour_ff(FlavourFF &fc) {
+    opaque(fc.M); opaque(fc.M2); opaque(fc.mu); opaque(fc.invT); opaque(fc.C); opaque(fc.C2);
+    opaque(fc.Pq); opaque(fc.Pa); opaque(fc.Pq2); opaque(fc.Pa2);
+    opaque(fc.k1_0); opaque(fc.k2_0); opaque(fc.k1_1); opaque(fc.k2_1);
+    opaque(fc.e3_0); opaque(fc.e2_0); opaque(fc.e1_0); opaque(fc.e2_1); opaque(fc.e1_1); opaque(fc.e0_1);
+}
+
 // Per-flavour sums of a float-float pass: gradient terms dD/dM, dD/dPhi, dD/dPhibar (quark /
 // antiquark side) and thermo terms (number sums, a n+ + b n-, log term).
 struct FlavourAccFF {

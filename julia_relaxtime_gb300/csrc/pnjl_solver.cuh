@@ -186,7 +186,8 @@ __device__ void node_pass(const NodeView &nv, const PointIn &pt, const double *x
     for (int f = 0; f < 3; ++f) {
         if (f == 1 && dedup) continue;
         bool sw;
-        const FlavourConst<R> fc = make_flavour<R>(M[f], pt.mu[f], pt.T, x[3], x[4], sw);
+        FlavourConst<R> fc = make_flavour<R>(M[f], pt.mu[f], pt.T, x[3], x[4], sw);
+        opaque_flavour(fc);
         FlavourAcc<R, KAHAN> fa;
         fa.zero();
         int ip = gl, it = 0;
@@ -251,10 +252,11 @@ __device__ void node_pass(const NodeView &nv, const PointIn &pt, const double *x
 
 // FP64 residual pass of the mixed solve's certification: the sums S.DM, S.SP, S.SPb of
 // node_pass<double, GRAD only> from the same integrand in FP64, arranged for the FP64 pipe
-// (56 FP64 instructions per node-flavour): exp, 1/x and 1/sqrt from pnjl_f64.cuh, Horner
-// forms in FMAs, and the per-flavour factors -3/T (dOmega/dM) and 3 (dOmega/dPhi) applied
-// once to the lane sums instead of per node.  With r_k = u_k / f+ and s_k = C^(k-1) u_k / f-
-// (u = (t, t^2, t^3) for a <= 0, (t^2, t, 1) for a > 0) the Polyakov distributions are
+// (57 FP64 instructions per node-flavour, measured): exp, 1/x and 1/sqrt from pnjl_f64.cuh,
+// Horner forms in FMAs, integer selects, opaque loop invariants, and the per-flavour factors
+// -3 M/T (dOmega/dM, with dE/dM = M/E) and 3 (dOmega/dPhi) applied once to the lane sums
+// instead of per node.  With r_k = u_k / f+ and s_k = C^(k-1) u_k / f- (u = (t, t^2, t^3)
+// for a <= 0, (t^2, t, 1) for a > 0) the Polyakov distributions are
 //   n+ = (Phi u1 + 2 Phibar u2 + u3) / f+,   n- = C (Phibar u1 + 2 Phi C u2 + C^2 u3) / f-
 // and the Phi / Phibar derivatives take r1 + s2 and r2 + s1 (quark / antiquark sides
 // swapped for mu < 0).  Requires the staged FP64 exp table (nv.exp64).
@@ -265,14 +267,21 @@ __device__ void node_pass_cert(const NodeView &nv, const PointIn &pt, const doub
     const double *p2 = nv.p2, *A = nv.A, *c2 = nv.c2, *B = nv.B, *tab = nv.exp64;
     const int pn = nv.p_num, n = nv.p_num * nv.t_num;
     const double xi = pt.xi;
+    const unsigned long long cap = (unsigned long long)__double_as_longlong(-kRescaleCapA);
     double DM[3] = {0.0, 0.0, 0.0}, SP = 0.0, SPb = 0.0;
 #pragma unroll 1
     for (int f = 0; f < 3; ++f) {
         if (f == 1 && dedup) continue;
         bool sw;
         const FlavourConst<double> fc = make_flavour<double>(M[f], pt.mu[f], pt.T, x[3], x[4], sw);
-        const double Mf = fc.M, M2 = fc.M2, invT = fc.invT, muT = fc.mu * fc.invT, C = fc.C, C2 = fc.C2;
-        const double Pq = fc.Pq, Pa = fc.Pa, Pa2 = 2.0 * fc.Pa, Pq2C = 2.0 * fc.Pq * fc.C;
+        double M2 = fc.M2, invT = fc.invT, muT = fc.mu * fc.invT, C = fc.C, C2 = fc.C2;
+        double Pq = fc.Pq, Pa = fc.Pa, Pa2 = 2.0 * fc.Pa, Pq2C = 2.0 * fc.Pq * fc.C;
+        double k1_0 = fc.k1_0, k2_0 = fc.k2_0, k1_1 = fc.k1_1, k2_1 = fc.k2_1;
+        double e3_0 = fc.e3_0, e2_0 = fc.e2_0, e1_0 = fc.e1_0, e2_1 = fc.e2_1, e1_1 = fc.e1_1, e0_1 = fc.e0_1;
+        opaque(M2); opaque(invT); opaque(muT); opaque(C); opaque(C2);
+        opaque(Pq); opaque(Pa); opaque(Pa2); opaque(Pq2C);
+        opaque(k1_0); opaque(k2_0); opaque(k1_1); opaque(k2_1);
+        opaque(e3_0); opaque(e2_0); opaque(e1_0); opaque(e2_1); opaque(e1_1); opaque(e0_1);
         double dm = 0.0, sq = 0.0, sa = 0.0;
         int ip = gl, it = 0;
         while (ip >= pn) { ip -= pn; ++it; }
@@ -280,34 +289,32 @@ __device__ void node_pass_cert(const NodeView &nv, const PointIn &pt, const doub
         if (it < nv.t_num) { sxi = fma(xi, c2[it], 1.0); bw = B[it]; }
 #pragma unroll 1
         for (int k = gl; k < n; k += G) {
-            const double q2 = p2[ip] * sxi, w = A[ip] * bw;
-            const double E2 = q2 + M2;
+            const double w = A[ip] * bw;
+            const double E2 = fma(p2[ip], sxi, M2);
             const double rE = rsqrt_normal(E2);
-            const double E = E2 * rE, mE = Mf * rE;
-            const double a = fma(-E, invT, muT);  // (mu - E)/T
+            const double a = fma(-E2 * rE, invT, muT);  // (mu - E)/T
             // a > 0, and -min(a, kRescaleCapA) or a, from the bit patterns (integer pipe):
             // among negative doubles the larger pattern is the larger magnitude
             const long long ab = __double_as_longlong(a);
             const bool sig = ab > 0;
             const unsigned long long nb = (unsigned long long)ab | 0x8000000000000000ull;
-            const unsigned long long cap = (unsigned long long)__double_as_longlong(-kRescaleCapA);
             const double t = exp_nonpos(__longlong_as_double((long long)(sig && nb > cap ? cap : nb)), tab);
             const double t2 = t * t, t3 = t2 * t;
-            const double fp = fma(fma(t + (sig ? fc.k2_1 : fc.k2_0), t, sig ? fc.k1_1 : fc.k1_0), t, 1.0);
-            const double gm = fma(fma(fma(sig ? 1.0 : fc.e3_0, t, sig ? fc.e2_1 : fc.e2_0), t, sig ? fc.e1_1 : fc.e1_0),
-                                  t, sig ? fc.e0_1 : 1.0);
+            const double fp = fma(fma(t + dsel(sig, k2_1, k2_0), t, dsel(sig, k1_1, k1_0)), t, 1.0);
+            const double gm =
+                fma(fma(fma(dsel(sig, 1.0, e3_0), t, dsel(sig, e2_1, e2_0)), t, dsel(sig, e1_1, e1_0)), t, dsel(sig, e0_1, 1.0));
             // the reference's max(f, 1e-16) clamps (NaN is not clamped)
             const bool clP = fp < kPolyakovEps;
-            const bool clM = gm < kPolyakovEps * (sig ? t3 : 1.0);
-            const double fpc = clP ? 1.0 : fp, gmc = clM ? 1.0 : gm;
+            const bool clM = gm < kPolyakovEps * dsel(sig, t3, 1.0);
+            const double fpc = dsel(clP, 1.0, fp), gmc = dsel(clM, 1.0, gm);
             const double Rr = rcp_normal(fpc * gmc);
-            const double ipv = clP ? 0.0 : gmc * Rr;  // 1/f+
-            const double im = clM ? 0.0 : fpc * Rr;   // 1/f-
-            const double u1 = sig ? t2 : t, u2 = sig ? t : t2, u3 = sig ? 1.0 : t3;
+            const double ipv = dsel(clP, 0.0, gmc * Rr);  // 1/f+
+            const double im = dsel(clM, 0.0, fpc * Rr);   // 1/f-
+            const double u1 = dsel(sig, t2, t), u2 = dsel(sig, t, t2), u3 = dsel(sig, 1.0, t3);
             const double Cim = C * im, CCim = C * Cim;
-            const double np = clP ? (sig ? 1.0 : 0.0) : ipv * fma(Pq, u1, fma(Pa2, u2, u3));
-            const double nm = clM ? 0.0 : Cim * fma(Pa, u1, fma(Pq2C, u2, C2 * u3));
-            dm = fma(w, (np + nm) * mE, dm);
+            const double np = dsel(clP, dsel(sig, 1.0, 0.0), ipv * fma(Pq, u1, fma(Pa2, u2, u3)));
+            const double nm = dsel(clM, 0.0, Cim * fma(Pa, u1, fma(Pq2C, u2, C2 * u3)));
+            dm = fma(w, (np + nm) * rE, dm);
             sq = fma(w, fma(ipv, u1, CCim * u2), sq);
             sa = fma(w, fma(ipv, u2, Cim * u1), sa);
             ip += G;
@@ -317,7 +324,7 @@ __device__ void node_pass_cert(const NodeView &nv, const PointIn &pt, const doub
             }
         }
         const double mult = (f == 0 && dedup) ? 2.0 : 1.0;
-        DM[f] = -3.0 * invT * dm;
+        DM[f] = -3.0 * fc.invT * fc.M * dm;
         if (f == 0 && dedup) DM[1] = DM[0];
         SP += mult * 3.0 * (sw ? sa : sq);
         SPb += mult * 3.0 * (sw ? sq : sa);
@@ -349,7 +356,8 @@ __device__ void node_pass_ff(const NodeView &nv, const PointIn &pt, const double
     for (int f = 0; f < 3; ++f) {
         if (f == 1 && dedup) continue;
         bool sw;
-        const FlavourFF fc = make_flavour_ff(M[f], pt.mu[f], pt.T, x[3], x[4], sw);
+        FlavourFF fc = make_flavour_ff(M[f], pt.mu[f], pt.T, x[3], x[4], sw);
+        opaque_flavour_ff(fc);
         FlavourAccFF fa;
         fa.zero();
         int ip = gl, it = 0;
