@@ -463,7 +463,9 @@ def main():
         best, tried = eng.autotune(n0, d_in["T"].data_ptr(), m0, m0, m0, d_in["xi"].data_ptr(), ptrs,
                                    seed_table=table, seed_table_hot=hot, opts=arm.opts, learned=arm.learned, reps=2)
         eng.synchronize()
-        tuning = {"chosen": best, "candidates": len(tried)}
+        tuning = {"chosen": best, "candidates": len(tried),
+                  "tried": [[t["blocks_per_sm"], t["pipeline_chunks"], round(t["ms"], 3)] for t in tried],
+                  "tried_fields": ["blocks_per_sm", "pipeline_chunks", "ms"]}
     main_rec = run_arm(arm, args.steps, args.warmup, True)
 
     # the dominant kernel's own launches, for the roofline: the fused kernel (one launch per

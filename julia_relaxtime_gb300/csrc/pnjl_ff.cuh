@@ -211,7 +211,7 @@ struct FlavourAccFF {
 // float-float), with the reference's clamps max(f, 1e-16) decided on the leading parts.
 template <bool GRAD, bool THERMO, bool HESS = false>
 __device__ __forceinline__ void node_flavour_ff(const FlavourFF &fc, ff q2, ff w, const float *etab,
-                                                FlavourAccFF &acc) {
+                                                FlavourAccFF &acc, bool thermo = true) {
     const ff E2 = ff_add(q2, fc.M2);
     const ff rE = ff_rsqrt(E2);
     const ff E = ff_mul(E2, rE);
@@ -280,7 +280,7 @@ __device__ __forceinline__ void node_flavour_ff(const FlavourFF &fc, ff q2, ff w
             acc.Saa = ff_add(acc.Saa, ff_mul_f(ff_mul(w, ff_add(ff_mul(r2, r2), ff_mul(s1, s1))), -9.0f));
         }
     }
-    if (THERMO) {
+    if (THERMO && thermo) {
         acc.Nq = ff_add(acc.Nq, ff_mul(w, np));
         acc.Na = ff_add(acc.Na, ff_mul(w, nm));
         const ff b = ff_sub(a, ff_mul_f(ff_mul(fc.mu, fc.invT), 2.0f));

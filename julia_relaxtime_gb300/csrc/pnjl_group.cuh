@@ -371,12 +371,20 @@ struct Group {
 
     // Residual at x from the float-float pass (FP32 pipe, ~1e-12 accurate); false when the
     // float-float tables are not staged or a sum is not finite (FP32 range exceeded).
+    // The float-float residual pass, with or without the thermo sums: one compiled loop for
+    // both (the two run back to back on every point, and one loop body keeps the instruction
+    // cache of an SM sub-partition freer for the other warps' loops).
+    __device__ __noinline__ void ff_pass_grad(const PointIn &pt, const double *x, const double *M, PassSums &S,
+                                              bool thermo, int64_t &evals) {
+        node_pass_ff<G, true, true>(nv, pt, x, M, gl, mask, S, evals, thermo);
+    }
+
     __device__ __noinline__ bool eval_grad_ff(const PointIn &pt, const double *x, double *F) {
         if (!nv.p2l) return false;
         double M[3];
         masses(P, x, M);
         PassSums S;
-        node_pass_ff<G, true, false>(nv, pt, x, M, gl, mask, S, cnt.v[kStatEvalsFF]);
+        ff_pass_grad(pt, x, M, S, false, cnt.v[kStatEvalsFF]);
         Eval ev;
         double V, V1[3], V2[3];
         vacuum_terms<G>(P, M, gl, mask, leader(), V, V1, V2);
@@ -415,7 +423,7 @@ struct Group {
         double M[3];
         masses(P, c.x, M);
         PassSums S;
-        node_pass_ff<G, true, true>(nv, pt, c.x, M, gl, mask, S, cnt.v[kStatEvalsFFGradThermo]);
+        ff_pass_grad(pt, c.x, M, S, true, cnt.v[kStatEvalsFFGradThermo]);
         Eval ev;
         double V, V1[3], V2[3];
         vacuum_terms<G>(P, M, gl, mask, leader(), V, V1, V2);

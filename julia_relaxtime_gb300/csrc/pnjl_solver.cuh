@@ -344,7 +344,8 @@ __device__ void node_pass_cert(const NodeView &nv, const PointIn &pt, const doub
 // staged float-float tables (nv.p2l != null).  Non-finite sums are returned as such.
 template <int G, bool GRAD, bool THERMO, bool HESS = false>
 __device__ void node_pass_ff(const NodeView &nv, const PointIn &pt, const double *x, const double *M, int gl,
-                             unsigned mask, PassSums &S, int64_t &evals) {
+                             unsigned mask, PassSums &S, int64_t &evals, bool thermo_rt = true) {
+    const bool TH = THERMO && thermo_rt;  // THERMO with a run-time switch: one loop serves both
     const bool dedup = (M[1] == M[0]) && (pt.mu[1] == pt.mu[0]);
     const int pn = nv.p_num, n = nv.p_num * nv.t_num;
     const ff xi = ff_from_double(pt.xi);
@@ -371,7 +372,7 @@ __device__ void node_pass_ff(const NodeView &nv, const PointIn &pt, const double
         for (int k = gl; k < n; k += G) {
             const ff q2 = ff_mul(ff{nv.p2f[ip], nv.p2l[ip]}, sxi);
             const ff w = ff_mul(ff{nv.Af[ip], nv.Al[ip]}, bw);
-            node_flavour_ff<GRAD, THERMO, HESS>(fc, q2, w, nv.expt, fa);
+            node_flavour_ff<GRAD, THERMO, HESS>(fc, q2, w, nv.expt, fa, TH);
             ip += G;
             if (ip >= pn) {
                 do { ip -= pn; ++it; } while (ip >= pn);
@@ -398,7 +399,7 @@ __device__ void node_pass_ff(const NodeView &nv, const PointIn &pt, const double
             SPPb = ff_add(SPPb, dbl(fa.Sqa));
             SPbPb = ff_add(SPbPb, dbl(sw ? fa.Sqq : fa.Saa));
         }
-        if (THERMO) {
+        if (TH) {
             Nq[f] = sw ? fa.Na : fa.Nq;
             Na[f] = sw ? fa.Nq : fa.Na;
             if (two) { Nq[1] = Nq[0]; Na[1] = Na[0]; }
@@ -409,16 +410,16 @@ __device__ void node_pass_ff(const NodeView &nv, const PointIn &pt, const double
     }
     for (int f = 0; f < 3; ++f) {
         S.DM[f] = GRAD ? ff_to_double(group_sum_ffv<G>(DM[f], mask)) : 0.0;
-        S.Nq[f] = THERMO ? ff_to_double(group_sum_ffv<G>(Nq[f], mask)) : 0.0;
-        S.Na[f] = THERMO ? ff_to_double(group_sum_ffv<G>(Na[f], mask)) : 0.0;
+        S.Nq[f] = TH ? ff_to_double(group_sum_ffv<G>(Nq[f], mask)) : 0.0;
+        S.Na[f] = TH ? ff_to_double(group_sum_ffv<G>(Na[f], mask)) : 0.0;
         S.DMM[f] = HESS ? ff_to_double(group_sum_ffv<G>(DMM[f], mask)) : 0.0;
         S.DMP[f] = HESS ? ff_to_double(group_sum_ffv<G>(DMP[f], mask)) : 0.0;
         S.DMPb[f] = HESS ? ff_to_double(group_sum_ffv<G>(DMPb[f], mask)) : 0.0;
     }
     S.SP = GRAD ? ff_to_double(group_sum_ffv<G>(SP, mask)) : 0.0;
     S.SPb = GRAD ? ff_to_double(group_sum_ffv<G>(SPb, mask)) : 0.0;
-    S.SAN = THERMO ? ff_to_double(group_sum_ffv<G>(SAN, mask)) : 0.0;
-    S.SL = THERMO ? ff_to_double(group_sum_ffv<G>(SL, mask)) : 0.0;
+    S.SAN = TH ? ff_to_double(group_sum_ffv<G>(SAN, mask)) : 0.0;
+    S.SL = TH ? ff_to_double(group_sum_ffv<G>(SL, mask)) : 0.0;
     S.SPP = HESS ? ff_to_double(group_sum_ffv<G>(SPP, mask)) : 0.0;
     S.SPPb = HESS ? ff_to_double(group_sum_ffv<G>(SPPb, mask)) : 0.0;
     S.SPbPb = HESS ? ff_to_double(group_sum_ffv<G>(SPbPb, mask)) : 0.0;
