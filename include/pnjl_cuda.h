@@ -267,11 +267,12 @@ int pnjl_autotune(pnjl_ctx *ctx, int64_t n, const double *d_T, const double *d_m
  * issued by one lane per warp (FLOP/s of the active lanes). */
 int pnjl_probe_peak(pnjl_ctx *ctx, int32_t kind, double *ops_per_s);
 
-/* Element-wise FP64 functions of the mixed solver's certification pass, for checking them
- * against the library functions (no counterpart in the reference): y[i] = f(x[i]) on the
- * device, host arrays of n.  fn 0: e^x by the table method (for -700 <= x <= 0; other x take
- * the library exp), 1: 1/x from the hardware approximation and a Newton correction, 2:
- * 1/sqrt(x) likewise; 3, 4, 5: the library exp, division and rsqrt. */
+/* Element-wise functions of the mixed solver's passes, for checking them against the library
+ * functions (no counterpart in the reference): y[i] = f(x[i]) on the device, host arrays of
+ * n.  fn 0: e^x by the FP64 table method (for -700 <= x <= 0; other x take the library exp),
+ * 1: 1/x from the hardware approximation and a Newton correction, 2: 1/sqrt(x) likewise; 3,
+ * 4, 5: the library exp, division and rsqrt; 6, 7: the float-float e^x and ln x of x rounded
+ * to a float pair (hi + lo returned). */
 int pnjl_f64_math(pnjl_ctx *ctx, int32_t fn, int64_t n, const double *x, double *y);
 
 /* ---- learned seed: MLP (T, mu, xi) -> (phi_u, phi_d, phi_s, Phi, Phibar) ----------------

@@ -25,13 +25,17 @@ struct ff {
     float h, l;
 };
 
-// exp tables in shared memory: e^k (k = -kExpMaxN..kExpMaxN) and e^(j/16) (j = -8..8), as (h, l)
-// float pairs, then (from float kExp64Offset, 8-byte aligned) the kExp64N doubles 2^(j/64) of
-// the FP64 exponential (pnjl_f64.cuh)
+// Function tables in shared memory, as (h, l) float pairs: e^k (k = -kExpMaxN..kExpMaxN),
+// e^(j/256) (j = 0..255), ln c_j and 1/c_j for c_j = 1 + (2j + 1)/256 (j = 0..127); then (from
+// float kExp64Offset, 8-byte aligned) the kExp64N doubles 2^(j/64) of the FP64 exponential
+// (pnjl_f64.cuh).
 constexpr int kExpMaxN = 88;
 constexpr int kExpIntN = 2 * kExpMaxN + 1;
-constexpr int kExpFracN = 17;
-constexpr int kExp64Offset = 2 * (kExpIntN + kExpFracN);
+constexpr int kExpFracN = 256;
+constexpr int kLogN = 128;
+constexpr int kExpFracOff = 2 * kExpIntN;             // floats
+constexpr int kLogOff = kExpFracOff + 2 * kExpFracN;  // ln c_j pairs, then 1/c_j pairs
+constexpr int kExp64Offset = kLogOff + 4 * kLogN;
 constexpr int kExpTableFloats = kExp64Offset + 2 * 64;
 static_assert(kExp64Offset % 2 == 0, "FP64 table alignment");
 
@@ -112,40 +116,49 @@ __device__ __forceinline__ ff ff_rsqrt(ff x) {
     return fast_two_sum(y0, __fmul_rn(__fmul_rn(y0, e), __fmaf_rn(e, 0.375f, 0.5f)));
 }
 
-// e^x for |x| <= 88 (0 below, +inf above): x = n + f with n = rint(x), |f| <= 1/2; f = j/16 + g
-// with |g| <= 1/32; e^g by Taylor to degree 7 (remainder below 2e-17), the terms from g^4 on
-// in FP32.
+// e^x for |x| <= 88 (0 below, +inf above), a table method: x = n + j/256 + g with
+// n + j/256 = round(256 x)/256 (j = 0..255) and |g| <= 1/512; e^x = e^n e^(j/256) e^g with
+// e^g = 1 + g + g^2/2 + g^3 (1/6 + g/24) -- the remainder g^5/120 is below 2.5e-16 -- where
+// g^2/2 is kept exact as a pair and the cubic tail, below 1.3e-9, in FP32.
 __device__ __forceinline__ ff ff_exp(ff x, const float *tab) {
     if (!(x.h > -88.0f)) return ff{0.0f, 0.0f};
     if (!(x.h < 88.0f)) return ff{__int_as_float(0x7f800000), 0.0f};
-    const float nf = rintf(x.h);
-    const int n = (int)nf;                           // -88..88
-    const ff f = two_sum(__fsub_rn(x.h, nf), x.l);  // x.h - nf is exact
-    const float jf = rintf(f.h * 16.0f);
-    const int j = (int)jf;  // -8..8
-    const ff g = fast_two_sum(__fsub_rn(f.h, jf * 0.0625f), f.l);
-    const float gh = g.h;
-    // q = 1/24 + g/120 + g^2/720 + g^3/5040
-    float q = __fmaf_rn(gh, 1.0f / 5040.0f, 1.0f / 720.0f);
-    q = __fmaf_rn(gh, q, 1.0f / 120.0f);
-    q = __fmaf_rn(gh, q, 1.0f / 24.0f);
-    // e^g = 1 + g + g^2 (1/2 + g (1/6 + g q))
-    const ff sixth{0.166666671633720398f, -4.96705388e-09f};  // 1/6 as float-float
-    ff u = ff_add(sixth, two_prod(gh, q));
-    u = ff_add_f(ff_mul(g, u), 0.5f);
-    u = ff_mul(ff_mul(g, g), u);
-    const ff eg = ff_add(ff_add_f(g, 1.0f), u);
+    const float mf = rintf(x.h * 256.0f);
+    const int m = (int)mf;
+    const int n = m >> 8, j = m & 255;                    // m = 256 n + j
+    const ff g = two_sum(__fsub_rn(x.h, mf * 0.00390625f), x.l);  // x.h - m/256 is exact
+    ff q = two_prod(g.h, g.h);                            // g^2 (+ the g.h g.l cross term)
+    q.l = __fmaf_rn(2.0f * g.h, g.l, q.l);
+    const float tail = __fmul_rn(__fmul_rn(q.h, g.h), __fmaf_rn(g.h, 1.0f / 24.0f, 1.0f / 6.0f));
+    const ff s = two_sum(1.0f, g.h);
+    const ff eg = ff_add(s, ff{0.5f * q.h, __fadd_rn(__fadd_rn(0.5f * q.l, g.l), tail)});
     const ff en{tab[2 * (n + kExpMaxN)], tab[2 * (n + kExpMaxN) + 1]};
-    const ff ej{tab[2 * (kExpIntN + j + 8)], tab[2 * (kExpIntN + j + 8) + 1]};
+    const ff ej{tab[kExpFracOff + 2 * j], tab[kExpFracOff + 2 * j + 1]};
     return ff_mul(ff_mul(en, ej), eg);
 }
 
-// ln x for x > 0: one Newton step y = y0 + x e^-y0 - 1 from the FP32 logarithm (its error
-// squares: ~1e-7 -> ~1e-14).
+// ln x for positive normal x: x = 2^k m (m in [1, 2)), c the centre of m's 1/128-wide
+// interval, u = (m - c)/c with |u| <= 1/257, ln x = k ln2 + ln c + log1p(u),
+// log1p(u) = u - u^2/2 + u^3 (1/3 - u/4 + u^2/5 - u^3/6) (remainder below 3e-17), with u^2
+// exact as a pair and the cubic tail in FP32.
 __device__ __forceinline__ ff ff_log(ff x, const float *tab) {
-    const float y0 = logf(x.h);
-    const ff e = ff_mul(x, ff_exp(ff_make(-y0), tab));
-    return ff_add_f(ff_add_f(e, -1.0f), y0);
+    if (!(x.h >= 1.17549435e-38f && x.h < 1.7014118e38f)) return ff{__int_as_float(0x7fc00000), 0.0f};
+    const unsigned b = __float_as_uint(x.h);
+    const int k = (int)((b >> 23) & 0xffu) - 127;
+    const int j = (int)((b >> 16) & 0x7fu);               // top 7 bits of the significand
+    const float mh = __uint_as_float((b & 0x007fffffu) | 0x3f800000u);
+    const float ml = __fmul_rn(x.l, __uint_as_float((unsigned)(127 - k) << 23));  // x.l 2^-k (exact)
+    const float c = __fmaf_rn((float)j, 0.0078125f, 1.00390625f);                 // 1 + (2j + 1)/256
+    const ff d = two_sum(__fsub_rn(mh, c), ml);           // m - c (the subtraction is exact)
+    const ff u = ff_mul(d, ff{tab[kLogOff + 2 * kLogN + 2 * j], tab[kLogOff + 2 * kLogN + 2 * j + 1]});
+    ff q = two_prod(u.h, u.h);
+    q.l = __fmaf_rn(2.0f * u.h, u.l, q.l);
+    const float p = __fmaf_rn(__fmaf_rn(__fmaf_rn(u.h, -1.0f / 6.0f, 0.2f), u.h, -0.25f), u.h, 1.0f / 3.0f);
+    const float tail = __fmul_rn(__fmul_rn(q.h, u.h), p);
+    const ff l1p = ff_add(u, ff{-0.5f * q.h, __fadd_rn(-0.5f * q.l, tail)});
+    const ff kl = ff_mul_f(ff{0x1.62e43p-1f, -0x1.05c61p-29f}, (float)k);  // k ln2 (ln2 as a pair)
+    const ff lc{tab[kLogOff + 2 * j], tab[kLogOff + 2 * j + 1]};
+    return ff_add(ff_add(kl, lc), l1p);
 }
 
 // Per-flavour constants of a float-float pass (the same branch-free form as FlavourConst).

@@ -82,25 +82,26 @@ inline void separable_tables(int p_num, int t_num, const double *xp, const doubl
         for (int i = 0; i < m; ++i) hl[i] = (float)(h[i] - (double)hf[i]);
 }
 
-// exp tables (pnjl_ff.cuh, pnjl_f64.cuh): e^k for k = -kExpMaxN..kExpMaxN, then e^(j/16) for
-// j = -8..8, each as (hi, lo) floats, from long-double exp; then 2^(j/64), j = 0..63, as
-// doubles rounded from long-double exp2.
+// Function tables (pnjl_ff.cuh, pnjl_f64.cuh), from long-double exp / log: e^k for
+// k = -kExpMaxN..kExpMaxN and e^(j/256) for j = 0..255, ln c_j and 1/c_j for
+// c_j = 1 + (2j + 1)/256, j = 0..127, each as a (hi, lo) float pair; then 2^(j/64),
+// j = 0..63, as doubles.
+inline void ff_pair_into(long double v, float *out) {
+    const float h = (float)v;
+    out[0] = h;
+    out[1] = (float)(v - (long double)h);
+}
 inline void ff_exp_tables(float *out) {
+    for (int k = -kExpMaxN; k <= kExpMaxN; ++k) ff_pair_into(expl((long double)k), out + 2 * (k + kExpMaxN));
+    for (int j = 0; j < kExpFracN; ++j) ff_pair_into(expl((long double)j / 256.0L), out + kExpFracOff + 2 * j);
+    for (int j = 0; j < kLogN; ++j) {
+        const long double c = 1.0L + (2.0L * j + 1.0L) / 256.0L;
+        ff_pair_into(logl(c), out + kLogOff + 2 * j);
+        ff_pair_into(1.0L / c, out + kLogOff + 2 * kLogN + 2 * j);
+    }
     for (int j = 0; j < kExp64N; ++j) {
         const double v = (double)exp2l((long double)j / 64.0L);
         std::memcpy(out + kExp64Offset + 2 * j, &v, sizeof v);
-    }
-    for (int k = -kExpMaxN; k <= kExpMaxN; ++k) {
-        const long double v = expl((long double)k);
-        const float h = (float)v;
-        out[2 * (k + kExpMaxN)] = h;
-        out[2 * (k + kExpMaxN) + 1] = (float)(v - (long double)h);
-    }
-    for (int j = -8; j <= 8; ++j) {
-        const long double v = expl((long double)j / 16.0L);
-        const float h = (float)v;
-        out[2 * (kExpIntN + j + 8)] = h;
-        out[2 * (kExpIntN + j + 8) + 1] = (float)(v - (long double)h);
     }
 }
 

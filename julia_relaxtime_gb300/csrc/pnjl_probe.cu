@@ -53,12 +53,14 @@ __global__ void __launch_bounds__(256) ex2_probe(float *out, int iters) {
     out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
-// y[i] = f(x[i]): fn 0 exp_nonpos, 1 rcp_normal, 2 rsqrt_normal, 3 exp, 4 1/x, 5 rsqrt
+// y[i] = f(x[i]): fn 0 exp_nonpos, 1 rcp_normal, 2 rsqrt_normal, 3 exp, 4 1/x, 5 rsqrt,
+// 6 ff_exp, 7 ff_log (of x as a float-float pair, returned as hi + lo)
 __global__ void __launch_bounds__(256) f64_math_kernel(int fn, int64_t n, const double *x, double *y,
-                                                       const double *tab_global) {
-    __shared__ double tab[kExp64N];
-    for (int i = threadIdx.x; i < kExp64N; i += blockDim.x) tab[i] = tab_global[i];
+                                                       const float *tab_global) {
+    __shared__ __align__(16) float tabf[kExpTableFloats];
+    for (int i = threadIdx.x; i < kExpTableFloats; i += blockDim.x) tabf[i] = tab_global[i];
     __syncthreads();
+    const double *tab = (const double *)(tabf + kExp64Offset);
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const double v = x[i];
         double r;
@@ -68,7 +70,9 @@ __global__ void __launch_bounds__(256) f64_math_kernel(int fn, int64_t n, const 
             case 2: r = rsqrt_normal(v); break;
             case 3: r = exp(v); break;
             case 4: r = 1.0 / v; break;
-            default: r = rsqrt(v); break;
+            case 5: r = rsqrt(v); break;
+            case 6: r = ff_to_double(ff_exp(ff_from_double(v), tabf)); break;
+            default: r = ff_to_double(ff_log(ff_from_double(v), tabf)); break;
         }
         y[i] = r;
     }
@@ -77,18 +81,19 @@ __global__ void __launch_bounds__(256) f64_math_kernel(int fn, int64_t n, const 
 }  // namespace pnjl
 
 extern "C" int pnjl_f64_math_impl(int device, int fn, int64_t n, const double *x, double *y) {
-    if (fn < 0 || fn > 5 || n < 0 || (n > 0 && (!x || !y))) return PNJL_ERR_INVALID_ARGUMENT;
+    if (fn < 0 || fn > 7 || n < 0 || (n > 0 && (!x || !y))) return PNJL_ERR_INVALID_ARGUMENT;
     if (n == 0) return PNJL_OK;
     if (cudaSetDevice(device) != cudaSuccess) return PNJL_ERR_CUDA;
     std::vector<float> tabs(pnjl::kExpTableFloats);
     pnjl::ff_exp_tables(tabs.data());
     double *d = nullptr;
     const size_t bytes = (size_t)n * sizeof(double);
-    if (cudaMalloc(&d, 2 * bytes + pnjl::kExp64N * sizeof(double)) != cudaSuccess) return PNJL_ERR_OUT_OF_MEMORY;
-    double *dx = d, *dy = d + n, *dt = d + 2 * n;
+    if (cudaMalloc(&d, 2 * bytes + pnjl::kExpTableFloats * sizeof(float)) != cudaSuccess) return PNJL_ERR_OUT_OF_MEMORY;
+    double *dx = d, *dy = d + n;
+    float *dt = (float *)(d + 2 * n);
     cudaError_t e = cudaMemcpy(dx, x, bytes, cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
-        e = cudaMemcpy(dt, tabs.data() + pnjl::kExp64Offset, pnjl::kExp64N * sizeof(double), cudaMemcpyHostToDevice);
+        e = cudaMemcpy(dt, tabs.data(), pnjl::kExpTableFloats * sizeof(float), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
         const int64_t blocks = std::min<int64_t>((n + 255) / 256, 4096);
         pnjl::f64_math_kernel<<<(int)blocks, 256>>>(fn, n, dx, dy, dt);

@@ -293,9 +293,10 @@ class GapEngine:
         return float(v.value)
 
     def f64_math(self, fn: str, x) -> np.ndarray:
-        """Element-wise FP64 function of the certification pass on the device (pnjl_f64_math):
-        "exp", "rcp", "rsqrt" (the pass's own) or "exp_lib", "rcp_lib", "rsqrt_lib"."""
-        k = {"exp": 0, "rcp": 1, "rsqrt": 2, "exp_lib": 3, "rcp_lib": 4, "rsqrt_lib": 5}[fn]
+        """Element-wise function on the device (pnjl_f64_math): "exp", "rcp", "rsqrt" (the FP64
+        certification pass's own), "exp_lib", "rcp_lib", "rsqrt_lib" (the library's), or
+        "ff_exp", "ff_log" (the float-float passes', on x rounded to a float pair)."""
+        k = {"exp": 0, "rcp": 1, "rsqrt": 2, "exp_lib": 3, "rcp_lib": 4, "rsqrt_lib": 5, "ff_exp": 6, "ff_log": 7}[fn]
         x = np.ascontiguousarray(x, dtype=np.float64)
         y = np.empty_like(x)
         dp = C.POINTER(C.c_double)

@@ -147,6 +147,35 @@ def test_f64_math_functions_within_ulps(engine_factory):
     np.testing.assert_array_equal(eng.f64_math("rsqrt", edge), eng.f64_math("rsqrt_lib", edge))
 
 
+def test_ff_exp_log_accuracy(engine_factory):
+    """Float-float e^x and ln x of the mixed solver's passes (tables of e^k, e^(j/256), ln c_j,
+    1/c_j): within 2e-14 relative (ln x: of max(|ln x|, 1)) of long-double references at the
+    float-pair value of x."""
+    eng = engine_factory(12, 6)
+    rng = np.random.default_rng(5)
+    ld = np.longdouble
+
+    def pair(x):
+        h = x.astype(np.float32).astype(np.float64)
+        return h + (x - h).astype(np.float32).astype(np.float64)
+
+    # float-pair precision holds while the low part is a normal float: e^x >= 2^-102 (x >= -70)
+    x = pair(np.concatenate([rng.uniform(-70.0, 87.9, 20000), rng.uniform(-1e-3, 1e-3, 2000),
+                             [0.0, -0.5 / 256, 1.0 / 512, -70.0, 87.5]]))
+    y = eng.f64_math("ff_exp", x)
+    ref = np.exp(x.astype(ld))
+    assert np.max(np.abs((y - ref) / ref)) <= 2e-14
+    x = pair(rng.uniform(-87.0, -70.0, 2000))  # below: the resolution of the high part (subnormal at the end)
+    y = eng.f64_math("ff_exp", x)
+    ref = np.exp(x.astype(ld))
+    assert np.max(np.abs((y - ref) / ref)) <= 1e-6
+    x = pair(np.concatenate([np.exp(rng.uniform(-80, 80, 20000)), rng.uniform(0.99, 1.01, 2000),
+                             [1.0, 2.0, 0.5, 1.00390625, 1.99999]]))
+    y = eng.f64_math("ff_log", x)
+    ref = np.log(x.astype(ld))
+    assert np.max(np.abs(y - ref) / np.maximum(np.abs(ref), 1.0)) <= 2e-14
+
+
 def test_thermo_matches_oracle(engine_factory, P):
     eng = engine_factory(64, 8)
     nd = orc.Nodes(64, 8)
