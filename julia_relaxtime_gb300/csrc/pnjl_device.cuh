@@ -130,7 +130,12 @@ __device__ __forceinline__ void opaque_flavour(FlavourConst<R> &fc) {
 __device__ __forceinline__ double fast_exp(double x) { return exp(x); }
 __device__ __forceinline__ float fast_exp(float x) { return __expf(x); }
 __device__ __forceinline__ double fast_rcp(double x) { return 1.0 / x; }
-__device__ __forceinline__ float fast_rcp(float x) { return __frcp_rn(x); }
+// hardware approximation (MUFU, ~1 ulp): the FP32 passes' error budget is far above it
+__device__ __forceinline__ float fast_rcp(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 __device__ __forceinline__ double fast_rsqrt(double x) { return rsqrt(x); }
 __device__ __forceinline__ float fast_rsqrt(float x) { return rsqrtf(x); }
 __device__ __forceinline__ double fast_log(double x) { return log(x); }
@@ -160,7 +165,11 @@ struct Acc<float, true> {
 // Per-flavour accumulators of one lane over its share of the nodes.
 template <typename R, bool KAHAN>
 struct FlavourAcc {
-    Acc<R, KAHAN> DM, DMM, DMq, DMa, Nq, Na, SL, Sq, Sa, Sqq, Sqa, Saa, SAN;
+    Acc<R, KAHAN> DM, Nq, Na, SL, Sq, Sa, SAN;
+    // second derivatives (the Jacobian of the FP32 Newton steps): plain sums -- their lane
+    // sums carry ~1e-6 relative error, far below what the steps and the refinement's
+    // secant updates tolerate
+    Acc<R, false> DMM, DMq, DMa, Sqq, Sqa, Saa;
     __device__ __forceinline__ void zero() {
         DM.zero(); DMM.zero(); DMq.zero(); DMa.zero(); Nq.zero(); Na.zero();
         SL.zero(); Sq.zero(); Sa.zero(); Sqq.zero(); Sqa.zero(); Saa.zero(); SAN.zero();

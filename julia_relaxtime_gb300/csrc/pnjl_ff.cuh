@@ -95,20 +95,22 @@ __device__ __forceinline__ ff ff_mul_f(ff a, float b) {
 }
 __device__ __forceinline__ ff ff_sel(bool c, ff a, ff b) { return ff{c ? a.h : b.h, c ? a.l : b.l}; }
 
-// 1/b: one Newton step y = y0 + y0 e, e = 1 - b y0, from the correctly rounded FP32
-// reciprocal y0.  1 - b.h y0 is exactly representable (|e| < 2^-23 with bits down to
-// 2^-48), so one FMA gives it; the b.l term is small.  Relative error ~e^2 + 2^-48.
+// 1/b: one Newton step y = y0 + y0 e, e = 1 - b y0, from the hardware FP32 reciprocal y0
+// (~1 ulp).  1 - b.h y0 is exactly representable (|e| < 2^-22 with bits down to 2^-47), so
+// one FMA gives it; the b.l term is small.  Relative error ~e^2 + 2^-48.
 __device__ __forceinline__ ff ff_rcp(ff b) {
-    const float y0 = __frcp_rn(b.h);
+    float y0;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y0) : "f"(b.h));
     float e = __fmaf_rn(-b.h, y0, 1.0f);
     e = __fmaf_rn(-b.l, y0, e);
     return fast_two_sum(y0, __fmul_rn(y0, e));
 }
 
-// 1/sqrt(x): y = y0 (1 + e/2 + 3e^2/8), e = 1 - x y0^2, from the correctly rounded FP32 value
-// y0 (y0^2 exact as a pair; 1 - x.h y0^2 is again exact in one FMA).
+// 1/sqrt(x): y = y0 (1 + e/2 + 3e^2/8), e = 1 - x y0^2, from the hardware FP32 value y0
+// (~2 ulp; y0^2 exact as a pair, 1 - x.h y0^2 within 2^-47 in one FMA; the remainder of the
+// series is ~e^3).
 __device__ __forceinline__ ff ff_rsqrt(ff x) {
-    const float y0 = __frsqrt_rn(x.h);
+    const float y0 = rsqrtf(x.h);
     const ff p = two_prod(y0, y0);
     float e = __fmaf_rn(-x.h, p.h, 1.0f);
     e = __fmaf_rn(-x.h, p.l, e);

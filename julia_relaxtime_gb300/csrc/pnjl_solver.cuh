@@ -150,6 +150,13 @@ struct PassAcc<float, true> {
         for (int i = 0; i < 25; ++i) h[i] = l[i] = 0.0f;
     }
     __device__ __forceinline__ void set(int i, const Acc<float, true> &a) { h[i] = a.s; l[i] = -a.c; }
+    __device__ __forceinline__ void set(int i, const Acc<float, false> &a) { h[i] = a.s; l[i] = 0.0f; }
+    __device__ __forceinline__ void add(int i, bool twice, const Acc<float, false> &a) {
+        Acc<float, true> k;
+        k.s = a.s;
+        k.c = 0.0f;
+        add(i, twice, k);
+    }
     __device__ __forceinline__ void add(int i, bool twice, const Acc<float, true> &a) {
         const float m = twice ? 2.0f : 1.0f;  // exact scaling
         const float bh = m * a.s, bl = -m * a.c;
