@@ -255,7 +255,7 @@ constexpr unsigned kIdleSleepNs = 500;
 // start as soon as their point is listed and share the GPU with the remaining points, instead
 // of forming a second launch whose elapsed time is set by its longest seeds.
 template <int G>
-__global__ void __launch_bounds__(kSolveThreads, 2) mixed_fused_kernel(SolveArgs a) {
+__global__ void __launch_bounds__(kSolveThreads, 1) mixed_fused_kernel(SolveArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const NodeView nv = stage_nodes(a.nodes, smem_raw);
     __syncthreads();
