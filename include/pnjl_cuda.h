@@ -52,6 +52,8 @@ extern "C" {
                              solver refines with (gradient and Hessian; omega is NaN)       */
 #define PNJL_PREC_FP64_CERT 3 /* pnjl_eval_batch only: the FP64 residual pass that certifies
                              the mixed solver's roots (gradient; omega, Hessian NaN)        */
+#define PNJL_PREC_FP32_NEWTON 4 /* pnjl_eval_batch only: the FP32 pass of the mixed solver's
+                             Newton steps (gradient and Hessian; omega NaN)                 */
 
 /* Model constants in fm units; src/Constants_PNJL.jl:82-103 (hbarc, N_color, rho0,
  * Lambda, G, K, m_ud0, m_s0, T0, a0, a1, a2, b3). */
@@ -187,8 +189,8 @@ int pnjl_get_nodes(const pnjl_ctx *ctx, double *p_mesh, double *c_mesh, double *
  * calculate_omega (Thermodynamics.jl:181-195) and the ForwardDiff gradient/Jacobian of
  * gap_conditions (Conditions.jl:72-86; F = -grad_x Omega).  precision: PNJL_PREC_FP64,
  * PNJL_PREC_MIXED (FP32-Kahan integrand, FP64 assembly), PNJL_PREC_FF_RESIDUAL (float-float
- * gradient and Hessian) or PNJL_PREC_FP64_CERT (gradient from the certification pass).  Host
- * pointers; NULL skips. */
+ * gradient and Hessian), PNJL_PREC_FP64_CERT (gradient from the certification pass) or
+ * PNJL_PREC_FP32_NEWTON (the mixed solver's FP32 Newton pass).  Host pointers; NULL skips. */
 int pnjl_eval_batch(pnjl_ctx *ctx, int64_t n, const double *x, const double *T,
                     const double *mu_u, const double *mu_d, const double *mu_s,
                     const double *xi, int32_t precision,

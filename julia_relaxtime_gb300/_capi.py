@@ -35,6 +35,7 @@ PNJL_PREC_FP64 = 0
 PNJL_PREC_MIXED = 1
 PNJL_PREC_FF_RESIDUAL = 2  # pnjl_eval_batch only
 PNJL_PREC_FP64_CERT = 3  # pnjl_eval_batch only
+PNJL_PREC_FP32_NEWTON = 4  # pnjl_eval_batch only
 
 dp = C.POINTER(C.c_double)
 i32p = C.POINTER(C.c_int32)

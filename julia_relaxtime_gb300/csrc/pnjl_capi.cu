@@ -394,9 +394,10 @@ static int eval_common(pnjl_ctx *ctx, int64_t n, const double *x, const double *
     if (n < 0 || (n > 0 && (!x || !T || !mu_u || !mu_d || !mu_s || !xi)))
         return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "null input array");
     if (precision != PNJL_PREC_FP64 && precision != PNJL_PREC_MIXED && precision != PNJL_PREC_FF_RESIDUAL &&
-        precision != PNJL_PREC_FP64_CERT)
+        precision != PNJL_PREC_FP64_CERT && precision != PNJL_PREC_FP32_NEWTON)
         return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "unknown precision");
-    if ((precision == PNJL_PREC_FF_RESIDUAL || precision == PNJL_PREC_FP64_CERT) && out)
+    if ((precision == PNJL_PREC_FF_RESIDUAL || precision == PNJL_PREC_FP64_CERT ||
+         precision == PNJL_PREC_FP32_NEWTON) && out)
         return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "this pass gives the residual only");
     if (n == 0) return PNJL_OK;
     cudaSetDevice(ctx->device);
@@ -431,7 +432,7 @@ static int eval_common(pnjl_ctx *ctx, int64_t n, const double *x, const double *
     pnjl::EvalArgs a{};
     a.P = ctx->dp;
     a.nodes = kernel_nodes(ctx);
-    const int mode = precision;  // 0 FP64, 1 FP32-Kahan, 2 float-float residual, 3 FP64 certification
+    const int mode = precision;  // 0 FP64, 1 FP32-Kahan, 2 float-float, 3 FP64 certification, 4 FP32 Newton
     const size_t smem = pnjl::node_smem_bytes(ctx->p_num, ctx->t_num);
     a.n = n;
     a.x = dx; a.T = dT; a.mu_u = du; a.mu_d = dd; a.mu_s = ds; a.xi = dxi;

@@ -325,7 +325,7 @@ struct Group {
         double M[3];
         masses(P, x, M);
         PassSums S;
-        node_pass<float, true, true, true, false, G>(nv, pt, x, M, gl, mask, S, cnt.v[kStatEvals32]);
+        node_pass_newton32<G>(nv, pt, x, M, gl, mask, S, cnt.v[kStatEvals32]);
         Eval ev;
         double V, V1[3], V2[3];
         vacuum_terms<G>(P, M, gl, mask, leader(), V, V1, V2);

@@ -149,7 +149,8 @@ __global__ void __launch_bounds__(kSolveThreads, 2) solve_kernel(SolveArgs a) {
 
 // One full pass + assembly per state: Omega, grad_x Omega, Hessian_x Omega and thermo
 // (MODE 0 FP64, 1 FP32-Kahan); MODE 2: the float-float residual and Jacobian pass alone;
-// MODE 3: the FP64 certification residual pass (node_pass_cert) alone.
+// MODE 3: the FP64 certification residual pass (node_pass_cert) alone; MODE 4: the FP32 Newton
+// pass (node_pass_newton32: residual and Jacobian).
 template <int G, int MODE>
 __global__ void __launch_bounds__(kSolveThreads) eval_kernel(EvalArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -176,18 +177,20 @@ __global__ void __launch_bounds__(kSolveThreads) eval_kernel(EvalArgs a) {
         PassSums S;
         Eval ev;
         double V, V1[3], V2[3];
-        if constexpr (MODE == 2 || MODE == 3) {
+        if constexpr (MODE >= 2) {
             if constexpr (MODE == 2) {
                 node_pass_ff<G, true, false, true>(nv, pt, x, M, gl, mask, S, evals);
-            } else {
+            } else if constexpr (MODE == 3) {
                 node_pass_cert<G>(nv, pt, x, M, gl, mask, S, evals);
+            } else {
+                node_pass_newton32<G>(nv, pt, x, M, gl, mask, S, evals);
             }
             vacuum_terms<G>(a.P, M, gl, mask, lane & ~(G - 1), V, V1, V2);
-            assemble<true, MODE == 2, false>(a.P, pt, x, M, S, V, V1, V2, ev);
+            assemble<true, MODE != 3, false>(a.P, pt, x, M, S, V, V1, V2, ev);
             if (gl == 0) {
                 if (a.omega) a.omega[i] = qnan();
                 if (a.grad) for (int k = 0; k < 5; ++k) a.grad[5 * i + k] = -ev.F[k];
-                if (a.hess) for (int k = 0; k < 25; ++k) a.hess[25 * i + k] = MODE == 2 ? -ev.J[k] : qnan();
+                if (a.hess) for (int k = 0; k < 25; ++k) a.hess[25 * i + k] = MODE != 3 ? -ev.J[k] : qnan();
             }
             continue;
         } else if constexpr (MODE == 1) {
@@ -247,6 +250,7 @@ cudaError_t launch_eval(const EvalArgs &a, int mode, int grid, size_t smem, cuda
         case 1: return launch_eval_g<32, 1>(a, grid, smem, s);
         case 2: return launch_eval_g<32, 2>(a, grid, smem, s);
         case 3: return launch_eval_g<32, 3>(a, grid, smem, s);
+        case 4: return launch_eval_g<32, 4>(a, grid, smem, s);
         default: return cudaErrorInvalidValue;
     }
 }

@@ -257,6 +257,146 @@ __device__ void node_pass(const NodeView &nv, const PointIn &pt, const double *x
     S.SAN = r[24];
 }
 
+// FP32 Newton pass of the mixed solver: the residual and Jacobian sums of
+// node_pass<float, KAHAN, GRAD, HESS> in a form with fewer instructions per node-flavour --
+// it runs on most of the solver's node evaluations.  Per node, with u, r_k = u_k/f+,
+// s_k = C^(k-1) u_k/f-, n+ and n- as in node_pass_cert, and m = M/E:
+//   D   = sum w (n+ + n-) m                       -> S.DM  = -3/T D
+//   Q   = sum w (r1 + s2),  A = sum w (r2 + s1)   -> S.SP, S.SPb = 3 Q, 3 A (sides by mu's sign)
+//   H1  = sum w (L++ + L--) m^2,  H2 = sum w (n+ + n-)(1 - m^2)/E
+//                                                 -> S.DMM = H1/T^2 - 3 H2/T
+//       with L++ = 3 n+ + 6 (Phibar r2 + r3) - 9 n+^2, L-- = 3 n- + 6 (Phi s2 + s3) - 9 n-^2
+//   Pq  = sum w m (r1 (1 - 3n+) + s2 (2 - 3n-)), Pa = sum w m (r2 (2 - 3n+) + s1 (1 - 3n-))
+//                                                 -> S.DMP, S.DMPb = -3/T Pq, -3/T Pa
+//   Sqq, Sqa, Saa = sum w (r1^2 + s2^2), (r1 r2 + s1 s2), (r2^2 + s1^2) -> times -9
+// (the second derivatives of node_flavour regrouped; a clamped factor contributes no Phi
+// terms).  The three residual sums are Kahan-compensated, the Jacobian's plain; all are
+// reduced over the lanes as float pairs.
+template <int G>
+__device__ void node_pass_newton32(const NodeView &nv, const PointIn &pt, const double *x, const double *M, int gl,
+                                   unsigned mask, PassSums &S, int64_t &evals) {
+    const bool dedup = (M[1] == M[0]) && (pt.mu[1] == pt.mu[0]);
+    const float *p2 = nv.p2f, *A = nv.Af, *c2 = nv.c2f, *B = nv.Bf;
+    const int pn = nv.p_num, n = nv.p_num * nv.t_num;
+    const float xi = (float)pt.xi;
+    // per-flavour results (lane partials) as float pairs: 0 D, 1 H1, 2 H2, 3 Pq, 4 Pa
+    float fh[3][5], fl[3][5];
+    // side sums over the flavours: 0 Q-side (Phi), 1 A-side (Phibar), 2 Sqq-side, 3 Sqa, 4 Saa-side
+    float sh[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, sl[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    auto pair_add = [](float &h, float &l, float bh, float bl) {
+        const float sum = __fadd_rn(h, bh);
+        const float hp = __fsub_rn(sum, bh);
+        const float err = __fadd_rn(__fsub_rn(h, hp), __fsub_rn(bh, __fsub_rn(sum, hp)));
+        l = __fadd_rn(__fadd_rn(l, bl), err);
+        h = sum;
+    };
+    for (int f = 0; f < 3; ++f)
+        for (int k = 0; k < 5; ++k) fh[f][k] = fl[f][k] = 0.0f;
+#pragma unroll 1
+    for (int f = 0; f < 3; ++f) {
+        if (f == 1 && dedup) continue;
+        bool sw;
+        FlavourConst<float> fc = make_flavour<float>(M[f], pt.mu[f], pt.T, x[3], x[4], sw);
+        float muT = fc.mu * fc.invT, Pa2 = 2.0f * fc.Pa, Pq2 = 2.0f * fc.Pq;
+        opaque_flavour(fc);
+        opaque(muT); opaque(Pa2); opaque(Pq2);
+        Acc<float, true> aD, aQ, aA;
+        aD.zero(); aQ.zero(); aA.zero();
+        float H1 = 0.f, H2 = 0.f, PQ = 0.f, PA = 0.f, Sqq = 0.f, Sqa = 0.f, Saa = 0.f;
+        int ip = gl, it = 0;
+        while (ip >= pn) { ip -= pn; ++it; }
+        float sxi = 1.0f, bw = 0.0f;
+        if (it < nv.t_num) { sxi = __fmaf_rn(xi, c2[it], 1.0f); bw = B[it]; }
+#pragma unroll 1
+        for (int k = gl; k < n; k += G) {
+            const float w = A[ip] * bw;
+            const float E2 = __fmaf_rn(p2[ip], sxi, fc.M2);
+            const float rE = rsqrtf(E2);
+            const float E = E2 * rE, m = fc.M * rE;
+            const float a = __fmaf_rn(-E, fc.invT, muT);
+            const bool sig = a > 0.0f;
+            const float t = __expf(sig ? -a : a);
+            const float t2 = t * t, t3 = t2 * t;
+            const float fp = __fmaf_rn(__fmaf_rn(t + (sig ? fc.k2_1 : fc.k2_0), t, sig ? fc.k1_1 : fc.k1_0), t, 1.0f);
+            const float gm = __fmaf_rn(__fmaf_rn(__fmaf_rn(sig ? 1.0f : fc.e3_0, t, sig ? fc.e2_1 : fc.e2_0), t,
+                                                 sig ? fc.e1_1 : fc.e1_0), t, sig ? fc.e0_1 : 1.0f);
+            const bool clP = fp < 1e-16f;
+            const bool clM = gm < 1e-16f * (sig ? t3 : 1.0f);
+            const float ipv = clP ? 0.0f : fast_rcp(fp);
+            const float im = clM ? 0.0f : fast_rcp(gm);
+            const float u1 = sig ? t2 : t, u2 = sig ? t : t2, u3 = sig ? 1.0f : t3;
+            const float r1 = u1 * ipv, r2 = u2 * ipv, r3 = u3 * ipv;
+            const float C1 = fc.C * im, C2i = fc.C * C1, C3i = fc.C * C2i;
+            const float s1 = u1 * C1, s2 = u2 * C2i, s3 = u3 * C3i;
+            const float np = clP ? (sig ? 1.0f : 0.0f) : __fmaf_rn(fc.Pq, r1, __fmaf_rn(Pa2, r2, r3));
+            const float nm = clM ? 0.0f : __fmaf_rn(fc.Pa, s1, __fmaf_rn(Pq2, s2, s3));
+            const float npnm = np + nm;
+            aD.add(w * (npnm * m));
+            aQ.add(w * (r1 + s2));
+            aA.add(w * (r2 + s1));
+            const float Lpp = clP ? 0.0f : __fmaf_rn(-9.0f * np, np, __fmaf_rn(6.0f, __fmaf_rn(fc.Pa, r2, r3), 3.0f * np));
+            const float Lmm = clM ? 0.0f : __fmaf_rn(-9.0f * nm, nm, __fmaf_rn(6.0f, __fmaf_rn(fc.Pq, s2, s3), 3.0f * nm));
+            const float m2 = m * m;
+            const float wm = w * m;
+            H1 = __fmaf_rn(wm * m, Lpp + Lmm, H1);
+            H2 = __fmaf_rn(w * npnm, (1.0f - m2) * rE, H2);
+            const float np3 = 3.0f * np, nm3 = 3.0f * nm;
+            PQ = __fmaf_rn(wm, __fmaf_rn(r1, 1.0f - np3, s2 * (2.0f - nm3)), PQ);
+            PA = __fmaf_rn(wm, __fmaf_rn(r2, 2.0f - np3, s1 * (1.0f - nm3)), PA);
+            Sqq = __fmaf_rn(w, __fmaf_rn(r1, r1, s2 * s2), Sqq);
+            Sqa = __fmaf_rn(w, __fmaf_rn(r1, r2, s1 * s2), Sqa);
+            Saa = __fmaf_rn(w, __fmaf_rn(r2, r2, s1 * s1), Saa);
+            ip += G;
+            if (ip >= pn) {
+                do { ip -= pn; ++it; } while (ip >= pn);
+                if (it < nv.t_num) { sxi = __fmaf_rn(xi, c2[it], 1.0f); bw = B[it]; }
+            }
+        }
+        const bool two = (f == 0 && dedup);
+        const float mult = two ? 2.0f : 1.0f;  // exact scaling
+        fh[f][0] = aD.s; fl[f][0] = -aD.c;
+        fh[f][1] = H1; fh[f][2] = H2;
+        fh[f][3] = sw ? PA : PQ;
+        fh[f][4] = sw ? PQ : PA;
+        const Acc<float, true> &qq = sw ? aA : aQ, &aa = sw ? aQ : aA;
+        pair_add(sh[0], sl[0], mult * qq.s, -mult * qq.c);
+        pair_add(sh[1], sl[1], mult * aa.s, -mult * aa.c);
+        pair_add(sh[2], sl[2], mult * (sw ? Saa : Sqq), 0.0f);
+        pair_add(sh[3], sl[3], mult * Sqa, 0.0f);
+        pair_add(sh[4], sl[4], mult * (sw ? Sqq : Saa), 0.0f);
+        if (two)
+            for (int k = 0; k < 5; ++k) { fh[1][k] = fh[0][k]; fl[1][k] = fl[0][k]; }
+        if (gl == 0) evals += (int64_t)n;
+    }
+    double r[3][5];
+    for (int f = 0; f < 3; ++f)
+        for (int k = 0; k < 5; ++k) {
+            float hh = fh[f][k], ll = fl[f][k];
+            group_sum_ff<G>(hh, ll, mask);
+            r[f][k] = (double)hh + (double)ll;
+        }
+    double q[5];
+    for (int k = 0; k < 5; ++k) {
+        float hh = sh[k], ll = sl[k];
+        group_sum_ff<G>(hh, ll, mask);
+        q[k] = (double)hh + (double)ll;
+    }
+    const double iT = 1.0 / pt.T;
+    for (int f = 0; f < 3; ++f) {
+        S.DM[f] = -3.0 * iT * r[f][0];
+        S.DMM[f] = iT * iT * r[f][1] - 3.0 * iT * r[f][2];
+        S.DMP[f] = -3.0 * iT * r[f][3];
+        S.DMPb[f] = -3.0 * iT * r[f][4];
+        S.Nq[f] = S.Na[f] = 0.0;
+    }
+    S.SP = 3.0 * q[0];
+    S.SPb = 3.0 * q[1];
+    S.SPP = -9.0 * q[2];
+    S.SPPb = -9.0 * q[3];
+    S.SPbPb = -9.0 * q[4];
+    S.SL = S.SAN = 0.0;
+}
+
 // FP64 residual pass of the mixed solve's certification: the sums S.DM, S.SP, S.SPb of
 // node_pass<double, GRAD only> from the same integrand in FP64, arranged for the FP64 pipe
 // (57 FP64 instructions per node-flavour, measured): exp, 1/x and 1/sqrt from pnjl_f64.cuh,

@@ -14,7 +14,8 @@ from . import _capi as api
 from .constants import PNJLParams
 
 PRECISIONS = {"fp64": api.PNJL_PREC_FP64, "mixed": api.PNJL_PREC_MIXED}
-EVAL_PRECISIONS = dict(PRECISIONS, ff_residual=api.PNJL_PREC_FF_RESIDUAL, fp64_cert=api.PNJL_PREC_FP64_CERT)
+EVAL_PRECISIONS = dict(PRECISIONS, ff_residual=api.PNJL_PREC_FF_RESIDUAL, fp64_cert=api.PNJL_PREC_FP64_CERT,
+                       fp32_newton=api.PNJL_PREC_FP32_NEWTON)
 
 
 @dataclass

@@ -66,6 +66,23 @@ def test_eval_fp64_matches_oracle(engine_factory, P, p_num, t_num, mu_neg, asym)
         assert np.abs(h[i] - h_ref).max() <= 1e-11 * sh, (i, h[i], h_ref)
 
 
+@pytest.mark.parametrize("mu_neg,asym", [(False, False), (True, True)])
+def test_eval_fp32_newton_pass_close_to_fp64(engine_factory, mu_neg, asym):
+    """The mixed solver's FP32 Newton pass (regrouped second derivatives, uncompensated
+    Jacobian sums): gradient within 1e-5 and Hessian within 1e-4 of their scale of the FP64
+    pass (the FP32 resolution of the node sums)."""
+    eng = engine_factory(128, 32)
+    x, T, mu, xi = random_states(64, 8 + int(mu_neg), mu_neg, asym)
+    T = np.maximum(T, 45.0 / HBARC)
+    _, g, h = eng.evaluate(x, T, mu, xi)
+    _, g32, h32 = eng.evaluate(x, T, mu, xi, precision="fp32_newton")
+    for i in range(len(T)):
+        sg = max(1.0, np.abs(g[i]).max())
+        sh = max(1.0, np.abs(h[i]).max())
+        assert np.abs(g32[i] - g[i]).max() <= 1e-5 * sg, (i, g32[i] - g[i])
+        assert np.abs(h32[i] - h[i]).max() <= 1e-4 * sh, (i, h32[i] - h[i])
+
+
 def test_eval_mixed_fp32_pass_close_to_fp64(engine_factory):
     eng = engine_factory(128, 32)
     x, T, mu, xi = random_states(64, 7)
