@@ -464,8 +464,8 @@ def main():
                                    seed_table=table, seed_table_hot=hot, opts=arm.opts, learned=arm.learned, reps=2)
         eng.synchronize()
         tuning = {"chosen": best, "candidates": len(tried),
-                  "tried": [[t["blocks_per_sm"], t["pipeline_chunks"], round(t["ms"], 3)] for t in tried],
-                  "tried_fields": ["blocks_per_sm", "pipeline_chunks", "ms"]}
+                  "tried": [[t["blocks_per_sm"], t["pipeline_chunks"], t["cert_warps"], round(t["ms"], 3)] for t in tried],
+                  "tried_fields": ["blocks_per_sm", "pipeline_chunks", "cert_warps", "ms"]}
     main_rec = run_arm(arm, args.steps, args.warmup, True)
 
     # the dominant kernel's own launches, for the roofline: the fused kernel (one launch per

@@ -242,6 +242,12 @@ int pnjl_set_tuning(pnjl_ctx *ctx, int32_t lanes_per_point, int32_t blocks_per_s
  * piece c overlaps the per-point kernel of piece c+1.  Results do not depend on it.
  * pnjl_get_tuning reads the current launch shape. */
 int pnjl_set_pipeline(pnjl_ctx *ctx, int32_t chunks);
+/* Certifying warps per block of the fused kernel (0..7; 0 by default): these warps run only
+ * the FP64 certification passes that the other warps queue, a steady supply of work for the
+ * FP64 pipe.  0: every warp certifies its own seeds (measured fastest on the 256 x 256 x 9
+ * scan; the autotuner tries 0..4).  Results do not depend on it. */
+int pnjl_set_cert_warps(pnjl_ctx *ctx, int32_t warps);
+int pnjl_get_cert_warps(const pnjl_ctx *ctx, int32_t *warps);
 int pnjl_get_tuning(const pnjl_ctx *ctx, int32_t *lanes_per_point, int32_t *blocks_per_sm, int32_t *chunks);
 
 /* One launch shape and its measured solve time (device time of the solve kernels, CUDA events). */
@@ -249,13 +255,15 @@ typedef struct pnjl_tuning {
     int32_t lanes_per_point;
     int32_t blocks_per_sm;
     int32_t pipeline_chunks;
+    int32_t cert_warps;     /* certifying warps per block of the fused kernel */
     double ms;
 } pnjl_tuning;
 
 /* Autotuner (no counterpart in the reference): solves the given representative batch (device
  * pointers, as pnjl_solve_batch_device, or pnjl_solve_batch_learned_device when `learned`) with
  * every candidate launch shape -- resident blocks per SM from the occupancy maximum down to 1,
- * and for mixed per-point solves the launch forms 1, -1, 2, 4 of pnjl_set_pipeline -- `reps` times each, keeps
+ * and for mixed per-point solves the fused kernel with 0..4 certifying warps and the launch
+ * forms -1, 2, 4 of pnjl_set_pipeline -- `reps` times each, keeps
  * the fastest (minimum over repetitions) and sets it on the context.  `tried` (optional) receives
  * up to max_tried candidates with their times; d_out receives the last solve's results. */
 int pnjl_autotune(pnjl_ctx *ctx, int64_t n, const double *d_T, const double *d_mu_u, const double *d_mu_d,

@@ -101,7 +101,7 @@ class pnjl_stats(C.Structure):
 
 class pnjl_tuning(C.Structure):
     _fields_ = [("lanes_per_point", C.c_int32), ("blocks_per_sm", C.c_int32), ("pipeline_chunks", C.c_int32),
-                ("ms", C.c_double)]
+                ("cert_warps", C.c_int32), ("ms", C.c_double)]
 
 
 # name -> (restype, argtypes); every function declared in include/pnjl_cuda.h
@@ -125,6 +125,8 @@ SIGNATURES = {
     "pnjl_device_sm_count": (C.c_int, [C.c_void_p]),
     "pnjl_set_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "pnjl_set_pipeline": (C.c_int, [C.c_void_p, C.c_int32]),
+    "pnjl_set_cert_warps": (C.c_int, [C.c_void_p, C.c_int32]),
+    "pnjl_get_cert_warps": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "pnjl_autotune": (C.c_int, [C.c_void_p, C.c_int64, dp, dp, dp, dp, dp, C.POINTER(pnjl_solve_opts),
                                 C.POINTER(pnjl_result_soa), C.c_int32, C.c_int32, C.POINTER(pnjl_tuning),
                                 C.POINTER(pnjl_tuning), C.c_int32, C.POINTER(C.c_int32)]),

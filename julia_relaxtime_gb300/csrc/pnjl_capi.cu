@@ -46,6 +46,7 @@ struct pnjl_ctx {
     int group = 32;
     int blocks_per_sm = 0;  // 0 = occupancy maximum
     int pipeline_chunks = 0;  // mixed per-point solves: chunks over two streams (0 = automatic)
+    int cert_warps = pnjl::kDefaultCertWarps;  // fused kernel: certifying warps per block
     cudaStream_t stream2 = nullptr;  // second stream of the chunk pipeline
     cudaEvent_t ev_chunk[pnjl::kMaxPipelineChunks] = {};
     cudaEvent_t ev_join = nullptr;
@@ -517,6 +518,10 @@ static pnjl::SolveArgs chunk_args(const pnjl::SolveArgs &a, int64_t lo, int64_t 
     c.list_count = ctrl3 + 1;
     c.queue2 = ctrl3 + 2;
     c.points_done = nullptr;
+    c.cert_warps = 0;
+    c.jobs = nullptr;
+    c.job_ready = nullptr;
+    c.job_count = c.job_head = nullptr;
     return c;
 }
 
@@ -544,8 +549,9 @@ static size_t solve_scratch_bytes(int64_t n, const pnjl_solve_opts *o) {
         return al256(nn * sizeof(int)) + nn * o->n_seeds * sizeof(pnjl::CandRec);
     if (mixed && S > 0)
         return al256(nn * sizeof(int)) + al256(nn * S * sizeof(int)) + al256(nn * sizeof(int)) +
-               al256(nn * (S + 1) * sizeof(pnjl::CandRec)) + al256(nn * S * 5 * sizeof(double)) +
-               al256(nn * sizeof(long long));
+               al256(nn * (S + 1) * sizeof(int)) + al256(nn * (S + 1) * sizeof(pnjl::CandRec)) +
+               al256(nn * S * 5 * sizeof(double)) + al256(nn * sizeof(long long)) +
+               al256(nn * (S + 1) * sizeof(pnjl::CertJob));
     return 0;
 }
 
@@ -571,17 +577,27 @@ static cudaError_t solve_enqueue(const pnjl_ctx *ctx, const pnjl::KernelNodes &n
         // slots: every point (table mode) or the points the per-point kernel defers
         const size_t nn = (size_t)n;
         const size_t b_done = al256(nn * sizeof(int)), b_flag = al256(nn * S * sizeof(int));
-        const size_t b_mode = al256(nn * sizeof(int));
+        const size_t b_mode = al256(nn * sizeof(int)), b_ready = al256(nn * (S + 1) * sizeof(int));
         const size_t b_cand = al256(nn * (S + 1) * sizeof(pnjl::CandRec)), b_roots = al256(nn * S * 5 * sizeof(double));
+        const size_t b_list = al256(nn * sizeof(long long));
         unsigned char *q = r.scratch;
         a.done = (int *)q;
-        a.root_flag = (int *)(q + b_done);
-        a.list_mode = (int *)(q + b_done + b_flag);
-        a.cand = (pnjl::CandRec *)(q + b_done + b_flag + b_mode);
-        a.roots = (double *)(q + b_done + b_flag + b_mode + b_cand);
-        a.list = (long long *)(q + b_done + b_flag + b_mode + b_cand + b_roots);
-        // done, root_flag and list_mode are adjacent: one memset clears them
-        if ((e = cudaMemsetAsync(q, 0, b_done + b_flag + b_mode, s)) != cudaSuccess) return e;
+        q += b_done;
+        a.root_flag = (int *)q;
+        q += b_flag;
+        a.list_mode = (int *)q;
+        q += b_mode;
+        a.job_ready = (int *)q;
+        q += b_ready;
+        a.cand = (pnjl::CandRec *)q;
+        q += b_cand;
+        a.roots = (double *)q;
+        q += b_roots;
+        a.list = (long long *)q;
+        q += b_list;
+        a.jobs = (pnjl::CertJob *)q;
+        // done, root_flag, list_mode and job_ready are adjacent: one memset clears them
+        if ((e = cudaMemsetAsync(r.scratch, 0, b_done + b_flag + b_mode + b_ready, s)) != cudaSuccess) return e;
     }
     if ((e = cudaMemsetAsync(r.ctrl, 0, pnjl::kCtrlSlots * sizeof(long long), s)) != cudaSuccess) return e;
     a.P = ctx->dp;
@@ -603,6 +619,9 @@ static cudaError_t solve_enqueue(const pnjl_ctx *ctx, const pnjl::KernelNodes &n
     a.list_count = r.ctrl + 1 + pnjl::kStatCount;
     a.queue2 = r.ctrl + 2 + pnjl::kStatCount;
     a.points_done = r.ctrl + 3 + pnjl::kStatCount;
+    a.job_count = r.ctrl + 4 + pnjl::kStatCount;
+    a.job_head = r.ctrl + 5 + pnjl::kStatCount;
+    a.cert_warps = 0;
     const int group = ctx->group;
     int grid = 0, grid_tasks = 0, grid_fused = 0;
     *launches = 1;
@@ -634,7 +653,8 @@ static cudaError_t solve_enqueue(const pnjl_ctx *ctx, const pnjl::KernelNodes &n
         e = pnjl::launch_mixed_tasks(a, grid_tasks, smem, s);
     } else if (two && pipeline_chunks(ctx, n) == 1) {
         // one launch: the per-point seeds and the tasks they defer (verification, MultiSeed
-        // fallback) share the persistent grid
+        // fallback) share the persistent grid; the first cert_warps warps of each block certify
+        a.cert_warps = ctx->cert_warps;
         e = pnjl::launch_mixed_fused(a, grid_fused, smem, s);
         *launches = 1;
     } else if (two && pipeline_chunks(ctx, n) > 1) {
@@ -1155,6 +1175,20 @@ int pnjl_set_pipeline(pnjl_ctx *ctx, int32_t chunks) {
     return PNJL_OK;
 }
 
+int pnjl_set_cert_warps(pnjl_ctx *ctx, int32_t warps) {
+    if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
+    if (warps < 0 || warps > pnjl::kSolveThreads / 32 - 1)
+        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "certifying warps out of range (0..7)");
+    ctx->cert_warps = warps;
+    return PNJL_OK;
+}
+
+int pnjl_get_cert_warps(const pnjl_ctx *ctx, int32_t *warps) {
+    if (!ctx || !warps) return PNJL_ERR_INVALID_ARGUMENT;
+    *warps = ctx->cert_warps;
+    return PNJL_OK;
+}
+
 int pnjl_get_tuning(const pnjl_ctx *ctx, int32_t *lanes_per_point, int32_t *blocks_per_sm, int32_t *chunks) {
     if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
     if (lanes_per_point) *lanes_per_point = ctx->group;
@@ -1175,16 +1209,19 @@ int pnjl_autotune(pnjl_ctx *ctx, int64_t n, const double *d_T, const double *d_m
     int occ_max = mixed ? std::max(pnjl::solve_mixed_occupancy(pnjl::kMixedFused,
                                                                pnjl::node_smem_bytes(ctx->p_num, ctx->t_num)), 1)
                         : std::max(pnjl::solve_kernel_occupancy(32, pnjl::node_smem_bytes(ctx->p_num, ctx->t_num)), 1);
-    const int chunk_list[] = {1, -1, 2, 4};
-    const int n_chunk = (mixed && per_point) ? 4 : 1;
-    const int old_bps = ctx->blocks_per_sm, old_c = ctx->pipeline_chunks;
+    // launch forms (pipeline chunks, certifying warps): the fused kernel with 0..4 certifying
+    // warps per block, the two kernels in sequence, the two-stream chunk pipeline
+    const int form_list[][2] = {{1, 0}, {1, 1}, {1, 2}, {1, 3}, {1, 4}, {-1, 0}, {2, 0}, {4, 0}};
+    const int n_form = (mixed && per_point) ? 8 : 1;
+    const int old_bps = ctx->blocks_per_sm, old_c = ctx->pipeline_chunks, old_k = ctx->cert_warps;
     pnjl_tuning b{};
     b.ms = 1e300;
     int count = 0;
     for (int bps = occ_max; bps >= 1; --bps) {
-        for (int ci = 0; ci < n_chunk; ++ci) {
+        for (int ci = 0; ci < n_form; ++ci) {
             ctx->blocks_per_sm = bps;
-            ctx->pipeline_chunks = chunk_list[ci];
+            ctx->pipeline_chunks = form_list[ci][0];
+            ctx->cert_warps = form_list[ci][1];
             double t_min = 1e300;
             for (int r = 0; r < reps; ++r) {
                 rc = learned ? pnjl_solve_batch_learned_device(ctx, n, d_T, d_mu_u, d_mu_d, d_mu_s, d_xi, opts, d_out)
@@ -1192,6 +1229,7 @@ int pnjl_autotune(pnjl_ctx *ctx, int64_t n, const double *d_T, const double *d_m
                 if (rc) {
                     ctx->blocks_per_sm = old_bps;
                     ctx->pipeline_chunks = old_c;
+                    ctx->cert_warps = old_k;
                     return rc;
                 }
                 PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
@@ -1199,7 +1237,7 @@ int pnjl_autotune(pnjl_ctx *ctx, int64_t n, const double *d_T, const double *d_m
                 PNJL_CUDA_TRY(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
                 t_min = std::min(t_min, (double)ms);
             }
-            pnjl_tuning t{32, bps, chunk_list[ci], t_min};
+            pnjl_tuning t{32, bps, form_list[ci][0], form_list[ci][1], t_min};
             if (tried && count < max_tried) tried[count] = t;
             ++count;
             if (t_min < b.ms) b = t;
@@ -1208,6 +1246,7 @@ int pnjl_autotune(pnjl_ctx *ctx, int64_t n, const double *d_T, const double *d_m
     if (n_tried) *n_tried = count;
     ctx->blocks_per_sm = b.blocks_per_sm;
     ctx->pipeline_chunks = b.pipeline_chunks;
+    ctx->cert_warps = b.pipeline_chunks == 1 || b.pipeline_chunks == 0 ? b.cert_warps : old_k;
     *best = b;
     return PNJL_OK;
 }

@@ -602,9 +602,12 @@ struct Group {
     // reference's NLsolve counts one budget per seed) bounds the steps; a seed that spends it
     // is not converged.  Steps that stop contracting even with fresh FP32 Jacobians hand the
     // rest of the budget to FP64 Newton steps (FP64 Hessian passes) from the best state.
+    // The refinement stops at its first certification attempt and returns true: c.x is the
+    // state to certify (certify(), at once or by a certifying warp), *th_valid whether c's
+    // thermo fields are those of c.x.  False: c is final (an FP64-only refinement).
     static constexpr int kMaxRefreshJ = 12;
-    __device__ void refine64(const PointIn &pt, const SolveOpts &o, const double *J32, const double *x32, Candidate &c,
-                             int &steps, int budget) {
+    __device__ bool refine64(const PointIn &pt, const SolveOpts &o, const double *J32, const double *x32, Candidate &c,
+                             int &steps, int budget, int *th_out) {
         double F[5], Fo[5], p[5], B[25], xb[5], Jn[25];
         for (int i = 0; i < 25; ++i) B[i] = J32[i];
         for (int i = 0; i < 5; ++i) c.x[i] = xb[i] = x32[i];
@@ -635,11 +638,8 @@ struct Group {
                 fb = fn;
             }
             if (!bad && !is64 && (fn < 0.1 * o.ftol || (fn < o.ftol && !(fn < 0.5 * fprev)))) {
-                eval_grad64(pt, c.x, F);  // certification attempt at the current state
-                is64 = true;
-                if (norm_inf5(F) < o.ftol) continue;
-                use_ff = false;  // float-float and FP64 disagree here: continue in FP64
-                continue;
+                *th_out = th_valid ? 1 : 0;  // certification attempt at the current state
+                return true;
             }
             const bool stalled = steps > 0 && !(fn < 0.5 * fprev);
             if (steps >= budget) {  // the seed's iteration budget is spent: not converged
@@ -652,7 +652,7 @@ struct Group {
                 cnt.v[kStatRescue64] += 1;
                 newton(pt, xb, o, c, budget - used);
                 steps = used + c.iterations;
-                return;
+                return false;
             }
             if (stalled) {
                 // a Newton step with the float-float Jacobian at x (its residual replaces F:
@@ -700,15 +700,20 @@ struct Group {
         // the outputs at the final state: from its float-float residual pass when that was
         // the last one, else a float-float thermo pass (FP64 pass if unavailable)
         if (!th_valid && !eval_thermo_ff(pt, o, c)) eval_thermo(pt, o, c);
+        return false;
     }
 
     // Mixed-precision counterpart of solve_seed.  `dup` is set when the FP32 solution is a
     // root that the dedup policy `dd` has already seen (the same FP64 root, which this seed
     // cannot take from an earlier one under the min-Omega tie rule); then no FP64 work is
     // spent on it.  D provides seen(x) and remember(x), uniform over the group.
+    // With `cs` (fused kernel with certifying warps) a seed whose refinement reaches its FP64
+    // certification returns true at that point with `out` and `cs` holding its state: the
+    // certifying warp finishes it (mixed_seed_finish).  Otherwise the seed is finished here,
+    // by the same steps.
     template <class D>
-    __device__ __noinline__ void mixed_solve_seed(const PointIn &pt, const double *x0, const SolveOpts &o, Candidate &out,
-                                     bool &converged, bool &dup, D &dd) {
+    __device__ __noinline__ bool mixed_solve_seed(const PointIn &pt, const double *x0, const SolveOpts &o, Candidate &out,
+                                                  bool &converged, bool &dup, D &dd, CertState *cs = nullptr) {
         cnt.v[kStatSeeds] += 1;
         dup = false;
         double x32[5], J32[25];
@@ -717,16 +722,26 @@ struct Group {
         if (r < 0) {  // decide a non-finite FP32 residual at the seed with the FP64 path
             cnt.v[kStatSeeds] -= 1;
             solve_seed(pt, x0, o, out, converged);
-            return;
+            return false;
         }
         out.exception = false;
         if (r > 0) {
-            if (dd.seen(x32)) { dup = true; converged = false; return; }
+            if (dd.seen(x32)) { dup = true; converged = false; return false; }
             dd.remember(x32);
-            if (cannot_win(pt, x32, dd.omega_bound())) { dup = true; converged = false; return; }
-            int st = 0;
-            refine64(pt, o, J32, x32, out, st, o.max_iter - it32);
-            out.iterations = it32 + st;
+            if (cannot_win(pt, x32, dd.omega_bound())) { dup = true; converged = false; return false; }
+            CertState s;
+            s.steps = 0;
+            if (refine64(pt, o, J32, x32, out, s.steps, o.max_iter - it32, &s.th_valid)) {
+                for (int k = 0; k < 5; ++k) s.x32[k] = x32[k];
+                s.it32 = it32;
+                if (cs) {
+                    *cs = s;
+                    return true;
+                }
+                mixed_seed_finish(pt, x0, o, out, converged, dd, s);
+                return false;
+            }
+            out.iterations = it32 + s.steps;
         } else {
             for (int i = 0; i < 5; ++i) out.x[i] = x32[i];
             out.f_converged = false;
@@ -735,6 +750,47 @@ struct Group {
             for (int k = 0; k < 3; ++k) out.rho[k] = out.nq[k] = out.naq[k] = qnan();
             out.iterations = it32;
         }
+        seed_fallback(pt, x0, o, out, converged, dd);
+        return false;
+    }
+
+    // FP64 certification of the refined state c.x (refine64 returned true): the root is
+    // accepted when the FP64 residual ||grad_x Omega||_inf < ftol.  A state it does not
+    // certify (float-float and FP64 disagree, rare) is finished by FP64 Newton steps for the
+    // rest of the seed's budget.  `steps` counts the refinement steps on entry and on exit.
+    __device__ void certify(const PointIn &pt, const SolveOpts &o, Candidate &c, int &steps, int budget, int th_valid) {
+        double F[5];
+        eval_grad64(pt, c.x, F);
+        const double fn = norm_inf5(F);
+        if (fn < o.ftol) {
+            c.residual_norm = fn;
+            c.f_converged = true;
+            if (!th_valid && !eval_thermo_ff(pt, o, c)) eval_thermo(pt, o, c);
+            return;
+        }
+        double xs[5];
+        for (int k = 0; k < 5; ++k) xs[k] = c.x[k];
+        cnt.v[kStatRescue64] += 1;
+        if (budget < 2) budget = 2;
+        newton(pt, xs, o, c, max(budget - steps, 1));
+        steps += c.iterations;
+    }
+
+    // The certification of a deferred seed (see mixed_solve_seed) and the rest of its solve.
+    template <class D>
+    __device__ __noinline__ void mixed_seed_finish(const PointIn &pt, const double *x0, const SolveOpts &o,
+                                                   Candidate &out, bool &converged, D &dd, const CertState &cs) {
+        int st = cs.steps;
+        certify(pt, o, out, st, o.max_iter - cs.it32, cs.th_valid);
+        out.iterations = cs.it32 + st;
+        seed_fallback(pt, x0, o, out, converged, dd);
+    }
+
+    // The reference's trust-region fallback for an unusable Newton result
+    // (ImplicitSolver.jl:130-151, FP32 passes here) and the seed's final verdict.
+    template <class D>
+    __device__ void seed_fallback(const PointIn &pt, const double *x0, const SolveOpts &o, Candidate &out,
+                                  bool &converged, D &dd) {
         if (!cand_good(out, o.residual_norm_max) && o.trust_region_fallback) {
             cnt.v[kStatTrRuns] += 1;
             double y32[5], K32[25];
@@ -746,8 +802,8 @@ struct Group {
                     return;
                 }
                 Candidate f;
-                int st = 0;
-                refine64(pt, o, K32, y32, f, st, o.max_iter - itt);
+                int st = 0, th = 0;
+                if (refine64(pt, o, K32, y32, f, st, o.max_iter - itt, &th)) certify(pt, o, f, st, o.max_iter - itt, th);
                 f.iterations = itt + st;
                 if (choose_fallback(out, f, o.residual_norm_max)) out = f;
             }

@@ -30,6 +30,25 @@ struct CandRec {
     int iterations, flags;
 };
 
+// State of a seed whose FP64 certification is deferred (see Group::mixed_solve_seed): its
+// FP32 root, FP32 iterations, refinement steps so far, whether the candidate's thermo fields
+// belong to its state.
+struct CertState {
+    double x32[5];
+    int it32, steps, th_valid;
+};
+
+// Scratch record of a deferred seed, from the warp that refined it to a certifying warp:
+// the item (a point of the per-point queue or a (slot, seed) task), its CertState and the
+// candidate (state, thermo fields, flags: bit 0 f_converged, 1 exception, 2 phys).
+enum JobKind { kJobTask = 1, kJobPoint = 2 };
+struct CertJob {
+    long long t;
+    int kind, flags, iterations, pad;
+    CertState cs;
+    double x[5], residual_norm, omega, entropy, rho[3], nq[3], naq[3];
+};
+
 // Counter slots of SolveArgs::stats
 enum StatSlot {
     kStatPasses64 = 0, kStatEvalsNewton64, kStatEvalsThermo64, kStatSeeds, kStatTrRuns, kStatMsFallbacks,
@@ -61,7 +80,13 @@ struct SolveArgs {
                                   // point and record are written (zeroed: 0 = not yet)
     long long *list_count;        // entries in list (zeroed)
     long long *queue2;            // work-queue head of the task kernel (zeroed)
-    long long *points_done;       // fused kernel: points whose own seed is finished (zeroed)
+    long long *points_done;       // fused kernel: points completed (written or listed) (zeroed)
+    // fused kernel with certifying warps (cert_warps > 0 per block)
+    int cert_warps;
+    CertJob *jobs;                // [n * (n_seeds + 1)] deferred seeds
+    int *job_ready;               // [n * (n_seeds + 1)] 1 once jobs[j] is written (zeroed)
+    long long *job_count;         // jobs reserved (zeroed)
+    long long *job_head;          // jobs taken (zeroed)
 };
 
 // Modes of a slot of the mixed task kernel: min-Omega over all seeds (MultiSeed table mode);
@@ -73,7 +98,9 @@ constexpr int kCtrlSlots = 80;
 // per-chunk queue heads of the pipelined mixed per-point solve: queue, list length, task queue
 constexpr int kMaxPipelineChunks = 16;
 constexpr int kChunkCtrlBase = 24;
-static_assert(1 + kStatCount + 3 <= kChunkCtrlBase, "control block too small");
+static_assert(1 + kStatCount + 5 <= kChunkCtrlBase, "control block too small");
+// certifying warps per block of the fused kernel (pnjl_set_cert_warps), by default
+constexpr int kDefaultCertWarps = 0;
 static_assert(kChunkCtrlBase + 3 * kMaxPipelineChunks <= kCtrlSlots, "chunk control slots");
 
 enum ListMode { kListFull = 0, kListVerify = 1, kListFallback = 2 };

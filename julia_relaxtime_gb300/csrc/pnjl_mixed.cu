@@ -32,14 +32,104 @@
 
 namespace pnjl {
 
-// The per-point seed of point i (one group).  A converged point outside the verification
-// region is written at once; the others are appended to the device list: the point index,
-// its record (slot S of the slot's candidates) and, last, its mode + 1, which marks the slot
-// complete for a task that is already waiting on it.
+// Ready flags of the device lists (list_mode, job_ready) are written last, after a fence, by
+// the lane that wrote the entry; a reader that has taken an entry polls its flag (the writer
+// is a running group a few stores away from setting it; the limit is never reached in
+// practice) and reads the entry through L2.
+constexpr unsigned kReadyPolls = 1u << 24;
+constexpr unsigned kReadySleepNs = 64;
+
+__device__ __forceinline__ int wait_ready(const int *flag) {
+    int m = *(volatile const int *)flag;
+    for (unsigned k = 0; m == 0 && k < kReadyPolls; ++k) {
+        __nanosleep(kReadySleepNs);
+        m = *(volatile const int *)flag;
+    }
+    return m;
+}
+
+// Append a deferred seed to the certification queue (lane 0).
+__device__ __forceinline__ void push_job(const SolveArgs &a, int kind, long long t, const Candidate &c,
+                                         const CertState &cs) {
+    const long long j = (long long)atomicAdd((unsigned long long *)a.job_count, 1ull);
+    CertJob &jb = a.jobs[j];
+    jb.t = t;
+    jb.kind = kind;
+    jb.flags = (c.f_converged ? 1 : 0) | (c.exception ? 2 : 0) | (c.phys ? 4 : 0);
+    jb.iterations = c.iterations;
+    jb.cs = cs;
+    for (int k = 0; k < 5; ++k) jb.x[k] = c.x[k];
+    jb.residual_norm = c.residual_norm;
+    jb.omega = c.omega;
+    jb.entropy = c.entropy;
+    for (int k = 0; k < 3; ++k) { jb.rho[k] = c.rho[k]; jb.nq[k] = c.nq[k]; jb.naq[k] = c.naq[k]; }
+    __threadfence();
+    atomicExch(&a.job_ready[j], 1);
+}
+
+__device__ __forceinline__ void load_job(const CertJob *jp, long long &t, int &kind, Candidate &c, CertState &cs) {
+    t = __ldcg(&jp->t);
+    kind = __ldcg(&jp->kind);
+    const int fl = __ldcg(&jp->flags);
+    c.f_converged = fl & 1;
+    c.exception = (fl & 2) != 0;
+    c.phys = (fl & 4) != 0;
+    c.iterations = __ldcg(&jp->iterations);
+    for (int k = 0; k < 5; ++k) { cs.x32[k] = __ldcg(&jp->cs.x32[k]); c.x[k] = __ldcg(&jp->x[k]); }
+    cs.it32 = __ldcg(&jp->cs.it32);
+    cs.steps = __ldcg(&jp->cs.steps);
+    cs.th_valid = __ldcg(&jp->cs.th_valid);
+    c.residual_norm = __ldcg(&jp->residual_norm);
+    c.omega = __ldcg(&jp->omega);
+    c.entropy = __ldcg(&jp->entropy);
+    for (int k = 0; k < 3; ++k) {
+        c.rho[k] = __ldcg(&jp->rho[k]);
+        c.nq[k] = __ldcg(&jp->nq[k]);
+        c.naq[k] = __ldcg(&jp->naq[k]);
+    }
+}
+
+// The end of point i's own seed: a converged point outside the verification region is
+// written at once; the others are appended to the device list -- the point index, its record
+// (slot S of the slot's candidates) and, last, its mode + 1, which marks the slot complete
+// for a task already waiting on it.  Counts the point as completed (fused kernel).
 template <int G>
-__device__ void point_step(Group<G> &grp, const SolveArgs &a, int64_t i, int gl, Counters &cnt) {
+__device__ void point_complete(const SolveArgs &a, const PointIn &pt, int64_t i, const double *x0,
+                               const Candidate &single, bool conv, int gl, Counters &cnt) {
     const SolveOpts &o = a.opts;
     const int S = a.n_seeds;
+    int mode = -1;
+    if (single.exception) {
+        mode = -2;
+    } else if (conv) {
+        if (S > 0 && needs_verification(o, pt, a.P.hbarc, x0, single.x)) mode = kListVerify;
+    } else if (o.auto_multiseed_fallback && S > 0) {
+        mode = kListFallback;
+        cnt.v[kStatMsFallbacks] += 1;
+    }
+    if (gl != 0) return;
+    if (mode == -2) {
+        write_point(a.P, pt, a.out, i, single, false, -1, PNJL_POINT_EXCEPTION);
+    } else if (mode < 0) {
+        write_point(a.P, pt, a.out, i, single, conv, -1, conv ? PNJL_POINT_CONVERGED : PNJL_POINT_NOT_CONVERGED);
+    } else {
+        const long long slot = atomicAdd((unsigned long long *)a.list_count, 1ull);
+        a.list[slot] = i;
+        store_record(&a.cand[slot * (S + 1) + S], single, conv);
+        __threadfence();
+        atomicExch(&a.list_mode[slot], mode + 1);
+    }
+    if (a.points_done) {
+        __threadfence();
+        atomicAdd((unsigned long long *)a.points_done, 1ull);
+    }
+}
+
+// The per-point seed of point i (one group).  With certifying warps (defer) a seed that
+// reaches its FP64 certification is queued instead of completed here.
+template <int G>
+__device__ void point_step(Group<G> &grp, const SolveArgs &a, int64_t i, int gl, Counters &cnt, bool defer) {
+    const SolveOpts &o = a.opts;
     PointIn pt;
     load_point(a, i, pt);
     if (!valid_point(pt)) {
@@ -47,6 +137,10 @@ __device__ void point_step(Group<G> &grp, const SolveArgs &a, int64_t i, int gl,
             Candidate c;
             nan_candidate(c, nullptr);
             write_point(a.P, pt, a.out, i, c, false, -1, PNJL_POINT_INVALID_INPUT);
+            if (a.points_done) {
+                __threadfence();
+                atomicAdd((unsigned long long *)a.points_done, 1ull);
+            }
         }
         return;
     }
@@ -54,75 +148,123 @@ __device__ void point_step(Group<G> &grp, const SolveArgs &a, int64_t i, int gl,
     for (int k = 0; k < 5; ++k) x0[k] = a.point_seeds[5 * i + k];
     Candidate single;
     bool conv, dup;
+    CertState cs;
     // no slot: dedup within the seed's own runs only (the same instantiation of the solve
     // as the tasks', so that the fused kernel holds one copy of it)
     PublishedRoots own{nullptr, nullptr, 0, 0, nullptr, grp.mask, grp.leader(), gl, qnan()};
-    grp.mixed_solve_seed(pt, x0, o, single, conv, dup, own);
-    if (single.exception) {
-        if (gl == 0) write_point(a.P, pt, a.out, i, single, false, -1, PNJL_POINT_EXCEPTION);
+    if (grp.mixed_solve_seed(pt, x0, o, single, conv, dup, own, defer ? &cs : nullptr)) {
+        if (gl == 0) push_job(a, kJobPoint, i, single, cs);
         return;
     }
-    int mode = -1;
-    if (conv) {
-        if (S > 0 && needs_verification(o, pt, a.P.hbarc, x0, single.x)) mode = kListVerify;
-    } else if (o.auto_multiseed_fallback && S > 0) {
-        mode = kListFallback;
-        cnt.v[kStatMsFallbacks] += 1;
-    }
-    if (gl != 0) return;
-    if (mode < 0) {
-        write_point(a.P, pt, a.out, i, single, conv, -1, conv ? PNJL_POINT_CONVERGED : PNJL_POINT_NOT_CONVERGED);
-        return;
-    }
-    const long long slot = atomicAdd((unsigned long long *)a.list_count, 1ull);
-    a.list[slot] = i;
-    store_record(&a.cand[slot * (S + 1) + S], single, conv);
-    __threadfence();
-    atomicExch(&a.list_mode[slot], mode + 1);
+    point_complete<G>(a, pt, i, x0, single, conv, gl, cnt);
 }
 
-// Polls of a task on a listed slot whose point is still being written (a few stores by a
-// running group; the limit is never reached in practice) and sleep per poll (ns).
-constexpr unsigned kReadyPolls = 1u << 24;
-constexpr unsigned kReadySleepNs = 64;
-
-// Task t = (slot, seed) of the task list.  The task that completes a slot's last seed applies
-// the min-Omega selection and writes the point.
-template <int G>
-__device__ void task_step(Group<G> &grp, const SolveArgs &a, int64_t t, bool table_mode, int gl, unsigned mask,
-                          int leader, Counters &cnt) {
-    const SolveOpts &o = a.opts;
+// Slot, seed, point and mode of task t (waits for the slot's ready flag in per-point mode).
+// False when the slot never became ready (counted; the host reports it).
+__device__ __forceinline__ bool task_slot(const SolveArgs &a, int64_t t, bool table_mode, int gl, unsigned mask,
+                                          int leader, Counters &cnt, int64_t &slot, int &s, int64_t &i, int &mode) {
     const int S = a.n_seeds;
-    const int64_t slot = t / S;
-    const int s = (int)(t - slot * S);
-    int64_t i;
-    int mode;
+    slot = t / S;
+    s = (int)(t - slot * S);
     if (table_mode) {
         i = slot;
         mode = kListFull;
-    } else {
-        int m = 0;
+        return true;
+    }
+    int m = 0;
+    if (gl == 0) m = wait_ready(&a.list_mode[slot]);
+    m = __shfl_sync(mask, m, leader);
+    if (m == 0) {
+        cnt.v[kStatWaitTimeouts] += 1;
+        return false;
+    }
+    __threadfence();
+    i = __ldcg(&a.list[slot]);
+    mode = m - 1;
+    return true;
+}
+
+// The end of a task: its record, and for the task that completes the slot's last seed the
+// min-Omega selection over the slot's records and the point's output.
+template <int G>
+__device__ void task_complete(const SolveArgs &a, const PointIn &pt, int64_t i, int64_t slot, int s, int mode,
+                              const Candidate &c, bool conv, bool dup, int gl, unsigned mask, int leader) {
+    const SolveOpts &o = a.opts;
+    const int S = a.n_seeds;
+    const int count = mode == kListVerify ? o.verify_seeds : S;
+    CandRec *rec = a.cand + slot * (S + 1);
+    int old = 0;
+    if (gl == 0) {
+        store_record(&rec[s], c, conv);
+        if (dup) rec[s].flags |= 16;
+        __threadfence();
+        old = atomicAdd(&a.done[slot], 1);
+    }
+    old = __shfl_sync(mask, old, leader);
+    if (old == count - 1) {
+        // this task completed the slot: select among its records
+        __threadfence();
         if (gl == 0) {
-            m = *(volatile const int *)&a.list_mode[slot];
-            for (unsigned k = 0; m == 0 && k < kReadyPolls; ++k) {
-                __nanosleep(kReadySleepNs);
-                m = *(volatile const int *)&a.list_mode[slot];
+            Candidate best, first;
+            bool have = false;
+            int chosen = -1, first_idx = -1;
+            if (mode == kListVerify) {
+                bool cv;
+                load_record(&rec[S], best, cv);
+                have = true;
+            }
+            for (int q = 0; q < count; ++q) {
+                Candidate cq;
+                bool cv;
+                load_record(&rec[q], cq, cv);
+                if (cq.exception || (__ldcg(&rec[q].flags) & 16)) continue;
+                if (first_idx < 0) { first = cq; first_idx = q; }
+                if (!cv) continue;
+                if (better(cq, best, have, o.omega_tie_rtol)) { best = cq; chosen = q; have = true; }
+            }
+            if (have) write_point(a.P, pt, a.out, i, best, true, chosen, PNJL_POINT_CONVERGED);
+            else if (mode == kListFallback) {
+                Candidate single;
+                bool cv;
+                load_record(&rec[S], single, cv);
+                write_point(a.P, pt, a.out, i, single, false, -1, PNJL_POINT_NOT_CONVERGED);
+            } else if (first_idx >= 0) write_point(a.P, pt, a.out, i, first, false, first_idx, PNJL_POINT_ALL_SEEDS_FAILED);
+            else {
+                Candidate cz;
+                nan_candidate(cz, table_row(a, pt, 0));
+                write_point(a.P, pt, a.out, i, cz, false, -1, PNJL_POINT_ALL_SEEDS_FAILED);
             }
         }
-        m = __shfl_sync(mask, m, leader);
-        if (m == 0) {  // the slot never completed: counted, the host reports it
-            cnt.v[kStatWaitTimeouts] += 1;
-            return;
-        }
-        __threadfence();
-        i = __ldcg(&a.list[slot]);
-        mode = m - 1;
     }
-    const int count = mode == kListVerify ? o.verify_seeds : S;
+}
+
+// The dedup policy of a task (see PublishedRoots).
+__device__ __forceinline__ PublishedRoots task_roots(const SolveArgs &a, int64_t slot, int s, int mode, double *prior,
+                                                     unsigned mask, int leader, int gl) {
+    const int S = a.n_seeds;
+    const CandRec *rec = a.cand + slot * (S + 1);
+    double prior_omega = qnan();
+    if (mode == kListVerify) {
+        for (int k = 0; k < 5; ++k) prior[k] = __ldcg(&rec[S].x[k]);
+        prior_omega = __ldcg(&rec[S].omega);
+    }
+    return PublishedRoots{a.roots, a.root_flag, slot * S, s, mode == kListVerify ? prior : nullptr, mask, leader, gl,
+                          prior_omega};
+}
+
+// Task t = (slot, seed) of the task list.  With certifying warps (defer) a seed that reaches
+// its FP64 certification is queued instead of completed here.
+template <int G>
+__device__ void task_step(Group<G> &grp, const SolveArgs &a, int64_t t, bool table_mode, int gl, unsigned mask,
+                          int leader, Counters &cnt, bool defer = false) {
+    const SolveOpts &o = a.opts;
+    int64_t slot, i;
+    int s, mode;
+    if (!task_slot(a, t, table_mode, gl, mask, leader, cnt, slot, s, i, mode)) return;
+    const int count = mode == kListVerify ? o.verify_seeds : a.n_seeds;
     if (s >= count) return;
     PointIn pt;
     load_point(a, i, pt);
-    CandRec *rec = a.cand + slot * (S + 1);
     if (!valid_point(pt)) {  // table mode only: listed points are valid
         if (s == 0 && gl == 0) {
             Candidate c;
@@ -134,56 +276,59 @@ __device__ void task_step(Group<G> &grp, const SolveArgs &a, int64_t t, bool tab
     const double *row = table_row(a, pt, s);
     double x0[5], prior[5];
     for (int k = 0; k < 5; ++k) x0[k] = row[k];
-    double prior_omega = qnan();
-    if (mode == kListVerify) {
-        for (int k = 0; k < 5; ++k) prior[k] = __ldcg(&rec[S].x[k]);
-        prior_omega = __ldcg(&rec[S].omega);
-    }
-    PublishedRoots dd{a.roots, a.root_flag, slot * S, s, mode == kListVerify ? prior : nullptr, mask, leader, gl,
-                      prior_omega};
+    PublishedRoots dd = task_roots(a, slot, s, mode, prior, mask, leader, gl);
     Candidate c;
     bool conv, dup;
-    grp.mixed_solve_seed(pt, x0, o, c, conv, dup, dd);
-    int old = 0;
-    if (gl == 0) {
-        store_record(&rec[s], c, conv);
-        if (dup) rec[s].flags |= 16;
-        __threadfence();
-        old = atomicAdd(&a.done[slot], 1);
+    CertState cs;
+    if (grp.mixed_solve_seed(pt, x0, o, c, conv, dup, dd, defer ? &cs : nullptr)) {
+        if (gl == 0) push_job(a, kJobTask, t, c, cs);
+        return;
     }
-    old = __shfl_sync(mask, old, leader);
-    if (old != count - 1) return;
-    // this task completed the slot: select among its records
+    task_complete<G>(a, pt, i, slot, s, mode, c, conv, dup, gl, mask, leader);
+}
+
+// Certification job j: the FP64 residual pass of a deferred seed, the rest of its solve, and
+// the completion of its point or task.
+template <int G>
+__device__ void job_step(Group<G> &grp, const SolveArgs &a, long long j, int gl, unsigned mask, int leader,
+                         Counters &cnt) {
+    const SolveOpts &o = a.opts;
+    int ready = 0;
+    if (gl == 0) ready = wait_ready(&a.job_ready[j]);
+    ready = __shfl_sync(mask, ready, leader);
+    if (!ready) {
+        cnt.v[kStatWaitTimeouts] += 1;
+        return;
+    }
     __threadfence();
-    if (gl != 0) return;
-    Candidate best, first;
-    bool have = false;
-    int chosen = -1, first_idx = -1;
-    if (mode == kListVerify) {
-        bool cv;
-        load_record(&rec[S], best, cv);
-        have = true;
-    }
-    for (int q = 0; q < count; ++q) {
-        Candidate cq;
-        bool cv;
-        load_record(&rec[q], cq, cv);
-        if (cq.exception || (__ldcg(&rec[q].flags) & 16)) continue;
-        if (first_idx < 0) { first = cq; first_idx = q; }
-        if (!cv) continue;
-        if (better(cq, best, have, o.omega_tie_rtol)) { best = cq; chosen = q; have = true; }
-    }
-    if (have) write_point(a.P, pt, a.out, i, best, true, chosen, PNJL_POINT_CONVERGED);
-    else if (mode == kListFallback) {
-        Candidate single;
-        bool cv;
-        load_record(&rec[S], single, cv);
-        write_point(a.P, pt, a.out, i, single, false, -1, PNJL_POINT_NOT_CONVERGED);
-    } else if (first_idx >= 0) write_point(a.P, pt, a.out, i, first, false, first_idx, PNJL_POINT_ALL_SEEDS_FAILED);
-    else {
-        Candidate cz;
-        nan_candidate(cz, table_row(a, pt, 0));
-        write_point(a.P, pt, a.out, i, cz, false, -1, PNJL_POINT_ALL_SEEDS_FAILED);
+    long long t;
+    int kind;
+    Candidate c;
+    CertState cs;
+    load_job(&a.jobs[j], t, kind, c, cs);
+    bool conv = false;
+    if (kind == kJobPoint) {
+        PointIn pt;
+        load_point(a, t, pt);
+        double x0[5];
+        for (int k = 0; k < 5; ++k) x0[k] = a.point_seeds[5 * t + k];
+        PublishedRoots own{nullptr, nullptr, 0, 0, nullptr, mask, leader, gl, qnan()};
+        own.own.remember(cs.x32);
+        grp.mixed_seed_finish(pt, x0, o, c, conv, own, cs);
+        point_complete<G>(a, pt, t, x0, c, conv, gl, cnt);
+    } else {
+        int64_t slot, i;
+        int s, mode;
+        if (!task_slot(a, t, false, gl, mask, leader, cnt, slot, s, i, mode)) return;
+        PointIn pt;
+        load_point(a, i, pt);
+        const double *row = table_row(a, pt, s);
+        double x0[5], prior[5];
+        for (int k = 0; k < 5; ++k) x0[k] = row[k];
+        PublishedRoots dd = task_roots(a, slot, s, mode, prior, mask, leader, gl);
+        dd.own.remember(cs.x32);
+        grp.mixed_seed_finish(pt, x0, o, c, conv, dd, cs);
+        task_complete<G>(a, pt, i, slot, s, mode, c, conv, false, gl, mask, leader);
     }
 }
 
@@ -211,7 +356,7 @@ __global__ void __launch_bounds__(kSolveThreads, 2) mixed_points_kernel(SolveArg
         if (gl == 0) t = atomicAdd((unsigned long long *)a.queue, 1ull);
         t = __shfl_sync(mask, t, leader);
         if (t >= a.n) break;
-        point_step(grp, a, t, gl, cnt);
+        point_step(grp, a, t, gl, cnt, false);
     }
     flush_counters<G>(a, cnt, gl);
 }
@@ -243,17 +388,36 @@ __global__ void __launch_bounds__(kSolveThreads, 2) mixed_tasks_kernel(SolveArgs
 }
 
 // Polls of a group that found no work while points are still being solved (their seeds may
-// still defer them), and sleep per poll (ns).  A group that gives up simply exits: the tasks
-// listed later are taken by the groups still running, at the latest by the one that listed
-// them.
+// still list them), and sleep per poll (ns).  A group that gives up simply exits: the work
+// listed later is taken by the groups still running, at the latest by the one that listed it.
 constexpr unsigned kIdlePolls = 1u << 22;
 constexpr unsigned kIdleSleepNs = 500;
 
-// Per-point seeds and the tasks they defer in one persistent launch.  A group takes, in this
-// order: a listed (slot, seed) task not yet taken; the next point; and, when both queues are
-// empty while points are still in flight, waits for their tasks.  Verification seeds thus
-// start as soon as their point is listed and share the GPU with the remaining points, instead
-// of forming a second launch whose elapsed time is set by its longest seeds.
+// Take the next entry of a device queue whose length grows while the kernel runs (head <
+// avail): CAS so that no index beyond the published length is ever taken.  -1 when none.
+__device__ __forceinline__ long long take_bounded(long long *head, long long avail) {
+    long long h = *(volatile const long long *)head;
+    while (h < avail) {
+        const long long old =
+            (long long)atomicCAS((unsigned long long *)head, (unsigned long long)h, (unsigned long long)(h + 1));
+        if (old == h) return h;
+        h = old;
+    }
+    return -1;
+}
+
+// Per-point seeds and the tasks they list in one persistent launch.  A group takes, in this
+// order: a listed (slot, seed) task not yet taken; the next point; a queued certification;
+// and, when nothing is left while points are still in flight, waits for their work.
+// Verification seeds thus start as soon as their point is listed and share the GPU with the
+// remaining points, instead of forming a second launch whose elapsed time is set by its
+// longest seeds.
+// With cert_warps = K > 0 the first K warps of every block are certifying warps: they take
+// only queued certifications (the FP64 residual pass of a seed whose float-float refinement
+// is done, and the rest of that seed), and the other warps queue them instead of running the
+// FP64 pass themselves.  The FP64 pipe -- about 2 FMA per clock per SM on the GB300 -- then
+// has a steady supply of work beside the FP32-pipe Newton and float-float passes.  (Measured
+// on the 256 x 256 x 9 scan: no faster than K = 0, the default; the autotuner tries 0..4.)
 template <int G>
 __global__ void __launch_bounds__(kSolveThreads, 1) mixed_fused_kernel(SolveArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -267,32 +431,38 @@ __global__ void __launch_bounds__(kSolveThreads, 1) mixed_fused_kernel(SolveArgs
     for (int k = 0; k < kStatCount; ++k) cnt.v[k] = 0;
     Group<G> grp{a.P, nv, gl, mask, cnt};
     const long long S = a.n_seeds;
+    const bool defer = a.cert_warps > 0;
+    const bool certifier = defer && (int)(threadIdx.x >> 5) < a.cert_warps;
     unsigned idle = 0;
     while (true) {
         long long t = 0;
-        int kind = 0;  // 1 task, 2 point, 0 nothing yet, -1 all work taken
+        int kind = 0;  // 1 task, 2 point, 3 certification, 0 nothing yet, -1 all work taken
         if (gl == 0) {
-            // read "all points finished" before the list length: every slot listed by then
-            // is included in it
+            // read "all points completed" before the queue lengths: every slot listed by then
+            // is included in them
             const bool all_points = *(volatile const long long *)a.points_done >= a.n;
             __threadfence();
-            const long long avail = *(volatile const long long *)a.list_count * S;
-            long long h = *(volatile const long long *)a.queue2;
-            while (h < avail) {
-                const long long old = (long long)atomicCAS((unsigned long long *)a.queue2, (unsigned long long)h,
-                                                           (unsigned long long)(h + 1));
-                if (old == h) {
-                    kind = 1;
-                    t = h;
-                    break;
+            const long long jobs = defer ? *(volatile const long long *)a.job_count : 0;
+            if (certifier) {
+                t = take_bounded(a.job_head, jobs);
+                if (t >= 0) kind = 3;
+            } else {
+                t = take_bounded(a.queue2, *(volatile const long long *)a.list_count * S);
+                if (t >= 0) kind = 1;
+                if (kind == 0 && *(volatile const long long *)a.queue < a.n) {
+                    t = (long long)atomicAdd((unsigned long long *)a.queue, 1ull);
+                    if (t < a.n) kind = 2;
                 }
-                h = old;
+                if (kind == 0 && defer) {
+                    t = take_bounded(a.job_head, jobs);
+                    if (t >= 0) kind = 3;
+                }
             }
-            if (kind == 0 && *(volatile const long long *)a.queue < a.n) {
-                t = (long long)atomicAdd((unsigned long long *)a.queue, 1ull);
-                if (t < a.n) kind = 2;
+            if (kind == 0 && all_points) {
+                // nothing left to take: done, unless tasks remain for a non-certifying warp
+                const bool tasks_left = *(volatile const long long *)a.queue2 < *(volatile const long long *)a.list_count * S;
+                if (!(certifier && tasks_left)) kind = -1;
             }
-            if (kind == 0 && all_points) kind = -1;
         }
         kind = __shfl_sync(mask, kind, leader);
         t = __shfl_sync(mask, t, leader);
@@ -303,15 +473,9 @@ __global__ void __launch_bounds__(kSolveThreads, 1) mixed_fused_kernel(SolveArgs
             continue;
         }
         idle = 0;
-        if (kind == 1) {
-            task_step(grp, a, t, false, gl, mask, leader, cnt);
-        } else {
-            point_step(grp, a, t, gl, cnt);
-            if (gl == 0) {
-                __threadfence();
-                atomicAdd((unsigned long long *)a.points_done, 1ull);
-            }
-        }
+        if (kind == 1) task_step(grp, a, t, false, gl, mask, leader, cnt, defer);
+        else if (kind == 2) point_step(grp, a, t, gl, cnt, defer);
+        else job_step(grp, a, t, gl, mask, leader, cnt);
     }
     flush_counters<G>(a, cnt, gl);
 }

@@ -305,16 +305,22 @@ class GapEngine:
                     "pnjl_f64_math")
         return y
 
-    def set_tuning(self, lanes_per_point: int, blocks_per_sm: int = 0, pipeline_chunks: int | None = None):
+    def set_tuning(self, lanes_per_point: int, blocks_per_sm: int = 0, pipeline_chunks: int | None = None,
+                   cert_warps: int | None = None):
         self._check(self._lib.pnjl_set_tuning(self._ctx, int(lanes_per_point), int(blocks_per_sm)),
                     "pnjl_set_tuning")
         if pipeline_chunks is not None:
             self._check(self._lib.pnjl_set_pipeline(self._ctx, int(pipeline_chunks)), "pnjl_set_pipeline")
+        if cert_warps is not None:
+            self._check(self._lib.pnjl_set_cert_warps(self._ctx, int(cert_warps)), "pnjl_set_cert_warps")
 
     def tuning(self) -> dict:
         a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
         self._check(self._lib.pnjl_get_tuning(self._ctx, C.byref(a), C.byref(b), C.byref(c)), "pnjl_get_tuning")
-        return {"lanes_per_point": a.value, "blocks_per_sm": b.value, "pipeline_chunks": c.value}
+        k = C.c_int32()
+        self._check(self._lib.pnjl_get_cert_warps(self._ctx, C.byref(k)), "pnjl_get_cert_warps")
+        return {"lanes_per_point": a.value, "blocks_per_sm": b.value, "pipeline_chunks": c.value,
+                "cert_warps": k.value}
 
     def autotune(self, n: int, d_T: int, d_mu_u: int, d_mu_d: int, d_mu_s: int, d_xi: int, d_out: dict, *,
                  seed_table=None, seed_table_hot=None, hot_T_MeV: float = 300.0, opts: SolveOptions | None = None,

@@ -425,9 +425,10 @@ def test_tmu_scan_gpu_matches_oracle(engine_factory):
 
 
 def test_mixed_pipeline_chunks_and_autotune(engine_factory):
-    """The launch forms of mixed per-point solves (one fused kernel; the per-point and task
-    kernels one after the other; the two-stream chunk pipeline) and the autotuner change
-    launch shapes only: bit-identical results for every shape."""
+    """The launch forms of mixed per-point solves (one fused kernel, with 0, 1 or 3
+    certifying warps per block; the per-point and task kernels one after the other; the
+    two-stream chunk pipeline) and the autotuner change launch shapes only: bit-identical
+    results for every shape."""
     import torch
 
     eng = engine_factory(32, 8)
@@ -441,8 +442,8 @@ def test_mixed_pipeline_chunks_and_autotune(engine_factory):
     opts = SolveOptions(iterations=40, ftol=1e-10, precision="mixed", verify_seeds=-1, verify_T_max_MeV=170.0,
                         verify_max_step=0.3)
     outs = []
-    for chunks in (1, -1, 3, 7):
-        eng.set_tuning(32, 0, pipeline_chunks=chunks)
+    for chunks, cert in ((1, 0), (1, 1), (1, 3), (-1, 0), (3, 0), (7, 0)):
+        eng.set_tuning(32, 0, pipeline_chunks=chunks, cert_warps=cert)
         outs.append(eng.solve(T, mu, xi, seed_table=table, seed_table_hot=hot, point_seeds=seeds, opts=opts))
         st = eng.stats()
         assert st["kernel_launches"] > 0 and st["device_wait_timeouts"] == 0
@@ -467,7 +468,7 @@ def test_mixed_pipeline_chunks_and_autotune(engine_factory):
     ref = eng.solve(T, mu, xi, seed_table=table, seed_table_hot=hot,
                     opts=SolveOptions(iterations=40, ftol=1e-10, precision="mixed"))
     np.testing.assert_array_equal(d_out["omega"].cpu().numpy(), ref["omega"])
-    eng.set_tuning(32, 0, pipeline_chunks=0)
+    eng.set_tuning(32, 0, pipeline_chunks=0, cert_warps=0)
 
 
 def test_plan_mixed_orders_one_graph(engine_factory):
