@@ -47,6 +47,8 @@ struct Counters {
 
 __device__ __forceinline__ double qnan() { return __longlong_as_double(0x7ff8000000000000ll); }
 
+__device__ __forceinline__ bool same_root(const double *x, const double *y);
+
 template <int G>
 struct Group {
     const DevParams &P;
@@ -483,8 +485,12 @@ struct Group {
     // linear convergence of a nearly singular Jacobian, which the refinement then finishes);
     // the iteration limit, handed on only with a small residual.  Far from the floor the FP32
     // iteration goes on as the reference's FP64 Newton iteration would, within the same
-    // iteration budget.
-    __device__ int newton32(const PointIn &pt, const double *x0, const SolveOpts &o, double *x, double *J, int &iters) {
+    // iteration budget.  With `prior` (a certified root of the same point), an iterate that
+    // comes within the duplicate tolerance of it ends the phase at once (1): it is inside that
+    // root's Newton basin, and the seed is a duplicate of it (same_root), so the rest of its
+    // iterations would be spent on a root already certified.
+    __device__ int newton32(const PointIn &pt, const double *x0, const SolveOpts &o, double *x, double *J, int &iters,
+                            const double *prior = nullptr) {
         double F[5], p[5];
         for (int i = 0; i < 5; ++i) x[i] = x0[i];
         eval_newton32(pt, x, F, J);
@@ -504,6 +510,7 @@ struct Group {
             const double pn = norm_inf5(p), xn = norm_inf5(x);
             for (int i = 0; i < 5; ++i) x[i] += p[i];
             ++iters;
+            if (prior && same_root(x, prior)) return 1;
             eval_newton32(pt, x, F, J);
             if (any_nan5(x) || any_nan5(F)) return 0;
             const double fnew = norm_inf5(F);
@@ -718,7 +725,7 @@ struct Group {
         dup = false;
         double x32[5], J32[25];
         int it32 = 0;
-        const int r = newton32(pt, x0, o, x32, J32, it32);
+        const int r = newton32(pt, x0, o, x32, J32, it32, dd.prior_root());
         if (r < 0) {  // decide a non-finite FP32 residual at the seed with the FP64 path
             cnt.v[kStatSeeds] -= 1;
             solve_seed(pt, x0, o, out, converged);
@@ -852,6 +859,7 @@ struct LocalRoots {
         ++n;
     }
     __device__ double omega_bound() const { return __longlong_as_double(0x7ff8000000000000ll); }
+    __device__ const double *prior_root() const { return nullptr; }
 };
 
 // Dedup policy of the task kernel.  Seed s of a slot skips its FP64 work when its FP32 root
@@ -876,6 +884,7 @@ struct PublishedRoots {
     double prior_omega;   // Omega of `prior` (NaN when there is none)
     LocalRoots own;
     __device__ double omega_bound() const { return prior_omega; }
+    __device__ const double *prior_root() const { return prior; }
     __device__ bool seen(const double *x) const {
         if (own.seen(x)) return true;
         int hit = 0;
