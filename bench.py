@@ -47,12 +47,12 @@ if ROOT not in sys.path:
 
 HBARC = 197.327
 # DRAM bytes (read + write) per launch of the dominant kernel from one ncu capture of a
-# 9,216-point launch (0.279 GB + 0.778 GB), scaled by points to the 18,432-point step; it is
-# local-memory (stack) write-back, not data (inputs and outputs are 240 B per point)
-TRAFFIC = {"mixed_points_kernel<32>": {
-    "bytes_per_launch": 2 * (0.279048448e9 + 0.778367e9),
-    "source": "ncu --set full of one 9,216-point launch (profiles/mixed_points_and_tasks_kernels_surrogate_aniso_"
-              "9216pt.md), scaled by points; local-memory write-back"}}
+# 9,216-point launch (0.053 GB + 0.246 GB), scaled by points to the 18,432-point step; it is
+# mostly local-memory (stack) write-back (inputs and outputs are 240 B per point)
+TRAFFIC = {"mixed_fused_kernel<32>": {
+    "bytes_per_launch": 2 * (0.052924160e9 + 0.246385664e9),
+    "source": "ncu --set full of one 9,216-point launch (profiles/mixed_fused_kernel_surrogate_aniso_9216pt.md), "
+              "scaled by points; mostly local-memory write-back"}}
 METRIC = "gap solves/s at \u2016\u2202\u03a9\u2016\u22641e-10: surrogate-seeded vs plain FP64 Newton, 1 GB300"
 # Floating-point operations per node-flavour evaluation, counted from the source of
 # pnjl_device.cuh::node_flavour (FMA = 2, loop invariants hoisted, selects and compares not
