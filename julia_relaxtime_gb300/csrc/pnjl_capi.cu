@@ -638,8 +638,9 @@ static cudaError_t solve_enqueue(const pnjl_ctx *ctx, const pnjl::KernelNodes &n
         const int64_t task_need = table ? (n * S + wpb - 1) / wpb : (int64_t)ctx->sm_count * occ_of(pnjl::kMixedTasks);
         grid_tasks = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->sm_count * occ_of(pnjl::kMixedTasks),
                                                                  task_need));
+        const int64_t wpf = pnjl::kFusedThreads / 32;
         grid_fused = (int)std::max<int64_t>(
-            1, std::min<int64_t>((int64_t)ctx->sm_count * occ_of(pnjl::kMixedFused), (n * (S + 1) + wpb - 1) / wpb));
+            1, std::min<int64_t>((int64_t)ctx->sm_count * occ_of(pnjl::kMixedFused), (n * (S + 1) + wpf - 1) / wpf));
         *launches = table ? 1 : (S > 0 ? 2 : 1);
     } else {
         const int64_t n_tasks = opts->seed_mode == PNJL_SEEDS_TABLE ? n * (int64_t)opts->n_seeds : n;
@@ -1177,7 +1178,7 @@ int pnjl_set_pipeline(pnjl_ctx *ctx, int32_t chunks) {
 
 int pnjl_set_cert_warps(pnjl_ctx *ctx, int32_t warps) {
     if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
-    if (warps < 0 || warps > pnjl::kSolveThreads / 32 - 1)
+    if (warps < 0 || warps > pnjl::kFusedThreads / 32 - 1)
         return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "certifying warps out of range (0..7)");
     ctx->cert_warps = warps;
     return PNJL_OK;

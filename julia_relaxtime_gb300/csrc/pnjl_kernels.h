@@ -11,6 +11,8 @@
 namespace pnjl {
 
 static constexpr int kSolveThreads = 256;
+// threads per block of the fused mixed kernel (one block per SM)
+static constexpr int kFusedThreads = 256;
 
 // Separable node tables on the device (FP64 and an FP32 copy).
 struct KernelNodes {

@@ -419,7 +419,7 @@ __device__ __forceinline__ long long take_bounded(long long *head, long long ava
 // has a steady supply of work beside the FP32-pipe Newton and float-float passes.  (Measured
 // on the 256 x 256 x 9 scan: no faster than K = 0, the default; the autotuner tries 0..4.)
 template <int G>
-__global__ void __launch_bounds__(kSolveThreads, 1) mixed_fused_kernel(SolveArgs a) {
+__global__ void __launch_bounds__(kFusedThreads, 1) mixed_fused_kernel(SolveArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const NodeView nv = stage_nodes(a.nodes, smem_raw);
     __syncthreads();
@@ -491,7 +491,7 @@ cudaError_t launch_mixed_tasks(const SolveArgs &a, int grid, size_t smem, cudaSt
 }
 
 cudaError_t launch_mixed_fused(const SolveArgs &a, int grid, size_t smem, cudaStream_t s) {
-    mixed_fused_kernel<32><<<grid, kSolveThreads, smem, s>>>(a);
+    mixed_fused_kernel<32><<<grid, kFusedThreads, smem, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -501,7 +501,7 @@ int solve_mixed_occupancy(int kernel, size_t smem) {
     if (kernel == kMixedTasks)
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, mixed_tasks_kernel<32>, kSolveThreads, smem);
     else if (kernel == kMixedFused)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, mixed_fused_kernel<32>, kSolveThreads, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, mixed_fused_kernel<32>, kFusedThreads, smem);
     else
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, mixed_points_kernel<32>, kSolveThreads, smem);
     return e == cudaSuccess ? nb : 0;
