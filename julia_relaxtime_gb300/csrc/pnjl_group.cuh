@@ -331,7 +331,7 @@ struct Group {
         Eval ev;
         double V, V1[3], V2[3];
         vacuum_terms<G>(P, M, gl, mask, leader(), V, V1, V2);
-        assemble<true, true, false>(P, pt, x, M, S, V, V1, V2, ev);
+        assemble<true, true, false, true>(P, pt, x, M, S, V, V1, V2, ev);
         for (int i = 0; i < 5; ++i) F[i] = ev.F[i];
         for (int i = 0; i < 25; ++i) J[i] = ev.J[i];
         cnt.v[kStatPasses32] += 1;

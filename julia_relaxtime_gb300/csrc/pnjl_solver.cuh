@@ -575,7 +575,9 @@ __device__ void node_pass_ff(const NodeView &nv, const PointIn &pt, const double
 // FP64 assembly of Omega, grad, Hessian and thermo from the pass sums and the vacuum terms.
 // (An FP32 assembly of the Jacobian for the mixed mode was measured slower: the less
 // accurate J32 costs extra FP64 refinement passes.)
-template <bool GRAD, bool HESS, bool LOG>
+// J32: the Hessian block in FP32 arithmetic (the FP32 Newton pass's Jacobian: its sums carry
+// ~1e-6 relative error, far above FP32 rounding of the assembly), the gradient in FP64.
+template <bool GRAD, bool HESS, bool LOG, bool J32 = false>
 __device__ void assemble(const DevParams &P, const PointIn &pt, const double *x, const double *M, const PassSums &S,
                          double V, const double *V1, const double *V2, Eval &ev) {
     const double T = pt.T;
@@ -613,7 +615,7 @@ __device__ void assemble(const DevParams &P, const PointIn &pt, const double *x,
     for (int i = 0; i < 5; ++i) ev.F[i] = -gO[i];
     if (LOG) ev.omega = chi + U + V + Dsc * S.SL;
     else ev.omega = 0.0;
-    if (HESS) {
+    if (HESS && !J32) {
         double H[5][5];
         const double chih[3][3] = {{G4, -K4 * ps, -K4 * pd}, {-K4 * ps, G4, -K4 * pu}, {-K4 * pd, -K4 * pu, G4}};
         for (int a = 0; a < 3; ++a)
@@ -647,6 +649,55 @@ __device__ void assemble(const DevParams &P, const PointIn &pt, const double *x,
             for (int b = a; b < 5; ++b) {
                 ev.J[a * 5 + b] = -H[a][b];
                 ev.J[b * 5 + a] = -H[a][b];
+            }
+    }
+    if (HESS && J32) {
+        float H[5][5];
+        const float g4 = (float)G4, k2 = (float)K2, k4 = (float)K4;
+        const float fu = (float)pu, fd = (float)pd, fs = (float)ps, fP = (float)Ph, fPb = (float)Pb;
+        const float Jf[3][3] = {{-g4, k2 * fs, k2 * fd}, {k2 * fs, -g4, k2 * fu}, {k2 * fd, k2 * fu, -g4}};
+        const float chih[3][3] = {{g4, -k4 * fs, -k4 * fd}, {-k4 * fs, g4, -k4 * fu}, {-k4 * fd, -k4 * fu, g4}};
+        const float ds = (float)Dsc;
+        float w2[3], w1[3], wp[3], wpb[3];
+        for (int f = 0; f < 3; ++f) {
+            w2[f] = (float)(V2[f] + Dsc * S.DMM[f]);
+            w1[f] = (float)(V1[f] + Dsc * S.DM[f]);
+            wp[f] = ds * (float)S.DMP[f];
+            wpb[f] = ds * (float)S.DMPb[f];
+        }
+        for (int a = 0; a < 3; ++a)
+            for (int b = a; b < 3; ++b) {
+                float sab = chih[a][b];
+                for (int f = 0; f < 3; ++f) sab += Jf[f][a] * Jf[f][b] * w2[f];
+                H[a][b] = sab;
+            }
+        H[0][1] += w1[2] * k2;
+        H[0][2] += w1[1] * k2;
+        H[1][2] += w1[0] * k2;
+        for (int a = 0; a < 3; ++a) {
+            float s3 = 0.0f, s4 = 0.0f;
+            for (int f = 0; f < 3; ++f) {
+                s3 += Jf[f][a] * wp[f];
+                s4 += Jf[f][a] * wpb[f];
+            }
+            H[a][3] = s3;
+            H[a][4] = s4;
+        }
+        const float t4 = (float)T4, tb = (float)Tb, ta = (float)Ta, igf = (float)ig;
+        const float gPf = (float)gP, gPbf = (float)gPb;
+        const float gPP = 24.0f * fP - 6.0f * fPb * fPb;
+        const float gPbPb = 24.0f * fPb - 6.0f * fP * fP;
+        const float gPPb = -6.0f - 12.0f * fP * fPb;
+        const float UPP = gcl ? 0.0f : t4 * tb * (gPP * igf - gPf * gPf * igf * igf);
+        const float UPbPb = gcl ? 0.0f : t4 * tb * (gPbPb * igf - gPbf * gPbf * igf * igf);
+        const float UPPb = t4 * (-0.5f * ta + (gcl ? 0.0f : tb * (gPPb * igf - gPf * gPbf * igf * igf)));
+        H[3][3] = UPP + ds * (float)S.SPP;
+        H[3][4] = UPPb + ds * (float)S.SPPb;
+        H[4][4] = UPbPb + ds * (float)S.SPbPb;
+        for (int a = 0; a < 5; ++a)
+            for (int b = a; b < 5; ++b) {
+                ev.J[a * 5 + b] = -(double)H[a][b];
+                ev.J[b * 5 + a] = -(double)H[a][b];
             }
     }
     if (LOG) {
@@ -777,27 +828,32 @@ __device__ __forceinline__ void lu_solve_factored5(const double *A, const int *p
     for (int i = 0; i < 5; ++i) x[i] = y[i];
 }
 
+// The 5-vector checks on the bit patterns (integer pipe; the FP64 pipe is the scarce one):
+// |v| as the pattern without the sign orders like the value for non-negative doubles, and a
+// NaN's pattern is above +inf's.
+__device__ __forceinline__ unsigned long long abs_bits(double v) {
+    return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+}
 __device__ __forceinline__ double norm_inf5(const double *v) {
-    double m = 0.0;
-    bool nan = false;
+    unsigned long long m = 0;
 #pragma unroll
     for (int i = 0; i < 5; ++i) {
-        const double a = fabs(v[i]);
-        nan |= isnan(a);
-        m = a > m ? a : m;
+        const unsigned long long b = abs_bits(v[i]);
+        m = b > m ? b : m;
     }
-    return nan ? __longlong_as_double(0x7ff8000000000000ll) : m;
+    // NaN if any component is NaN (its pattern is the largest)
+    return m > 0x7ff0000000000000ull ? __longlong_as_double(0x7ff8000000000000ll) : __longlong_as_double((long long)m);
 }
 __device__ __forceinline__ bool any_nan5(const double *v) {
     bool r = false;
 #pragma unroll
-    for (int i = 0; i < 5; ++i) r |= isnan(v[i]);
+    for (int i = 0; i < 5; ++i) r |= abs_bits(v[i]) > 0x7ff0000000000000ull;
     return r;
 }
 __device__ __forceinline__ bool all_finite5(const double *v) {
     bool r = true;
 #pragma unroll
-    for (int i = 0; i < 5; ++i) r &= isfinite(v[i]);
+    for (int i = 0; i < 5; ++i) r &= abs_bits(v[i]) < 0x7ff0000000000000ull;
     return r;
 }
 
