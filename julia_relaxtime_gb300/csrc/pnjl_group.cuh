@@ -790,6 +790,7 @@ struct Group {
         int st = cs.steps;
         certify(pt, o, out, st, o.max_iter - cs.it32, cs.th_valid);
         out.iterations = cs.it32 + st;
+        if (out.f_converged) dd.publish(cs.x32);
         seed_fallback(pt, x0, o, out, converged, dd);
     }
 
@@ -812,6 +813,7 @@ struct Group {
                 int st = 0, th = 0;
                 if (refine64(pt, o, K32, y32, f, st, o.max_iter - itt, &th)) certify(pt, o, f, st, o.max_iter - itt, th);
                 f.iterations = itt + st;
+                if (f.f_converged) dd.publish(y32);
                 if (choose_fallback(out, f, o.residual_norm_max)) out = f;
             }
         }
@@ -860,15 +862,17 @@ struct LocalRoots {
     }
     __device__ double omega_bound() const { return __longlong_as_double(0x7ff8000000000000ll); }
     __device__ const double *prior_root() const { return nullptr; }
+    __device__ void publish(const double *) {}
 };
 
 // Dedup policy of the task kernel.  Seed s of a slot skips its FP64 work when its FP32 root
-// equals one that an earlier seed s' < s of the same slot has already produced (published as
-// soon as that seed's FP32 phase ends), or `prior`, the certified root of the slot's
-// per-point seed in verification mode.  Only earlier seeds suppress a later one, and a
-// suppressed seed would reach the same FP64 root and lose the min-Omega tie to the earlier
-// seed; an earlier seed still running is not waited for (both are refined, the tie rule
-// keeps the earlier).  omega_bound() is the per-point candidate's Omega (verification mode)
+// equals that of an earlier seed s' < s of the same slot whose candidate is already certified
+// (published after its certification), or `prior`, the certified root of the slot's
+// per-point seed in verification mode.  Only earlier, certified seeds suppress a later one,
+// and a suppressed seed would reach the same FP64 root and lose the min-Omega tie to the
+// earlier seed; an earlier seed still running is not waited for (both are refined, the tie
+// rule keeps the earlier).  A root published before certification could suppress the only
+// seed that certifies it when the earlier one then fails -- a timing-dependent outcome.  omega_bound() is the per-point candidate's Omega (verification mode)
 // -- a bound fixed before any task of the slot starts, so which candidates are discarded as
 // unable to win does not depend on timing; in MultiSeed table mode there is none.  The leader
 // lane reads and writes; answers are broadcast.  With roots = null (a per-point seed, which
@@ -900,13 +904,16 @@ struct PublishedRoots {
         }
         return __shfl_sync(mask, hit, leader) != 0;
     }
-    __device__ void remember(const double *x) {
-        if (own.n == 0 && gl == 0 && roots) {
+    __device__ void remember(const double *x) { own.remember(x); }
+    // Publish the FP32 root x of a certified candidate (once per seed): only certified roots
+    // suppress later seeds, so whether a later seed is skipped never changes which candidate
+    // the min-Omega selection keeps.
+    __device__ void publish(const double *x) {
+        if (gl == 0 && roots && *(volatile const int *)&flag[base + s] == 0) {
             for (int i = 0; i < 5; ++i) __stcg(&roots[5 * (base + s) + i], x[i]);
             __threadfence();
             atomicExch(&flag[base + s], 1);
         }
-        own.remember(x);
     }
 };
 

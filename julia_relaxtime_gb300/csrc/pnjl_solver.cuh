@@ -720,6 +720,11 @@ __device__ void assemble(const DevParams &P, const PointIn &pt, const double *x,
 // FP32-phase steps): each pivot's reciprocal is taken once, by rcp_normal, and multiplied in
 // -- LAPACK's dgetf2 scales the column by the pivot's reciprocal the same way -- instead of
 // 15 IEEE divisions.
+// |v| as a bit pattern: orders like the value for non-negative doubles; NaN above +inf.
+__device__ __forceinline__ unsigned long long abs_bits(double v) {
+    return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+}
+
 template <bool FAST = false>
 __device__ __forceinline__ bool lu_solve5(const double *Ain, const double *b, double *x) {
     double A[25], y[5], inv[5];
@@ -730,13 +735,23 @@ __device__ __forceinline__ bool lu_solve5(const double *Ain, const double *b, do
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
         int p = k;
-        double best = fabs(A[k * 5 + k]);
+        if (FAST) {  // the same first maximal pivot, compared on the bit patterns (integer pipe)
+            unsigned long long bb = abs_bits(A[k * 5 + k]);
 #pragma unroll
-        for (int i = k + 1; i < 5; ++i) {
-            const double v = fabs(A[i * 5 + k]);
-            if (v > best) { best = v; p = i; }
+            for (int i = k + 1; i < 5; ++i) {
+                const unsigned long long v = abs_bits(A[i * 5 + k]);
+                if (v > bb) { bb = v; p = i; }
+            }
+            if (bb == 0) return false;
+        } else {
+            double best = fabs(A[k * 5 + k]);
+#pragma unroll
+            for (int i = k + 1; i < 5; ++i) {
+                const double v = fabs(A[i * 5 + k]);
+                if (v > best) { best = v; p = i; }
+            }
+            if (A[p * 5 + k] == 0.0) return false;
         }
-        if (A[p * 5 + k] == 0.0) return false;
         if (p != k) {
 #pragma unroll
             for (int j = 0; j < 5; ++j) {
@@ -831,9 +846,6 @@ __device__ __forceinline__ void lu_solve_factored5(const double *A, const int *p
 // The 5-vector checks on the bit patterns (integer pipe; the FP64 pipe is the scarce one):
 // |v| as the pattern without the sign orders like the value for non-negative doubles, and a
 // NaN's pattern is above +inf's.
-__device__ __forceinline__ unsigned long long abs_bits(double v) {
-    return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
-}
 __device__ __forceinline__ double norm_inf5(const double *v) {
     unsigned long long m = 0;
 #pragma unroll
