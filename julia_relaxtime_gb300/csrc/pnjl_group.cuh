@@ -790,7 +790,7 @@ struct Group {
         int st = cs.steps;
         certify(pt, o, out, st, o.max_iter - cs.it32, cs.th_valid);
         out.iterations = cs.it32 + st;
-        if (out.f_converged) dd.publish(cs.x32);
+        if (cand_good(out, o.residual_norm_max)) dd.publish(cs.x32);
         seed_fallback(pt, x0, o, out, converged, dd);
     }
 
@@ -813,7 +813,7 @@ struct Group {
                 int st = 0, th = 0;
                 if (refine64(pt, o, K32, y32, f, st, o.max_iter - itt, &th)) certify(pt, o, f, st, o.max_iter - itt, th);
                 f.iterations = itt + st;
-                if (f.f_converged) dd.publish(y32);
+                if (cand_good(f, o.residual_norm_max)) dd.publish(y32);
                 if (choose_fallback(out, f, o.residual_norm_max)) out = f;
             }
         }
@@ -867,12 +867,10 @@ struct LocalRoots {
 
 // Dedup policy of the task kernel.  Seed s of a slot skips its FP64 work when its FP32 root
 // equals that of an earlier seed s' < s of the same slot whose candidate is already certified
-// (published after its certification), or `prior`, the certified root of the slot's
-// per-point seed in verification mode.  Only earlier, certified seeds suppress a later one,
-// and a suppressed seed would reach the same FP64 root and lose the min-Omega tie to the
-// earlier seed; an earlier seed still running is not waited for (both are refined, the tie
-// rule keeps the earlier).  A root published before certification could suppress the only
-// seed that certifies it when the earlier one then fails -- a timing-dependent outcome.  omega_bound() is the per-point candidate's Omega (verification mode)
+// and usable (see publish()), or `prior`, the certified root of the slot's per-point seed in
+// verification mode.  Only such earlier seeds suppress a later one, and a suppressed seed
+// would reach the same FP64 root and lose the min-Omega tie to the earlier seed; an earlier
+// seed still running is not waited for (both are refined, the tie rule keeps the earlier).  omega_bound() is the per-point candidate's Omega (verification mode)
 // -- a bound fixed before any task of the slot starts, so which candidates are discarded as
 // unable to win does not depend on timing; in MultiSeed table mode there is none.  The leader
 // lane reads and writes; answers are broadcast.  With roots = null (a per-point seed, which
@@ -905,9 +903,11 @@ struct PublishedRoots {
         return __shfl_sync(mask, hit, leader) != 0;
     }
     __device__ void remember(const double *x) { own.remember(x); }
-    // Publish the FP32 root x of a certified candidate (once per seed): only certified roots
-    // suppress later seeds, so whether a later seed is skipped never changes which candidate
-    // the min-Omega selection keeps.
+    // Publish the FP32 root x of a certified, usable candidate (converged and physical, once
+    // per seed): it is this seed's final candidate, so whether a later seed reaching the same
+    // root is skipped never changes which candidate the min-Omega selection keeps.  (A root
+    // published earlier -- before certification, or unphysical -- could suppress the only
+    // seed that ends with a usable candidate for it: a timing-dependent outcome.)
     __device__ void publish(const double *x) {
         if (gl == 0 && roots && *(volatile const int *)&flag[base + s] == 0) {
             for (int i = 0; i < 5; ++i) __stcg(&roots[5 * (base + s) + i], x[i]);
@@ -994,13 +994,11 @@ __device__ __forceinline__ const double *table_row(const SolveArgs &a, const Poi
     return (hot && a.seed_table_hot) ? a.seed_table_hot + 5 * s : a.seed_table + 5 * s;
 }
 
-// Whether a converged per-point solution gets the verification seeds: in the first-order
-// region (T below verify_T_max_MeV) or when the root lies far from the seed.
-__device__ __forceinline__ bool needs_verification(const SolveOpts &o, const PointIn &pt, double hbarc,
-                                                   const double *x0, const double *x) {
+// The part of needs_verification known before the solve: the point lies in a flagged cell of
+// the verification map (or outside it), or below verify_T_max_MeV without a map.
+__device__ __forceinline__ bool verification_region(const SolveOpts &o, const PointIn &pt, double hbarc) {
     if (o.verify_seeds <= 0) return false;
     if (o.vmap) {
-        // flagged cell of the (T, mu_u, xi) map; outside the map: always
         const double v[3] = {pt.T, pt.mu[0], pt.xi};
         int64_t idx = 0;
         for (int k = 0; k < 3; ++k) {
@@ -1009,10 +1007,17 @@ __device__ __forceinline__ bool needs_verification(const SolveOpts &o, const Poi
             const int c = min((int)f, o.vn[k] - 1);
             idx = idx * o.vn[k] + c;
         }
-        if (o.vmap[idx]) return true;
-    } else if (pt.T * hbarc < o.verify_T_max_MeV) {
-        return true;
+        return o.vmap[idx] != 0;
     }
+    return pt.T * hbarc < o.verify_T_max_MeV;
+}
+
+// Whether a converged per-point solution gets the verification seeds: in the first-order
+// region (T below verify_T_max_MeV) or when the root lies far from the seed.
+__device__ __forceinline__ bool needs_verification(const SolveOpts &o, const PointIn &pt, double hbarc,
+                                                   const double *x0, const double *x) {
+    if (o.verify_seeds <= 0) return false;
+    if (verification_region(o, pt, hbarc)) return true;
     if (o.verify_max_step > 0.0) {
         double d = 0.0;
         for (int k = 0; k < 5; ++k) d = fmax(d, fabs(x[k] - x0[k]));

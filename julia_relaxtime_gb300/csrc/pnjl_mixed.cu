@@ -449,9 +449,20 @@ __global__ void __launch_bounds__(kFusedThreads, 1) mixed_fused_kernel(SolveArgs
             } else {
                 t = take_bounded(a.queue2, *(volatile const long long *)a.list_count * S);
                 if (t >= 0) kind = 1;
-                if (kind == 0 && *(volatile const long long *)a.queue < a.n) {
+                // two passes over the points: first those in the verification region, whose
+                // listed tasks then start early, then the rest (a point is taken in one pass
+                // and skipped in the other)
+                while (kind == 0 && *(volatile const long long *)a.queue < 2 * a.n) {
                     t = (long long)atomicAdd((unsigned long long *)a.queue, 1ull);
-                    if (t < a.n) kind = 2;
+                    if (t >= 2 * a.n) break;
+                    const int64_t i = t < a.n ? t : t - a.n;
+                    PointIn pt;
+                    load_point(a, i, pt);
+                    const bool first = a.n_seeds > 0 && valid_point(pt) && verification_region(a.opts, pt, a.P.hbarc);
+                    if ((t < a.n) == first) {
+                        kind = 2;
+                        t = i;
+                    }
                 }
                 if (kind == 0 && defer) {
                     t = take_bounded(a.job_head, jobs);
