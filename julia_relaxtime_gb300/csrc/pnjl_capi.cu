@@ -39,6 +39,9 @@ struct pnjl_ctx {
     // workspace for the host entry points
     unsigned char *d_ws = nullptr;
     size_t ws_cap = 0;
+    // pinned host mirror of the workspace for the host-array solves (one DMA each way)
+    unsigned char *h_stage = nullptr;
+    size_t stage_cap = 0;
     // solver scratch: candidate records and per-point completion counters (MultiSeed mode)
     unsigned char *d_scratch = nullptr;
     size_t scratch_cap = 0;
@@ -117,6 +120,26 @@ int ensure_ws(pnjl_ctx *ctx, size_t bytes) {
     }
     ctx->ws_cap = cap;
     return PNJL_OK;
+}
+
+// Pinned staging of at least `bytes`; false (and the caller copies pageable memory
+// directly) when pinned memory is not available.
+bool ensure_stage(pnjl_ctx *ctx, size_t bytes) {
+    if (bytes <= ctx->stage_cap) return true;
+    if (ctx->h_stage) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFreeHost(ctx->h_stage);
+        ctx->h_stage = nullptr;
+        ctx->stage_cap = 0;
+    }
+    const size_t cap = bytes + bytes / 4;
+    if (cudaHostAlloc(&ctx->h_stage, cap, cudaHostAllocDefault) != cudaSuccess) {
+        ctx->h_stage = nullptr;
+        cudaGetLastError();  // clear the failed call
+        return false;
+    }
+    ctx->stage_cap = cap;
+    return true;
 }
 
 pnjl::KernelNodes kernel_nodes(const pnjl_ctx *ctx) {
@@ -285,6 +308,7 @@ int pnjl_destroy(pnjl_ctx *ctx) {
     cudaFree(ctx->d_seed_tables);
     cudaFree(ctx->d_vmap);
     cudaFree(ctx->d_ws);
+    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     cudaFree(ctx->d_scratch);
     cudaFree(ctx->mlp.params);
     cudaFree(ctx->mlp.wb);
@@ -1022,38 +1046,70 @@ static int solve_batch_host(pnjl_ctx *ctx, int64_t n, const double *T, const dou
     d.status = carve<int32_t>(p, nn);
     d.converged = carve<uint8_t>(p, nn);
     cudaStream_t s = ctx->stream;
-    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dT, T, nn * 8, cudaMemcpyHostToDevice, s));
-    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(du, mu_u, nn * 8, cudaMemcpyHostToDevice, s));
-    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dd, mu_d, nn * 8, cudaMemcpyHostToDevice, s));
-    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(ds, mu_s, nn * 8, cudaMemcpyHostToDevice, s));
-    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dxi, xi, nn * 8, cudaMemcpyHostToDevice, s));
+    // inputs and outputs cross through a pinned mirror of the workspace: one DMA each way
+    // (pageable copies are staged by the driver in small synchronous pieces)
+    const size_t in_bytes = (size_t)((unsigned char *)d.x - ctx->d_ws);
+    const size_t out_off = in_bytes, out_bytes = (size_t)(p - ctx->d_ws) - in_bytes;
+    const bool staged = ensure_stage(ctx, in_bytes + out_bytes);
     pnjl_solve_opts o2 = *opts;
-    if (per_point) {
-        PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dseeds, opts->point_seeds, 5 * nn * 8, cudaMemcpyHostToDevice, s));
-        o2.point_seeds = dseeds;
+    if (staged) {
+        unsigned char *h = ctx->h_stage;
+        std::memcpy(h + ((unsigned char *)dT - ctx->d_ws), T, nn * 8);
+        std::memcpy(h + ((unsigned char *)du - ctx->d_ws), mu_u, nn * 8);
+        std::memcpy(h + ((unsigned char *)dd - ctx->d_ws), mu_d, nn * 8);
+        std::memcpy(h + ((unsigned char *)ds - ctx->d_ws), mu_s, nn * 8);
+        std::memcpy(h + ((unsigned char *)dxi - ctx->d_ws), xi, nn * 8);
+        if (per_point) std::memcpy(h + ((unsigned char *)dseeds - ctx->d_ws), opts->point_seeds, 5 * nn * 8);
+        PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_ws, h, in_bytes, cudaMemcpyHostToDevice, s));
+    } else {
+        PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dT, T, nn * 8, cudaMemcpyHostToDevice, s));
+        PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(du, mu_u, nn * 8, cudaMemcpyHostToDevice, s));
+        PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dd, mu_d, nn * 8, cudaMemcpyHostToDevice, s));
+        PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(ds, mu_s, nn * 8, cudaMemcpyHostToDevice, s));
+        PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dxi, xi, nn * 8, cudaMemcpyHostToDevice, s));
+        if (per_point)
+            PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dseeds, opts->point_seeds, 5 * nn * 8, cudaMemcpyHostToDevice, s));
     }
+    if (per_point) o2.point_seeds = dseeds;
     rc = learned ? pnjl_solve_batch_learned_device(ctx, n, dT, du, dd, ds, dxi, &o2, &d)
                  : pnjl_solve_batch_device(ctx, n, dT, du, dd, ds, dxi, &o2, &d);
     if (rc) return rc;
-#define PNJL_D2H(field, count, elem)                                                                              \
-    if (out->field)                                                                                                \
-        PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(out->field, d.field, (count) * (elem), cudaMemcpyDeviceToHost, s));
-    PNJL_D2H(x, 5 * nn, 8)
-    PNJL_D2H(omega, nn, 8)
-    PNJL_D2H(pressure, nn, 8)
-    PNJL_D2H(rho_norm, nn, 8)
-    PNJL_D2H(entropy, nn, 8)
-    PNJL_D2H(energy, nn, 8)
-    PNJL_D2H(residual_norm, nn, 8)
-    PNJL_D2H(masses, 3 * nn, 8)
-    PNJL_D2H(rho, 3 * nn, 8)
-    PNJL_D2H(n_q, 3 * nn, 8)
-    PNJL_D2H(n_aq, 3 * nn, 8)
-    PNJL_D2H(iterations, nn, 4)
-    PNJL_D2H(chosen_seed, nn, 4)
-    PNJL_D2H(status, nn, 4)
-    PNJL_D2H(converged, nn, 1)
-#undef PNJL_D2H
+    if (staged) {
+        unsigned char *h = ctx->h_stage;
+        PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(h + out_off, ctx->d_ws + out_off, out_bytes, cudaMemcpyDeviceToHost, s));
+        PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+        if (out->x) std::memcpy(out->x, h + ((unsigned char *)d.x - ctx->d_ws), (5 * nn) * 8);
+        if (out->omega) std::memcpy(out->omega, h + ((unsigned char *)d.omega - ctx->d_ws), (nn) * 8);
+        if (out->pressure) std::memcpy(out->pressure, h + ((unsigned char *)d.pressure - ctx->d_ws), (nn) * 8);
+        if (out->rho_norm) std::memcpy(out->rho_norm, h + ((unsigned char *)d.rho_norm - ctx->d_ws), (nn) * 8);
+        if (out->entropy) std::memcpy(out->entropy, h + ((unsigned char *)d.entropy - ctx->d_ws), (nn) * 8);
+        if (out->energy) std::memcpy(out->energy, h + ((unsigned char *)d.energy - ctx->d_ws), (nn) * 8);
+        if (out->residual_norm) std::memcpy(out->residual_norm, h + ((unsigned char *)d.residual_norm - ctx->d_ws), (nn) * 8);
+        if (out->masses) std::memcpy(out->masses, h + ((unsigned char *)d.masses - ctx->d_ws), (3 * nn) * 8);
+        if (out->rho) std::memcpy(out->rho, h + ((unsigned char *)d.rho - ctx->d_ws), (3 * nn) * 8);
+        if (out->n_q) std::memcpy(out->n_q, h + ((unsigned char *)d.n_q - ctx->d_ws), (3 * nn) * 8);
+        if (out->n_aq) std::memcpy(out->n_aq, h + ((unsigned char *)d.n_aq - ctx->d_ws), (3 * nn) * 8);
+        if (out->iterations) std::memcpy(out->iterations, h + ((unsigned char *)d.iterations - ctx->d_ws), (nn) * 4);
+        if (out->chosen_seed) std::memcpy(out->chosen_seed, h + ((unsigned char *)d.chosen_seed - ctx->d_ws), (nn) * 4);
+        if (out->status) std::memcpy(out->status, h + ((unsigned char *)d.status - ctx->d_ws), (nn) * 4);
+        if (out->converged) std::memcpy(out->converged, h + ((unsigned char *)d.converged - ctx->d_ws), (nn) * 1);
+    } else {
+        if (out->x) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(out->x, d.x, (5 * nn) * 8, cudaMemcpyDeviceToHost, s));
+        if (out->omega) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(out->omega, d.omega, (nn) * 8, cudaMemcpyDeviceToHost, s));
+        if (out->pressure) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(out->pressure, d.pressure, (nn) * 8, cudaMemcpyDeviceToHost, s));
+        if (out->rho_norm) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(out->rho_norm, d.rho_norm, (nn) * 8, cudaMemcpyDeviceToHost, s));
+        if (out->entropy) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(out->entropy, d.entropy, (nn) * 8, cudaMemcpyDeviceToHost, s));
+        if (out->energy) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(out->energy, d.energy, (nn) * 8, cudaMemcpyDeviceToHost, s));
+        if (out->residual_norm) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(out->residual_norm, d.residual_norm, (nn) * 8, cudaMemcpyDeviceToHost, s));
+        if (out->masses) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(out->masses, d.masses, (3 * nn) * 8, cudaMemcpyDeviceToHost, s));
+        if (out->rho) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(out->rho, d.rho, (3 * nn) * 8, cudaMemcpyDeviceToHost, s));
+        if (out->n_q) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(out->n_q, d.n_q, (3 * nn) * 8, cudaMemcpyDeviceToHost, s));
+        if (out->n_aq) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(out->n_aq, d.n_aq, (3 * nn) * 8, cudaMemcpyDeviceToHost, s));
+        if (out->iterations) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(out->iterations, d.iterations, (nn) * 4, cudaMemcpyDeviceToHost, s));
+        if (out->chosen_seed) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(out->chosen_seed, d.chosen_seed, (nn) * 4, cudaMemcpyDeviceToHost, s));
+        if (out->status) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(out->status, d.status, (nn) * 4, cudaMemcpyDeviceToHost, s));
+        if (out->converged) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(out->converged, d.converged, (nn) * 1, cudaMemcpyDeviceToHost, s));
+    }
     PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(s));
     if (pnjl_get_stats(ctx, &ctx->stats) != PNJL_OK) return PNJL_ERR_CUDA;
     if (ctx->stats.device_wait_timeouts)
