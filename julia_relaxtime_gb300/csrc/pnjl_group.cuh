@@ -736,6 +736,7 @@ struct Group {
             if (dd.seen(x32)) { dup = true; converged = false; return false; }
             dd.remember(x32);
             if (cannot_win(pt, x32, dd.omega_bound())) { dup = true; converged = false; return false; }
+            if (!cs) dd.pending(x32);
             CertState s;
             s.steps = 0;
             if (refine64(pt, o, J32, x32, out, s.steps, o.max_iter - it32, &s.th_valid)) {
@@ -749,6 +750,7 @@ struct Group {
                 return false;
             }
             out.iterations = it32 + s.steps;
+            dd.withdraw();
         } else {
             for (int i = 0; i < 5; ++i) out.x[i] = x32[i];
             out.f_converged = false;
@@ -791,6 +793,7 @@ struct Group {
         certify(pt, o, out, st, o.max_iter - cs.it32, cs.th_valid);
         out.iterations = cs.it32 + st;
         if (cand_good(out, o.residual_norm_max)) dd.publish(cs.x32);
+        else dd.withdraw();
         seed_fallback(pt, x0, o, out, converged, dd);
     }
 
@@ -839,6 +842,24 @@ struct Group {
 };
 
 // ---------------------------------------------------------------------------------------
+// States of a (slot, seed) root flag: no root; a root being certified; a certified, usable root.
+constexpr int kRootNone = 0, kRootPending = 1, kRootUsable = 2;
+// A pending root's verdict comes at the end of one seed's certification (FP64 passes and at
+// most the rest of its iteration budget): polled with a sleep, and given up after about
+// kVerdictPolls x kVerdictSleepNs (then the waiting seed certifies the root itself, the result
+// it reaches without waiting).
+constexpr unsigned kVerdictPolls = 1u << 20;
+constexpr unsigned kVerdictSleepNs = 128;
+
+__device__ __forceinline__ int wait_verdict(const int *flag) {
+    int f = *(volatile const int *)flag;
+    for (unsigned k = 0; f == kRootPending && k < kVerdictPolls; ++k) {
+        __nanosleep(kVerdictSleepNs);
+        f = *(volatile const int *)flag;
+    }
+    return f;
+}
+
 // Duplicate-root test of two FP32 solutions (both within the FP32 noise of one root).
 __device__ __forceinline__ bool same_root(const double *x, const double *y) {
     bool same = true;
@@ -863,14 +884,20 @@ struct LocalRoots {
     __device__ double omega_bound() const { return __longlong_as_double(0x7ff8000000000000ll); }
     __device__ const double *prior_root() const { return nullptr; }
     __device__ void publish(const double *) {}
+    __device__ void pending(const double *) {}
+    __device__ void withdraw() {}
 };
 
 // Dedup policy of the task kernel.  Seed s of a slot skips its FP64 work when its FP32 root
 // equals that of an earlier seed s' < s of the same slot whose candidate is already certified
 // and usable (see publish()), or `prior`, the certified root of the slot's per-point seed in
 // verification mode.  Only such earlier seeds suppress a later one, and a suppressed seed
-// would reach the same FP64 root and lose the min-Omega tie to the earlier seed; an earlier
-// seed still running is not waited for (both are refined, the tie rule keeps the earlier).  omega_bound() is the per-point candidate's Omega (verification mode)
+// would reach the same FP64 root and lose the min-Omega tie to the earlier seed.  An earlier
+// seed still certifying the same root (pending()) is waited for when wait_pending is set, so
+// the later seed ends as it would had the earlier one finished first; with certification
+// deferred to certifying warps it is not (both are refined, the tie rule keeps the earlier).
+// Waits point only to earlier seeds that are certifying, which wait for nothing before their
+// verdict, so every wait ends.  omega_bound() is the per-point candidate's Omega (verification mode)
 // -- a bound fixed before any task of the slot starts, so which candidates are discarded as
 // unable to win does not depend on timing; in MultiSeed table mode there is none.  The leader
 // lane reads and writes; answers are broadcast.  With roots = null (a per-point seed, which
@@ -885,6 +912,7 @@ struct PublishedRoots {
     int leader, gl;
     double prior_omega;   // Omega of `prior` (NaN when there is none)
     LocalRoots own;
+    bool wait_pending = false;  // wait for the verdict on an earlier seed's pending root
     __device__ double omega_bound() const { return prior_omega; }
     __device__ const double *prior_root() const { return prior; }
     __device__ bool seen(const double *x) const {
@@ -893,26 +921,51 @@ struct PublishedRoots {
         if (gl == 0) {
             if (prior && same_root(x, prior)) hit = 1;
             for (int q = 0; q < s && !hit; ++q) {
-                if (*(volatile const int *)&flag[base + q] == 0) continue;
+                int f = *(volatile const int *)&flag[base + q];
+                if (f == kRootNone) continue;
                 __threadfence();
                 double y[5];
                 for (int i = 0; i < 5; ++i) y[i] = __ldcg(&roots[5 * (base + q) + i]);
+                if (f == kRootPending) {
+                    // seed q is certifying this root: its verdict decides, as it would had q
+                    // finished first (skipped when q's root is usable, refined otherwise)
+                    if (!wait_pending || !same_root(x, y)) continue;
+                    f = wait_verdict(&flag[base + q]);
+                    if (f != kRootUsable) continue;
+                    __threadfence();
+                    for (int i = 0; i < 5; ++i) y[i] = __ldcg(&roots[5 * (base + q) + i]);
+                }
                 if (same_root(x, y)) hit = 1;
             }
         }
         return __shfl_sync(mask, hit, leader) != 0;
     }
     __device__ void remember(const double *x) { own.remember(x); }
+    // The FP32 root x that this seed goes on to certify, visible to later seeds of the slot
+    // as pending until publish() or withdraw() gives the verdict.  Only where the later seeds
+    // may wait for it (no deferred certification: the certifying seed runs on, never waiting
+    // itself before its verdict, so every wait ends).
+    __device__ void pending(const double *x) {
+        if (!wait_pending || gl != 0 || !roots || *(volatile const int *)&flag[base + s] != kRootNone) return;
+        for (int i = 0; i < 5; ++i) __stcg(&roots[5 * (base + s) + i], x[i]);
+        __threadfence();
+        atomicExch(&flag[base + s], kRootPending);
+    }
+    // The pending root was not certified usable.
+    __device__ void withdraw() {
+        if (gl == 0 && roots && *(volatile const int *)&flag[base + s] == kRootPending)
+            atomicExch(&flag[base + s], kRootNone);
+    }
     // Publish the FP32 root x of a certified, usable candidate (converged and physical, once
     // per seed): it is this seed's final candidate, so whether a later seed reaching the same
     // root is skipped never changes which candidate the min-Omega selection keeps.  (A root
     // published earlier -- before certification, or unphysical -- could suppress the only
     // seed that ends with a usable candidate for it: a timing-dependent outcome.)
     __device__ void publish(const double *x) {
-        if (gl == 0 && roots && *(volatile const int *)&flag[base + s] == 0) {
+        if (gl == 0 && roots && *(volatile const int *)&flag[base + s] != kRootUsable) {
             for (int i = 0; i < 5; ++i) __stcg(&roots[5 * (base + s) + i], x[i]);
             __threadfence();
-            atomicExch(&flag[base + s], 1);
+            atomicExch(&flag[base + s], kRootUsable);
         }
     }
 };

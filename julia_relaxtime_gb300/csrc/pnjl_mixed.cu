@@ -277,6 +277,7 @@ __device__ void task_step(Group<G> &grp, const SolveArgs &a, int64_t t, bool tab
     double x0[5], prior[5];
     for (int k = 0; k < 5; ++k) x0[k] = row[k];
     PublishedRoots dd = task_roots(a, slot, s, mode, prior, mask, leader, gl);
+    dd.wait_pending = !defer;
     Candidate c;
     bool conv, dup;
     CertState cs;
