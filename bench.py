@@ -86,22 +86,80 @@ def pass_flops(st: dict):
                       st["node_evals_ff_grad_thermo"] * FLOP_GRAD_THERMO)
 
 
+XI9 = np.round(np.arange(-0.4, 0.4001, 0.1), 10)  # -0.4, -0.3, ..., 0.4
+
+
+def stored_grid(T, mu_u, mu_s, xi, **kw):
+    """A workload held as arrays (T, mu in fm^-1); at(idx) -> (T, mu_u, mu_s, xi)."""
+    return dict(n=T.size, at=lambda idx: (T[idx], mu_u[idx], mu_s[idx], xi[idx]), **kw)
+
+
 def workload_grid(name: str):
+    """The bench workloads: points (T, mu_u = mu_d, mu_s, xi), node counts, seed table and,
+    for the surrogate arm, the network's training box."""
+    from julia_relaxtime_gb300 import pnjl
+    from julia_relaxtime_gb300.learned_seed import TrainConfig
+
     if name == "aniso_scan_256x256x9":
         T = np.linspace(50.0, 300.0, 256)
         mu = np.linspace(0.0, 400.0, 256)
-        xi = np.round(np.arange(-0.4, 0.4001, 0.1), 10)
-        Tg, mg, xg = np.meshgrid(T, mu, xi, indexing="ij")
-        return dict(T=Tg.ravel() / HBARC, mu=mg.ravel() / HBARC, xi=xg.ravel().copy(), p_num=128, t_num=32,
-                    n_seeds=4, desc="256x256 (T 50-300 MeV, mu 0-400 MeV) x 9 xi, p128 x t32, 4 seeds, min-Omega")
+        Tg, mg, xg = np.meshgrid(T, mu, XI9, indexing="ij")
+        mu = mg.ravel() / HBARC
+        return stored_grid(Tg.ravel() / HBARC, mu, mu, xg.ravel().copy(), p_num=128, t_num=32, n_seeds=4, extra=(),
+                           chunks=32, train=TrainConfig(),
+                           desc="256x256 (T 50-300 MeV, mu 0-400 MeV) x 9 xi, p128 x t32, 4 seeds, min-Omega")
     if name == "iso_scan_32x32":
         T = np.linspace(50.0, 300.0, 32)
         mu = np.linspace(0.0, 400.0, 32)
         Tg, mg = np.meshgrid(T, mu, indexing="ij")
         n = Tg.size
-        return dict(T=Tg.ravel() / HBARC, mu=mg.ravel() / HBARC, xi=np.zeros(n), p_num=64, t_num=8, n_seeds=6,
-                    desc="32x32 (T 50-300 MeV, mu 0-400 MeV), xi = 0, p64 x t8, MultiSeed (6), min-Omega")
+        mu = mg.ravel() / HBARC
+        return stored_grid(Tg.ravel() / HBARC, mu, mu, np.zeros(n), p_num=64, t_num=8, n_seeds=6, extra=(), chunks=1,
+                           train=TrainConfig(),
+                           desc="32x32 (T 50-300 MeV, mu 0-400 MeV), xi = 0, p64 x t8, MultiSeed (6), min-Omega")
+    if name == "surrogate_eval_2p20":
+        # 2^20 points uniform in the training box, from a counter-based generator (Philox, key
+        # 20240611): the same points on every machine and numpy version
+        rng = np.random.Generator(np.random.Philox(key=20240611))
+        n = 1 << 20
+        T = rng.uniform(50.0, 300.0, n) / HBARC
+        mu = rng.uniform(0.0, 400.0, n) / HBARC
+        xi = rng.uniform(-0.5, 0.5, n)
+        return stored_grid(T, mu, mu, xi, p_num=128, t_num=32, n_seeds=6, extra=(), chunks=32, train=TrainConfig(),
+                           desc="2^20 points U[50,300] MeV x U[0,400] MeV x U[-0.5,0.5] (Philox key 20240611), "
+                                "p128 x t32, MultiSeed (6), min-Omega")
+    if name == "first_order_2048x2048x9":
+        # 37,748,736 points, decoded from the flat index (T slowest, xi fastest) when a slice
+        # is loaded; mu_s = 0.5 mu_u
+        nT = nm = 2048
+        Tv = np.linspace(20.0, 150.0, nT) / HBARC
+        mv = np.linspace(250.0, 450.0, nm) / HBARC
+
+        def at(idx):
+            idx = np.asarray(idx, dtype=np.int64)
+            ix = idx % XI9.size
+            r = idx // XI9.size
+            mu_u = mv[r % nm]
+            return Tv[r // nm], mu_u, 0.5 * mu_u, XI9[ix]
+
+        extra = (pnjl.MEDIUM_SEED_5, pnjl.HIGH_DENSITY_SEED_5)
+        return dict(n=nT * nm * XI9.size, at=at, p_num=128, t_num=32, n_seeds=6, extra=extra, chunks=2048,
+                    train=TrainConfig(T_MeV=(20.0, 150.0, 64), mu_MeV=(250.0, 450.0, 64), xi=(-0.5, 0.5, 5),
+                                      mu_s_ratio=0.5, label_seeds=6, label_extra=extra),
+                    desc="2048x2048 (T 20-150 MeV, mu_u 250-450 MeV, mu_s = mu_u/2) x 9 xi, p128 x t32, "
+                         "8 seeds (MultiSeed + MEDIUM, HIGH_DENSITY), min-Omega")
     raise SystemExit(f"unknown workload {name}")
+
+
+def slice_indices(n: int, rank: int, world: int, chunks: int, c: int) -> np.ndarray:
+    """Global indices of slice c (mod chunks) of rank's shard: shard_points(n, rank, world)[c::chunks],
+    computed without materialising the shard."""
+    n_local = len(range(rank, n, world))
+    return rank + world * np.arange(c % chunks, n_local, chunks, dtype=np.int64)
+
+
+def seed_count(grid) -> int:
+    return grid["n_seeds"] + len(grid["extra"])
 
 
 class ClockSampler:
@@ -163,17 +221,24 @@ def run_reference(args, grid, sample_points: int):
     P = orc.default_params()
     nd = orc.Nodes(grid["p_num"], grid["t_num"])
     threads = os.cpu_count() or 1
-    n = grid["T"].size
+    n = grid["n"]
     rng = np.random.default_rng(1234)
     idx = np.sort(rng.choice(n, size=min(sample_points, n), replace=False))
     opts = orc.default_opts(max_iter=40, ftol=1e-10)
-    T = grid["T"][idx]
-    mu3 = np.repeat(grid["mu"][idx][:, None], 3, axis=1)
-    xi = grid["xi"][idx]
+    T, mu_u, mu_s, xi = grid["at"](idx)
+    mu3 = np.stack([mu_u, mu_u, mu_s], axis=1)
+    kw = dict(n_seeds=grid["n_seeds"])
+    if grid["extra"]:
+        # an explicit candidate table: the MultiSeed candidates below T = 300 MeV plus the extra
+        # rows (the workloads with extra rows lie below 300 MeV, where the table is fixed)
+        from julia_relaxtime_gb300.pnjl import multiseed_table
+
+        assert float(np.max(T)) * HBARC < 300.0
+        kw = dict(seeds=multiseed_table(grid["n_seeds"], grid["extra"])[0], multiseed_rule=False)
     times, solved = [], 0
     for it in range(args.warmup + args.steps):
         t0 = time.perf_counter()
-        rs = orc.solve_batch(P, nd, T, mu3, xi, multi=True, n_seeds=grid["n_seeds"], opts=opts, threads=threads)
+        rs = orc.solve_batch(P, nd, T, mu3, xi, multi=True, opts=opts, threads=threads, **kw)
         dt = time.perf_counter() - t0
         if it >= args.warmup:
             times.append(dt)
@@ -191,7 +256,8 @@ class Arm:
 
     def launch(self, n, d_in, ptrs):
         m = d_in["mu"].data_ptr()
-        self.eng.solve_device(n, d_in["T"].data_ptr(), m, m, m, d_in["xi"].data_ptr(), ptrs, seed_table=self.table,
+        self.eng.solve_device(n, d_in["T"].data_ptr(), m, m, d_in["mu_s"].data_ptr(), d_in["xi"].data_ptr(), ptrs,
+                              seed_table=self.table,
                               seed_table_hot=self.hot, opts=self.opts, learned=self.learned)
 
 
@@ -206,7 +272,7 @@ def run_orders(args):
     from julia_relaxtime_gb300.pnjl import multiseed_table
 
     grid = workload_grid("iso_scan_32x32")
-    T, mu, xi = grid["T"], grid["mu"], grid["xi"]
+    T, mu, _, xi = grid["at"](np.arange(grid["n"]))
     n = T.size
     orders = (64, 128, 256)
     eng = GapEngine(p_num=64, t_num=8)
@@ -290,7 +356,9 @@ def main():
                          "precision, errors against the FP64 solve of the same kernel)")
     ap.add_argument("--precision", default=None, choices=("fp64", "mixed"),
                     help="precision of the timed arm (default: mixed for surrogate, fp64 for multiseed)")
-    ap.add_argument("--chunks", type=int, default=32, help="the grid is solved in this many strided slices")
+    ap.add_argument("--chunks", type=int, default=None,
+                    help="the grid is solved in this many strided slices (default: per workload -- 32, or 2048 "
+                         "for the 37.7 M-point first-order scan, 1 for the 32 x 32 grid)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 multi-seed comparison arm")
     ap.add_argument("--cpu-sample", type=int, default=48, help="points per step of the CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -305,8 +373,10 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     grid = workload_grid(args.workload)
-    config = {"workload": args.workload, "grid": grid["desc"], "points": int(grid["T"].size),
-              "points_per_step": int(math.ceil(grid["T"].size / world / args.chunks)), "ftol": 1e-10,
+    if args.chunks is None:
+        args.chunks = grid["chunks"]
+    config = {"workload": args.workload, "grid": grid["desc"], "points": int(grid["n"]),
+              "points_per_step": int(math.ceil(grid["n"] / world / args.chunks)), "ftol": 1e-10,
               "max_iter": 40, "mode": args.mode, "precision": precision,
               "l2": "256 MiB device buffer written before every timed step"}
 
@@ -336,21 +406,25 @@ def main():
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
     torch.cuda.set_device(local_rank)
-    from julia_relaxtime_gb300.engine import GapEngine, SolveOptions, shard_points
-    from julia_relaxtime_gb300.learned_seed import TrainConfig, default_learned_opts, train_learned_seed
-    from julia_relaxtime_gb300.pnjl import MultiSeed, multiseed_table
+    from julia_relaxtime_gb300.engine import GapEngine, SolveOptions
+    from julia_relaxtime_gb300.learned_seed import default_learned_opts, train_learned_seed
+    from julia_relaxtime_gb300.pnjl import DefaultSeed, MultiSeed, multiseed_table
 
     eng = GapEngine(device=local_rank, p_num=grid["p_num"], t_num=grid["t_num"])
-    table, hot = multiseed_table(grid["n_seeds"])
+    table, hot = multiseed_table(grid["n_seeds"], grid["extra"])
     train = None
     if args.mode == "surrogate":
         # set-up, untimed: label the 64 x 64 x 5 training grid with the multi-seed solver and
         # train the network on it (both on this GPU); reported as train_s
+        tc = grid["train"]
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        ls = train_learned_seed(eng, TrainConfig())
-        train = {"seconds": time.perf_counter() - t0, "labels": "64 x 64 x 5 (T, mu, xi) grid, MultiSeed (6) mixed",
-                 "epochs": TrainConfig().epochs}
+        ls = train_learned_seed(eng, tc)
+        train = {"seconds": time.perf_counter() - t0,
+                 "labels": f"64 x 64 x 5 (T {tc.T_MeV[0]:g}-{tc.T_MeV[1]:g} MeV, mu {tc.mu_MeV[0]:g}-{tc.mu_MeV[1]:g} "
+                           f"MeV, xi {tc.xi[0]:g}..{tc.xi[1]:g}) grid, mu_s = {tc.mu_s_ratio:g} mu_u, "
+                           f"MultiSeed ({tc.label_seeds + len(tc.label_extra)}) mixed",
+                 "epochs": tc.epochs}
         arm = Arm("surrogate", eng, table, hot,
                   default_learned_opts(ftol=1e-10, precision=precision, verify_map=ls.verify_map), True)
         train["verify_map_cells_flagged"] = ls.verify_map.fraction()
@@ -358,14 +432,17 @@ def main():
         arm = Arm("multiseed", eng, table, hot, SolveOptions(iterations=40, ftol=1e-10, precision=precision), False)
     plain = Arm("plain_fp64", eng, table, hot, SolveOptions(iterations=40, ftol=1e-10, precision="fp64"), False)
 
-    # this rank's share of the points: a strided shard (no data exchange between ranks)
-    mine = shard_points(grid["T"].size, rank, world)
-    T_all, mu_all, xi_all = grid["T"][mine], grid["mu"][mine], grid["xi"][mine]
-    chunks = [np.arange(c, T_all.size, args.chunks) for c in range(args.chunks)]
+    # this rank's share of the points: a strided shard (shard_points: no data exchange between
+    # ranks), solved in strided slices; slice c holds the shard's points c, c + chunks, ...
+    n_local = len(range(rank, grid["n"], world))
+
+    def chunk_points(c):
+        return grid["at"](slice_indices(grid["n"], rank, world, args.chunks, c))
+
     dev = torch.device("cuda", local_rank)
     stream = torch.cuda.ExternalStream(eng.stream(), device=dev)
-    maxn = max(len(c) for c in chunks)
-    d_in = {k: torch.empty(maxn, dtype=torch.float64, device=dev) for k in ("T", "mu", "xi")}
+    maxn = int(math.ceil(n_local / args.chunks))
+    d_in = {k: torch.empty(maxn, dtype=torch.float64, device=dev) for k in ("T", "mu", "mu_s", "xi")}
     f64 = lambda *s: torch.empty(*s, dtype=torch.float64, device=dev)  # noqa: E731
     d_out = {"x": f64(maxn * 5), "omega": f64(maxn), "pressure": f64(maxn), "rho_norm": f64(maxn),
              "entropy": f64(maxn), "energy": f64(maxn), "residual_norm": f64(maxn), "masses": f64(maxn * 3),
@@ -378,12 +455,11 @@ def main():
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
 
     def load_chunk(c):
-        idx = chunks[c]
-        n = idx.size
+        T, mu_u, mu_s, xi = chunk_points(c)
+        n = T.size
         with torch.cuda.stream(stream):
-            d_in["T"][:n].copy_(torch.from_numpy(T_all[idx]))
-            d_in["mu"][:n].copy_(torch.from_numpy(mu_all[idx]))
-            d_in["xi"][:n].copy_(torch.from_numpy(xi_all[idx]))
+            for k, v in (("T", T), ("mu", mu_u), ("mu_s", mu_s), ("xi", xi)):
+                d_in[k][:n].copy_(torch.from_numpy(np.ascontiguousarray(v)))
         stream.synchronize()
         return n
 
@@ -460,7 +536,7 @@ def main():
     if not args.no_autotune:
         n0 = load_chunk(0)
         m0 = d_in["mu"].data_ptr()
-        best, tried = eng.autotune(n0, d_in["T"].data_ptr(), m0, m0, m0, d_in["xi"].data_ptr(), ptrs,
+        best, tried = eng.autotune(n0, d_in["T"].data_ptr(), m0, m0, d_in["mu_s"].data_ptr(), d_in["xi"].data_ptr(), ptrs,
                                    seed_table=table, seed_table_hot=hot, opts=arm.opts, learned=arm.learned, reps=2)
         eng.synchronize()
         tuning = {"chosen": best, "candidates": len(tried),
@@ -498,7 +574,7 @@ def main():
                 n_rel += int(np.sum(rel.max(axis=1) > 1e-9))
                 dPhi = max(dPhi, float(np.max(np.abs(xr[:, 3:] - xq[:, 3:]))))
         plain_line = {"value": prec["value"], "unit": "solves/s", "ms_per_step": prec["total_ms"] / args.steps,
-                      "precision": "fp64", "seeds": grid["n_seeds"], "speedup": main_rec["value"] / prec["value"],
+                      "precision": "fp64", "seeds": seed_count(grid), "speedup": main_rec["value"] / prec["value"],
                       "phase_misassignments": mis, "points_compared": both_n, "max_rel_dphi": dphi,
                       "points_rel_dphi_above_1e-9": n_rel, "max_abs_dphi": dphi_abs, "max_abs_dPhi": dPhi,
                       "work_per_step": {k: v / args.steps for k, v in prec["kinds"].items()}}
@@ -509,13 +585,14 @@ def main():
     if not args.no_e2e:
         e2e_solved, e2e_s, h2d, d2h = 0, 0.0, 0, 0
         # the same candidates as the device-array arm (the first n_seeds of MultiSeed)
-        e2e_ms = MultiSeed(candidates=MultiSeed().candidates[:grid["n_seeds"]])
+        e2e_ms = MultiSeed(candidates=MultiSeed().candidates[:grid["n_seeds"]] +
+                           [DefaultSeed(tuple(r), tuple(r), "hadron") for r in grid["extra"]])
         for k in range(-1, args.steps):  # k = -1: one untimed call (allocates the pinned staging)
-            idx = chunks[k % args.chunks]
-            n = idx.size
-            Th = torch.from_numpy(T_all[idx]).pin_memory().numpy()
-            Mh = torch.from_numpy(mu_all[idx]).pin_memory().numpy()
-            Xh = torch.from_numpy(xi_all[idx]).pin_memory().numpy()
+            T_, mu_u, mu_s, xi_ = chunk_points(k)
+            n = T_.size
+            Th = torch.from_numpy(np.ascontiguousarray(T_)).pin_memory().numpy()
+            Mh = torch.from_numpy(np.stack([mu_u, mu_u, mu_s], axis=1)).pin_memory().numpy()
+            Xh = torch.from_numpy(np.ascontiguousarray(xi_)).pin_memory().numpy()
             t0 = time.perf_counter()
             if arm.learned:
                 r = ls.solve(Th, Mh, Xh, opts=arm.opts, multiseed=e2e_ms)
@@ -578,7 +655,7 @@ def main():
         line["surrogate"] = {"train": train,
                              "fallback_rate": main_rec["kinds"].get("multiseed_fallbacks", 0) /
                              max(1, config["points_per_step"] * args.steps),
-                             "verify": {"seeds": grid["n_seeds"] if arm.opts.verify_seeds < 0 else arm.opts.verify_seeds,
+                             "verify": {"seeds": seed_count(grid) if arm.opts.verify_seeds < 0 else arm.opts.verify_seeds,
                                         "region": "verification map (flagged cells of the label grid)"
                                         if arm.opts.verify_map is not None else
                                         f"T < {arm.opts.verify_T_max_MeV} MeV",

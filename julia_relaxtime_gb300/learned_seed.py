@@ -29,7 +29,8 @@ def param_count() -> int:
 
 @dataclass
 class TrainConfig:
-    """The training set: a 64 x 64 x 5 solver-labelled (T 50-300 MeV, mu 0-400 MeV, xi -0.5..0.5) grid."""
+    """The training set: a 64 x 64 x 5 solver-labelled (T 50-300 MeV, mu 0-400 MeV, xi -0.5..0.5) grid.
+    mu is mu_u = mu_d; mu_s = mu_s_ratio * mu_u (the network's input is mu_u)."""
     T_MeV: tuple = (50.0, 300.0, 64)
     mu_MeV: tuple = (0.0, 400.0, 64)
     xi: tuple = (-0.5, 0.5, 5)
@@ -39,6 +40,8 @@ class TrainConfig:
     seed: int = 20240611
     label_seeds: int = 6          # MultiSeed candidates used to label the grid
     label_precision: str = "mixed"
+    mu_s_ratio: float = 1.0
+    label_extra: tuple = ()       # seed rows appended to the label table (e.g. MEDIUM, HIGH_DENSITY)
 
 
 def grid_points(cfg: TrainConfig):
@@ -47,6 +50,20 @@ def grid_points(cfg: TrainConfig):
     xi = np.linspace(*cfg.xi)
     Tg, mg, xg = np.meshgrid(T, mu, xi, indexing="ij")
     return Tg.ravel(), mg.ravel(), xg.ravel()
+
+
+def flavour_mu(cfg: TrainConfig, mu):
+    """(mu_u, mu_d, mu_s) of the label points: mu_u = mu_d = mu, mu_s = mu_s_ratio * mu."""
+    mu = np.asarray(mu, dtype=np.float64)
+    if cfg.mu_s_ratio == 1.0:
+        return mu
+    return np.stack([mu, mu, cfg.mu_s_ratio * mu], axis=1)
+
+
+def label_table(cfg: TrainConfig):
+    from .pnjl import multiseed_table
+
+    return multiseed_table(cfg.label_seeds, cfg.label_extra)
 
 
 class LearnedSeed(SeedStrategy):
@@ -68,10 +85,15 @@ class LearnedSeed(SeedStrategy):
         self._check(self._lib.pnjl_mlp_set_scaling(self.engine._ctx, *(_dp(a) for a in arrs)), "pnjl_mlp_set_scaling")
         self.scaling = arrs
 
-    def default_scaling(self, targets):
+    def default_scaling(self, targets, cfg: TrainConfig | None = None):
+        """Inputs mapped to [-1, 1] over the training box (cfg; the default box without it),
+        outputs standardised."""
+        cfg = cfg or TrainConfig()
         t = np.asarray(targets, dtype=np.float64)
-        in_shift = np.array([175.0 / HBARC_MEV_FM, 200.0 / HBARC_MEV_FM, 0.0])
-        in_scale = np.array([125.0 / HBARC_MEV_FM, 200.0 / HBARC_MEV_FM, 0.5])
+        lo = np.array([cfg.T_MeV[0] / HBARC_MEV_FM, cfg.mu_MeV[0] / HBARC_MEV_FM, cfg.xi[0]])
+        hi = np.array([cfg.T_MeV[1] / HBARC_MEV_FM, cfg.mu_MeV[1] / HBARC_MEV_FM, cfg.xi[1]])
+        in_shift = 0.5 * (lo + hi)
+        in_scale = np.maximum(0.5 * (hi - lo), 1e-6)
         out_shift = t.mean(axis=0)
         out_scale = np.maximum(t.std(axis=0), 1e-6)
         self.set_scaling(in_shift, in_scale, out_shift, out_scale)
@@ -168,11 +190,9 @@ def default_learned_opts(**kw) -> SolveOptions:
 def label_grid(engine: GapEngine, cfg: TrainConfig, opts: SolveOptions | None = None):
     """Solve the training grid with the multi-seed solver; returns the converged points."""
     T, mu, xi = grid_points(cfg)
-    from .pnjl import multiseed_table
-
-    table, hot = multiseed_table(cfg.label_seeds)
+    table, hot = label_table(cfg)
     opts = opts or SolveOptions(iterations=40, ftol=1e-10, precision=cfg.label_precision)
-    res = engine.solve(T, mu, xi, seed_table=table, seed_table_hot=hot, opts=opts)
+    res = engine.solve(T, flavour_mu(cfg, mu), xi, seed_table=table, seed_table_hot=hot, opts=opts)
     ok = res["converged"]
     return T[ok], mu[ok], xi[ok], res["x"][ok], res
 
@@ -180,10 +200,9 @@ def label_grid(engine: GapEngine, cfg: TrainConfig, opts: SolveOptions | None = 
 def candidate_roots(engine: GapEngine, cfg: TrainConfig):
     """Root (NaN where not converged) and Omega of every MultiSeed candidate alone at every
     label-grid point: [N, S, 5] and [N, S]."""
-    from .pnjl import multiseed_table
-
     T, mu, xi = grid_points(cfg)
-    table, hot = multiseed_table(cfg.label_seeds)
+    mu = flavour_mu(cfg, mu)
+    table, hot = label_table(cfg)
     opts = SolveOptions(iterations=40, ftol=1e-10, precision=cfg.label_precision)
     roots, omegas = [], []
     for s in range(table.shape[0]):  # each candidate alone: a one-row MultiSeed table
@@ -253,6 +272,7 @@ def train_learned_seed(engine: GapEngine, cfg: TrainConfig | None = None) -> Lea
     cfg = cfg or TrainConfig()
     T, mu, xi, x, res = label_grid(engine, cfg)
     ls = LearnedSeed(engine, seed=cfg.seed)
+    ls.default_scaling(x, cfg)
     ls.fit(T, mu, xi, x, epochs=cfg.epochs, batch=cfg.batch, lr=cfg.lr, shuffle_seed=cfg.seed + 1)
     ls.verify_map = coexistence_map(engine, cfg, res)
     return ls

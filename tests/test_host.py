@@ -320,3 +320,33 @@ def test_shard_points_two_ranks_gloo():
     assert set(a) | set(b) == set(range(10)) and not set(a) & set(b)
     with pytest.raises(ValueError):
         shard_points(10, 2, 2)
+
+
+def test_bench_slices_and_workload_grids():
+    """The bench's slices partition each rank's shard; the lazily decoded first-order grid
+    (2048 x 2048 x 9, mu_s = mu_u / 2) is the meshgrid of its axes, T slowest and xi fastest;
+    the 2^20-point set is reproducible."""
+    import bench
+    from julia_relaxtime_gb300.engine import shard_points
+
+    n, world, chunks = 1000 + 7, 2, 13
+    for rank in range(world):
+        mine = shard_points(n, rank, world)
+        parts = [bench.slice_indices(n, rank, world, chunks, c) for c in range(chunks)]
+        assert np.array_equal(np.sort(np.concatenate(parts)), mine)
+        assert np.array_equal(parts[3], mine[3::chunks])
+    g = bench.workload_grid("first_order_2048x2048x9")
+    assert g["n"] == 2048 * 2048 * 9 and bench.seed_count(g) == 8
+    idx = np.array([0, 1, 8, 9, 2048 * 9 - 1, 2048 * 9, 123_456_7, g["n"] - 1])
+    T, mu_u, mu_s, xi = g["at"](idx)
+    iT, im, ix = np.unravel_index(idx, (2048, 2048, 9))
+    np.testing.assert_allclose(T * HBARC, np.linspace(20.0, 150.0, 2048)[iT], rtol=1e-14)
+    np.testing.assert_allclose(mu_u * HBARC, np.linspace(250.0, 450.0, 2048)[im], rtol=1e-14)
+    np.testing.assert_array_equal(mu_s, 0.5 * mu_u)
+    np.testing.assert_allclose(xi, np.round(np.arange(-0.4, 0.4001, 0.1), 10)[ix])
+    a, b = bench.workload_grid("surrogate_eval_2p20"), bench.workload_grid("surrogate_eval_2p20")
+    assert a["n"] == 1 << 20
+    pa, pb = a["at"](np.arange(0, a["n"], 4099)), b["at"](np.arange(0, b["n"], 4099))
+    for u, v in zip(pa, pb):
+        np.testing.assert_array_equal(u, v)
+    assert 50.0 <= pa[0].min() * HBARC and pa[0].max() * HBARC <= 300.0 and np.abs(pa[3]).max() <= 0.5
