@@ -86,6 +86,14 @@ struct Group {
     }
 
     // Omega, entropy, rho_f and number densities at x (one thermo pass) -> candidate fields
+    // det5_negative of the FP64 Jacobian at x (a root of the FP64 path, which keeps no
+    // Jacobian with its candidate): one FP64 Newton pass.
+    __device__ bool unstable_root(const PointIn &pt, const double *x) {
+        double F[5], J[25];
+        eval_newton(pt, x, F, J);
+        return det5_negative(J);
+    }
+
     __device__ __noinline__ void eval_thermo(const PointIn &pt, const SolveOpts &o, Candidate &c) {
         double M[3];
         masses(P, c.x, M);
@@ -723,6 +731,7 @@ struct Group {
                                                   bool &converged, bool &dup, D &dd, CertState *cs = nullptr) {
         cnt.v[kStatSeeds] += 1;
         dup = false;
+        out.unstable = false;
         double x32[5], J32[25];
         int it32 = 0;
         const int r = newton32(pt, x0, o, x32, J32, it32, dd.prior_root());
@@ -739,6 +748,8 @@ struct Group {
             if (!cs) dd.pending(x32);
             CertState s;
             s.steps = 0;
+            // only where the result may be verified; J32 before the refinement's Broyden updates
+            s.unstable = o.verify_seeds > 0 && dd.per_point() && det5_negative(J32) ? 1 : 0;
             if (refine64(pt, o, J32, x32, out, s.steps, o.max_iter - it32, &s.th_valid)) {
                 for (int k = 0; k < 5; ++k) s.x32[k] = x32[k];
                 s.it32 = it32;
@@ -792,6 +803,7 @@ struct Group {
         int st = cs.steps;
         certify(pt, o, out, st, o.max_iter - cs.it32, cs.th_valid);
         out.iterations = cs.it32 + st;
+        out.unstable = cs.unstable != 0;
         if (cand_good(out, o.residual_norm_max)) dd.publish(cs.x32);
         else dd.withdraw();
         seed_fallback(pt, x0, o, out, converged, dd);
@@ -813,9 +825,11 @@ struct Group {
                     return;
                 }
                 Candidate f;
+                const bool unst = o.verify_seeds > 0 && dd.per_point() && det5_negative(K32);
                 int st = 0, th = 0;
                 if (refine64(pt, o, K32, y32, f, st, o.max_iter - itt, &th)) certify(pt, o, f, st, o.max_iter - itt, th);
                 f.iterations = itt + st;
+                f.unstable = unst;
                 if (cand_good(f, o.residual_norm_max)) dd.publish(y32);
                 if (choose_fallback(out, f, o.residual_norm_max)) out = f;
             }
@@ -883,6 +897,7 @@ struct LocalRoots {
     }
     __device__ double omega_bound() const { return __longlong_as_double(0x7ff8000000000000ll); }
     __device__ const double *prior_root() const { return nullptr; }
+    __device__ bool per_point() const { return true; }
     __device__ void publish(const double *) {}
     __device__ void pending(const double *) {}
     __device__ void withdraw() {}
@@ -915,6 +930,8 @@ struct PublishedRoots {
     bool wait_pending = false;  // wait for the verdict on an earlier seed's pending root
     __device__ double omega_bound() const { return prior_omega; }
     __device__ const double *prior_root() const { return prior; }
+    // a per-point seed (no slot), whose root may be sent to the verification seeds
+    __device__ bool per_point() const { return roots == nullptr; }
     __device__ bool seen(const double *x) const {
         if (own.seen(x)) return true;
         int hit = 0;
@@ -1065,11 +1082,13 @@ __device__ __forceinline__ bool verification_region(const SolveOpts &o, const Po
     return pt.T * hbarc < o.verify_T_max_MeV;
 }
 
-// Whether a converged per-point solution gets the verification seeds: in the first-order
-// region (T below verify_T_max_MeV) or when the root lies far from the seed.
+// Whether a converged per-point solution gets the verification seeds: on an unstable branch
+// (det5_negative), in the first-order region (a flagged cell of the verification map, or T
+// below verify_T_max_MeV without one) or when the root lies far from the seed.
 __device__ __forceinline__ bool needs_verification(const SolveOpts &o, const PointIn &pt, double hbarc,
-                                                   const double *x0, const double *x) {
+                                                   const double *x0, const double *x, bool unstable) {
     if (o.verify_seeds <= 0) return false;
+    if (unstable) return true;  // an unstable branch is never the min-Omega phase: find the others
     if (verification_region(o, pt, hbarc)) return true;
     if (o.verify_max_step > 0.0) {
         double d = 0.0;

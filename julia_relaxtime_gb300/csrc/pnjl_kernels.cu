@@ -111,7 +111,8 @@ __global__ void __launch_bounds__(kSolveThreads, 2) solve_kernel(SolveArgs a) {
                 if (gl == 0) write_point(a.P, pt, a.out, i, single, false, -1, PNJL_POINT_EXCEPTION);
                 continue;
             }
-            if (conv && needs_verification(o, pt, a.P.hbarc, x0, single.x)) {
+            if (conv && o.verify_seeds > 0 &&
+                needs_verification(o, pt, a.P.hbarc, x0, single.x, grp.unstable_root(pt, single.x))) {
                 Candidate best = single;
                 int chosen = -1;
                 for (int s = 0; s < o.verify_seeds; ++s) {

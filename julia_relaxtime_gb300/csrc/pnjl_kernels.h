@@ -37,7 +37,7 @@ struct CandRec {
 // belong to its state.
 struct CertState {
     double x32[5];
-    int it32, steps, th_valid;
+    int it32, steps, th_valid, unstable;
 };
 
 // Scratch record of a deferred seed, from the warp that refined it to a certifying warp:

@@ -79,6 +79,7 @@ __device__ __forceinline__ void load_job(const CertJob *jp, long long &t, int &k
     cs.it32 = __ldcg(&jp->cs.it32);
     cs.steps = __ldcg(&jp->cs.steps);
     cs.th_valid = __ldcg(&jp->cs.th_valid);
+    cs.unstable = __ldcg(&jp->cs.unstable);
     c.residual_norm = __ldcg(&jp->residual_norm);
     c.omega = __ldcg(&jp->omega);
     c.entropy = __ldcg(&jp->entropy);
@@ -102,7 +103,7 @@ __device__ void point_complete(const SolveArgs &a, const PointIn &pt, int64_t i,
     if (single.exception) {
         mode = -2;
     } else if (conv) {
-        if (S > 0 && needs_verification(o, pt, a.P.hbarc, x0, single.x)) mode = kListVerify;
+        if (S > 0 && needs_verification(o, pt, a.P.hbarc, x0, single.x, single.unstable)) mode = kListVerify;
     } else if (o.auto_multiseed_fallback && S > 0) {
         mode = kListFallback;
         cnt.v[kStatMsFallbacks] += 1;

@@ -725,6 +725,53 @@ __device__ __forceinline__ unsigned long long abs_bits(double v) {
     return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
 }
 
+// Whether the root with Jacobian J = Hessian_x P (= -Hessian_x Omega, 5 x 5) lies on an
+// unstable branch: det J < 0.  A thermodynamically stable root -- the min-Omega phase, or a
+// metastable one -- has exactly one negative eigenvalue of Hessian_x Omega, the saddle of the
+// Polyakov-loop potential in (Phi, Phibar), so det J > 0; the branch between two coexisting
+// phases has a second one.  (Checked with the oracle's Hessians on 600 random points of the
+// (T, mu, xi) boxes of the scans: every min-Omega root has one negative eigenvalue, every
+// root with two has det J < 0.)  Elimination with partial pivoting on a copy; a singular or
+// non-finite J counts as unstable.
+static __device__ __noinline__ bool det5_negative(const double *Jin) {
+    double A[25];
+#pragma unroll
+    for (int i = 0; i < 25; ++i) A[i] = Jin[i];
+    bool neg = false;
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+        int p = c;
+        double big = fabs(A[c * 5 + c]);
+#pragma unroll
+        for (int r = c + 1; r < 5; ++r) {
+            const double v = fabs(A[r * 5 + c]);
+            if (v > big) { big = v; p = r; }
+        }
+        if (!(big > 0.0 && big <= 1.7976931348623157e308)) return true;
+#pragma unroll
+        for (int r = c + 1; r < 5; ++r)
+            if (r == p) {
+#pragma unroll
+                for (int k = c; k < 5; ++k) {
+                    const double t = A[c * 5 + k];
+                    A[c * 5 + k] = A[r * 5 + k];
+                    A[r * 5 + k] = t;
+                }
+                neg = !neg;
+            }
+        const double d = A[c * 5 + c];
+        if (d < 0.0) neg = !neg;
+        const double inv = 1.0 / d;
+#pragma unroll
+        for (int r = c + 1; r < 5; ++r) {
+            const double f = A[r * 5 + c] * inv;
+#pragma unroll
+            for (int k = c + 1; k < 5; ++k) A[r * 5 + k] = fma(-f, A[c * 5 + k], A[r * 5 + k]);
+        }
+    }
+    return neg;
+}
+
 template <bool FAST = false>
 __device__ __forceinline__ bool lu_solve5(const double *Ain, const double *b, double *x) {
     double A[25], y[5], inv[5];
@@ -875,6 +922,7 @@ struct Candidate {
     double residual_norm;
     int iterations;
     bool f_converged, exception, phys;
+    bool unstable = false;  // the root lies on an unstable branch (det5_negative)
     double omega, entropy, rho[3], nq[3], naq[3];
 };
 

@@ -568,3 +568,32 @@ def test_plan_mixed_orders_one_graph(engine_factory):
     both = first[0]["converged"].astype(bool) & first[2]["converged"].astype(bool)
     assert np.median(np.abs(d64[both] - d256[both])) < 1e-2
     plan.close()
+
+
+def test_unstable_branch_root_gets_verified(engine_factory):
+    """A per-point seed that converges to the unstable branch between two coexisting phases
+    (T = 136.35 MeV, mu_u = mu_d = 250 MeV, mu_s = 125 MeV, xi = -0.4; three roots) is
+    verified by the MultiSeed candidates although the point lies outside the verification
+    region and the root is close to the seed: the result is the min-Omega root of the plain
+    multi-seed solve, in mixed precision and in FP64."""
+    eng = engine_factory(128, 32)
+    T = np.array([136.3458720078163]) / HBARC
+    mu = np.array([[250.0, 250.0, 125.0]]) / HBARC
+    xi = np.array([-0.4])
+    seed = np.array([[-1.1634, -1.1634, -2.111, 0.2479, 0.2862]])  # the learned seed there
+    table, hot = pnjl.multiseed_table(6, (pnjl.MEDIUM_SEED_5, pnjl.HIGH_DENSITY_SEED_5))
+    ref = eng.solve(T, mu, xi, seed_table=table, seed_table_hot=hot,
+                    opts=SolveOptions(iterations=40, ftol=1e-10, precision="fp64"))
+    assert ref["converged"][0]
+    for precision, cert in (("mixed", 0), ("mixed", 2), ("fp64", 0)):
+        eng.set_tuning(32, 0, pipeline_chunks=0, cert_warps=cert)  # 2: certification deferred to other warps
+        base = dict(iterations=40, ftol=1e-10, precision=precision, verify_T_max_MeV=0.0, verify_max_step=10.0)
+        alone = eng.solve(T, mu, xi, seed_table=table, seed_table_hot=hot, point_seeds=seed,
+                          opts=SolveOptions(verify_seeds=0, **base))
+        assert alone["converged"][0] and alone["omega"][0] > ref["omega"][0] + 1e-3  # the unstable branch
+        r = eng.solve(T, mu, xi, seed_table=table, seed_table_hot=hot, point_seeds=seed,
+                      opts=SolveOptions(verify_seeds=-1, **base))
+        assert r["converged"][0] and r["residual_norm"][0] <= 1e-10
+        assert abs(r["omega"][0] - ref["omega"][0]) <= 1e-10 * abs(ref["omega"][0]), precision
+        np.testing.assert_allclose(r["x"][0], ref["x"][0], rtol=1e-8, atol=1e-10)
+    eng.set_tuning(32, 0, pipeline_chunks=0, cert_warps=0)

@@ -220,3 +220,27 @@ def test_golden_tmu_scan_six_decimals(P):
         assert abs(th["entropy"] - float(r["entropy_fm3"])) < 2e-5
         assert abs(th["energy"] - float(r["energy_fm4"])) < 2e-5
         assert abs(th["rho_norm"] - float(r["rho"])) < 2e-5 * max(1.0, abs(float(r["rho"])))
+
+
+def test_unstable_branch_has_negative_jacobian_determinant(P):
+    """Three roots coexist at T = 136.35 MeV, mu_u = mu_d = 250 MeV, mu_s = 125 MeV, xi = -0.4
+    (p128 x t32): the min-Omega and the metastable roots have one negative eigenvalue of
+    Hessian_x Omega (the Polyakov-loop saddle), so det(Hessian_x P) > 0; the root between them,
+    highest in Omega, has two and det < 0 -- the test the per-point solve uses to send a root
+    on the unstable branch to the verification seeds."""
+    nd = orc.Nodes(128, 32)
+    opts = orc.default_opts(max_iter=40, ftol=1e-10)
+    T = 136.3458720078163 / HBARC
+    mu = np.array([250.0, 250.0, 125.0]) / HBARC
+    found = []
+    for s in ([-1.4068, -1.4068, -2.1412, 0.2184, 0.2607], [-0.4315, -0.4315, -2.0259, 0.3319, 0.3579],
+              [-0.9002, -0.9002, -2.0692, 0.2964, 0.3273]):
+        r = orc.solve_point(P, nd, T, mu, -0.4, np.array(s), multi=False, opts=opts)
+        assert r["converged"] and r["residual_norm"] <= 1e-10
+        _, _, h = orc.evaluate(P, nd, r["x"], mu, T, -0.4)
+        ev = np.linalg.eigvalsh(0.5 * (h + h.T))
+        found.append((r["omega"], int(np.sum(ev < 0)), np.linalg.det(-h)))
+    (o1, n1, d1), (o2, n2, d2), (o3, n3, d3) = found
+    assert o1 < o2 < o3  # hadron-like (min), quark-like (metastable), middle branch
+    assert (n1, n2, n3) == (1, 1, 2)
+    assert d1 > 0 and d2 > 0 and d3 < 0
