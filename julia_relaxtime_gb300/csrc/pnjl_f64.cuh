@@ -13,14 +13,15 @@
 
 namespace pnjl {
 
-// 2^(j/64), j = 0..63, rounded to double (host-built table, staged in shared memory)
-constexpr int kExp64N = 64;
+// 2^(j/256), j = 0..255, rounded to double (host-built table, staged in shared memory)
+constexpr int kExp64Bits = 8;
+constexpr int kExp64N = 1 << kExp64Bits;
 
-// Cody-Waite split of ln2/64: kLn2HiD64 = (ln2 truncated to 33 significant bits)/64, so that
-// k * kLn2HiD64 is exact for |k| < 2^20; kLn2LoD64 = the rest of ln2/64, rounded.
-constexpr double kInvLn2x64 = 0x1.71547652b82fep+6;  // 64/ln2
-constexpr double kLn2HiD64 = 0x1.62e42fefp-7;
-constexpr double kLn2LoD64 = 0x1.473de6af278edp-40;
+// Cody-Waite split of ln2/256: kLn2HiD = (ln2 truncated to 33 significant bits)/256, so that
+// k * kLn2HiD is exact for |k| < 2^20; kLn2LoD = the rest of ln2/256, rounded.
+constexpr double kInvLn2xN = 0x1.71547652b82fep+8;  // 256/ln2
+constexpr double kLn2HiD = 0x1.62e42fefp-9;
+constexpr double kLn2LoD = 0x1.473de6af278edp-42;
 constexpr double kRoundShifter = 0x1.8p52;           // 1.5*2^52: adding it rounds to an integer
 
 // c ? a : b as a 64-bit integer select (selp.b64).  The compiler otherwise turns some
@@ -45,26 +46,25 @@ static __device__ __noinline__ double rcp_library(double x) { return 1.0 / x; }
 static __device__ __noinline__ double rsqrt_library(double x) { return rsqrt(x); }
 
 // e^x for -700 <= x <= 0 by Tang's table-driven method (P. T. P. Tang, ACM TOMS 15(2),
-// 144-157, 1989), in base 2 with 64 table entries: x = (64 m + j) ln2/64 + r with
-// |r| <= ln2/128, e^x = 2^m * 2^(j/64) * (1 + p(r)), p the degree-5 Taylor polynomial of
-// e^r - 1 (truncation error below 3.5e-17 relative).  10 FP64 instructions.  The result lies
+// 144-157, 1989), in base 2 with 256 table entries: x = (256 m + j) ln2/256 + r with
+// |r| <= ln2/512, e^x = 2^m * 2^(j/256) * (1 + p(r)), p the degree-4 Taylor polynomial of
+// e^r - 1 (truncation error below 4e-17 relative).  9 FP64 instructions.  The result lies
 // in [2^-1011, 1] (normal), so 2^m is applied by an integer add to its exponent field.
 __device__ __forceinline__ double exp_nonpos(double x, const double *tab) {
     const unsigned hi = (unsigned)__double2hiint(x);
     // sign set and |x| <= 700 (the high word of -700.0 is 0xC085E000); -0.0 included
     if (!(hi >= 0x80000000u && hi <= 0xC085E000u)) return exp_library(x);
-    const double z = fma(x, kInvLn2x64, kRoundShifter);
-    const int k = __double2loint(z);  // round(64 x / ln2), two's complement in the low word
+    const double z = fma(x, kInvLn2xN, kRoundShifter);
+    const int k = __double2loint(z);  // round(256 x / ln2), two's complement in the low word
     const double kd = z - kRoundShifter;
-    double r = fma(kd, -kLn2HiD64, x);
-    r = fma(kd, -kLn2LoD64, r);
-    double c = fma(r, 1.0 / 120.0, 1.0 / 24.0);
-    c = fma(c, r, 1.0 / 6.0);
+    double r = fma(kd, -kLn2HiD, x);
+    r = fma(kd, -kLn2LoD, r);
+    double c = fma(r, 1.0 / 24.0, 1.0 / 6.0);
     c = fma(c, r, 0.5);
     c = fma(c, r, 1.0);
     const double tj = tab[k & (kExp64N - 1)];
     const double y = fma(tj, c * r, tj);
-    const int m = k >> 6;  // floor(k / 64) (arithmetic shift)
+    const int m = k >> kExp64Bits;  // floor(k / 256) (arithmetic shift)
     return __hiloint2double(__double2hiint(y) + m * (1 << 20), __double2loint(y));
 }
 

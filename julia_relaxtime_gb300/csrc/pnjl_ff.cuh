@@ -19,6 +19,8 @@
 
 #include <cuda_runtime.h>
 
+#include "pnjl_f64.cuh"
+
 namespace pnjl {
 
 struct ff {
@@ -27,7 +29,7 @@ struct ff {
 
 // Function tables in shared memory, as (h, l) float pairs: e^k (k = -kExpMaxN..kExpMaxN),
 // e^(j/256) (j = 0..255), ln c_j and 1/c_j for c_j = 1 + (2j + 1)/256 (j = 0..127); then (from
-// float kExp64Offset, 8-byte aligned) the kExp64N doubles 2^(j/64) of the FP64 exponential
+// float kExp64Offset, 8-byte aligned) the kExp64N doubles 2^(j/256) of the FP64 exponential
 // (pnjl_f64.cuh).
 constexpr int kExpMaxN = 88;
 constexpr int kExpIntN = 2 * kExpMaxN + 1;
@@ -36,7 +38,7 @@ constexpr int kLogN = 128;
 constexpr int kExpFracOff = 2 * kExpIntN;             // floats
 constexpr int kLogOff = kExpFracOff + 2 * kExpFracN;  // ln c_j pairs, then 1/c_j pairs
 constexpr int kExp64Offset = kLogOff + 4 * kLogN;
-constexpr int kExpTableFloats = kExp64Offset + 2 * 64;
+constexpr int kExpTableFloats = kExp64Offset + 2 * kExp64N;
 static_assert(kExp64Offset % 2 == 0, "FP64 table alignment");
 
 __device__ __forceinline__ ff ff_make(float h) { return ff{h, 0.0f}; }

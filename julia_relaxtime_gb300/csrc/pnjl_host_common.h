@@ -84,8 +84,8 @@ inline void separable_tables(int p_num, int t_num, const double *xp, const doubl
 
 // Function tables (pnjl_ff.cuh, pnjl_f64.cuh), from long-double exp / log: e^k for
 // k = -kExpMaxN..kExpMaxN and e^(j/256) for j = 0..255, ln c_j and 1/c_j for
-// c_j = 1 + (2j + 1)/256, j = 0..127, each as a (hi, lo) float pair; then 2^(j/64),
-// j = 0..63, as doubles.
+// c_j = 1 + (2j + 1)/256, j = 0..127, each as a (hi, lo) float pair; then 2^(j/256),
+// j = 0..255, as doubles.
 inline void ff_pair_into(long double v, float *out) {
     const float h = (float)v;
     out[0] = h;
@@ -100,7 +100,7 @@ inline void ff_exp_tables(float *out) {
         ff_pair_into(1.0L / c, out + kLogOff + 2 * kLogN + 2 * j);
     }
     for (int j = 0; j < kExp64N; ++j) {
-        const double v = (double)exp2l((long double)j / 64.0L);
+        const double v = (double)exp2l((long double)j / (long double)kExp64N);
         std::memcpy(out + kExp64Offset + 2 * j, &v, sizeof v);
     }
 }

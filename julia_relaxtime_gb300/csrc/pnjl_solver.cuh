@@ -39,7 +39,7 @@ struct NodeView {
     const float *p2f, *Af, *c2f, *Bf;
     const float *p2l, *Al, *c2l, *Bl;  // float-float low parts (null when not staged)
     const float *expt;                 // float-float exp tables (null when not staged)
-    const double *exp64;               // 2^(j/64) table of exp_nonpos (null when not staged)
+    const double *exp64;               // 2^(j/256) table of exp_nonpos (null when not staged)
     int p_num, t_num;
 };
 
@@ -399,10 +399,11 @@ __device__ void node_pass_newton32(const NodeView &nv, const PointIn &pt, const 
 
 // FP64 residual pass of the mixed solve's certification: the sums S.DM, S.SP, S.SPb of
 // node_pass<double, GRAD only> from the same integrand in FP64, arranged for the FP64 pipe
-// (57 FP64 instructions per node-flavour, measured): exp, 1/x and 1/sqrt from pnjl_f64.cuh,
-// Horner forms in FMAs, integer selects, opaque loop invariants, and the per-flavour factors
-// -3 M/T (dOmega/dM, with dE/dM = M/E) and 3 (dOmega/dPhi) applied once to the lane sums
-// instead of per node.  With r_k = u_k / f+ and s_k = C^(k-1) u_k / f- (u = (t, t^2, t^3)
+// (52 FP64 instructions per node-flavour, measured): exp, 1/x and 1/sqrt from pnjl_f64.cuh,
+// Horner forms in FMAs, integer selects and clamp compares, opaque loop invariants, and the
+// per-flavour factors -3 M/T (dOmega/dM, with dE/dM = M/E), 3 (dOmega/dPhi) and C, C^2 (the
+// Phi derivatives' f- terms, summed without them) applied once to the lane sums instead of
+// per node.  With r_k = u_k / f+ and s_k = C^(k-1) u_k / f- (u = (t, t^2, t^3)
 // for a <= 0, (t^2, t, 1) for a > 0) the Polyakov distributions are
 //   n+ = (Phi u1 + 2 Phibar u2 + u3) / f+,   n- = C (Phibar u1 + 2 Phi C u2 + C^2 u3) / f-
 // and the Phi / Phibar derivatives take r1 + s2 and r2 + s1 (quark / antiquark sides
@@ -415,6 +416,7 @@ __device__ void node_pass_cert(const NodeView &nv, const PointIn &pt, const doub
     const int pn = nv.p_num, n = nv.p_num * nv.t_num;
     const double xi = pt.xi;
     const unsigned long long cap = (unsigned long long)__double_as_longlong(-kRescaleCapA);
+    const long long epsb = __double_as_longlong(kPolyakovEps);
     double DM[3] = {0.0, 0.0, 0.0}, SP = 0.0, SPb = 0.0;
 #pragma unroll 1
     for (int f = 0; f < 3; ++f) {
@@ -429,7 +431,8 @@ __device__ void node_pass_cert(const NodeView &nv, const PointIn &pt, const doub
         opaque(Pq); opaque(Pa); opaque(Pa2); opaque(Pq2C);
         opaque(k1_0); opaque(k2_0); opaque(k1_1); opaque(k2_1);
         opaque(e3_0); opaque(e2_0); opaque(e1_0); opaque(e2_1); opaque(e1_1); opaque(e0_1);
-        double dm = 0.0, sq = 0.0, sa = 0.0;
+        // sq = s1 + C^2 s4 and sa = s2 + C s3: the sums of w/f+ u_k and w/f- u_k
+        double dm = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0, s4 = 0.0;
         int ip = gl, it = 0;
         while (ip >= pn) { ip -= pn; ++it; }
         double sxi = 1.0, bw = 0.0;
@@ -450,20 +453,25 @@ __device__ void node_pass_cert(const NodeView &nv, const PointIn &pt, const doub
             const double fp = fma(fma(t + dsel(sig, k2_1, k2_0), t, dsel(sig, k1_1, k1_0)), t, 1.0);
             const double gm =
                 fma(fma(fma(dsel(sig, 1.0, e3_0), t, dsel(sig, e2_1, e2_0)), t, dsel(sig, e1_1, e1_0)), t, dsel(sig, e0_1, 1.0));
-            // the reference's max(f, 1e-16) clamps (NaN is not clamped)
-            const bool clP = fp < kPolyakovEps;
-            const bool clM = gm < kPolyakovEps * dsel(sig, t3, 1.0);
+            // the reference's max(f, 1e-16) clamps, compared as bit patterns on the integer pipe
+            // (the same order as the doubles' for all but -0.0 and negative NaNs, which f+ and
+            // f- -- polynomials in t in [0, 1] with finite coefficients -- never take)
+            const bool clP = __double_as_longlong(fp) < epsb;
+            const bool clM = __double_as_longlong(gm) < __double_as_longlong(kPolyakovEps * dsel(sig, t3, 1.0));
             const double fpc = dsel(clP, 1.0, fp), gmc = dsel(clM, 1.0, gm);
             const double Rr = rcp_normal(fpc * gmc);
             const double ipv = dsel(clP, 0.0, gmc * Rr);  // 1/f+
             const double im = dsel(clM, 0.0, fpc * Rr);   // 1/f-
             const double u1 = dsel(sig, t2, t), u2 = dsel(sig, t, t2), u3 = dsel(sig, 1.0, t3);
-            const double Cim = C * im, CCim = C * Cim;
+            const double Cim = C * im;
             const double np = dsel(clP, dsel(sig, 1.0, 0.0), ipv * fma(Pq, u1, fma(Pa2, u2, u3)));
             const double nm = dsel(clM, 0.0, Cim * fma(Pa, u1, fma(Pq2C, u2, C2 * u3)));
             dm = fma(w, (np + nm) * rE, dm);
-            sq = fma(w, fma(ipv, u1, CCim * u2), sq);
-            sa = fma(w, fma(ipv, u2, Cim * u1), sa);
+            const double wp = w * ipv, wm = w * im;
+            s1 = fma(wp, u1, s1);
+            s2 = fma(wp, u2, s2);
+            s3 = fma(wm, u1, s3);
+            s4 = fma(wm, u2, s4);
             ip += G;
             if (ip >= pn) {
                 do { ip -= pn; ++it; } while (ip >= pn);
@@ -471,6 +479,7 @@ __device__ void node_pass_cert(const NodeView &nv, const PointIn &pt, const doub
             }
         }
         const double mult = (f == 0 && dedup) ? 2.0 : 1.0;
+        const double sq = fma(fc.C2, s4, s1), sa = fma(fc.C, s3, s2);
         DM[f] = -3.0 * fc.invT * fc.M * dm;
         if (f == 0 && dedup) DM[1] = DM[0];
         SP += mult * 3.0 * (sw ? sa : sq);
