@@ -10,14 +10,18 @@ n_chunks-th point, a different slice each step), so the timed steps are spread o
 
 Headline (``--mode surrogate``): surrogate-seeded mixed-precision solves -- the trained
 network's seed per point (BF16 tensor-core inference kernel), one mixed-precision Newton solve
-(FP32 Kahan node passes, FP64 solve/update/residual), verification by two MultiSeed
-candidates where a second phase can exist, MultiSeed fallback where the learned seed fails.
-The network is trained in an untimed set-up on this GPU (labels: a 64 x 64 x 5 (T, mu, xi)
-multi-seed solve; 400 epochs), reported as ``surrogate.train``.  The same chunks are then
-solved by the plain FP64 multi-seed Newton (the first four MultiSeed candidates, min-Omega
-selection, trust-region fallback): ``plain_fp64`` holds its rate, the speed-up, and the phase
-misassignments of the surrogate path against it.  ``--mode multiseed --precision fp64|mixed``
-times the MultiSeed table path alone.
+(FP32 Kahan node passes, FP64 solve/update/residual), verification by every MultiSeed
+candidate where a second phase can exist (the cells of the network's verification map, roots
+far from the seed, roots on an unstable branch), MultiSeed fallback where the learned seed
+fails.  The network is trained in an untimed set-up on this GPU (labels: a 64 x 64 x 5
+(T, mu, xi) multi-seed solve; 400 epochs), reported as ``surrogate.train``.  The same chunks
+are then solved by the plain FP64 multi-seed Newton (the workload's MultiSeed candidates,
+min-Omega selection, trust-region fallback): ``plain_fp64`` holds its rate, the speed-up, and
+the phase misassignments of the surrogate path against it.  ``--mode multiseed --precision
+fp64|mixed`` times the MultiSeed table path alone; ``--mode orders`` the 32 x 32 grid at three
+quadrature orders in one graph.  Other workloads: ``surrogate_eval_2p20`` (2^20 uniform points,
+MultiSeed (6)) and ``first_order_2048x2048x9`` (T 20-150 MeV, mu_u 250-450 MeV, mu_s = mu_u/2,
+9 xi, 8 seeds; the network trained on that box).
 
 value: converged solves per second with inputs already in HBM (pnjl_solve_batch_learned_device
 or pnjl_solve_batch_device), timed with CUDA events on the library's stream; e2e: the same
@@ -47,10 +51,10 @@ if ROOT not in sys.path:
 
 HBARC = 197.327
 # DRAM bytes (read + write) per launch of the dominant kernel from one ncu capture of a
-# 9,216-point launch (0.062 GB + 0.279 GB), scaled by points to the 18,432-point step; it is
+# 9,216-point launch (0.058 GB + 0.274 GB), scaled by points to the 18,432-point step; it is
 # mostly local-memory (stack) write-back (inputs and outputs are 240 B per point)
 TRAFFIC = {"mixed_fused_kernel<32>": {
-    "bytes_per_launch": 2 * (0.061842432e9 + 0.279333376e9),
+    "bytes_per_launch": 2 * (0.057730048e9 + 0.273578240e9),
     "source": "ncu --set full of one 9,216-point launch (profiles/mixed_fused_kernel_surrogate_aniso_9216pt.md), "
               "scaled by points; mostly local-memory write-back"}}
 METRIC = "gap solves/s at \u2016\u2202\u03a9\u2016\u22641e-10: surrogate-seeded vs plain FP64 Newton, 1 GB300"
