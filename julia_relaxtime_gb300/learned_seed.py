@@ -60,6 +60,14 @@ def flavour_mu(cfg: TrainConfig, mu):
     return np.stack([mu, mu, cfg.mu_s_ratio * mu], axis=1)
 
 
+def box_scaling(cfg: TrainConfig):
+    """(in_shift, in_scale) of the network's inputs (T, mu_u in fm^-1, xi): the training box
+    mapped to [-1, 1]."""
+    lo = np.array([cfg.T_MeV[0] / HBARC_MEV_FM, cfg.mu_MeV[0] / HBARC_MEV_FM, cfg.xi[0]])
+    hi = np.array([cfg.T_MeV[1] / HBARC_MEV_FM, cfg.mu_MeV[1] / HBARC_MEV_FM, cfg.xi[1]])
+    return 0.5 * (lo + hi), np.maximum(0.5 * (hi - lo), 1e-6)
+
+
 def label_table(cfg: TrainConfig):
     from .pnjl import multiseed_table
 
@@ -88,12 +96,8 @@ class LearnedSeed(SeedStrategy):
     def default_scaling(self, targets, cfg: TrainConfig | None = None):
         """Inputs mapped to [-1, 1] over the training box (cfg; the default box without it),
         outputs standardised."""
-        cfg = cfg or TrainConfig()
         t = np.asarray(targets, dtype=np.float64)
-        lo = np.array([cfg.T_MeV[0] / HBARC_MEV_FM, cfg.mu_MeV[0] / HBARC_MEV_FM, cfg.xi[0]])
-        hi = np.array([cfg.T_MeV[1] / HBARC_MEV_FM, cfg.mu_MeV[1] / HBARC_MEV_FM, cfg.xi[1]])
-        in_shift = 0.5 * (lo + hi)
-        in_scale = np.maximum(0.5 * (hi - lo), 1e-6)
+        in_shift, in_scale = box_scaling(cfg or TrainConfig())
         out_shift = t.mean(axis=0)
         out_scale = np.maximum(t.std(axis=0), 1e-6)
         self.set_scaling(in_shift, in_scale, out_shift, out_scale)

@@ -350,3 +350,34 @@ def test_bench_slices_and_workload_grids():
     for u, v in zip(pa, pb):
         np.testing.assert_array_equal(u, v)
     assert 50.0 <= pa[0].min() * HBARC and pa[0].max() * HBARC <= 300.0 and np.abs(pa[3]).max() <= 0.5
+
+
+def test_training_box_of_the_first_order_scan():
+    """The label grid of a flavour-asymmetric box (mu_s = mu_u / 2) solves at (mu, mu, mu/2),
+    its table holds the MultiSeed candidates plus the extra rows, and the network's inputs are
+    scaled to [-1, 1] over the box (the default box: the constants of the 50-300 / 0-400 MeV,
+    xi +-0.5 grid)."""
+    from julia_relaxtime_gb300 import pnjl
+    from julia_relaxtime_gb300.learned_seed import TrainConfig, box_scaling, flavour_mu, grid_points, label_table
+
+    cfg = TrainConfig(T_MeV=(20.0, 150.0, 4), mu_MeV=(250.0, 450.0, 3), xi=(-0.5, 0.5, 2), mu_s_ratio=0.5,
+                      label_extra=(pnjl.MEDIUM_SEED_5, pnjl.HIGH_DENSITY_SEED_5))
+    T, mu, xi = grid_points(cfg)
+    assert T.size == 24 and mu.ndim == 1
+    m3 = flavour_mu(cfg, mu)
+    np.testing.assert_array_equal(m3[:, 0], mu)
+    np.testing.assert_array_equal(m3[:, 1], mu)
+    np.testing.assert_array_equal(m3[:, 2], 0.5 * mu)
+    assert flavour_mu(TrainConfig(), mu).ndim == 1  # mu_u = mu_d = mu_s: one array
+    cold, hot = label_table(cfg)
+    assert cold.shape == (8, 5) and hot.shape == (8, 5)
+    np.testing.assert_array_equal(cold[6], pnjl.MEDIUM_SEED_5)
+    np.testing.assert_array_equal(cold[:6], pnjl.multiseed_table(6)[0])
+    shift, scale = box_scaling(cfg)
+    lo = np.array([20.0 / HBARC, 250.0 / HBARC, -0.5])
+    hi = np.array([150.0 / HBARC, 450.0 / HBARC, 0.5])
+    np.testing.assert_allclose((lo - shift) / scale, -1.0, rtol=1e-14)
+    np.testing.assert_allclose((hi - shift) / scale, 1.0, rtol=1e-14)
+    s0, c0 = box_scaling(TrainConfig())
+    np.testing.assert_allclose(s0, [175.0 / HBARC, 200.0 / HBARC, 0.0], rtol=1e-14, atol=1e-15)
+    np.testing.assert_allclose(c0, [125.0 / HBARC, 200.0 / HBARC, 0.5], rtol=1e-14)
