@@ -97,7 +97,11 @@ typedef struct pnjl_solve_opts {
                                     also checked against the first verify_seeds rows of the seed
                                     table at T*hbarc < verify_T_max_MeV (where a first-order line
                                     allows a lower-Omega branch); min-Omega with the per-point
-                                    seed first.  0 disables (the reference's single-seed path). */
+                                    seed first.  Also verified, at any T: a solution on an
+                                    unstable branch (det of the Jacobian of grad_x P negative: a
+                                    second negative eigenvalue of the Hessian of Omega besides
+                                    the Polyakov-loop saddle, so never the min-Omega phase).
+                                    0 disables (the reference's single-seed path). */
     double verify_T_max_MeV;
     double verify_max_step;      /* ... and, at any T, when the converged state lies farther than
                                     this (infinity norm) from its per-point seed: the seed did not
