@@ -1047,7 +1047,7 @@ static int solve_batch_host(pnjl_ctx *ctx, int64_t n, const double *T, const dou
     d.converged = carve<uint8_t>(p, nn);
     cudaStream_t s = ctx->stream;
     // inputs and outputs cross through a pinned mirror of the workspace: one DMA each way
-    // (pageable copies are staged by the driver in small synchronous pieces)
+    // (the CUDA runtime stages pageable copies through its own buffers in pieces)
     const size_t in_bytes = (size_t)((unsigned char *)d.x - ctx->d_ws);
     const size_t out_off = in_bytes, out_bytes = (size_t)(p - ctx->d_ws) - in_bytes;
     const bool staged = ensure_stage(ctx, in_bytes + out_bytes);
