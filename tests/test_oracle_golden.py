@@ -244,3 +244,17 @@ def test_unstable_branch_has_negative_jacobian_determinant(P):
     assert o1 < o2 < o3  # hadron-like (min), quark-like (metastable), middle branch
     assert (n1, n2, n3) == (1, 1, 2)
     assert d1 > 0 and d2 > 0 and d3 < 0
+
+
+def test_solver_known_answers_at_reference_inputs(P):
+    """test_solver_implicit.jl:212-240 at its inputs (T = 0.5 fm^-1, mu = 1.0 fm^-1, p24 x t6,
+    the default seed): positive masses, M_s above M_u and M_d, and M_u = M_d (isospin)."""
+    nd = orc.Nodes(24, 6)
+    seed = orc.multiseed_seeds(P, 0.5)[0]
+    r = orc.solve_point(P, nd, 0.5, np.array([1.0, 1.0, 1.0]), 0.0, seed, multi=False,
+                        opts=orc.default_opts(max_iter=40, ftol=1e-9))
+    assert r["converged"]
+    m = r["masses"]
+    assert np.all(m > 0)
+    assert m[2] > m[0] and m[2] > m[1]
+    assert m[0] == pytest.approx(m[1], rel=1e-6)
