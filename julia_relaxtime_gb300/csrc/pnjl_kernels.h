@@ -76,7 +76,7 @@ struct SolveArgs {
     long long *stats;             // device counters [kStatCount]
     // mixed-precision task kernel (zeroed before the launch where noted)
     double *roots;                // [n*n_seeds*5] FP32 roots published per (slot, seed)
-    int *root_flag;               // [n*n_seeds] 1 once roots[slot, seed] is written (zeroed)
+    int *root_flag;               // [n*n_seeds] state of roots[slot, seed]: none / pending / usable (zeroed)
     long long *list;              // [n] points deferred by the per-point kernel
     int *list_mode;               // [n] kListVerify / kListFallback, stored + 1 once the slot's
                                   // point and record are written (zeroed: 0 = not yet)
