@@ -258,3 +258,40 @@ def test_solver_known_answers_at_reference_inputs(P):
     assert np.all(m > 0)
     assert m[2] > m[0] and m[2] > m[1]
     assert m[0] == pytest.approx(m[1], rel=1e-6)
+
+
+def test_stable_roots_have_one_negative_hessian_eigenvalue(P):
+    """The unstable-branch test over random points of the first-order box (T 20-150 MeV, mu_u
+    250-450 MeV, mu_s = mu_u/2, xi +-0.5; p64 x t8; the 8 seeds of that scan): every min-Omega
+    root has exactly one negative eigenvalue of Hessian_x Omega, and every root with more has
+    det(Hessian_x P) < 0."""
+    from julia_relaxtime_gb300.pnjl import HIGH_DENSITY_SEED_5, MEDIUM_SEED_5, multiseed_table
+
+    nd = orc.Nodes(64, 8)
+    opts = orc.default_opts(max_iter=40, ftol=1e-10)
+    table = multiseed_table(6, (MEDIUM_SEED_5, HIGH_DENSITY_SEED_5))[0]
+    rng = np.random.default_rng(11)
+    n_min = n_unstable = 0
+    for _ in range(40):
+        T = rng.uniform(20.0, 150.0) / HBARC
+        m = rng.uniform(250.0, 450.0) / HBARC
+        xi = rng.uniform(-0.5, 0.5)
+        mu = np.array([m, m, 0.5 * m])
+        roots = []
+        for s in table:
+            r = orc.solve_point(P, nd, T, mu, xi, s, multi=False, opts=opts)
+            if r["converged"] and r["phys"]:
+                _, _, h = orc.evaluate(P, nd, r["x"], mu, T, xi)
+                neg = int(np.sum(np.linalg.eigvalsh(0.5 * (h + h.T)) < 0))
+                roots.append((r["omega"], neg, np.linalg.det(-h)))
+        if not roots:
+            continue
+        omin = min(o for o, _, _ in roots)
+        for o, neg, det in roots:
+            if o <= omin + 1e-12 * abs(omin):
+                assert neg == 1 and det > 0
+                n_min += 1
+            if neg >= 2:
+                assert neg == 2 and det < 0
+                n_unstable += 1
+    assert n_min >= 40 * 4 and n_unstable >= 1
