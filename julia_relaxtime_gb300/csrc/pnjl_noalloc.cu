@@ -1,13 +1,16 @@
 // pnjl_noalloc.cu -- pnjl_solve_batch_noalloc: a batched solve that allocates nothing.
 //
 // Who needs it: callers that may not allocate device memory at the moment they solve --
-// code that runs while a CUDA stream is being captured (cudaMalloc is not allowed inside a
-// global-mode capture), hosts whose device memory is owned by another allocator (a Julia
-// or PyTorch memory pool that must account for every byte), and long-running services that
-// reserve all memory at start-up so that no call can fail for lack of it later.  They pass
-// device inputs and outputs; everything else the solve needs lives in one file-scope static
-// device array declared below, so no call makes a context, cudaMalloc, cudaFree or any
-// allocating library routine.
+// hosts whose device memory is owned by another allocator (a Julia or PyTorch memory pool
+// that must account for every byte, and would be bypassed by a cudaMalloc here), and
+// long-running services that reserve all memory at start-up so that no call can fail for
+// lack of it later.  They pass device inputs and outputs; everything else the solve needs
+// lives in one file-scope static device array declared below, so no call makes a context,
+// cudaMalloc, cudaFree or any allocating library routine.
+//
+// Precision: only the plain FP64 path (PNJL_PREC_FP64).  The mixed-precision solver needs
+// per-seed records, published roots and a certification queue that this fixed array does
+// not hold, so opts->precision = PNJL_PREC_MIXED is rejected with PNJL_ERR_INVALID_ARGUMENT.
 //
 // The scratch is the same as pnjl_solve_batch_device's: per-(point, seed) candidate records
 // and per-point completion counters of the MultiSeed selection, the work-queue head and the
@@ -90,6 +93,7 @@ extern "C" int pnjl_solve_batch_noalloc(const pnjl_params *params, int32_t p_num
     const char *msg = "";
     if (pnjl::validate_opts(opts, &msg) != PNJL_OK) return PNJL_ERR_INVALID_ARGUMENT;
     if (opts->verify_map) return PNJL_ERR_INVALID_ARGUMENT;  // no device copy without an allocation
+    if (opts->precision != PNJL_PREC_FP64) return PNJL_ERR_INVALID_ARGUMENT;  // FP64 kernel only
     if (p_num < 1 || p_num > pnjl::kMaxPNodes || t_num < 1 || t_num > pnjl::kMaxTNodes || !(p_max > 0.0))
         return PNJL_ERR_INVALID_ARGUMENT;
     if (n < 0 || (n > 0 && (!d_T || !d_mu_u || !d_mu_d || !d_mu_s || !d_xi))) return PNJL_ERR_INVALID_ARGUMENT;
