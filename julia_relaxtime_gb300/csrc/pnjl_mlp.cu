@@ -4,16 +4,20 @@
 // PhaseAwareContinuitySeed initial guess (src/pnjl/solver/SeedStrategies.jl) and is
 // trained on solutions the GPU solver itself produces.
 //
-//   mlp_fwd_bwd_kernel   one 32-sample tile per CTA: forward, loss, backward; the two
-//                        128x128 layers (forward, input gradient and weight gradient) run on
-//                        the tensor cores as mma.sync m16n8k16 BF16 x BF16 -> FP32 tiles with
-//                        operands staged in shared memory; the 3- and 5-wide layers are FP32
-//                        SIMT loops over the same BF16-rounded weights; weight gradients of
-//                        the tile are added into FP32 global buffers.
-//   mlp_adam_kernel      Adam on the FP32 master weights, then the BF16 copies are refreshed.
+//   mlp_fwd_bwd_kernel   32-sample tiles: forward, loss, backward; the two 128x128 layers
+//                        (forward, input gradient and weight gradient) run on the tensor
+//                        cores as mma.sync m16n8k16 BF16 x BF16 -> FP32 tiles with operands
+//                        staged in shared memory; the 3- and 5-wide layers are FP32 SIMT
+//                        loops over the same BF16-rounded weights.  CTA c takes tiles
+//                        c, c + grid, ... and keeps the sum of their gradients (and losses)
+//                        in its own slot of a partial-gradient buffer: no atomics.
+//   mlp_update_kernel    per parameter: the slots summed in slot order (a fixed order, so a
+//                        training run is bit-reproducible), Adam on the FP32 master, the
+//                        BF16 copy refreshed; the step's loss from the slot losses.
+//   mlp_reduce_kernel    the slot sums alone (gradient and loss of one batch, no update).
 //   mlp_infer_kernel     forward only; writes de-standardised seeds for the solver.
-// Training steps are captured once in a CUDA graph (step counter, zeroing, fwd/bwd, Adam)
-// and replayed.
+// One epoch of training steps (step counter, fwd/bwd, update) is captured once in a CUDA
+// graph and replayed once per epoch; the epochs' sample permutations are uploaded up front.
 #include <cmath>
 #include <cstring>
 #include <cuda_bf16.h>
@@ -121,12 +125,15 @@ __device__ __forceinline__ void frag_coord(int j, int e, int &row, int &col) {
     col = 64 * (w >> 1) + 8 * j + 2 * t + (e & 1);
 }
 
-// Weight gradient G[H x H] += D^T . Hin over the tile (K = TILE samples): D(m=out, k=sample)
-// = d[k*LDH + m], Hin(k=sample, n=in) = h[k*LDH + n].  Warp w owns output rows 32w..32w+31 in
-// two passes of 64 columns; results are added into the FP32 global gradient.
-__device__ __forceinline__ void weight_grad(const __nv_bfloat16 *d, const __nv_bfloat16 *h, float *gW, int valid) {
+// Accumulate one tile's gradient entry into the CTA's slot: the slot's first tile stores,
+// later tiles add (each entry has exactly one writer in the CTA, so no atomics are needed).
+__device__ __forceinline__ void slot_acc(float *p, float v, bool first) { *p = first ? v : *p + v; }
+
+// Weight gradient G[H x H] of the tile (K = TILE samples): G = D^T . Hin with D(m=out,
+// k=sample) = d[k*LDH + m], Hin(k=sample, n=in) = h[k*LDH + n].  Warp w owns output rows
+// 32w..32w+31 in two passes of 64 columns; results go to the CTA's gradient slot.
+__device__ __forceinline__ void weight_grad(const __nv_bfloat16 *d, const __nv_bfloat16 *h, float *gW, bool first) {
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    (void)valid;
 #pragma unroll 1
     for (int half = 0; half < 2; ++half) {
         float acc[2][8][4];
@@ -155,19 +162,20 @@ __device__ __forceinline__ void weight_grad(const __nv_bfloat16 *d, const __nv_b
                 for (int e = 0; e < 4; ++e) {
                     const int row = 32 * w + 16 * i + g + (e >= 2 ? 8 : 0);
                     const int col = 64 * half + 8 * j + 2 * t + (e & 1);
-                    atomicAdd(&gW[row * H + col], acc[i][j][e]);
+                    slot_acc(&gW[row * H + col], acc[i][j][e], first);
                 }
     }
 }
 
-__device__ __forceinline__ void block_reduce_add(float v, float *red, float *dst) {
+// Block sum of v (fixed tree order) accumulated into *dst by thread 0.
+__device__ __forceinline__ void block_reduce_acc(float v, float *red, float *dst, bool first) {
     red[threadIdx.x] = v;
     __syncthreads();
     for (int s = NT / 2; s > 0; s >>= 1) {
         if ((int)threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
         __syncthreads();
     }
-    if (threadIdx.x == 0) atomicAdd(dst, red[0]);
+    if (threadIdx.x == 0) slot_acc(dst, red[0], first);
     __syncthreads();
 }
 
@@ -243,138 +251,176 @@ __global__ void __launch_bounds__(NT) mlp_fwd_bwd_kernel(MlpDev m, TrainBatch b)
     extern __shared__ __align__(16) unsigned char smem[];
     float *X = (float *)(smem + SmemLayout::X), *Y = (float *)(smem + SmemLayout::Y),
           *DO = (float *)(smem + SmemLayout::DO), *red = (float *)(smem + SmemLayout::RED);
-    // the tile's samples: a slice of this step's mini-batch of a shuffled epoch
+    // this step's mini-batch: a slice of the shuffled epoch (perm is epoch-major)
     const long long step = b.step ? (*b.step - 1) : 0;
-    const long long base = (b.steps_per_epoch > 0 ? (step % b.steps_per_epoch) : 0) * (long long)b.batch +
-                           (long long)blockIdx.x * TILE;
+    const long long epoch = b.steps_per_epoch > 0 ? step / b.steps_per_epoch : 0;
+    const long long batch0 = (b.steps_per_epoch > 0 ? (step % b.steps_per_epoch) : 0) * (long long)b.batch;
     const long long limit = b.steps_per_epoch > 0 ? (long long)b.n : (long long)b.batch;
-    int valid = (int)(limit - base);
-    if (valid > TILE) valid = TILE;
-    if (valid < 0) valid = 0;
-    for (int i = threadIdx.x; i < TILE; i += NT) {
-        const bool ok = i < valid;
-        const long long idx = ok ? (b.perm ? b.perm[base + i] : base + i) : 0;
-        for (int k = 0; k < IN; ++k) X[i * IN + k] = ok ? b.x[idx * IN + k] : 0.f;
-        for (int k = 0; k < OUT; ++k) Y[i * OUT + k] = ok ? b.y[idx * OUT + k] : 0.f;
-    }
-    __syncthreads();
-    float *out = DO;  // forward writes predictions here, backward turns them into dL/dout
-    forward_tile(m, X, valid, smem, out);
+    const int tiles = (b.batch + TILE - 1) / TILE;
+    float *slot = m.partial + (size_t)blockIdx.x * kParamCount;
+    float *gW4 = slot + OFF_W4, *gB4 = slot + OFF_B4, *gW1 = slot + OFF_W1, *gB1 = slot + OFF_B1;
+    float *gW[2] = {slot + OFF_W3, slot + OFF_W2};
+    float *gB[2] = {slot + OFF_B3, slot + OFF_B2};
     __nv_bfloat16 *W2s = (__nv_bfloat16 *)(smem + SmemLayout::W2);
     __nv_bfloat16 *W3s = (__nv_bfloat16 *)(smem + SmemLayout::W3);
     float *Z1 = (float *)(smem + SmemLayout::Z1), *Z2 = (float *)(smem + SmemLayout::Z2),
           *Z3 = (float *)(smem + SmemLayout::Z3);
     __nv_bfloat16 *H1 = (__nv_bfloat16 *)(smem + SmemLayout::H1), *H2 = (__nv_bfloat16 *)(smem + SmemLayout::H2),
                   *H3 = (__nv_bfloat16 *)(smem + SmemLayout::H3);
-    float *W1s = (float *)(smem + SmemLayout::W1), *W4s = (float *)(smem + SmemLayout::W4);
+    float *W4s = (float *)(smem + SmemLayout::W4);
     // loss = mean over (batch, outputs) of the squared error in standardised units
     const float inv = 1.0f / ((float)b.batch * (float)OUT);
-    float lsum = 0.f;
-    for (int i = threadIdx.x; i < TILE * OUT; i += NT) {
-        const int s = i / OUT;
-        float dlt = (s < valid) ? (out[i] - Y[i]) : 0.f;
-        lsum += dlt * dlt;
-        out[i] = 2.0f * dlt * inv;
-    }
-    block_reduce_add(lsum * inv, red, b.loss);
-    // layer 4: dW4 = dout^T h3, db4 = sum dout  (FP32 SIMT)
-    for (int i = threadIdx.x; i < OUT * H; i += NT) {
-        const int o = i / H, k = i % H;
-        float g = 0.f;
-        for (int s = 0; s < TILE; ++s) g += DO[s * OUT + o] * __bfloat162float(H3[s * LDH + k]);
-        atomicAdd(&m.grad[OFF_W4 + i], g);
-    }
-    if (threadIdx.x < OUT) {
-        float g = 0.f;
-        for (int s = 0; s < TILE; ++s) g += DO[s * OUT + threadIdx.x];
-        atomicAdd(&m.grad[OFF_B4 + threadIdx.x], g);
-    }
-    __syncthreads();
-    // delta3 = (dout W4) * silu'(z3) -> BF16 into H3's buffer
-    for (int i = threadIdx.x; i < TILE * H; i += NT) {
-        const int s = i / H, k = i % H;
-        float v = 0.f;
-#pragma unroll
-        for (int o = 0; o < OUT; ++o) v += DO[s * OUT + o] * W4s[o * H + k];
-        v *= silu_grad(Z3[s * H + k]);
-        if (s >= valid) v = 0.f;
-        H3[s * LDH + k] = __float2bfloat16_rn(v);
-    }
-    __syncthreads();
-    // layers 3 and 2 on the tensor cores
-    __nv_bfloat16 *Dl[2] = {H3, H2};   // delta of layer 3 (in H3), then of layer 2 (into H2)
-    const __nv_bfloat16 *Hin[2] = {H2, H1};
-    const __nv_bfloat16 *Wl[2] = {W3s, W2s};
-    float *Zin[2] = {Z2, Z1};
-    float *gW[2] = {m.grad + OFF_W3, m.grad + OFF_W2};
-    float *gB[2] = {m.grad + OFF_B3, m.grad + OFF_B2};
 #pragma unroll 1
-    for (int l = 0; l < 2; ++l) {
-        // bias gradient: column sums of delta
-        for (int k = threadIdx.x; k < H; k += NT) {
-            float g = 0.f;
-            for (int s = 0; s < TILE; ++s) g += __bfloat162float(Dl[l][s * LDH + k]);
-            atomicAdd(&gB[l][k], g);
+    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const bool first = tile == (int)blockIdx.x;
+        const long long base = batch0 + (long long)tile * TILE;
+        int valid = (int)(limit - base);
+        if (valid > TILE) valid = TILE;
+        if (valid < 0) valid = 0;
+        for (int i = threadIdx.x; i < TILE; i += NT) {
+            const bool ok = i < valid;
+            const long long idx = ok ? (b.perm ? (long long)b.perm[epoch * b.n + base + i] : base + i) : 0;
+            for (int k = 0; k < IN; ++k) X[i * IN + k] = ok ? b.x[idx * IN + k] : 0.f;
+            for (int k = 0; k < OUT; ++k) Y[i * OUT + k] = ok ? b.y[idx * OUT + k] : 0.f;
         }
-        // weight gradient G += delta^T . h_in
-        weight_grad(Dl[l], Hin[l], gW[l], valid);
         __syncthreads();
-        // input gradient: delta_in = (delta . W) * silu'(z_in), B(k=out, n=in) = W[k][n]
-        float acc[8][4];
-        gemm_tile_x_h(Dl[l], LDH, 1, Wl[l], LDH, 1, acc);
-        __syncthreads();  // every warp has read delta_l before delta_in overwrites h_in (l = 1)
+        float *out = DO;  // forward writes predictions here, backward turns them into dL/dout
+        forward_tile(m, X, valid, smem, out);
+        float lsum = 0.f;
+        for (int i = threadIdx.x; i < TILE * OUT; i += NT) {
+            const int s = i / OUT;
+            float dlt = (s < valid) ? (out[i] - Y[i]) : 0.f;
+            lsum += dlt * dlt;
+            out[i] = 2.0f * dlt * inv;
+        }
+        block_reduce_acc(lsum * inv, red, &m.loss_part[blockIdx.x], first);
+        // layer 4: dW4 = dout^T h3, db4 = sum dout  (FP32 SIMT)
+        for (int i = threadIdx.x; i < OUT * H; i += NT) {
+            const int o = i / H, k = i % H;
+            float g = 0.f;
+            for (int s = 0; s < TILE; ++s) g += DO[s * OUT + o] * __bfloat162float(H3[s * LDH + k]);
+            slot_acc(&gW4[i], g, first);
+        }
+        if (threadIdx.x < OUT) {
+            float g = 0.f;
+            for (int s = 0; s < TILE; ++s) g += DO[s * OUT + threadIdx.x];
+            slot_acc(&gB4[threadIdx.x], g, first);
+        }
+        __syncthreads();
+        // delta3 = (dout W4) * silu'(z3) -> BF16 into H3's buffer
+        for (int i = threadIdx.x; i < TILE * H; i += NT) {
+            const int s = i / H, k = i % H;
+            float v = 0.f;
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                int row, col;
-                frag_coord(j, e, row, col);
-                float v = acc[j][e] * silu_grad(Zin[l][row * H + col]);
-                if (row >= valid) v = 0.f;
-                if (l == 0) H2[row * LDH + col] = __float2bfloat16_rn(v);  // delta of layer 2
-                else Z1[row * H + col] = v;                                 // delta of layer 1 (FP32)
+            for (int o = 0; o < OUT; ++o) v += DO[s * OUT + o] * W4s[o * H + k];
+            v *= silu_grad(Z3[s * H + k]);
+            if (s >= valid) v = 0.f;
+            H3[s * LDH + k] = __float2bfloat16_rn(v);
+        }
+        __syncthreads();
+        // layers 3 and 2 on the tensor cores
+        __nv_bfloat16 *Dl[2] = {H3, H2};   // delta of layer 3 (in H3), then of layer 2 (into H2)
+        const __nv_bfloat16 *Hin[2] = {H2, H1};
+        const __nv_bfloat16 *Wl[2] = {W3s, W2s};
+        float *Zin[2] = {Z2, Z1};
+#pragma unroll 1
+        for (int l = 0; l < 2; ++l) {
+            // bias gradient: column sums of delta
+            for (int k = threadIdx.x; k < H; k += NT) {
+                float g = 0.f;
+                for (int s = 0; s < TILE; ++s) g += __bfloat162float(Dl[l][s * LDH + k]);
+                slot_acc(&gB[l][k], g, first);
             }
-        __syncthreads();
+            // weight gradient delta^T . h_in
+            weight_grad(Dl[l], Hin[l], gW[l], first);
+            __syncthreads();
+            // input gradient: delta_in = (delta . W) * silu'(z_in), B(k=out, n=in) = W[k][n]
+            float acc[8][4];
+            gemm_tile_x_h(Dl[l], LDH, 1, Wl[l], LDH, 1, acc);
+            __syncthreads();  // every warp has read delta_l before delta_in overwrites h_in (l = 1)
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    int row, col;
+                    frag_coord(j, e, row, col);
+                    float v = acc[j][e] * silu_grad(Zin[l][row * H + col]);
+                    if (row >= valid) v = 0.f;
+                    if (l == 0) H2[row * LDH + col] = __float2bfloat16_rn(v);  // delta of layer 2
+                    else Z1[row * H + col] = v;                                 // delta of layer 1 (FP32)
+                }
+            __syncthreads();
+        }
+        // layer 1: dW1 = delta1^T x, db1 = sum delta1  (FP32 SIMT; delta1 is in Z1)
+        for (int i = threadIdx.x; i < H * IN; i += NT) {
+            const int o = i / IN, k = i % IN;
+            float g = 0.f;
+            for (int s = 0; s < TILE; ++s) g += Z1[s * H + o] * X[s * IN + k];
+            slot_acc(&gW1[i], g, first);
+        }
+        for (int o = threadIdx.x; o < H; o += NT) {
+            float g = 0.f;
+            for (int s = 0; s < TILE; ++s) g += Z1[s * H + o];
+            slot_acc(&gB1[o], g, first);
+        }
+        __syncthreads();  // the next tile overwrites X, Y and the activations
     }
-    // layer 1: dW1 = delta1^T x, db1 = sum delta1  (FP32 SIMT; delta1 is in Z1)
-    for (int i = threadIdx.x; i < H * IN; i += NT) {
-        const int o = i / IN, k = i % IN;
-        float g = 0.f;
-        for (int s = 0; s < TILE; ++s) g += Z1[s * H + o] * X[s * IN + k];
-        atomicAdd(&m.grad[OFF_W1 + i], g);
-    }
-    for (int o = threadIdx.x; o < H; o += NT) {
-        float g = 0.f;
-        for (int s = 0; s < TILE; ++s) g += Z1[s * H + o];
-        atomicAdd(&m.grad[OFF_B1 + o], g);
-    }
-    (void)W1s;
 }
 
-// step counter and zeroing of the gradient / loss buffers (first node of the captured step)
-__global__ void mlp_step_begin_kernel(MlpDev m, long long *step, float *loss) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kParamCount; i += gridDim.x * blockDim.x) m.grad[i] = 0.f;
+// step counter (first node of a captured step)
+__global__ void mlp_step_begin_kernel(long long *step) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *step += 1;
+}
+
+// The step's gradient: the CTA slots summed in slot order (fixed, so bit-reproducible).
+__device__ __forceinline__ float slot_sum(const MlpDev &m, int slots, int i) {
+    float g = 0.f;
+    for (int c = 0; c < slots; ++c) g += m.partial[(size_t)c * kParamCount + i];
+    return g;
+}
+__device__ __forceinline__ void loss_sum(const MlpDev &m, int slots, float *loss) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        *step += 1;
-        *loss = 0.f;
+        float l = 0.f;
+        for (int c = 0; c < slots; ++c) l += m.loss_part[c];
+        *loss = l;
     }
 }
 
-__global__ void mlp_adam_kernel(MlpDev m, const long long *step, AdamCfg c) {
+// gradient and loss of one batch, no update (the oracle check of the backward pass)
+__global__ void mlp_reduce_kernel(MlpDev m, int slots, float *loss) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kParamCount; i += gridDim.x * blockDim.x)
+        m.grad[i] = slot_sum(m, slots, i);
+    loss_sum(m, slots, loss);
+}
+
+// BF16 copy of master parameter i (weights only; biases stay FP32)
+__device__ __forceinline__ void refresh_bf16_at(const MlpDev &m, int i, float w) {
+    const __nv_bfloat16 v = __float2bfloat16_rn(w);
+    if (i < OFF_B1) m.w1b[i - OFF_W1] = v;
+    else if (i >= OFF_W2 && i < OFF_B2) m.w2b[i - OFF_W2] = v;
+    else if (i >= OFF_W3 && i < OFF_B3) m.w3b[i - OFF_W3] = v;
+    else if (i >= OFF_W4 && i < OFF_B4) m.w4b[i - OFF_W4] = v;
+}
+
+// gradient (slot sums), Adam on the FP32 masters, BF16 refresh, the step's loss
+__global__ void mlp_update_kernel(MlpDev m, int slots, const long long *step, AdamCfg c, float *loss) {
     const long long t = *step;
     // cosine decay of the learning rate over the run
     const double frac = c.total_steps > 0 ? fmin(1.0, (double)(t - 1) / (double)c.total_steps) : 0.0;
     const float lr = (float)(c.lr_min + 0.5 * (c.lr - c.lr_min) * (1.0 + cos(M_PI * frac)));
     const float bc1 = 1.0f - powf(c.beta1, (float)t), bc2 = 1.0f - powf(c.beta2, (float)t);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kParamCount; i += gridDim.x * blockDim.x) {
-        const float g = m.grad[i];
+        const float g = slot_sum(m, slots, i);
+        m.grad[i] = g;
         const float mm = c.beta1 * m.adam_m[i] + (1.0f - c.beta1) * g;
         const float vv = c.beta2 * m.adam_v[i] + (1.0f - c.beta2) * g * g;
         m.adam_m[i] = mm;
         m.adam_v[i] = vv;
         const float w = m.master[i] - lr * (mm / bc1) / (sqrtf(vv / bc2) + c.eps);
         m.master[i] = w;
+        refresh_bf16_at(m, i, w);
     }
+    loss_sum(m, slots, loss);
 }
 
 // BF16 copies of the weight matrices from the FP32 masters
@@ -444,14 +490,19 @@ cudaError_t mlp_setup_attributes() {
                                 (int)mlp::SmemLayout::TOTAL);
 }
 
+int mlp_grad_slots(int batch) {
+    const int tiles = (batch + mlp::TILE - 1) / mlp::TILE;
+    return tiles < kMaxGradSlots ? tiles : kMaxGradSlots;
+}
+
 cudaError_t mlp_launch_step(const MlpDev &m, const TrainBatch &b, const AdamCfg &c, bool update, cudaStream_t s) {
-    mlp::mlp_step_begin_kernel<<<64, 256, 0, s>>>(m, b.step, b.loss);
-    const int tiles = (b.batch + mlp::TILE - 1) / mlp::TILE;
-    mlp::mlp_fwd_bwd_kernel<<<tiles, mlp::NT, mlp::SmemLayout::TOTAL, s>>>(m, b);
-    if (update) {
-        mlp::mlp_adam_kernel<<<128, 256, 0, s>>>(m, b.step, c);
-        mlp::mlp_refresh_bf16_kernel<<<64, 256, 0, s>>>(m);
-    }
+    mlp::mlp_step_begin_kernel<<<1, 32, 0, s>>>(b.step);
+    const int slots = mlp_grad_slots(b.batch);
+    mlp::mlp_fwd_bwd_kernel<<<slots, mlp::NT, mlp::SmemLayout::TOTAL, s>>>(m, b);
+    if (update)
+        mlp::mlp_update_kernel<<<128, 256, 0, s>>>(m, slots, b.step, c, b.loss);
+    else
+        mlp::mlp_reduce_kernel<<<128, 256, 0, s>>>(m, slots, b.loss);
     return cudaGetLastError();
 }
 

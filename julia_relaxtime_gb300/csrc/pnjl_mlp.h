@@ -15,11 +15,17 @@ constexpr int OUT = 5;   // (phi_u, phi_d, phi_s, Phi, Phibar)
 
 constexpr int kParamCount = mlp::H * mlp::IN + mlp::H + 2 * (mlp::H * mlp::H + mlp::H) + mlp::OUT * mlp::H + mlp::OUT;
 
+// Gradient slots of a training step: CTA c of the fwd/bwd kernel sums the gradients of its
+// tiles (c, c + slots, ...) into slot c; the slots are then added in slot order.
+constexpr int kMaxGradSlots = 256;
+
 // Device view of the network: FP32 masters, gradients and Adam moments (packed
-// W1[H][IN], b1, W2[H][H], b2, W3[H][H], b3, W4[OUT][H], b4) and BF16 weight copies.
+// W1[H][IN], b1, W2[H][H], b2, W3[H][H], b3, W4[OUT][H], b4), BF16 weight copies and the
+// per-CTA gradient slots [kMaxGradSlots][kParamCount] and slot losses [kMaxGradSlots].
 struct MlpDev {
     float *master, *grad, *adam_m, *adam_v;
     __nv_bfloat16 *w1b, *w2b, *w3b, *w4b;
+    float *partial, *loss_part;
 };
 
 // Standardisation of inputs (T, mu, xi in fm^-1) and outputs (x in the reference's units).
@@ -30,7 +36,7 @@ struct Scaling {
 struct TrainBatch {
     const float *x;   // [n][IN] standardised inputs
     const float *y;   // [n][OUT] standardised targets
-    const long long *perm;  // epoch permutation of [0, n) (null: identity)
+    const int *perm;  // [epochs][n]: epoch e's permutation of [0, n) at perm + e * n (null: identity)
     long long n;
     int batch;
     long long steps_per_epoch;  // 0: one pass over the first `batch` samples
@@ -45,6 +51,7 @@ struct AdamCfg {
 };
 
 size_t mlp_smem_bytes();
+int mlp_grad_slots(int batch);
 cudaError_t mlp_setup_attributes();
 cudaError_t mlp_launch_step(const MlpDev &m, const TrainBatch &b, const AdamCfg &c, bool update, cudaStream_t s);
 cudaError_t mlp_refresh_bf16(const MlpDev &m, cudaStream_t s);
