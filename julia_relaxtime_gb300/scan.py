@@ -3,12 +3,15 @@
 The reference walks xi -> muB -> T one point at a time (run_gap_transport_scan.jl:407-417):
 the first T of each (xi, muB) column is solved with MultiSeed, every later T with a
 PhaseAwareContinuitySeed tracker of that column (:412-441).  Columns are independent, so here
-all columns of one xi advance together: step k solves the k-th temperature of every column
-in one GPU launch (first points in MultiSeed mode, the others with their tracker's seed and
-the MultiSeed fallback), then each tracker is updated exactly as the reference updates it.
+the columns of every xi advance together: step k solves the k-th temperature of every column
+in at most two GPU launches (first points in MultiSeed mode, the others with their tracker's
+seed and the MultiSeed fallback), then each tracker is updated exactly as the reference
+updates it.
 Rows are written in the reference's order with the same 47 columns, metadata lines and
-resume keys (scripts/utils/scan_csv.jl:18-90).  The tau / transport columns belong to the
-relaxation-time chain, which this engine does not compute; they are written as NaN.
+resume keys (scripts/utils/scan_csv.jl:18-90).  Each row also keeps the point's K data
+(build_K_data, :297-305: the one-loop A per flavour, G^f and the effective couplings, from
+the GPU) -- the relaxation-time chain's input; the tau / transport columns themselves belong
+to that chain, which this engine does not compute, and are written as NaN.
 """
 from __future__ import annotations
 
@@ -20,7 +23,7 @@ from typing import Callable, Sequence
 import numpy as np
 
 from . import _capi as api
-from .constants import HBARC_MEV_FM
+from .constants import HBARC_MEV_FM, PNJLParams
 from .pnjl import PhaseAwareContinuitySeed, FixedMu, MultiSeed
 
 HEADER = [
@@ -102,6 +105,9 @@ class ScanOptions:
     cep_path: str | None = None
     precision: str = "fp64"
     metadata: dict = field(default_factory=dict)
+    # the PNJL parameter profile (Constants_PNJL.jl:82-103); None = the built-in default.
+    # rho_norm divides by its rho0 (run_gap_transport_scan.jl:500)
+    params: PNJLParams | None = None
 
 
 def julia_range(start: float, stop: float, step: float) -> list[float]:
@@ -115,62 +121,75 @@ def julia_range(start: float, stop: float, step: float) -> list[float]:
 PointSolver = Callable[..., dict]
 
 
-def gpu_point_solver(p_num: int, t_num: int, precision: str = "fp64", engine=None) -> PointSolver:
-    from .pnjl import solve_batch
+def gpu_point_solver(p_num: int, t_num: int, precision: str = "fp64", engine=None,
+                     params: PNJLParams | None = None, kdata: bool = True) -> PointSolver:
+    """The GPU point solver of the scan; with kdata, each result also carries build_K_data
+    (run_gap_transport_scan.jl:297-305, computed for every point as the script does) under
+    "kdata": {field: [n]}."""
+    from .pnjl import default_engine, solve_batch
+
+    eng = engine or default_engine(p_num, t_num, params=params)
 
     def solver(T, mu, xi, point_seeds, max_iter):
-        return solve_batch(T, mu, xi, seed_strategy=None if point_seeds is not None else MultiSeed(),
-                           point_seeds=point_seeds, p_num=p_num, t_num=t_num, iterations=max_iter,
-                           precision=precision, engine=engine)
+        res = solve_batch(T, mu, xi, seed_strategy=None if point_seeds is not None else MultiSeed(),
+                          point_seeds=point_seeds, p_num=p_num, t_num=t_num, iterations=max_iter,
+                          precision=precision, engine=eng)
+        if kdata:
+            res["kdata"] = eng.kdata(T, mu, mu, res["masses"], res["x"])
+        return res
 
     return solver
 
 
 def scan_rows(opts: ScanOptions, solver: PointSolver, skip: set | None = None) -> list[dict]:
-    """Solve the scan grid and return one dict per row, in the reference's order."""
+    """Solve the scan grid and return one dict per row, in the reference's order.
+
+    The reference walks xi -> muB -> T (run_gap_transport_scan.jl:407-417) with one
+    continuation tracker per (xi, muB) column.  Columns are independent, so one temperature
+    of every column of every xi is solved together: at most two launches per temperature,
+    one for the columns' first points (MultiSeed) and one for the continued columns (each
+    tracker's seed, MultiSeed fallback)."""
     T_values = julia_range(opts.tmin_mev, opts.tmax_mev, opts.tstep_mev)
     muB_values = sorted(set(float(v) for v in julia_range(opts.mubmin_mev, opts.mubmax_mev, opts.mubstep_mev)))
+    rho0 = (opts.params or PNJLParams.default()).rho0
     skip = skip or set()
+    xis = [float(x) for x in opts.xi_values]
+    cols = [(ix, c) for ix in range(len(xis)) for c in range(len(muB_values))]
+    trackers = {col: PhaseAwareContinuitySeed(xis[col[0]], boundary_path=opts.boundary_path,
+                                              cep_path=opts.cep_path) for col in cols}
+    col_rows = {col: [None] * len(T_values) for col in cols}
+    for k, T_mev in enumerate(T_values):
+        T_fm = T_mev / HBARC_MEV_FM
+        first, cont = [], []
+        for col in cols:
+            if (T_mev, muB_values[col[1]], xis[col[0]]) in skip:
+                continue
+            (first if trackers[col].previous_solution is None else cont).append(col)
+        for group, per_point in ((first, False), (cont, True)):
+            if not group:
+                continue
+            mus = np.array([muB_values[c] / 3.0 / HBARC_MEV_FM for _, c in group])
+            Ts = np.full(len(group), T_fm)
+            xa = np.array([xis[ix] for ix, _ in group])
+            seeds = None
+            if per_point:
+                seeds = np.array([trackers[col].get_seed([T_fm, mus[j]], FixedMu()) for j, col in enumerate(group)])
+            res = solver(Ts, mus, xa, seeds, opts.max_iter)
+            for j, col in enumerate(group):
+                # a point whose seeds all failed (the reference raises there) is written as
+                # not converged
+                ix, c = col
+                muq_mev = muB_values[c] / 3.0
+                if bool(res["converged"][j]):
+                    trackers[col].update(res["x"][j], T_mev, muq_mev)
+                col_rows[col][k] = _row(T_mev, muq_mev, muB_values[c], xis[ix], T_fm, mus[j], res, j, rho0)
     rows = []
-    for xi in opts.xi_values:
-        xi = float(xi)
-        trackers = [PhaseAwareContinuitySeed(xi, boundary_path=opts.boundary_path, cep_path=opts.cep_path)
-                    for _ in muB_values]
-        col_rows: list[list] = [[None] * len(T_values) for _ in muB_values]
-        for k, T_mev in enumerate(T_values):
-            T_fm = T_mev / HBARC_MEV_FM
-            first, cont = [], []
-            for c, muB in enumerate(muB_values):
-                if (T_mev, muB, xi) in skip:
-                    continue
-                (first if trackers[c].previous_solution is None else cont).append(c)
-            for group, per_point in ((first, False), (cont, True)):
-                if not group:
-                    continue
-                mus = np.array([muB_values[c] / 3.0 / HBARC_MEV_FM for c in group])
-                Ts = np.full(len(group), T_fm)
-                xis = np.full(len(group), xi)
-                seeds = None
-                if per_point:
-                    seeds = np.array([trackers[c].get_seed([T_fm, mus[j]], FixedMu()) for j, c in enumerate(group)])
-                res = solver(Ts, mus, xis, seeds, opts.max_iter)
-                for j, c in enumerate(group):
-                    if int(res["status"][j]) in (api.PNJL_POINT_EXCEPTION, api.PNJL_POINT_ALL_SEEDS_FAILED):
-                        # the reference raises here; the scan records the point as not converged
-                        pass
-                    muq_mev = muB_values[c] / 3.0
-                    conv = bool(res["converged"][j])
-                    if conv:
-                        trackers[c].update(res["x"][j], T_mev, muq_mev)
-                    col_rows[c][k] = _row(T_mev, muq_mev, muB_values[c], xi, T_fm, mus[j], res, j)
-        for c in range(len(muB_values)):
-            for k in range(len(T_values)):
-                if col_rows[c][k] is not None:
-                    rows.append(col_rows[c][k])
+    for col in cols:
+        rows.extend(r for r in col_rows[col] if r is not None)
     return rows
 
 
-def _row(T_mev, muq_mev, muB_mev, xi, T_fm, muq_fm, res, j) -> dict:
+def _row(T_mev, muq_mev, muB_mev, xi, T_fm, muq_fm, res, j, rho0: float) -> dict:
     x = res["x"][j]
     nq, naq = res["n_q"][j], res["n_aq"][j]
     rho_baryon = ((nq[0] - naq[0]) + (nq[1] - naq[1]) + (nq[2] - naq[2])) / 3.0
@@ -182,7 +201,7 @@ def _row(T_mev, muq_mev, muB_mev, xi, T_fm, muq_fm, res, j) -> dict:
         "converged": bool(res["converged"][j]), "iterations": int(res["iterations"][j]),
         "residual_norm": float(res["residual_norm"][j]), "Phi": float(x[3]), "Phibar": float(x[4]),
         "m_u": float(res["masses"][j][0]), "m_d": float(res["masses"][j][1]), "m_s": float(res["masses"][j][2]),
-        "rho_baryon": rho_baryon, "rho_norm": rho_baryon / 0.16,
+        "rho_baryon": rho_baryon, "rho_norm": rho_baryon / rho0,
         "omega_fm4inv": omega, "P_fm4inv": P, "epsilon_fm4inv": eps, "s_fm3inv": s,
         "omega_MeV_fm3": omega * HBARC_MEV_FM, "P_MeV_fm3": P * HBARC_MEV_FM, "epsilon_MeV_fm3": eps * HBARC_MEV_FM,
         "eps_minus_3P_over_T4": e3p,
@@ -190,6 +209,8 @@ def _row(T_mev, muq_mev, muB_mev, xi, T_fm, muq_fm, res, j) -> dict:
         "n_ubar": float(naq[0]), "n_dbar": float(naq[1]), "n_sbar": float(naq[2]),
         **{k: nan for k in HEADER[30:]},
         "status": int(res["status"][j]), "phi": np.array(x[:3]),
+        # build_K_data of the point (the relaxation-time chain's input), when the solver gives it
+        "kdata": {k: float(v[j]) for k, v in res["kdata"].items()} if "kdata" in res else None,
     }
 
 
@@ -235,7 +256,7 @@ def read_existing_keys(path: str, key_cols=("T_MeV", "muB_MeV", "xi")) -> set:
 
 def run_gap_transport_scan(opts: ScanOptions, solver: PointSolver | None = None) -> str:
     """The gap part of run_scan (run_gap_transport_scan.jl:362-550), writing opts.output."""
-    solver = solver or gpu_point_solver(opts.p_num, opts.t_num, opts.precision)
+    solver = solver or gpu_point_solver(opts.p_num, opts.t_num, opts.precision, params=opts.params)
     d = os.path.dirname(opts.output)
     if d:
         os.makedirs(d, exist_ok=True)
@@ -280,12 +301,15 @@ def main(argv: Sequence[str] | None = None):
     ap.add_argument("--boundary", default=None, help="boundary.csv of the phase-aware seed")
     ap.add_argument("--cep", default=None, help="cep.csv of the phase-aware seed")
     ap.add_argument("--precision", default="fp64", choices=("fp64", "mixed"))
+    ap.add_argument("--profile", default=None, help="PNJL parameter profile (default: $PNJL_PARAM_PROFILE)")
+    ap.add_argument("--config-dir", default=None, help="directory of the profile .toml files")
     a = ap.parse_args(argv)
+    params = PNJLParams.load(a.profile, a.config_dir) if (a.profile or a.config_dir) else None
     opts = ScanOptions(output=a.output, xi_values=[float(v) for v in a.xi.split(",")], tmin_mev=a.tmin,
                        tmax_mev=a.tmax, tstep_mev=a.tstep, mubmin_mev=a.mubmin, mubmax_mev=a.mubmax,
                        mubstep_mev=a.mubstep, overwrite=a.overwrite, resume=not a.no_resume, p_num=a.p_num,
                        t_num=a.t_num, max_iter=a.max_iter, boundary_path=a.boundary, cep_path=a.cep,
-                       precision=a.precision)
+                       precision=a.precision, params=params)
     print(run_gap_transport_scan(opts))
 
 

@@ -180,6 +180,39 @@ def test_scan_resume_skips_existing_rows(tmp_path):
     assert len(lines) == 5 and lines[-1].startswith("150.0,")
 
 
+def test_scan_rho_norm_uses_profile_rho0_and_batches_xi():
+    """rho_norm = rho_baryon / rho0 of the loaded profile (run_gap_transport_scan.jl:497-500), and
+    every xi's columns of one temperature go to the solver together (at most two calls per T)."""
+    import dataclasses
+
+    from julia_relaxtime_gb300.constants import PNJLParams
+    from julia_relaxtime_gb300.scan import scan_rows
+    from oracle_adapter import oracle_point_solver
+
+    base = oracle_point_solver(12, 6)
+    calls = []
+
+    def solver(T, mu, xi, seeds, max_iter):
+        calls.append((float(T[0]), len(T), seeds is None))
+        return base(T, mu, xi, seeds, max_iter)
+
+    params = dataclasses.replace(PNJLParams.default(), rho0=0.17)
+    opts = ScanOptions(xi_values=[0.0, 0.2], tmin_mev=120, tmax_mev=140, tstep_mev=10, mubmin_mev=0,
+                       mubmax_mev=600, mubstep_mev=300, params=params)
+    rows = scan_rows(opts, solver)
+    assert len(rows) == 2 * 3 * 3
+    # reference order: xi -> muB -> T
+    keys = [(r["xi"], r["muB_MeV"], r["T_MeV"]) for r in rows]
+    assert keys == sorted(keys)
+    # T = 120: one MultiSeed call for all 6 columns; later T: one continuation call each
+    assert calls[0][1:] == (6, True) and all(c[1:] == (6, False) for c in calls[1:]) and len(calls) == 3
+    for r in rows:
+        assert r["rho_norm"] == r["rho_baryon"] / 0.17
+    default_rows = scan_rows(dataclasses.replace(opts, params=None), base)
+    for a, b in zip(rows, default_rows):
+        assert b["rho_norm"] == b["rho_baryon"] / 0.16 and a["rho_baryon"] == b["rho_baryon"]
+
+
 # ---- TmuScan driver (TmuScan.jl) with the oracle as the point solver --------------------
 def _tmu_rows(Ts, solver):
     from julia_relaxtime_gb300 import scan
