@@ -102,6 +102,12 @@ def lib():
         L.or_multiseed_seeds.argtypes = [C.POINTER(Params), C.c_double, dp]
         L.or_builtin_seed.argtypes = [C.c_int, dp]
         L.or_max_threads.restype = C.c_int
+        L.or_const_integral_term_A.argtypes = [C.POINTER(Params), C.c_double]
+        L.or_const_integral_term_A.restype = C.c_double
+        L.or_one_loop_A.argtypes = [C.POINTER(Params), C.c_int, dp, dp] + [C.c_double] * 5
+        L.or_one_loop_A.restype = C.c_double
+        L.or_kdata.argtypes = [C.POINTER(Params), C.c_int, dp, dp] + [C.c_double] * 7 + [dp]
+        L.or_effective_couplings.argtypes = [C.c_double] * 4 + [dp]
         assert L.or_sizeof_result() == C.sizeof(Result), "Result layout mismatch"
         assert L.or_sizeof_opts() == C.sizeof(Opts), "Opts layout mismatch"
         assert L.or_sizeof_params() == C.sizeof(Params), "Params layout mismatch"
@@ -240,6 +246,62 @@ def solve_batch(params: Params, nodes: Nodes, T, mu, xi, *, seeds=None, multi=Tr
                          1 if multi else 0, ns, _dp(sd), 1 if (multi and multiseed_rule) else 0,
                          C.byref(opts), out, threads)
     return out
+
+
+def polish(params: Params, nodes: Nodes, T, mu, xi, x0, *, iters: int = 4, threads: int = 0):
+    """The roots x0 [n,5] converged to rounding: plain Newton (no trust region, no MultiSeed
+    fallback) from x0 with ftol 1e-13 and no step test, at most `iters` steps.  Near the
+    rounding floor the residual no longer falls below ftol, but the iterate stays within
+    |J^-1| x rounding of the root, so x is the reference a solve at ftol 1e-10 is measured
+    against.  Returns (x [n,5], omega [n], residual [n])."""
+    x0 = np.ascontiguousarray(np.asarray(x0, dtype=np.float64).reshape(-1, 5))
+    opts = default_opts(max_iter=iters, ftol=1e-13, xtol=0.0, trust_region_fallback=0, auto_multiseed_fallback=0)
+    rs = solve_batch(params, nodes, T, mu, xi, seeds=x0, multi=False, opts=opts, threads=threads)
+    x = np.array([list(r.x) for r in rs]).reshape(-1, 5)
+    return x, np.array([r.omega for r in rs]), np.array([r.residual_norm for r in rs])
+
+
+# build_K_data's output, in order (run_gap_transport_scan.jl:297-305, EffectiveCouplings.jl:273-278)
+KDATA_FIELDS = ("A_u", "A_d", "A_s", "G_u", "G_s", "K0_plus", "K0_minus", "K123_plus", "K123_minus",
+                "K4567_plus", "K4567_minus", "K8_plus", "K8_minus", "K08_plus", "K08_minus", "det_K_plus",
+                "det_K_minus")
+
+
+def const_integral_term_A(params: Params, m: float) -> float:
+    return lib().or_const_integral_term_A(C.byref(params), m)
+
+
+def one_loop_A(params: Params, p, w, m, mu, T, Phi, Phib) -> float:
+    p = np.ascontiguousarray(p, dtype=np.float64)
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    return lib().or_one_loop_A(C.byref(params), p.size, _dp(p), _dp(w), m, mu, T, Phi, Phib)
+
+
+def effective_couplings(G: float, K: float, G_u: float, G_s: float) -> dict:
+    """calculate_effective_couplings (EffectiveCouplings.jl:242-279)."""
+    out = np.zeros(12)
+    lib().or_effective_couplings(G, K, G_u, G_s, _dp(out))
+    return dict(zip(KDATA_FIELDS[5:], out.tolist()))
+
+
+def kdata(params: Params, T, mu_u, mu_s, masses, x, *, p_num: int = 64, p_max: float = 10.0) -> dict:
+    """build_K_data at n points: A on the p_num Gauss-Legendre nodes of [0, p_max] (the
+    reference's DEFAULT_MOMENTUM_NODES: 64 on [0, 10]); masses [n,3], x [n,5] (Phi = x[:,3],
+    Phibar = x[:,4]).  Returns {field: [n]} over KDATA_FIELDS."""
+    p, w = gauleg(0.0, p_max, p_num)
+    T = np.atleast_1d(np.asarray(T, dtype=np.float64))
+    n = T.size
+    mu_u = np.broadcast_to(np.asarray(mu_u, dtype=np.float64), (n,))
+    mu_s = np.broadcast_to(np.asarray(mu_s, dtype=np.float64), (n,))
+    masses = np.asarray(masses, dtype=np.float64).reshape(n, 3)
+    x = np.asarray(x, dtype=np.float64).reshape(n, 5)
+    out = np.zeros((n, len(KDATA_FIELDS)))
+    row = np.zeros(len(KDATA_FIELDS))
+    for i in range(n):
+        lib().or_kdata(C.byref(params), p.size, _dp(p), _dp(w), T[i], mu_u[i], mu_s[i], masses[i, 0], masses[i, 2],
+                       x[i, 3], x[i, 4], _dp(row))
+        out[i] = row
+    return {k: out[:, j].copy() for j, k in enumerate(KDATA_FIELDS)}
 
 
 def max_threads() -> int:
