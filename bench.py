@@ -1,35 +1,42 @@
 #!/usr/bin/env python
 """Throughput of the batched PNJL gap solve on one GB300 (bench contract of this repository).
 
-Workload (default ``--workload aniso_scan_256x256x9``): the batched anisotropic scan
-T = linspace(50, 300, 256) MeV x mu = linspace(0, 400, 256) MeV x xi in {-0.4, ..., 0.4}
-(589,824 points), 128 momentum x 32 cos(theta) Gauss-Legendre nodes, converged when
+Workload (default ``--workload first_order_2048x2048x9``, the largest single-GPU
+configuration): the first-order-region scan T = linspace(20, 150, 2048) MeV x
+mu_u = linspace(250, 450, 2048) MeV, mu_s = mu_u / 2, x xi in {-0.4, ..., 0.4} (37,748,736
+points), 128 momentum x 32 cos(theta) Gauss-Legendre nodes, 8 seed candidates (MultiSeed +
+MEDIUM, HIGH_DENSITY) with global-min-Omega selection, converged when
 ||grad_x Omega||_inf < 1e-10.  A "step" solves one strided slice of the grid (every
-n_chunks-th point, a different slice each step), so the timed steps are spread over the whole
-(T, mu, xi) box.  Inputs (T, mu, xi) are synthetic grid points: there is no dataset.
+n_chunks-th point, 18,432 points, a different slice each step), so the timed steps are spread
+over the whole (T, mu, xi) box; the slices are decoded from the flat index when loaded.
+Inputs (T, mu, xi) are synthetic grid points: there is no dataset.  Other workloads:
+``aniso_scan_256x256x9`` (T 50-300 MeV x mu 0-400 MeV x 9 xi, 589,824 points, 4 seeds),
+``surrogate_eval_2p20`` (2^20 uniform points, MultiSeed (6)) and ``iso_scan_32x32``.
 
 Headline (``--mode surrogate``): surrogate-seeded mixed-precision solves -- the trained
 network's seed per point (BF16 tensor-core inference kernel), one mixed-precision Newton solve
-(FP32 Kahan node passes, FP64 solve/update/residual), verification by every MultiSeed
-candidate where a second phase can exist (the cells of the network's verification map, roots
-far from the seed, roots on an unstable branch), MultiSeed fallback where the learned seed
-fails.  The network is trained in an untimed set-up on this GPU (labels: a 64 x 64 x 5
-(T, mu, xi) multi-seed solve; 400 epochs), reported as ``surrogate.train``.  The same chunks
-are then solved by the plain FP64 multi-seed Newton (the workload's MultiSeed candidates,
-min-Omega selection, trust-region fallback): ``plain_fp64`` holds its rate, the speed-up, and
-the phase misassignments of the surrogate path against it.  ``--mode multiseed --precision
-fp64|mixed`` times the MultiSeed table path alone; ``--mode orders`` the 32 x 32 grid at three
-quadrature orders in one graph.  Other workloads: ``surrogate_eval_2p20`` (2^20 uniform points,
-MultiSeed (6)) and ``first_order_2048x2048x9`` (T 20-150 MeV, mu_u 250-450 MeV, mu_s = mu_u/2,
-9 xi, 8 seeds; the network trained on that box).
+(FP32 Kahan node passes, FP64 solve/update/residual), verification by every seed candidate
+where a second phase can exist (the cells of the network's verification map, roots far from
+the seed, roots on an unstable branch), MultiSeed fallback where the learned seed fails.  The
+network is trained in an untimed set-up on this GPU (labels: a 64 x 64 x 5 (T, mu, xi)
+multi-seed solve over the workload's box; 400 epochs), reported as ``surrogate.train``, and
+``surrogate.amortised`` is the whole grid's rate with that set-up included.  The same chunks
+are then solved by the plain FP64 multi-seed Newton (the workload's candidates, min-Omega
+selection, trust-region fallback): ``plain_fp64`` holds its rate, the speed-up, and the phase
+misassignments of the surrogate path against it.  ``parity`` checks both arms' roots against
+the oracle's (root to rounding; phase from its MultiSeed solve) on the points where the arms
+disagree and on uniformly drawn points.  ``--mode multiseed --precision fp64|mixed`` times
+the MultiSeed table path alone; ``--mode orders`` the 32 x 32 grid at three quadrature orders
+in one graph.
 
 value: converged solves per second with inputs already in HBM (pnjl_solve_batch_learned_device
 or pnjl_solve_batch_device), timed with CUDA events on the library's stream; e2e: the same
 metric through the host-array entry point (pnjl_solve_batch_learned / pnjl_solve_batch),
-pinned host inputs, host<->device copies inside the timed region.  ``--impl reference``
-times the reference algorithm's CPU restatement (the oracle: nested forward-mode derivatives
-like the reference's ForwardDiff, NLsolve-style Newton, MultiSeed min-Omega) on a bounded
-sample of the same workload with all host threads.
+pinned host inputs, host<->device copies inside the timed region.  roofline: the dominant
+kernel's algorithmic FP64, FP32 and SFU (MUFU) rates against pipe peaks measured in the run.
+``--impl reference`` times the reference algorithm's CPU restatement (the oracle: nested
+forward-mode derivatives like the reference's ForwardDiff, NLsolve-style Newton, MultiSeed
+min-Omega) on a bounded sample of the same workload with all host threads.
 """
 from __future__ import annotations
 
@@ -79,6 +86,22 @@ FLOP_NEWTON32 = 150
 FLOP_THERMO32 = 64
 FLOP_FF = 53
 FLOP_FF_THERMO = 58
+# SFU (MUFU) operations per node-flavour evaluation, counted from the pass sources:
+#   FP32 Newton pass (node_pass_newton32): rsqrt, ex2 (__expf), 2 rcp.approx       = 4
+#   FP32 Omega pass: rsqrt, ex2, rcp, lg2 (__logf)                                   = 4
+#   float-float passes (pnjl_ff.cuh): rsqrt seed of ff_rsqrt, 2 rcp.approx seeds of
+#     ff_rcp (ff_exp and ff_log are table methods: no MUFU)                          = 3
+#   FP64 certification pass (node_pass_cert): rsqrt.approx.f64, rcp.approx.f64
+#     (its exp is a table method)                                                    = 2
+#   plain FP64 passes: the seeds of the library's double rsqrt and 1/x               = 2
+MUFU = {"node_evals_fp32": 4, "node_evals_fp32_thermo": 4, "node_evals_ff": 3, "node_evals_ff_thermo": 3,
+        "node_evals_ff_grad_thermo": 3, "node_evals_fp64_grad": 2, "node_evals_fp64_grad_thermo": 2,
+        "node_evals_fp64_newton": 2, "node_evals_fp64_thermo": 2}
+
+
+def pass_mufu(st: dict) -> float:
+    """SFU (MUFU) operations of one solve from the node-evaluation counters."""
+    return float(sum(st[k] * v for k, v in MUFU.items()))
 
 
 def pass_flops(st: dict):
@@ -218,13 +241,14 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def run_reference(args, grid, sample_points: int):
-    """The reference algorithm on the CPU (oracle restatement), bounded sample, all threads."""
+def run_reference(args, grid, sample_points: int, threads: int | None = None):
+    """The reference algorithm on the CPU (oracle restatement), bounded sample, all threads
+    (or `threads`)."""
     from oracle import oracle as orc
 
     P = orc.default_params()
     nd = orc.Nodes(grid["p_num"], grid["t_num"])
-    threads = os.cpu_count() or 1
+    threads = threads or os.cpu_count() or 1
     n = grid["n"]
     rng = np.random.default_rng(1234)
     idx = np.sort(rng.choice(n, size=min(sample_points, n), replace=False))
@@ -250,6 +274,89 @@ def run_reference(args, grid, sample_points: int):
     total = sum(times)
     return dict(value=solved / total, seconds=total, cores=threads, points=len(idx),
                 sample=f"{len(idx)} points drawn uniformly (seed 1234) from the workload grid, per step")
+
+
+def single_thread_rate(grid, sample_points: int) -> dict:
+    """The same CPU restatement on one thread, over a few of the same points (one pass)."""
+    class A:  # noqa: N801
+        warmup, steps = 0, 1
+    r = run_reference(A, grid, sample_points, threads=1)
+    return {"value": r["value"], "unit": "solves/s", "cores": 1, "sample": r["sample"]}
+
+
+def parity_vs_oracle(grid, arms: dict, chunk_points, n_uniform: int = 2000, n_phase: int = 384, seed: int = 4321):
+    """The timed arms' roots against the oracle (CPU, FP64 nested-jet Newton: the reference
+    algorithm), on the points where the arms disagree by more than 1e-9 (relative, per
+    condensate) plus n_uniform points drawn from the timed slices.
+
+    Reference root: the oracle's plain Newton at ftol 1e-13 (no step test) from the plain
+    FP64 arm's root -- the root to rounding (oracle.polish).  Phase: the oracle's MultiSeed
+    min-Omega solve at the bench's ftol on n_phase of the uniform points.  Per arm:
+    |dphi|_inf / |phi|_inf (the condensate vector), |dPhi|_inf (Phi, Phibar), |dOmega|/|Omega|."""
+    from oracle import oracle as orc
+
+    t0 = time.perf_counter()
+    names = list(arms)
+    pts, cols = [], {a: {"x": [], "omega": [], "ok": []} for a in names}
+    for k, rr in enumerate(arms[names[0]]):
+        T, mu_u, mu_s, xi = chunk_points(rr["chunk"])
+        pts.append(np.stack([T, mu_u, mu_s, xi], axis=1))
+        for a in names:
+            r = arms[a][k]
+            cols[a]["x"].append(r["x"])
+            cols[a]["omega"].append(r["omega"])
+            cols[a]["ok"].append(r["converged"])
+    pts = np.concatenate(pts)
+    X = {a: np.concatenate(cols[a]["x"]) for a in names}
+    OM = {a: np.concatenate(cols[a]["omega"]) for a in names}
+    ok = np.logical_and.reduce([np.concatenate(cols[a]["ok"]) for a in names])
+    a0, a1 = names
+    rel = np.abs(X[a0][:, :3] - X[a1][:, :3]) / np.maximum(np.abs(X[a1][:, :3]), 1e-300)
+    flagged = np.flatnonzero(ok & (rel.max(axis=1) > 1e-9))
+    rng = np.random.default_rng(seed)
+    rest = np.setdiff1d(np.flatnonzero(ok), flagged)
+    uni = np.sort(rng.choice(rest, size=min(n_uniform, rest.size), replace=False))
+    sel = np.concatenate([flagged, uni])
+    P = orc.default_params()
+    nd = orc.Nodes(grid["p_num"], grid["t_num"])
+    T, mu_u, mu_s, xi = (pts[sel, j].copy() for j in range(4))
+    mu3 = np.stack([mu_u, mu_u, mu_s], axis=1)
+    threads = os.cpu_count() or 1
+    xt, omt, rt = orc.polish(P, nd, T, mu3, xi, X["plain_fp64"][sel], threads=threads)
+    out = {"reference": "oracle root to rounding: plain Newton at ftol 1e-13 from the plain FP64 arm's root "
+                        "(oracle.polish); phase from the oracle's MultiSeed min-Omega solve (ftol 1e-10)",
+           "points": int(sel.size), "points_arms_differ_above_1e-9": int(flagged.size), "points_uniform": int(uni.size),
+           "bound": {"dphi_over_phi_inf": 1e-9, "dPhi_abs": 1e-10},
+           "oracle_residual_max": float(np.max(rt))}
+    phi_scale = np.abs(xt[:, :3]).max(axis=1)
+    for a in names:
+        x, om = X[a][sel], OM[a][sel]
+        dphi = np.abs(x[:, :3] - xt[:, :3]).max(axis=1) / phi_scale
+        dPhi = np.abs(x[:, 3:] - xt[:, 3:]).max(axis=1)
+        dom = np.abs(om - omt) / np.abs(omt)
+        out[a] = {"max_dphi_over_phi": float(dphi.max()), "points_dphi_above_1e-9": int(np.sum(dphi > 1e-9)),
+                  "max_abs_dPhi": float(dPhi.max()), "points_dPhi_above_1e-10": int(np.sum(dPhi > 1e-10)),
+                  "max_rel_domega": float(dom.max())}
+    # phase selection against the oracle's own MultiSeed solve
+    ph = uni[:min(n_phase, uni.size)]
+    T, mu_u, mu_s, xi = (pts[ph, j].copy() for j in range(4))
+    mu3 = np.stack([mu_u, mu_u, mu_s], axis=1)
+    kw = dict(n_seeds=grid["n_seeds"])
+    if grid["extra"]:
+        from julia_relaxtime_gb300.pnjl import multiseed_table
+
+        kw = dict(seeds=multiseed_table(grid["n_seeds"], grid["extra"])[0], multiseed_rule=False)
+    rs = orc.solve_batch(P, nd, T, mu3, xi, multi=True, opts=orc.default_opts(max_iter=40, ftol=1e-10),
+                         threads=threads, **kw)
+    om_o = np.array([r.omega for r in rs])
+    conv_o = np.array([bool(r.converged) for r in rs])
+    out["phase_check"] = {"points": int(ph.size), "oracle_converged": int(conv_o.sum())}
+    for a in names:
+        diff = np.abs(OM[a][ph] - om_o) > 1e-10 * np.abs(om_o)
+        out["phase_check"][f"misassignments_{a}"] = int(np.sum(diff & conv_o))
+    out["seconds"] = time.perf_counter() - t0
+    out["threads"] = threads
+    return out
 
 
 class Arm:
@@ -353,7 +460,8 @@ def main():
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=("gpu", "reference"))
-    ap.add_argument("--workload", default="aniso_scan_256x256x9")
+    ap.add_argument("--workload", default="first_order_2048x2048x9",
+                    choices=("first_order_2048x2048x9", "aniso_scan_256x256x9", "surrogate_eval_2p20", "iso_scan_32x32"))
     ap.add_argument("--mode", default="surrogate", choices=("surrogate", "multiseed", "orders"),
                     help="surrogate: learned seed + mixed precision (headline); multiseed: the MultiSeed table; "
                          "orders: the 32 x 32 isotropic grid at p = 64, 128, 256 in one CUDA graph (mixed "
@@ -367,6 +475,7 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=48, help="points per step of the CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-parity", action="store_true", help="skip the oracle check of the arms' roots")
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default launch shape")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -388,12 +497,13 @@ def main():
         if rank != 0:
             return
         ref = run_reference(args, grid, args.cpu_sample)
+        single = single_thread_rate(grid, max(4, args.cpu_sample // 8))
         line = {"metric": METRIC, "value": ref["value"], "unit": "solves/s", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * ref["seconds"] / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic", "config": config, "impl": "reference",
                 "cpu_baseline": {"value": ref["value"], "unit": "solves/s", "cores": ref["cores"], "kind": "port",
-                                 "sample": ref["sample"]},
+                                 "sample": ref["sample"], "single_thread": single},
                 "e2e": {"value": ref["value"], "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -475,7 +585,7 @@ def main():
         sampler = ClockSampler(local_rank) if sample_clocks else None
         rec = {"step_ms": [], "kernel_ms": [], "solved": 0, "flops64": 0.0, "flops32": 0.0, "flops_ff": 0.0,
                "evals": 0, "kinds": {}, "results": [], "k0_ms": [], "k1_ms": [], "k0_flops": [0.0, 0.0, 0.0],
-               "k0_evals": 0}
+               "k0_evals": 0, "mufu": 0.0, "k0_mufu": 0.0}
         launches0 = eng.stats()["kernel_launches"]
         if dist is not None:
             dist.barrier()
@@ -501,12 +611,14 @@ def main():
             rec["flops64"] += f64_
             rec["flops32"] += f32_
             rec["flops_ff"] += fff_
+            rec["mufu"] += pass_mufu(st)
             # the first kernel alone (the per-point kernel of a learned / per-point solve)
             s0, s1 = eng.stats(kernel=0), eng.stats(kernel=1)
             rec["k0_ms"].append(s0["last_kernel_ms"])
             rec["k1_ms"].append(s1["last_kernel_ms"])
             for j, v in enumerate(pass_flops(s0)):
                 rec["k0_flops"][j] += v
+            rec["k0_mufu"] += pass_mufu(s0)
             rec["k0_evals"] += s0["node_evals_fp64"] + s0["node_evals_fp32"] + s0["node_evals_fp32_thermo"] + \
                 s0["node_evals_ff"] + s0["node_evals_ff_thermo"] + s0["node_evals_ff_grad_thermo"]
             for kk in ("node_evals_fp64_newton", "node_evals_fp64_thermo", "node_evals_fp64_grad",
@@ -518,7 +630,7 @@ def main():
             res = d_out["residual_norm"][:n].cpu().numpy()
             rec["solved"] += int(np.sum(conv & (res <= 1e-10)))
             rec["results"].append({"converged": conv, "x": d_out["x"][:5 * n].cpu().numpy().reshape(n, 5),
-                                   "omega": d_out["omega"][:n].cpu().numpy()})
+                                   "omega": d_out["omega"][:n].cpu().numpy(), "residual_norm": res, "chunk": k % args.chunks})
         torch.cuda.synchronize()
         rec["clocks"] = sampler.stop() if sampler else None
         rec["launches"] = eng.stats()["kernel_launches"] - launches0
@@ -559,7 +671,7 @@ def main():
 
     # the plain FP64 multi-seed Newton on the same chunks: the denominator of the speed-up and
     # the FP64 judge of the surrogate's phase selection
-    plain_line = None
+    plain_line = prec = None
     if args.mode == "surrogate" and not args.no_plain:
         prec = run_arm(plain, args.steps, 1, False)
         mis, dphi, dphi_abs, dPhi, both_n, n_rel = 0, 0.0, 0.0, 0.0, 0, 0
@@ -618,19 +730,21 @@ def main():
         return
     peak_fp64 = eng.probe_peak("fp64")
     peak_fp32 = eng.probe_peak("fp32")
+    peak_sfu = eng.probe_peak("sfu")
     K = args.steps
     if precision == "fp64":
-        kname, k_ms, k_flops, k_evals = "solve_kernel<32>", main_rec["kernel_ms"], \
-            [main_rec["flops64"], main_rec["flops32"], main_rec["flops_ff"]], main_rec["evals"]
+        kname, k_ms, k_flops, k_evals, k_mufu = "solve_kernel<32>", main_rec["kernel_ms"], \
+            [main_rec["flops64"], main_rec["flops32"], main_rec["flops_ff"]], main_rec["evals"], main_rec["mufu"]
     elif args.mode == "surrogate":
-        kname, k_ms, k_flops, k_evals = "mixed_fused_kernel<32>", roof_rec["k0_ms"], roof_rec["k0_flops"], \
-            roof_rec["k0_evals"]
+        kname, k_ms, k_flops, k_evals, k_mufu = "mixed_fused_kernel<32>", roof_rec["k0_ms"], roof_rec["k0_flops"], \
+            roof_rec["k0_evals"], roof_rec["k0_mufu"]
     else:
-        kname, k_ms, k_flops, k_evals = "mixed_tasks_kernel<32>", main_rec["kernel_ms"], \
-            [main_rec["flops64"], main_rec["flops32"], main_rec["flops_ff"]], main_rec["evals"]
+        kname, k_ms, k_flops, k_evals, k_mufu = "mixed_tasks_kernel<32>", main_rec["kernel_ms"], \
+            [main_rec["flops64"], main_rec["flops32"], main_rec["flops_ff"]], main_rec["evals"], main_rec["mufu"]
     avg_k_s = (sum(k_ms) / len(k_ms)) * 1e-3
     ach64 = k_flops[0] / K / avg_k_s
     ach32 = k_flops[1] / K / avg_k_s
+    ach_sfu = k_mufu / K / avg_k_s
     step_kernels_ms = sum(roof_rec["kernel_ms"]) / K
     roof = {"bound": "fp64", "kernel": kname, "achieved": ach64 / 1e12, "peak": peak_fp64 / 1e12,
             "unit": "TFLOP/s", "frac": ach64 / peak_fp64,
@@ -647,6 +761,9 @@ def main():
             else None,
             "traffic_source": TRAFFIC.get(kname, {}).get("source"),
             "fp32": {"achieved": ach32 / 1e12, "peak": peak_fp32 / 1e12, "frac": ach32 / peak_fp32},
+            "sfu": {"achieved": ach_sfu / 1e12, "peak": peak_sfu / 1e12, "unit": "Tops/s", "frac": ach_sfu / peak_sfu,
+                    "mufu_per_node_flavour": MUFU,
+                    "peak_source": "measured in-run (pnjl_probe_peak: ex2.approx chains on every lane)"},
             "float_float_flop_per_launch": k_flops[2] / K}
     launches = main_rec["launches"]
     line = {"metric": METRIC, "value": main_rec["value"], "unit": "solves/s", "n_gpus": world, "steps": args.steps,
@@ -656,7 +773,12 @@ def main():
             "roofline": roof, "clocks": main_rec["clocks"], "solved": main_rec["solved"], "tuning": tuning,
             "work_per_step": {k: v / args.steps for k, v in main_rec["kinds"].items()}}
     if train is not None:
+        # the whole grid's rate with the set-up (labels, training, verification map) included
+        gn = float(grid["n"])
         line["surrogate"] = {"train": train,
+                             "amortised": {"value": gn / (gn / main_rec["value"] + train["seconds"]), "unit": "solves/s",
+                                           "grid_points": int(gn),
+                                           "how": "grid points / (grid points / value + train.seconds)"},
                              "fallback_rate": main_rec["kinds"].get("multiseed_fallbacks", 0) /
                              max(1, config["points_per_step"] * args.steps),
                              "verify": {"seeds": seed_count(grid) if arm.opts.verify_seeds < 0 else arm.opts.verify_seeds,
@@ -671,7 +793,12 @@ def main():
             warmup, steps = 0, 1
         ref = run_reference(A, grid, args.cpu_sample)
         line["cpu_baseline"] = {"value": ref["value"], "unit": "solves/s", "cores": ref["cores"], "kind": "port",
-                                "sample": ref["sample"]}
+                                "sample": ref["sample"],
+                                "single_thread": single_thread_rate(grid, max(4, args.cpu_sample // 8))}
+        if prec is not None and not args.no_parity:
+            # the checker: both timed arms' roots against the oracle's
+            line["parity"] = parity_vs_oracle(grid, {"surrogate_mixed": main_rec["results"],
+                                                     "plain_fp64": prec["results"]}, chunk_points)
     print(json.dumps(line))
     eng.close()
     if dist is not None:

@@ -354,18 +354,50 @@ int pnjl_plan_launch(pnjl_plan *plan);
 int pnjl_plan_stats(pnjl_plan *plan, int32_t segment, pnjl_stats *out);
 int pnjl_plan_destroy(pnjl_plan *plan);
 
+/* ---- K data of the relaxation-time chain ----------------------------------------------------
+ * build_K_data (scripts/relaxtime/run_gap_transport_scan.jl:297-305) for n solved points: the
+ * one-loop integral A_f = OneLoopIntegrals.A(m_f, mu_f, T, Phi, Phibar, nodes, weights)
+ * (src/relaxtime/OneLoopIntegrals.jl:507-543) on the p_num Gauss-Legendre nodes of [0, p_max]
+ * (the script uses DEFAULT_MOMENTUM_NODES: 64 on [0, 10]), G^f = calculate_G_from_A(A_f, m_f)
+ * (src/relaxtime/EffectiveCouplings.jl:56-60) and calculate_effective_couplings(G, K, G^u, G^s)
+ * (:242-279) with its determinants (:112-115).  Inputs per point: T, mu_u (used for u and d),
+ * mu_s (the script passes one quark chemical potential: pass mu_u again), masses [3n] and
+ * the solution x [5n] (Phi = x[3], Phibar = x[4]) -- the layout of pnjl_result_soa.  Any
+ * NULL output pointer skips that field.  FP64. */
+typedef struct pnjl_kdata_soa {
+    double *A_u, *A_d, *A_s;          /* [n] one-loop A per flavour (A_d = A_u, as build_K_data) */
+    double *G_u, *G_s;                /* [n] G^f = -N_c/(4 pi^2) m_f A_f                         */
+    double *K0_plus, *K0_minus;       /* [n] effective couplings K_alpha^+- (fm^2)               */
+    double *K123_plus, *K123_minus;
+    double *K4567_plus, *K4567_minus;
+    double *K8_plus, *K8_minus;
+    double *K08_plus, *K08_minus;
+    double *det_K_plus, *det_K_minus; /* [n] K0 K8 - K08^2 per channel (fm^4)                    */
+} pnjl_kdata_soa;
+/* Host arrays, synchronous. */
+int pnjl_kdata_batch(pnjl_ctx *ctx, int64_t n, int32_t p_num, double p_max, const double *T,
+                     const double *mu_u, const double *mu_s, const double *masses, const double *x,
+                     pnjl_kdata_soa *out);
+/* Device arrays, asynchronous on pnjl_stream(ctx) (e.g. straight from a solve's outputs). */
+int pnjl_kdata_batch_device(pnjl_ctx *ctx, int64_t n, int32_t p_num, double p_max, const double *d_T,
+                            const double *d_mu_u, const double *d_mu_s, const double *d_masses,
+                            const double *d_x, pnjl_kdata_soa *d_out);
+
 /* Largest batch of pnjl_solve_batch_noalloc, counted in tasks: n * n_seeds in
  * PNJL_SEEDS_TABLE mode, n in PNJL_SEEDS_PER_POINT mode (and n itself at most this). */
 #define PNJL_NOALLOC_MAX_TASKS 32768
 
 /* Batched solve that allocates nothing (no counterpart in the reference, which has no GPU
- * code; it is an allocation-free twin of pnjl_solve_batch_device).  For callers that may not
- * allocate device memory when they solve: code running inside a CUDA stream capture, hosts
- * whose device memory belongs to another allocator's pool, services that reserve all memory
- * at start-up.  They pass device inputs and outputs (same layout and meaning as
- * pnjl_solve_batch_device; opts->seed_table stays a host pointer, opts->point_seeds is a
- * device pointer, opts->verify_map must be NULL) and a stream; no context is used and the call makes no cudaMalloc,
- * cudaFree or other allocating call.  The scratch it needs (candidate records, completion
+ * code; it is an allocation-free twin of pnjl_solve_batch_device for the plain FP64 solve).
+ * For callers that may not allocate device memory when they solve: hosts whose device memory
+ * belongs to another allocator's pool that must account for every byte, and services that
+ * reserve all memory at start-up so that no later call can fail for lack of it.  They pass
+ * device inputs and outputs (same layout and meaning as pnjl_solve_batch_device;
+ * opts->seed_table stays a host pointer, opts->point_seeds is a device pointer) and a stream;
+ * no context is used and the call makes no cudaMalloc, cudaFree or other allocating call.
+ * Two options of pnjl_solve_batch_device are not available and return
+ * PNJL_ERR_INVALID_ARGUMENT: opts->verify_map must be NULL, and opts->precision must be
+ * PNJL_PREC_FP64 (the mixed-precision solver needs scratch this fixed array does not hold).  The scratch it needs (candidate records, completion
  * counters, queue head, node and seed tables) is one static device array of about 6 MB that
  * every GPU loading this library holds until exit; batches beyond PNJL_NOALLOC_MAX_TASKS
  * tasks return PNJL_ERR_TOO_LARGE.  The call is asynchronous on `stream` (NULL = the legacy

@@ -86,6 +86,15 @@ class pnjl_result_soa(C.Structure):
     ]
 
 
+KDATA_FIELDS = ("A_u", "A_d", "A_s", "G_u", "G_s", "K0_plus", "K0_minus", "K123_plus", "K123_minus",
+                "K4567_plus", "K4567_minus", "K8_plus", "K8_minus", "K08_plus", "K08_minus", "det_K_plus",
+                "det_K_minus")
+
+
+class pnjl_kdata_soa(C.Structure):
+    _fields_ = [(k, dp) for k in KDATA_FIELDS]
+
+
 class pnjl_stats(C.Structure):
     _fields_ = [
         ("points", C.c_int64), ("passes_fp64", C.c_int64), ("passes_fp32", C.c_int64),
@@ -154,6 +163,10 @@ SIGNATURES = {
     "pnjl_plan_launch": (C.c_int, [C.c_void_p]),
     "pnjl_plan_stats": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(pnjl_stats)]),
     "pnjl_plan_destroy": (C.c_int, [C.c_void_p]),
+    "pnjl_kdata_batch": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_double, dp, dp, dp, dp, dp,
+                                   C.POINTER(pnjl_kdata_soa)]),
+    "pnjl_kdata_batch_device": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_double, dp, dp, dp, dp, dp,
+                                          C.POINTER(pnjl_kdata_soa)]),
     "pnjl_solve_batch_noalloc": (C.c_int, [C.POINTER(pnjl_params), C.c_int32, C.c_int32, C.c_double, C.c_int64,
                                            dp, dp, dp, dp, dp, C.POINTER(pnjl_solve_opts),
                                            C.POINTER(pnjl_result_soa), C.c_void_p]),

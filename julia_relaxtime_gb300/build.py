@@ -23,7 +23,8 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE, "--expt-relaxed-constexpr"]
-SOURCES = ["pnjl_kernels.cu", "pnjl_mixed.cu", "pnjl_capi.cu", "pnjl_probe.cu", "pnjl_noalloc.cu", "pnjl_mlp.cu"]
+SOURCES = ["pnjl_kernels.cu", "pnjl_mixed.cu", "pnjl_capi.cu", "pnjl_probe.cu", "pnjl_noalloc.cu", "pnjl_mlp.cu",
+           "pnjl_kdata.cu"]
 
 
 def nvcc() -> str:

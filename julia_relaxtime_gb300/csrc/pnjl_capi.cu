@@ -42,6 +42,10 @@ struct pnjl_ctx {
     // pinned host mirror of the workspace for the host-array solves (one DMA each way)
     unsigned char *h_stage = nullptr;
     size_t stage_cap = 0;
+    // K data: Gauss-Legendre nodes and weights of the last (p_num, p_max) on the device
+    double *d_kd_nodes = nullptr;  // p[kMaxPNodes] | w[kMaxPNodes]
+    int kd_p_num = 0;
+    double kd_p_max = 0.0;
     // solver scratch: candidate records and per-point completion counters (MultiSeed mode)
     unsigned char *d_scratch = nullptr;
     size_t scratch_cap = 0;
@@ -63,8 +67,9 @@ struct pnjl_ctx {
         long long *step = nullptr;
         float *loss = nullptr;
         float *x = nullptr, *y = nullptr;
-        long long *perm = nullptr;
-        size_t cap = 0;
+        float *partial = nullptr;  // gradient slots [kMaxGradSlots][kParamCount], then slot losses
+        int *perm = nullptr;       // epoch permutations [epochs][n]
+        size_t cap = 0, perm_cap = 0;
         double *seeds = nullptr;  // per-point seeds of pnjl_solve_batch_learned*
         size_t seeds_cap = 0;
         pnjl::Scaling sc{};
@@ -208,6 +213,8 @@ pnjl::MlpDev mlp_dev(pnjl_ctx *ctx) {
     m.w2b = ctx->mlp.wb + H * IN;
     m.w3b = m.w2b + H * H;
     m.w4b = m.w3b + H * H;
+    m.partial = ctx->mlp.partial;
+    m.loss_part = ctx->mlp.partial + (size_t)pnjl::kMaxGradSlots * pnjl::kParamCount;
     return m;
 }
 
@@ -222,13 +229,23 @@ int mlp_ensure_data(pnjl_ctx *ctx, size_t n) {
     cudaStreamSynchronize(ctx->stream);
     cudaFree(ctx->mlp.x);
     cudaFree(ctx->mlp.y);
-    cudaFree(ctx->mlp.perm);
-    ctx->mlp.x = nullptr; ctx->mlp.y = nullptr; ctx->mlp.perm = nullptr; ctx->mlp.cap = 0;
+    ctx->mlp.x = nullptr; ctx->mlp.y = nullptr; ctx->mlp.cap = 0;
     if (cudaMalloc(&ctx->mlp.x, n * pnjl::mlp::IN * sizeof(float)) != cudaSuccess ||
-        cudaMalloc(&ctx->mlp.y, n * pnjl::mlp::OUT * sizeof(float)) != cudaSuccess ||
-        cudaMalloc(&ctx->mlp.perm, n * sizeof(long long)) != cudaSuccess)
+        cudaMalloc(&ctx->mlp.y, n * pnjl::mlp::OUT * sizeof(float)) != cudaSuccess)
         return fail(ctx, PNJL_ERR_OUT_OF_MEMORY, "MLP data allocation failed");
     ctx->mlp.cap = n;
+    return PNJL_OK;
+}
+
+int mlp_ensure_perm(pnjl_ctx *ctx, size_t count) {
+    if (count <= ctx->mlp.perm_cap) return PNJL_OK;
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(ctx->mlp.perm);
+    ctx->mlp.perm = nullptr;
+    ctx->mlp.perm_cap = 0;
+    if (cudaMalloc(&ctx->mlp.perm, count * sizeof(int)) != cudaSuccess)
+        return fail(ctx, PNJL_ERR_OUT_OF_MEMORY, "MLP permutation allocation failed");
+    ctx->mlp.perm_cap = count;
     return PNJL_OK;
 }
 
@@ -310,6 +327,7 @@ int pnjl_destroy(pnjl_ctx *ctx) {
     cudaFree(ctx->d_ws);
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     cudaFree(ctx->d_scratch);
+    cudaFree(ctx->d_kd_nodes);
     cudaFree(ctx->mlp.params);
     cudaFree(ctx->mlp.wb);
     cudaFree(ctx->mlp.step);
@@ -317,6 +335,7 @@ int pnjl_destroy(pnjl_ctx *ctx) {
     cudaFree(ctx->mlp.x);
     cudaFree(ctx->mlp.y);
     cudaFree(ctx->mlp.perm);
+    cudaFree(ctx->mlp.partial);
     cudaFree(ctx->mlp.seeds);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -490,6 +509,102 @@ int pnjl_eval_batch(pnjl_ctx *ctx, int64_t n, const double *x, const double *T, 
                     const double *mu_d, const double *mu_s, const double *xi, int32_t precision, double *omega,
                     double *grad, double *hess) {
     return eval_common(ctx, n, x, T, mu_u, mu_d, mu_s, xi, precision, omega, grad, hess, nullptr);
+}
+
+// ---- K data (build_K_data) ----------------------------------------------------------------
+static int kdata_nodes(pnjl_ctx *ctx, int32_t p_num, double p_max) {
+    if (ctx->d_kd_nodes && ctx->kd_p_num == p_num && ctx->kd_p_max == p_max) return PNJL_OK;
+    if (!ctx->d_kd_nodes)
+        PNJL_CUDA_TRY(ctx, cudaMalloc(&ctx->d_kd_nodes, 2 * (size_t)pnjl::kMaxPNodes * sizeof(double)));
+    std::vector<double> pw(2 * (size_t)p_num);
+    pnjl::gauss_legendre_into(p_num, 0.0, p_max, pw.data(), pw.data() + p_num);
+    // the stream may still read the previous table: the copy is ordered after it
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_kd_nodes, pw.data(), pw.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                       ctx->stream));
+    PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));  // pw is released on return
+    ctx->kd_p_num = p_num;
+    ctx->kd_p_max = p_max;
+    return PNJL_OK;
+}
+
+static int kdata_enqueue(pnjl_ctx *ctx, int64_t n, int32_t p_num, double p_max, const double *d_T,
+                         const double *d_mu_u, const double *d_mu_s, const double *d_masses, const double *d_x,
+                         const pnjl_kdata_soa &d_out) {
+    int rc = kdata_nodes(ctx, p_num, p_max);
+    if (rc) return rc;
+    pnjl::KDataArgs a{};
+    a.Lambda = ctx->params.Lambda;
+    a.G = ctx->params.G;
+    a.K = ctx->params.K;
+    a.p_num = p_num;
+    a.p = ctx->d_kd_nodes;
+    a.w = ctx->d_kd_nodes + p_num;
+    a.n = n;
+    a.T = d_T; a.mu_u = d_mu_u; a.mu_s = d_mu_s; a.masses = d_masses; a.x = d_x;
+    a.out = d_out;
+    cudaError_t e = pnjl::launch_kdata(a, ctx->sm_count, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "kdata_kernel launch");
+    ctx->stats.kernel_launches += 1;
+    return PNJL_OK;
+}
+
+static int kdata_check(pnjl_ctx *ctx, int64_t n, int32_t p_num, double p_max, const double *T, const double *mu_u,
+                       const double *mu_s, const double *masses, const double *x, const pnjl_kdata_soa *out) {
+    if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
+    if (!out) return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "null output struct");
+    if (p_num < 1 || p_num > pnjl::kMaxPNodes || !(p_max > 0.0) || !std::isfinite(p_max))
+        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "p_num must be 1..512 and p_max finite and positive");
+    if (n < 0 || (n > 0 && (!T || !mu_u || !mu_s || !masses || !x)))
+        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "null input array");
+    return PNJL_OK;
+}
+
+int pnjl_kdata_batch_device(pnjl_ctx *ctx, int64_t n, int32_t p_num, double p_max, const double *d_T,
+                            const double *d_mu_u, const double *d_mu_s, const double *d_masses, const double *d_x,
+                            pnjl_kdata_soa *d_out) {
+    int rc = kdata_check(ctx, n, p_num, p_max, d_T, d_mu_u, d_mu_s, d_masses, d_x, d_out);
+    if (rc || n == 0) return rc;
+    cudaSetDevice(ctx->device);
+    return kdata_enqueue(ctx, n, p_num, p_max, d_T, d_mu_u, d_mu_s, d_masses, d_x, *d_out);
+}
+
+int pnjl_kdata_batch(pnjl_ctx *ctx, int64_t n, int32_t p_num, double p_max, const double *T, const double *mu_u,
+                     const double *mu_s, const double *masses, const double *x, pnjl_kdata_soa *out) {
+    int rc = kdata_check(ctx, n, p_num, p_max, T, mu_u, mu_s, masses, x, out);
+    if (rc || n == 0) return rc;
+    cudaSetDevice(ctx->device);
+    const size_t nn = (size_t)n;
+    constexpr int kFields = 17;
+    double *const *hout[kFields] = {&out->A_u, &out->A_d, &out->A_s, &out->G_u, &out->G_s, &out->K0_plus,
+                                    &out->K0_minus, &out->K123_plus, &out->K123_minus, &out->K4567_plus,
+                                    &out->K4567_minus, &out->K8_plus, &out->K8_minus, &out->K08_plus,
+                                    &out->K08_minus, &out->det_K_plus, &out->det_K_minus};
+    rc = ensure_ws(ctx, (3 + kFields) * carve_size(nn, 8) + carve_size(3 * nn, 8) + carve_size(5 * nn, 8));
+    if (rc) return rc;
+    unsigned char *p = ctx->d_ws;
+    double *dT = carve<double>(p, nn), *du = carve<double>(p, nn), *ds = carve<double>(p, nn),
+           *dm = carve<double>(p, 3 * nn), *dx = carve<double>(p, 5 * nn);
+    pnjl_kdata_soa dout{};
+    double **dptr[kFields] = {&dout.A_u, &dout.A_d, &dout.A_s, &dout.G_u, &dout.G_s, &dout.K0_plus, &dout.K0_minus,
+                              &dout.K123_plus, &dout.K123_minus, &dout.K4567_plus, &dout.K4567_minus,
+                              &dout.K8_plus, &dout.K8_minus, &dout.K08_plus, &dout.K08_minus, &dout.det_K_plus,
+                              &dout.det_K_minus};
+    for (int k = 0; k < kFields; ++k) {
+        double *d = carve<double>(p, nn);
+        *dptr[k] = *hout[k] ? d : nullptr;
+    }
+    cudaStream_t s = ctx->stream;
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dT, T, nn * 8, cudaMemcpyHostToDevice, s));
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(du, mu_u, nn * 8, cudaMemcpyHostToDevice, s));
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(ds, mu_s, nn * 8, cudaMemcpyHostToDevice, s));
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dm, masses, 3 * nn * 8, cudaMemcpyHostToDevice, s));
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dx, x, 5 * nn * 8, cudaMemcpyHostToDevice, s));
+    rc = kdata_enqueue(ctx, n, p_num, p_max, dT, du, ds, dm, dx, dout);
+    if (rc) return rc;
+    for (int k = 0; k < kFields; ++k)
+        if (*hout[k]) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(*hout[k], *dptr[k], nn * 8, cudaMemcpyDeviceToHost, s));
+    PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    return PNJL_OK;
 }
 
 int pnjl_thermo_batch(pnjl_ctx *ctx, int64_t n, const double *x, const double *T, const double *mu_u,
@@ -778,6 +893,7 @@ int pnjl_mlp_init(pnjl_ctx *ctx, uint64_t seed) {
         PNJL_CUDA_TRY(ctx, cudaMalloc(&M.wb, (size_t)pnjl::kParamCount * sizeof(__nv_bfloat16)));
         PNJL_CUDA_TRY(ctx, cudaMalloc(&M.step, sizeof(long long)));
         PNJL_CUDA_TRY(ctx, cudaMalloc(&M.loss, sizeof(float)));
+        PNJL_CUDA_TRY(ctx, cudaMalloc(&M.partial, (size_t)pnjl::kMaxGradSlots * (pnjl::kParamCount + 1) * sizeof(float)));
         PNJL_CUDA_TRY(ctx, pnjl::mlp_setup_attributes());
     }
     // Kaiming-uniform weights (bound sqrt(6 / fan_in)), zero biases
@@ -860,7 +976,7 @@ int pnjl_mlp_loss_grad(pnjl_ctx *ctx, int64_t n, const double *T, const double *
                                            cudaMemcpyDeviceToHost, ctx->stream));
     PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     if (loss) *loss = l;
-    ctx->stats.kernel_launches += 2;
+    ctx->stats.kernel_launches += 3;
     return PNJL_OK;
 }
 
@@ -870,10 +986,13 @@ int pnjl_mlp_train(pnjl_ctx *ctx, int64_t n, const double *T, const double *mu, 
     if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
     int rc = mlp_require(ctx, true);
     if (rc) return rc;
-    if (n <= 0 || epochs < 1 || batch < 32 || batch % 32 || !(lr > 0) || !T || !mu || !xi || !targets)
+    if (n <= 0 || n > INT32_MAX || epochs < 1 || batch < 32 || batch % 32 || !(lr > 0) || !T || !mu || !xi ||
+        !targets)
         return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "bad training arguments (batch: multiple of 32)");
     cudaSetDevice(ctx->device);
     rc = mlp_upload(ctx, n, T, mu, xi, targets);
+    if (rc) return rc;
+    rc = mlp_ensure_perm(ctx, (size_t)n * (size_t)epochs);
     if (rc) return rc;
     cudaStream_t s = ctx->stream;
     const long long spe = (n + batch - 1) / batch;
@@ -882,37 +1001,40 @@ int pnjl_mlp_train(pnjl_ctx *ctx, int64_t n, const double *T, const double *mu, 
     PNJL_CUDA_TRY(ctx, cudaMemsetAsync(ctx->mlp.params + 2 * pnjl::kParamCount, 0,
                                        2 * (size_t)pnjl::kParamCount * sizeof(float), s));
     PNJL_CUDA_TRY(ctx, cudaMemsetAsync(ctx->mlp.step, 0, sizeof(long long), s));
-    // one training step as a CUDA graph, replayed steps_per_epoch x epochs times
+    // every epoch's shuffle (Fisher-Yates on a splitmix64 stream), uploaded once
+    std::vector<int> perm((size_t)n * (size_t)epochs);
+    uint64_t rs = shuffle_seed;
+    for (int ep = 0; ep < epochs; ++ep) {
+        int *p = perm.data() + (size_t)ep * (size_t)n;
+        for (long long i = 0; i < n; ++i) p[i] = (int)i;
+        for (long long i = n - 1; i > 0; --i) {
+            const long long j = (long long)(splitmix64(rs) % (uint64_t)(i + 1));
+            std::swap(p[i], p[j]);
+        }
+    }
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->mlp.perm, perm.data(), perm.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    // one epoch of training steps as a CUDA graph, replayed once per epoch
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(s));
     PNJL_CUDA_TRY(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    cudaError_t ce = pnjl::mlp_launch_step(mlp_dev(ctx), b, c, true, s);
+    cudaError_t ce = cudaSuccess;
+    for (long long k = 0; k < spe && ce == cudaSuccess; ++k) ce = pnjl::mlp_launch_step(mlp_dev(ctx), b, c, true, s);
     cudaError_t ee = cudaStreamEndCapture(s, &graph);
     if (ce != cudaSuccess || ee != cudaSuccess) {
         if (graph) cudaGraphDestroy(graph);
-        return cuda_fail(ctx, ce != cudaSuccess ? ce : ee, "MLP step capture");
+        return cuda_fail(ctx, ce != cudaSuccess ? ce : ee, "MLP epoch capture");
     }
     ce = cudaGraphInstantiate(&exec, graph, 0);
     cudaGraphDestroy(graph);
     if (ce != cudaSuccess) return cuda_fail(ctx, ce, "MLP graph instantiate");
-    std::vector<long long> perm(n);
-    uint64_t rs = shuffle_seed;
     float l = 0.f;
-    for (int ep = 0; ep < epochs && ce == cudaSuccess; ++ep) {
-        for (long long i = 0; i < n; ++i) perm[i] = i;
-        for (long long i = n - 1; i > 0; --i) {  // Fisher-Yates
-            const long long j = (long long)(splitmix64(rs) % (uint64_t)(i + 1));
-            std::swap(perm[i], perm[j]);
-        }
-        ce = cudaMemcpyAsync(ctx->mlp.perm, perm.data(), n * sizeof(long long), cudaMemcpyHostToDevice, s);
-        for (long long k = 0; k < spe && ce == cudaSuccess; ++k) ce = cudaGraphLaunch(exec, s);
-        if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);  // perm is host memory reused next epoch
-    }
+    for (int ep = 0; ep < epochs && ce == cudaSuccess; ++ep) ce = cudaGraphLaunch(exec, s);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
     if (ce == cudaSuccess) ce = cudaMemcpy(&l, ctx->mlp.loss, sizeof(float), cudaMemcpyDeviceToHost);
     cudaGraphExecDestroy(exec);
     if (ce != cudaSuccess) return cuda_fail(ctx, ce, "MLP training");
-    ctx->stats.kernel_launches += 4 * spe * (long long)epochs;
+    ctx->stats.kernel_launches += 3 * spe * (long long)epochs;
     if (last_loss) *last_loss = l;
     ctx->mlp.trained = true;
     return PNJL_OK;

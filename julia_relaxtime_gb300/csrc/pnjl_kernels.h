@@ -116,6 +116,17 @@ struct EvalArgs {
     pnjl_result_soa out;
 };
 
+// build_K_data per point (pnjl_kdata.cu): one thread per point, node table in shared memory
+struct KDataArgs {
+    double Lambda, G, K;
+    int p_num;
+    const double *p, *w;  // device Gauss-Legendre nodes and weights on [0, p_max]
+    int64_t n;
+    const double *T, *mu_u, *mu_s, *masses, *x;
+    pnjl_kdata_soa out;
+};
+cudaError_t launch_kdata(const KDataArgs &a, int sm_count, cudaStream_t s);
+
 size_t node_smem_bytes(int p_num, int t_num);
 cudaError_t launch_solve(const SolveArgs &a, int group, int grid, size_t smem, cudaStream_t s);
 // Mixed precision: per-point mode launches the fused kernel (points and the tasks they defer

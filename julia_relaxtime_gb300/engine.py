@@ -266,6 +266,35 @@ class GapEngine:
         self._check(rc, "pnjl_solve_batch_learned_device" if learned else "pnjl_solve_batch_device")
         self._keep = (st, sth)  # seed tables are read by the async host->device copy
 
+    # -- K data of the relaxation-time chain ------------------------------------------------
+    def kdata(self, T, mu_u, mu_s, masses, x, *, p_num: int = 64, p_max: float = 10.0) -> dict:
+        """build_K_data (run_gap_transport_scan.jl:297-305) at n solved points, host arrays:
+        one-loop A per flavour on p_num Gauss-Legendre nodes of [0, p_max] (the script's 64 on
+        [0, 10]), G^f and the effective couplings.  masses [n,3] and x [n,5] as a solve returns
+        them.  Returns {field: [n]} over _capi.KDATA_FIELDS."""
+        T = _f64(np.atleast_1d(T))
+        n = T.size
+        mu_u = _f64(np.broadcast_to(np.asarray(mu_u, dtype=np.float64), (n,)))
+        mu_s = _f64(np.broadcast_to(np.asarray(mu_s, dtype=np.float64), (n,)))
+        masses = _f64(masses, shape=(n, 3))
+        x = _f64(x, shape=(n, 5))
+        out = {k: np.zeros(n) for k in api.KDATA_FIELDS}
+        soa = api.pnjl_kdata_soa(**{k: _dp(v) for k, v in out.items()})
+        rc = self._lib.pnjl_kdata_batch(self._ctx, n, int(p_num), float(p_max), _dp(T), _dp(mu_u), _dp(mu_s),
+                                        _dp(masses), _dp(x), C.byref(soa))
+        self._check(rc, "pnjl_kdata_batch")
+        return out
+
+    def kdata_device(self, n: int, d_T: int, d_mu_u: int, d_mu_s: int, d_masses: int, d_x: int, d_out: dict, *,
+                     p_num: int = 64, p_max: float = 10.0):
+        """Asynchronous build_K_data on device pointers (integers), e.g. a solve's outputs;
+        d_out maps KDATA_FIELDS names to device pointers (missing ones are skipped)."""
+        soa = api.pnjl_kdata_soa(**{k: C.cast(C.c_void_p(v), api.dp) for k, v in d_out.items()})
+        cast = lambda p: C.cast(C.c_void_p(p), api.dp)  # noqa: E731
+        rc = self._lib.pnjl_kdata_batch_device(self._ctx, n, int(p_num), float(p_max), cast(d_T), cast(d_mu_u),
+                                               cast(d_mu_s), cast(d_masses), cast(d_x), C.byref(soa))
+        self._check(rc, "pnjl_kdata_batch_device")
+
     # -- misc ------------------------------------------------------------------------------
     def stream(self) -> int:
         return int(self._lib.pnjl_stream(self._ctx) or 0)

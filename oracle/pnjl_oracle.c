@@ -26,6 +26,9 @@
  *                          autoscaling; both restated from the published methods)
  *   solve / solve_multi .. src/pnjl/solver/ImplicitSolver.jl:211-328,532-559
  *   seeds ................ src/pnjl/solver/SeedStrategies.jl:56-95,204-284
+ *   K data (one-loop A,    src/relaxtime/OneLoopIntegrals.jl:507-543,
+ *   effective couplings)   src/relaxtime/EffectiveCouplings.jl:56-60,112-115,242-279,
+ *                          scripts/relaxtime/run_gap_transport_scan.jl:297-305
  *
  * Derivatives are taken the way the reference takes them: the reference differentiates
  * Omega with nested ForwardDiff duals (gradient for F, Jacobian of that for J).  Here a
@@ -980,3 +983,64 @@ int or_max_threads(void) {
 int or_sizeof_result(void) { return (int)sizeof(or_result); }
 int or_sizeof_opts(void) { return (int)sizeof(or_opts); }
 int or_sizeof_params(void) { return (int)sizeof(or_params); }
+
+/* ------------------------------------------------------------------------- */
+/* K data of the relaxation-time chain: build_K_data                          */
+/* (scripts/relaxtime/run_gap_transport_scan.jl:297-305)                      */
+/* ------------------------------------------------------------------------- */
+/* const_integral_term_A (OneLoopIntegrals.jl:507-517): int_0^Lambda p^2/E dp in closed form */
+double or_const_integral_term_A(const or_params *P, double m) {
+    const double L = P->Lambda;
+    const double mp = m > 0.0 ? m : 0.0;
+    if (mp < 1e-14) return L * L / 2.0;
+    const double r = sqrt(L * L + mp * mp);
+    return (L * r - mp * mp * log((L + r) / mp)) / 2.0;
+}
+
+/* A (OneLoopIntegrals.jl:531-543): 4 [ -const_integral_term_A(m)
+ *   + sum_i w_i p_i^2 / E_i (f+(E_i) + f-(E_i)) ],  E = sqrt(p^2 + m^2), with the PNJL
+ * distributions of QuarkDistribution.jl:14-51 (distribution_value, :14-61 of the same file) */
+double or_one_loop_A(const or_params *P, int n_nodes, const double *p, const double *w, double m, double mu,
+                     double T, double Phi, double Phib) {
+    double integral = -or_const_integral_term_A(P, m);
+    for (int i = 0; i < n_nodes; ++i) {
+        const double E = sqrt(p[i] * p[i] + m * m);
+        integral += w[i] * p[i] * p[i] / E * (quark_dist(E, mu, T, Phi, Phib) + antiquark_dist(E, mu, T, Phi, Phib));
+    }
+    return 4.0 * integral;
+}
+
+/* calculate_effective_couplings (EffectiveCouplings.jl:242-279) with
+ * coupling_matrix_determinant (:112-115): out[12] = K0+, K0-, K123+, K123-, K4567+, K4567-,
+ * K8+, K8-, K08+, K08-, det K+, det K- */
+void or_effective_couplings(double G, double K, double Gu, double Gs, double *out) {
+    const double t0 = (1.0 / 3.0) * K * (2.0 * Gu + Gs);
+    const double t123 = 0.5 * K * Gs;
+    const double t4567 = 0.5 * K * Gu;
+    const double t8 = (1.0 / 6.0) * K * (4.0 * Gu - Gs);
+    const double t08 = (1.0 / 6.0) * sqrt(2.0) * K * (Gu - Gs);
+    const double K0p = G - t0, K0m = G + t0, K8p = G + t8, K8m = G - t8, K08p = t08, K08m = -t08;
+    out[0] = K0p; out[1] = K0m;
+    out[2] = G + t123; out[3] = G - t123;
+    out[4] = G + t4567; out[5] = G - t4567;
+    out[6] = K8p; out[7] = K8m;
+    out[8] = K08p; out[9] = K08m;
+    out[10] = K0p * K8p - K08p * K08p;
+    out[11] = K0m * K8m - K08m * K08m;
+}
+
+/* build_K_data for one point: out[17] = A_u, A_d, A_s, G_u, G_s, then the 12 couplings of
+ * or_effective_couplings.  A_d = A_u as build_K_data sets it; G^f = -N_c/(4 pi^2) m_f A_f
+ * (calculate_G_from_A, EffectiveCouplings.jl:56-60, N_c = 3).  mu_u / mu_s: the reference
+ * passes one quark chemical potential for both. */
+void or_kdata(const or_params *P, int n_nodes, const double *p, const double *w, double T, double mu_u, double mu_s,
+              double m_u, double m_s, double Phi, double Phib, double *out) {
+    const double pi = 3.14159265358979323846;
+    const double Au = or_one_loop_A(P, n_nodes, p, w, m_u, mu_u, T, Phi, Phib);
+    const double As = or_one_loop_A(P, n_nodes, p, w, m_s, mu_s, T, Phi, Phib);
+    const double Nc = 3.0;
+    out[0] = Au; out[1] = Au; out[2] = As;
+    out[3] = -Nc / (4.0 * pi * pi) * (m_u * Au);
+    out[4] = -Nc / (4.0 * pi * pi) * (m_s * As);
+    or_effective_couplings(P->G, P->K, out[3], out[4], out + 5);
+}

@@ -291,6 +291,15 @@ def test_golden_scan_through_gpu(engine_factory):
         rows = scan_rows(opts, gpu_point_solver(12, 6, engine=eng))
         mism = check_scan_rows(rows, gk, exact_iterations=exact)
         assert mism <= 10
+        # every row carries build_K_data of its solution (run_gap_transport_scan.jl:436-438)
+        T = np.array([r["T_fm"] for r in rows])
+        mq = np.array([r["muq_fm"] for r in rows])
+        masses = np.array([[r["m_u"], r["m_d"], r["m_s"]] for r in rows])
+        x = np.array([[0.0, 0.0, 0.0, r["Phi"], r["Phibar"]] for r in rows])
+        ref = orc.kdata(orc.default_params(), T, mq, mq, masses, x)
+        for k, v in ref.items():
+            got = np.array([r["kdata"][k] for r in rows])
+            assert np.all(np.abs(got - v) <= 1e-13 * np.abs(v).max()), k
 
 
 def test_edge_cases(engine_factory, P):
