@@ -383,6 +383,33 @@ int pnjl_kdata_batch_device(pnjl_ctx *ctx, int64_t n, int32_t p_num, double p_ma
                             const double *d_mu_u, const double *d_mu_s, const double *d_masses,
                             const double *d_x, pnjl_kdata_soa *d_out);
 
+/* ---- implicit derivatives of solved states ---------------------------------------------------
+ * src/pnjl/derivatives/ThermoDerivatives.jl: mass_derivatives (order 1, :132-173),
+ * thermo_derivatives (:184-249) and bulk_viscosity_coefficients (:342-465) at n solved states
+ * x [5n] (the solution of a pnjl_solve_batch* call at the same T, mu, xi and the context's
+ * nodes).  theta = (T, mu) with every mu_f moved together (the reference's mu_u = mu_d = mu_s
+ * = mu); dx/dtheta = -(Hessian_x Omega)^-1 d(grad_x Omega)/dtheta (the implicit function
+ * theorem the reference applies with ImplicitDifferentiation.jl), then the chain rule.
+ * Analytic second derivatives, FP64.  Any NULL output pointer skips that field.  With unequal
+ * mu_f, eps's mu term uses their mean (the reference never calls these with unequal mu_f). */
+typedef struct pnjl_deriv_soa {
+    double *dx_dT, *dx_dmu;           /* [5n] dx/dT, dx/dmu                                    */
+    double *dM_dT, *dM_dmu;           /* [3n] dM_f/dT, dM_f/dmu_q (dM/dmu_B = dM/dmu_q / 3)    */
+    double *s, *n_B;                  /* [n]  entropy -dOmega/dT, baryon density sum(rho_f)/3  */
+    double *ds_dT, *ds_dmu, *dn_dT, *dn_dmu;          /* [n] total derivatives through x(theta) */
+    double *pressure, *dP_dT, *dP_dmu;                /* [n]                                    */
+    double *energy, *deps_dT, *deps_dmu;              /* [n] eps = -P + sum mu_f rho_f + T s    */
+    double *dP_deps_n, *dP_dn_eps;    /* [n] thermo_derivatives' dP/deps|n and dP/dn|eps      */
+    double *v_n_sq, *dmuB_dT_sigma;   /* [n] bulk_viscosity_coefficients' v_n^2, dmu_B/dT|s/n  */
+} pnjl_deriv_soa;
+/* Host arrays, synchronous. */
+int pnjl_derivs_batch(pnjl_ctx *ctx, int64_t n, const double *x, const double *T, const double *mu_u,
+                      const double *mu_d, const double *mu_s, const double *xi, pnjl_deriv_soa *out);
+/* Device arrays, asynchronous on pnjl_stream(ctx). */
+int pnjl_derivs_batch_device(pnjl_ctx *ctx, int64_t n, const double *d_x, const double *d_T,
+                             const double *d_mu_u, const double *d_mu_d, const double *d_mu_s,
+                             const double *d_xi, pnjl_deriv_soa *d_out);
+
 /* Largest batch of pnjl_solve_batch_noalloc, counted in tasks: n * n_seeds in
  * PNJL_SEEDS_TABLE mode, n in PNJL_SEEDS_PER_POINT mode (and n itself at most this). */
 #define PNJL_NOALLOC_MAX_TASKS 32768

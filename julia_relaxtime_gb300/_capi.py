@@ -95,6 +95,17 @@ class pnjl_kdata_soa(C.Structure):
     _fields_ = [(k, dp) for k in KDATA_FIELDS]
 
 
+# fields of pnjl_deriv_soa with their widths per point
+DERIV_FIELDS = (("dx_dT", 5), ("dx_dmu", 5), ("dM_dT", 3), ("dM_dmu", 3), ("s", 1), ("n_B", 1), ("ds_dT", 1),
+                ("ds_dmu", 1), ("dn_dT", 1), ("dn_dmu", 1), ("pressure", 1), ("dP_dT", 1), ("dP_dmu", 1),
+                ("energy", 1), ("deps_dT", 1), ("deps_dmu", 1), ("dP_deps_n", 1), ("dP_dn_eps", 1),
+                ("v_n_sq", 1), ("dmuB_dT_sigma", 1))
+
+
+class pnjl_deriv_soa(C.Structure):
+    _fields_ = [(k, dp) for k, _ in DERIV_FIELDS]
+
+
 class pnjl_stats(C.Structure):
     _fields_ = [
         ("points", C.c_int64), ("passes_fp64", C.c_int64), ("passes_fp32", C.c_int64),
@@ -167,6 +178,9 @@ SIGNATURES = {
                                    C.POINTER(pnjl_kdata_soa)]),
     "pnjl_kdata_batch_device": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_double, dp, dp, dp, dp, dp,
                                           C.POINTER(pnjl_kdata_soa)]),
+    "pnjl_derivs_batch": (C.c_int, [C.c_void_p, C.c_int64, dp, dp, dp, dp, dp, dp, C.POINTER(pnjl_deriv_soa)]),
+    "pnjl_derivs_batch_device": (C.c_int, [C.c_void_p, C.c_int64, dp, dp, dp, dp, dp, dp,
+                                           C.POINTER(pnjl_deriv_soa)]),
     "pnjl_solve_batch_noalloc": (C.c_int, [C.POINTER(pnjl_params), C.c_int32, C.c_int32, C.c_double, C.c_int64,
                                            dp, dp, dp, dp, dp, C.POINTER(pnjl_solve_opts),
                                            C.POINTER(pnjl_result_soa), C.c_void_p]),

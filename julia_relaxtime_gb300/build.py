@@ -24,7 +24,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE, "--expt-relaxed-constexpr"]
 SOURCES = ["pnjl_kernels.cu", "pnjl_mixed.cu", "pnjl_capi.cu", "pnjl_probe.cu", "pnjl_noalloc.cu", "pnjl_mlp.cu",
-           "pnjl_kdata.cu"]
+           "pnjl_kdata.cu", "pnjl_deriv.cu"]
 
 
 def nvcc() -> str:

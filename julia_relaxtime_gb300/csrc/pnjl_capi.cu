@@ -607,6 +607,90 @@ int pnjl_kdata_batch(pnjl_ctx *ctx, int64_t n, int32_t p_num, double p_max, cons
     return PNJL_OK;
 }
 
+// ---- implicit derivatives (ThermoDerivatives.jl) -------------------------------------------
+static double **deriv_field(pnjl_deriv_soa &o, int k, int &width) {
+    double **f[20] = {&o.dx_dT, &o.dx_dmu, &o.dM_dT, &o.dM_dmu, &o.s, &o.n_B, &o.ds_dT, &o.ds_dmu, &o.dn_dT,
+                      &o.dn_dmu, &o.pressure, &o.dP_dT, &o.dP_dmu, &o.energy, &o.deps_dT, &o.deps_dmu,
+                      &o.dP_deps_n, &o.dP_dn_eps, &o.v_n_sq, &o.dmuB_dT_sigma};
+    width = k < 2 ? 5 : (k < 4 ? 3 : 1);
+    return f[k];
+}
+
+static int derivs_enqueue(pnjl_ctx *ctx, int64_t n, const double *d_x, const double *d_T, const double *d_mu_u,
+                          const double *d_mu_d, const double *d_mu_s, const double *d_xi, const pnjl_deriv_soa &o) {
+    pnjl::DerivArgs a{};
+    a.P = ctx->dp;
+    a.nodes = kernel_nodes(ctx);
+    a.n = n;
+    a.x = d_x; a.T = d_T; a.mu_u = d_mu_u; a.mu_d = d_mu_d; a.mu_s = d_mu_s; a.xi = d_xi;
+    a.out = o;
+    const size_t smem = pnjl::node_smem_bytes(ctx->p_num, ctx->t_num);
+    const int64_t blocks = (n + 7) / 8;
+    const int grid = (int)std::min<int64_t>(blocks, (int64_t)ctx->sm_count * 8);
+    cudaError_t e = pnjl::launch_deriv(a, grid, smem, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "deriv_kernel launch");
+    ctx->stats.kernel_launches += 1;
+    return PNJL_OK;
+}
+
+static int derivs_check(pnjl_ctx *ctx, int64_t n, const double *x, const double *T, const double *mu_u,
+                        const double *mu_d, const double *mu_s, const double *xi, const pnjl_deriv_soa *out) {
+    if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
+    if (ctx->p_num == 0) return fail(ctx, PNJL_ERR_NO_NODES, "call pnjl_set_nodes first");
+    if (!out) return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "null output struct");
+    if (n < 0 || (n > 0 && (!x || !T || !mu_u || !mu_d || !mu_s || !xi)))
+        return fail(ctx, PNJL_ERR_INVALID_ARGUMENT, "null input array");
+    return PNJL_OK;
+}
+
+int pnjl_derivs_batch_device(pnjl_ctx *ctx, int64_t n, const double *d_x, const double *d_T, const double *d_mu_u,
+                             const double *d_mu_d, const double *d_mu_s, const double *d_xi, pnjl_deriv_soa *d_out) {
+    int rc = derivs_check(ctx, n, d_x, d_T, d_mu_u, d_mu_d, d_mu_s, d_xi, d_out);
+    if (rc || n == 0) return rc;
+    cudaSetDevice(ctx->device);
+    return derivs_enqueue(ctx, n, d_x, d_T, d_mu_u, d_mu_d, d_mu_s, d_xi, *d_out);
+}
+
+int pnjl_derivs_batch(pnjl_ctx *ctx, int64_t n, const double *x, const double *T, const double *mu_u,
+                      const double *mu_d, const double *mu_s, const double *xi, pnjl_deriv_soa *out) {
+    int rc = derivs_check(ctx, n, x, T, mu_u, mu_d, mu_s, xi, out);
+    if (rc || n == 0) return rc;
+    cudaSetDevice(ctx->device);
+    const size_t nn = (size_t)n;
+    rc = ensure_ws(ctx, carve_size(5 * nn, 8) + 5 * carve_size(nn, 8) + 4 * carve_size(5 * nn, 8) +
+                            18 * carve_size(nn, 8));
+    if (rc) return rc;
+    unsigned char *p = ctx->d_ws;
+    double *dx = carve<double>(p, 5 * nn), *dT = carve<double>(p, nn), *du = carve<double>(p, nn),
+           *dd = carve<double>(p, nn), *ds = carve<double>(p, nn), *dxi = carve<double>(p, nn);
+    pnjl_deriv_soa dout{};
+    pnjl_deriv_soa hout = *out;
+    for (int k = 0; k < 20; ++k) {
+        int w = 1;
+        double **h = deriv_field(hout, k, w);
+        double **d = deriv_field(dout, k, w);
+        double *buf = carve<double>(p, (size_t)w * nn);
+        *d = *h ? buf : nullptr;
+    }
+    cudaStream_t s = ctx->stream;
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dx, x, 5 * nn * 8, cudaMemcpyHostToDevice, s));
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dT, T, nn * 8, cudaMemcpyHostToDevice, s));
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(du, mu_u, nn * 8, cudaMemcpyHostToDevice, s));
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dd, mu_d, nn * 8, cudaMemcpyHostToDevice, s));
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(ds, mu_s, nn * 8, cudaMemcpyHostToDevice, s));
+    PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(dxi, xi, nn * 8, cudaMemcpyHostToDevice, s));
+    rc = derivs_enqueue(ctx, n, dx, dT, du, dd, ds, dxi, dout);
+    if (rc) return rc;
+    for (int k = 0; k < 20; ++k) {
+        int w = 1;
+        double **h = deriv_field(hout, k, w);
+        double **d = deriv_field(dout, k, w);
+        if (*h) PNJL_CUDA_TRY(ctx, cudaMemcpyAsync(*h, *d, (size_t)w * nn * 8, cudaMemcpyDeviceToHost, s));
+    }
+    PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    return PNJL_OK;
+}
+
 int pnjl_thermo_batch(pnjl_ctx *ctx, int64_t n, const double *x, const double *T, const double *mu_u,
                       const double *mu_d, const double *mu_s, const double *xi, pnjl_result_soa *out) {
     return eval_common(ctx, n, x, T, mu_u, mu_d, mu_s, xi, PNJL_PREC_FP64, nullptr, nullptr, nullptr, out);

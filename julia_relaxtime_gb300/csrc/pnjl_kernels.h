@@ -127,6 +127,16 @@ struct KDataArgs {
 };
 cudaError_t launch_kdata(const KDataArgs &a, int sm_count, cudaStream_t s);
 
+// implicit derivatives of solved states (pnjl_deriv.cu): one warp per point
+struct DerivArgs {
+    DevParams P;
+    KernelNodes nodes;
+    int64_t n;
+    const double *x, *T, *mu_u, *mu_d, *mu_s, *xi;
+    pnjl_deriv_soa out;
+};
+cudaError_t launch_deriv(const DerivArgs &a, int grid, size_t smem, cudaStream_t s);
+
 size_t node_smem_bytes(int p_num, int t_num);
 cudaError_t launch_solve(const SolveArgs &a, int group, int grid, size_t smem, cudaStream_t s);
 // Mixed precision: per-point mode launches the fused kernel (points and the tasks they defer

@@ -285,6 +285,31 @@ class GapEngine:
         self._check(rc, "pnjl_kdata_batch")
         return out
 
+    # -- implicit derivatives of solved states ----------------------------------------------
+    def derivs(self, x, T, mu, xi) -> dict:
+        """Implicit derivatives (ThermoDerivatives.jl) at solved states x [n,5], host arrays:
+        dx/dtheta, dM/dtheta, s, n_B and their total derivatives, P and eps with theirs, and
+        the bulk-viscosity combinations; theta = (T, mu) with every mu_f moved together.
+        Returns {field: [n] or [n, width]} over _capi.DERIV_FIELDS."""
+        n, T, mu_u, mu_d, mu_s, xi = self._point_arrays(T, mu, xi)
+        x = _f64(x, shape=(n, 5))
+        out = {k: np.zeros((n, w)) if w > 1 else np.zeros(n) for k, w in api.DERIV_FIELDS}
+        soa = api.pnjl_deriv_soa(**{k: _dp(v) for k, v in out.items()})
+        rc = self._lib.pnjl_derivs_batch(self._ctx, n, _dp(x), _dp(T), _dp(mu_u), _dp(mu_d), _dp(mu_s), _dp(xi),
+                                         C.byref(soa))
+        self._check(rc, "pnjl_derivs_batch")
+        return out
+
+    def derivs_device(self, n: int, d_x: int, d_T: int, d_mu_u: int, d_mu_d: int, d_mu_s: int, d_xi: int,
+                      d_out: dict):
+        """Asynchronous implicit derivatives on device pointers (integers); d_out maps
+        DERIV_FIELDS names to device pointers (missing ones are skipped)."""
+        soa = api.pnjl_deriv_soa(**{k: C.cast(C.c_void_p(v), api.dp) for k, v in d_out.items()})
+        cast = lambda p: C.cast(C.c_void_p(p), api.dp)  # noqa: E731
+        rc = self._lib.pnjl_derivs_batch_device(self._ctx, n, cast(d_x), cast(d_T), cast(d_mu_u), cast(d_mu_d),
+                                                cast(d_mu_s), cast(d_xi), C.byref(soa))
+        self._check(rc, "pnjl_derivs_batch_device")
+
     def kdata_device(self, n: int, d_T: int, d_mu_u: int, d_mu_s: int, d_masses: int, d_x: int, d_out: dict, *,
                      p_num: int = 64, p_max: float = 10.0):
         """Asynchronous build_K_data on device pointers (integers), e.g. a solve's outputs;

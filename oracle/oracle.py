@@ -108,6 +108,8 @@ def lib():
         L.or_one_loop_A.restype = C.c_double
         L.or_kdata.argtypes = [C.POINTER(Params), C.c_int, dp, dp] + [C.c_double] * 7 + [dp]
         L.or_effective_couplings.argtypes = [C.c_double] * 4 + [dp]
+        L.or_thermo_derivs.argtypes = [C.POINTER(Params), C.c_int, dp, dp, dp, dp, dp, C.c_double, C.c_double, dp]
+        L.or_thermo_derivs.restype = C.c_int
         assert L.or_sizeof_result() == C.sizeof(Result), "Result layout mismatch"
         assert L.or_sizeof_opts() == C.sizeof(Opts), "Opts layout mismatch"
         assert L.or_sizeof_params() == C.sizeof(Params), "Params layout mismatch"
@@ -302,6 +304,26 @@ def kdata(params: Params, T, mu_u, mu_s, masses, x, *, p_num: int = 64, p_max: f
                        x[i, 3], x[i, 4], _dp(row))
         out[i] = row
     return {k: out[:, j].copy() for j, k in enumerate(KDATA_FIELDS)}
+
+
+DERIV_FIELDS = ("dx_dT", "dx_dmu", "dM_dT", "dM_dmu", "s", "n_B", "ds_dT", "ds_dmu", "dn_dT", "dn_dmu", "pressure",
+                "dP_dT", "dP_dmu", "energy", "deps_dT", "deps_dmu", "dP_deps_n", "dP_dn_eps", "v_n_sq",
+                "dmuB_dT_sigma")
+
+
+def thermo_derivs(params: Params, nodes: Nodes, x, mu, T: float, xi: float) -> dict:
+    """Implicit derivatives of a solved state (ThermoDerivatives.jl): theta = (T, mu) with every
+    mu_f moved together; see or_thermo_derivs for the fields."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    mu = np.ascontiguousarray(np.broadcast_to(np.asarray(mu, dtype=np.float64), (3,)))
+    out = np.zeros(32)
+    rc = lib().or_thermo_derivs(C.byref(params), *nodes.args(), _dp(x), _dp(mu), T, xi, _dp(out))
+    if rc != 0:
+        raise ValueError("singular Hessian")
+    return dict(dx_dT=out[0:5].copy(), dx_dmu=out[5:10].copy(), dM_dT=out[10:13].copy(), dM_dmu=out[13:16].copy(),
+                s=out[16], n_B=out[17], ds_dT=out[18], ds_dmu=out[19], dn_dT=out[20], dn_dmu=out[21],
+                pressure=out[22], dP_dT=out[23], dP_dmu=out[24], energy=out[25], deps_dT=out[26],
+                deps_dmu=out[27], dP_deps_n=out[28], dP_dn_eps=out[29], v_n_sq=out[30], dmuB_dT_sigma=out[31])
 
 
 def max_threads() -> int:

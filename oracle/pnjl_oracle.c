@@ -26,6 +26,7 @@
  *                          autoscaling; both restated from the published methods)
  *   solve / solve_multi .. src/pnjl/solver/ImplicitSolver.jl:211-328,532-559
  *   seeds ................ src/pnjl/solver/SeedStrategies.jl:56-95,204-284
+ *   implicit derivatives . src/pnjl/derivatives/ThermoDerivatives.jl:132-173,184-249,342-465
  *   K data (one-loop A,    src/relaxtime/OneLoopIntegrals.jl:507-543,
  *   effective couplings)   src/relaxtime/EffectiveCouplings.jl:56-60,112-115,242-279,
  *                          scripts/relaxtime/run_gap_transport_scan.jl:297-305
@@ -1043,4 +1044,222 @@ void or_kdata(const or_params *P, int n_nodes, const double *p, const double *w,
     out[3] = -Nc / (4.0 * pi * pi) * (m_u * Au);
     out[4] = -Nc / (4.0 * pi * pi) * (m_s * As);
     or_effective_couplings(P->G, P->K, out[3], out[4], out + 5);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Implicit derivatives: ThermoDerivatives.jl (mass_derivatives :132-173,     */
+/* thermo_derivatives :184-249, bulk_viscosity_coefficients :342-465)          */
+/* ------------------------------------------------------------------------- */
+/* The reference differentiates the solution x(theta) of F(x; theta) = 0, theta = (T, mu)
+ * with every mu_f shifted together, by the implicit function theorem
+ * (ImplicitDifferentiation.jl: dx/dtheta = -(dF/dx)^-1 dF/dtheta) and ForwardDiff through
+ * calculate_thermo / calculate_rho.  Restated here with a second-order jet in the seven
+ * variables (phi_u, phi_d, phi_s, Phi, Phibar, T, mu): one jet evaluation of Omega gives every
+ * first and second derivative the chain rule needs, exactly as nested forward-mode AD does. */
+#define NV7 7
+#define NH7 28
+static int HI7[NH7], HJ7[NH7];
+static void init_h7(void) {
+    static int done = 0;
+    if (done) return;
+    int k = 0;
+    for (int i = 0; i < NV7; ++i)
+        for (int j = i; j < NV7; ++j) { HI7[k] = i; HJ7[k] = j; ++k; }
+    done = 1;
+}
+static int h7(int i, int j) { /* index of (i, j) in the packed upper triangle */
+    if (i > j) { int t = i; i = j; j = t; }
+    return i * NV7 - i * (i - 1) / 2 + (j - i);
+}
+typedef struct { double v, g[NV7], h[NH7]; } jet7;
+static jet7 k_const(double c) { jet7 r; memset(&r, 0, sizeof r); r.v = c; return r; }
+static jet7 k_var(double c, int i) { jet7 r = k_const(c); r.g[i] = 1.0; return r; }
+static jet7 k_add(jet7 a, jet7 b) {
+    jet7 r; r.v = a.v + b.v;
+    for (int i = 0; i < NV7; ++i) r.g[i] = a.g[i] + b.g[i];
+    for (int k = 0; k < NH7; ++k) r.h[k] = a.h[k] + b.h[k];
+    return r;
+}
+static jet7 k_scale(jet7 a, double c) {
+    jet7 r; r.v = a.v * c;
+    for (int i = 0; i < NV7; ++i) r.g[i] = a.g[i] * c;
+    for (int k = 0; k < NH7; ++k) r.h[k] = a.h[k] * c;
+    return r;
+}
+static jet7 k_sub(jet7 a, jet7 b) { return k_add(a, k_scale(b, -1.0)); }
+static jet7 k_addc(jet7 a, double c) { a.v += c; return a; }
+static jet7 k_mul(jet7 a, jet7 b) {
+    jet7 r; r.v = a.v * b.v;
+    for (int i = 0; i < NV7; ++i) r.g[i] = a.v * b.g[i] + b.v * a.g[i];
+    for (int k = 0; k < NH7; ++k)
+        r.h[k] = a.v * b.h[k] + b.v * a.h[k] + a.g[HI7[k]] * b.g[HJ7[k]] + a.g[HJ7[k]] * b.g[HI7[k]];
+    return r;
+}
+static jet7 k_fn(jet7 a, double f0, double f1, double f2) {
+    jet7 r; r.v = f0;
+    for (int i = 0; i < NV7; ++i) r.g[i] = f1 * a.g[i];
+    for (int k = 0; k < NH7; ++k) r.h[k] = f1 * a.h[k] + f2 * a.g[HI7[k]] * a.g[HJ7[k]];
+    return r;
+}
+static jet7 k_exp(jet7 a) { double e = exp(a.v); return k_fn(a, e, e, e); }
+static jet7 k_log(jet7 a) { double i = 1.0 / a.v; return k_fn(a, log(a.v), i, -i * i); }
+static jet7 k_sqrt(jet7 a) { double s = sqrt(a.v), d1 = 1.0 / (2.0 * s); return k_fn(a, s, d1, -d1 / (2.0 * a.v)); }
+static jet7 k_inv(jet7 a) { double i = 1.0 / a.v; return k_fn(a, i, -i * i, 2.0 * i * i * i); }
+static jet7 k_abs(jet7 a) { return signbit(a.v) ? k_scale(a, -1.0) : a; }
+static jet7 k_maxc(jet7 a, double c) { return (a.v < c) ? k_const(c) : a; }
+
+/* Integrals.jl:193-238 calculate_log_term with E, mu, T, Phi, Phibar all jets */
+static jet7 log_term_jet7(jet7 E, jet7 mu, jet7 T, jet7 Phi, jet7 Phib) {
+    jet7 invT = k_inv(T);
+    jet7 a = k_scale(k_mul(k_sub(E, mu), invT), -1.0);
+    jet7 b = k_scale(k_mul(k_add(E, mu), invT), -1.0);
+    jet7 tP = k_scale(Phi, 3.0), tPb = k_scale(Phib, 3.0), lfp, lfm;
+    if (a.v > 0) {
+        jet7 e1 = k_exp(k_scale(a, -2.0)), e2 = k_exp(k_scale(a, -1.0)), e0 = k_exp(k_scale(a, -3.0));
+        jet7 term = k_addc(k_add(k_add(e0, k_mul(tP, e1)), k_mul(tPb, e2)), 1.0);
+        lfp = k_add(k_scale(a, 3.0), k_log(k_maxc(term, POLYAKOV_EPS)));
+    } else {
+        jet7 e1 = k_exp(a), e2 = k_mul(e1, e1), e3 = k_mul(e1, e2);
+        jet7 f = k_add(k_add(k_addc(k_mul(tP, e1), 1.0), k_mul(tPb, e2)), e3);
+        lfp = k_log(k_maxc(f, POLYAKOV_EPS));
+    }
+    if (b.v > 0) {
+        jet7 e1 = k_exp(k_scale(b, -2.0)), e2 = k_exp(k_scale(b, -1.0)), e0 = k_exp(k_scale(b, -3.0));
+        jet7 term = k_addc(k_add(k_add(e0, k_mul(tPb, e1)), k_mul(tP, e2)), 1.0);
+        lfm = k_add(k_scale(b, 3.0), k_log(k_maxc(term, POLYAKOV_EPS)));
+    } else {
+        jet7 e1 = k_exp(b), e2 = k_mul(e1, e1), e3 = k_mul(e1, e2);
+        jet7 f = k_add(k_add(k_addc(k_mul(tPb, e1), 1.0), k_mul(tP, e2)), e3);
+        lfm = k_log(k_maxc(f, POLYAKOV_EPS));
+    }
+    return k_add(lfp, lfm);
+}
+
+/* calculate_omega (Thermodynamics.jl:181-195) with x, T and the common mu shift as jets:
+ * mu_f = mu0_f + s, s = 0 the seventh variable. */
+static jet7 omega_jet7(const or_params *P, const or_nodes *nd, const double *xv, const double *mu0, double T0v,
+                       double xi) {
+    init_h7();
+    jet7 x[5];
+    for (int i = 0; i < 5; ++i) x[i] = k_var(xv[i], i);
+    jet7 T = k_var(T0v, 5), s = k_var(0.0, 6);
+    jet7 sq = k_add(k_add(k_mul(x[0], x[0]), k_mul(x[1], x[1])), k_mul(x[2], x[2]));
+    jet7 chi = k_sub(k_scale(sq, 2.0 * P->G), k_scale(k_mul(k_mul(x[0], x[1]), x[2]), 4.0 * P->K));
+    /* U (Thermodynamics.jl:124-130), T a jet */
+    jet7 r = k_scale(k_inv(T), P->T0);
+    jet7 Ta = k_addc(k_add(k_scale(r, P->a1), k_scale(k_mul(r, r), P->a2)), P->a0);
+    jet7 Tb = k_scale(k_mul(k_mul(r, r), r), P->b3);
+    jet7 pp = k_mul(x[4], x[3]);
+    jet7 cub = k_add(k_mul(k_mul(x[4], x[4]), x[4]), k_mul(k_mul(x[3], x[3]), x[3]));
+    jet7 val = k_sub(k_add(k_addc(k_scale(pp, -6.0), 1.0), k_scale(cub, 4.0)), k_scale(k_mul(pp, pp), 3.0));
+    jet7 lg = (val.v <= 0 || val.v < POLYAKOV_EPS) ? k_const(log(POLYAKOV_EPS)) : k_log(val);
+    jet7 T2 = k_mul(T, T), T4 = k_mul(T2, T2);
+    jet7 U = k_mul(T4, k_add(k_mul(k_scale(Ta, -0.5), pp), k_mul(Tb, lg)));
+    /* masses and vacuum term (Integrals.jl:123-145) */
+    jet7 M[3];
+    M[0] = k_add(k_addc(k_scale(x[0], -4.0 * P->G), P->m_ud0), k_mul(k_scale(x[1], 2.0 * P->K), x[2]));
+    M[1] = k_add(k_addc(k_scale(x[1], -4.0 * P->G), P->m_ud0), k_mul(k_scale(x[0], 2.0 * P->K), x[2]));
+    M[2] = k_add(k_addc(k_scale(x[2], -4.0 * P->G), P->m_s0), k_mul(k_scale(x[0], 2.0 * P->K), x[1]));
+    jet7 vac = k_const(0.0);
+    const double L = P->Lambda;
+    for (int f = 0; f < 3; ++f) {
+        jet7 ms = k_addc(k_abs(M[f]), 1e-12);
+        jet7 ms2 = k_mul(ms, ms);
+        jet7 sqv = k_sqrt(k_addc(ms2, L * L));
+        jet7 poly = k_mul(k_scale(sqv, L), k_addc(ms2, 2.0 * L * L));
+        jet7 lt = k_mul(k_mul(ms2, ms2), k_log(k_mul(k_addc(sqv, L), k_inv(ms))));
+        vac = k_add(vac, k_scale(k_sub(poly, lt), 1.0 / (16.0 * M_PI * M_PI)));
+    }
+    jet7 esum = k_scale(vac, -2.0 * P->N_color);
+    /* Integrals.jl:248-259 */
+    jet7 total = k_const(0.0);
+    for (int f = 0; f < 3; ++f) {
+        jet7 M2 = k_mul(M[f], M[f]);
+        jet7 muf = k_addc(s, mu0[f]);
+        for (int k = 0; k < nd->n; ++k) {
+            const double p = nd->p[k], c = nd->c[k], pc = p * c;
+            jet7 E = k_sqrt(k_addc(M2, p * p + xi * (pc * pc)));
+            total = k_add(total, k_scale(log_term_jet7(E, muf, T, x[3], x[4]), nd->w[k]));
+        }
+    }
+    jet7 logsum = k_mul(k_scale(T, -2.0), total);
+    return k_add(k_add(k_add(chi, U), esum), logsum);
+}
+
+/* Derivatives of a solved state x at (T, mu_f), theta = (T, mu) with every mu_f moved together.
+ * out (OR_NDERIV doubles):
+ *   [0..4]  dx/dT            [5..9]  dx/dmu
+ *   [10..12] dM/dT           [13..15] dM/dmu
+ *   16 s = -dOmega/dT        17 n_B = -(1/3) dOmega/dmu (sum of rho_f / 3)
+ *   18 ds/dT  19 ds/dmu      20 dn_B/dT  21 dn_B/dmu     (total, through x(theta))
+ *   22 P      23 dP/dT       24 dP/dmu
+ *   25 eps = -P + 3 mu_mean n_B ... (below)  26 deps/dT  27 deps/dmu
+ *   28 dP/deps|n             29 dP/dn|eps                (thermo_derivatives :225-229)
+ *   30 v_n^2                 31 dmu_B/dT|sigma           (bulk_viscosity_coefficients :440-457)
+ * eps = -P + sum_f mu_f rho_f + T s (calculate_thermo, Thermodynamics.jl:233-244); the chain
+ * rule for it uses d(sum mu_f rho_f)/dtheta = sum_f mu_f drho_f/dtheta + [theta = mu] sum rho_f.
+ * Returns 0, or 1 when the Hessian is singular. */
+#define OR_NDERIV 32
+int or_thermo_derivs(const or_params *P, int n_nodes, const double *pm, const double *cm, const double *wm,
+                     const double *x, const double *mu, double T, double xi, double *out) {
+    or_nodes nd = {n_nodes, pm, cm, wm};
+    jet7 om = omega_jet7(P, &nd, x, mu, T, xi);
+    double H[25], rhsT[5], rhsM[5], dxT[5], dxM[5];
+    for (int i = 0; i < 5; ++i) {
+        for (int j = 0; j < 5; ++j) H[i * 5 + j] = om.h[h7(i, j)];
+        rhsT[i] = -om.h[h7(i, 5)];
+        rhsM[i] = -om.h[h7(i, 6)];
+    }
+    if (lu_solve(5, H, rhsT, dxT) != 0 || lu_solve(5, H, rhsM, dxM) != 0) return 1;
+    for (int i = 0; i < 5; ++i) { out[i] = dxT[i]; out[5 + i] = dxM[i]; }
+    /* dM/dtheta = dM/dx . dx/dtheta (Thermodynamics.jl:81-90) */
+    const double G4 = 4.0 * P->G, K2 = 2.0 * P->K;
+    const double Jm[3][3] = {{-G4, K2 * x[2], K2 * x[1]}, {K2 * x[2], -G4, K2 * x[0]}, {K2 * x[1], K2 * x[0], -G4}};
+    for (int f = 0; f < 3; ++f) {
+        double a = 0.0, b = 0.0;
+        for (int k = 0; k < 3; ++k) { a += Jm[f][k] * dxT[k]; b += Jm[f][k] * dxM[k]; }
+        out[10 + f] = a;
+        out[13 + f] = b;
+    }
+    /* s = -Omega_T and 3 n_B = sum rho_f = -Omega_mu, and their total derivatives */
+    const double OT = om.g[5], OM = om.g[6];
+    double sT = -om.h[h7(5, 5)], sM = -om.h[h7(5, 6)], nT = -om.h[h7(5, 6)], nM = -om.h[h7(6, 6)];
+    double PT = -OT, PM = -OM;
+    for (int i = 0; i < 5; ++i) {
+        sT -= om.h[h7(5, i)] * dxT[i];
+        sM -= om.h[h7(5, i)] * dxM[i];
+        nT -= om.h[h7(6, i)] * dxT[i];
+        nM -= om.h[h7(6, i)] * dxM[i];
+        PT -= om.g[i] * dxT[i];
+        PM -= om.g[i] * dxM[i];
+    }
+    const double s = -OT, nB = -OM / 3.0;
+    nT /= 3.0;
+    nM /= 3.0;
+    out[16] = s; out[17] = nB; out[18] = sT; out[19] = sM; out[20] = nT; out[21] = nM;
+    /* P and eps (calculate_thermo) with rho_f = -dOmega/dmu_f at fixed x: sum_f mu_f rho_f needs
+     * the per-flavour densities; with every mu_f moved together d(mu_f)/dmu = 1 */
+    double rho[3], murho = 0.0;
+    {
+        or_thermo th;
+        or_thermo_eval(P, n_nodes, pm, cm, wm, x, mu, T, xi, &th);
+        for (int f = 0; f < 3; ++f) { rho[f] = th.rho[f]; murho += mu[f] * rho[f]; }
+    }
+    const double Pv = -om.v;
+    /* d(sum mu_f rho_f)/dtheta: the per-flavour rho_f derivatives are not separated by the
+     * shared-mu jet, so for mu_u = mu_d = mu_s = mu it is mu * d(3 n_B)/dtheta (+ 3 n_B for
+     * theta = mu); the reference's thermo_derivatives always has equal mu_f. */
+    const double mubar = (mu[0] + mu[1] + mu[2]) / 3.0;
+    const double eps = -Pv + murho + T * s;
+    const double eT = -PT + mubar * 3.0 * nT + s + T * sT;
+    const double eM = -PM + 3.0 * nB + mubar * 3.0 * nM + T * sM;
+    out[22] = Pv; out[23] = PT; out[24] = PM; out[25] = eps; out[26] = eT; out[27] = eM;
+    const double den_e = eT * nM - eM * nT, den_n = nT * eM - nM * eT;
+    out[28] = den_e == 0 ? NAN : (PT * nM - PM * nT) / den_e;
+    out[29] = den_n == 0 ? NAN : (PT * eM - PM * eT) / den_n;
+    /* bulk_viscosity_coefficients: mu_B = 3 mu_q */
+    const double sMB = sM / 3.0, nMB = nM / 3.0;
+    out[30] = (s * nMB - nB * nT) / (T * (sT * nMB - sMB * nT));
+    out[31] = -(nB * sT - s * nT) / (nB * sMB - s * nMB);
+    return 0;
 }
