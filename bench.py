@@ -542,6 +542,8 @@ def main():
         arm = Arm("surrogate", eng, table, hot,
                   default_learned_opts(ftol=1e-10, precision=precision, verify_map=ls.verify_map), True)
         train["verify_map_cells_flagged"] = ls.verify_map.fraction()
+        train["verify_map_criteria"] = {"coexisting_phase_within_fm4": tc.map_gap_max, "label_jump_above": tc.map_jump,
+                                        "grow_cells": tc.map_grow}
     else:
         arm = Arm("multiseed", eng, table, hot, SolveOptions(iterations=40, ftol=1e-10, precision=precision), False)
     plain = Arm("plain_fp64", eng, table, hot, SolveOptions(iterations=40, ftol=1e-10, precision="fp64"), False)

@@ -42,6 +42,11 @@ class TrainConfig:
     label_precision: str = "mixed"
     mu_s_ratio: float = 1.0
     label_extra: tuple = ()       # seed rows appended to the label table (e.g. MEDIUM, HIGH_DENSITY)
+    # verification map (coexistence_map): coexisting phases within map_gap_max (fm^-4) of the
+    # minimum, label jumps above map_jump, flagged cells grown by map_grow
+    map_gap_max: float = 0.01
+    map_jump: float = 0.25
+    map_grow: int = 0
 
 
 def grid_points(cfg: TrainConfig):
@@ -278,5 +283,5 @@ def train_learned_seed(engine: GapEngine, cfg: TrainConfig | None = None) -> Lea
     ls = LearnedSeed(engine, seed=cfg.seed)
     ls.default_scaling(x, cfg)
     ls.fit(T, mu, xi, x, epochs=cfg.epochs, batch=cfg.batch, lr=cfg.lr, shuffle_seed=cfg.seed + 1)
-    ls.verify_map = coexistence_map(engine, cfg, res)
+    ls.verify_map = coexistence_map(engine, cfg, res, gap_max=cfg.map_gap_max, jump=cfg.map_jump, grow=cfg.map_grow)
     return ls

@@ -2,7 +2,7 @@
 
 Run once where the reference is mounted (it is read-only input; nothing is executed):
 
-    python tests/golden/make_golden.py --reference /root/reference
+    python tests/golden/make_golden.py --reference <path of the reference checkout>
 
 The fixtures are trimmed copies of files the reference itself produced or ships:
 

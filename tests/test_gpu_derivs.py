@@ -3,7 +3,9 @@
 values (tests/unit/relaxtime/test_bulk_viscosity_derivatives.jl: T = 150 MeV, mu_B = 800 MeV).
 
 Tolerance against the oracle: 1e-9 of each field's scale (both are exact derivatives in FP64;
-the 5 x 5 solve for dx/dtheta amplifies rounding by the Hessian's condition number).
+the 5 x 5 solve for dx/dtheta amplifies rounding by the Hessian's condition number); 1e-7 for
+the four ratios of differences of products (dP/deps|n, dP/dn|eps, v_n^2, dmu_B/dT|sigma),
+whose denominators cancel to a few digits at some points and amplify the same rounding.
 """
 import numpy as np
 import pytest
@@ -18,6 +20,7 @@ pytestmark = pytest.mark.gpu
 HBARC = 197.327
 SCALARS = ("s", "n_B", "ds_dT", "ds_dmu", "dn_dT", "dn_dmu", "pressure", "dP_dT", "dP_dmu", "energy", "deps_dT",
            "deps_dmu", "dP_deps_n", "dP_dn_eps", "v_n_sq", "dmuB_dT_sigma")
+RATIOS = ("dP_deps_n", "dP_dn_eps", "v_n_sq", "dmuB_dT_sigma")
 
 
 def test_bulk_viscosity_golden_point(engine_factory):
@@ -62,7 +65,8 @@ def test_derivatives_match_oracle(engine_factory, p_num, t_num):
         ref = np.array([r[k] for r in refs])
         scale = np.maximum(np.abs(ref), np.abs(ref).max(axis=0) * 1e-3)
         err = np.abs(got[k] - ref) / scale
-        assert err.max() <= 1e-9, (k, err.max(), int(np.argmax(err.max(axis=-1) if err.ndim > 1 else err)))
+        tol = 1e-7 if k in RATIOS else 1e-9
+        assert err.max() <= tol, (k, err.max(), int(np.argmax(err.max(axis=-1) if err.ndim > 1 else err)))
 
 
 def test_derivatives_device_entry_point(engine_factory):
