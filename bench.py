@@ -372,6 +372,97 @@ class Arm:
                               seed_table_hot=self.hot, opts=self.opts, learned=self.learned)
 
 
+def run_scan(args):
+    """The drop-in scan driver end to end: scan.run_gap_transport_scan (the gap part of
+    scripts/relaxtime/run_gap_transport_scan.jl) over T 50-300 MeV x mu_B 0-1200 MeV (32 x 32,
+    mu_q = mu_B / 3: the 32 x 32 isotropic grid's box) x xi in {0, 0.2, 0.4}, p64 x t8,
+    MultiSeed on each (xi, mu_B) column's first point and PhaseAwareContinuitySeed after it
+    (the reference's boundary.csv / cep.csv), build_K_data per row, CSV written.  Timed on the
+    host clock around the whole driver (trackers, launches, copies, CSV); the same driver over
+    the oracle on all host cores beside it."""
+    import tempfile
+
+    from julia_relaxtime_gb300.engine import GapEngine
+    from julia_relaxtime_gb300.scan import ScanOptions, gpu_point_solver, read_existing_keys, run_gap_transport_scan
+
+    golden = os.path.join(ROOT, "tests", "golden")
+    tmp = tempfile.mkdtemp(prefix="pnjl_scan_")
+
+    def opts(name, xi_values=(0.0, 0.2, 0.4)):
+        return ScanOptions(output=os.path.join(tmp, name), xi_values=list(xi_values), tmin_mev=50.0,
+                           tmax_mev=300.0, tstep_mev=250.0 / 31.0, mubmin_mev=0.0, mubmax_mev=1200.0,
+                           mubstep_mev=1200.0 / 31.0, overwrite=True, resume=False, p_num=64, t_num=8, max_iter=40,
+                           boundary_path=os.path.join(golden, "boundary.csv"), cep_path=os.path.join(golden, "cep.csv"))
+
+    eng = GapEngine(p_num=64, t_num=8)
+    solver = gpu_point_solver(64, 8, engine=eng)
+
+    def rows_of(path):
+        with open(path) as fh:
+            lines = [ln.rstrip("\n").split(",") for ln in fh if not ln.startswith("#")]
+        head = lines[0]
+        return [dict(zip(head, ln)) for ln in lines[1:]]
+
+    for _ in range(args.warmup):
+        run_gap_transport_scan(opts("warm.csv"), solver=solver)
+    times, launches0 = [], eng.stats()["kernel_launches"]
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        run_gap_transport_scan(opts(f"gpu{k}.csv"), solver=solver)
+        times.append(time.perf_counter() - t0)
+    launches = eng.stats()["kernel_launches"] - launches0
+    rows = rows_of(os.path.join(tmp, "gpu0.csv"))
+    conv = sum(1 for r in rows if r["converged"] == "true")
+    line = {"metric": "gap-transport scan rows/s through the drop-in driver (continuation seeds, FP64, ftol 1e-9)",
+            "value": conv * args.steps / sum(times), "unit": "rows/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "gap_transport_scan_32x32x3", "rows": len(rows), "p_num": 64, "t_num": 8,
+                       "grid": "T 50-300 MeV (32) x mu_B 0-1200 MeV (32) x xi 0, 0.2, 0.4",
+                       "seeds": "MultiSeed on each column's first T, PhaseAwareContinuitySeed after it"},
+            "gpu_launches": int(launches), "launches_per_scan": launches / args.steps,
+            "timing": "host wall clock around run_gap_transport_scan (solves, trackers, K data, CSV)"}
+    if not args.no_cpu_baseline:
+        # the checker: the same driver over the oracle, all host cores
+        from oracle import oracle as orc
+
+        P = orc.default_params()
+        nd = orc.Nodes(64, 8)
+        threads = os.cpu_count() or 1
+
+        def oracle_solver(T, mu, xi, point_seeds, max_iter):
+            o = orc.default_opts(max_iter=max_iter)
+            mu3 = np.repeat(np.asarray(mu, dtype=np.float64).reshape(-1, 1), 3, axis=1)
+            if point_seeds is None:
+                rs = orc.solve_batch(P, nd, T, mu3, xi, multi=True, multiseed_rule=True, opts=o, threads=threads)
+            else:
+                rs = orc.solve_batch(P, nd, T, mu3, xi, seeds=point_seeds, multi=False, opts=o, threads=threads)
+            n = len(rs)
+            return {"x": np.array([list(r.x) for r in rs]).reshape(n, 5), "omega": np.array([r.omega for r in rs]),
+                    "pressure": np.array([r.pressure for r in rs]), "entropy": np.array([r.entropy for r in rs]),
+                    "energy": np.array([r.energy for r in rs]), "rho_norm": np.array([r.rho_norm for r in rs]),
+                    "masses": np.array([list(r.masses) for r in rs]).reshape(n, 3),
+                    "n_q": np.array([list(r.nq) for r in rs]).reshape(n, 3),
+                    "n_aq": np.array([list(r.naq) for r in rs]).reshape(n, 3),
+                    "residual_norm": np.array([r.residual_norm for r in rs]),
+                    "iterations": np.array([r.iterations for r in rs]), "status": np.array([r.status for r in rs]),
+                    "converged": np.array([bool(r.converged) for r in rs])}
+
+        t0 = time.perf_counter()
+        run_gap_transport_scan(opts("oracle.csv"), solver=oracle_solver)
+        dt = time.perf_counter() - t0
+        orows = rows_of(os.path.join(tmp, "oracle.csv"))
+        oconv = sum(1 for r in orows if r["converged"] == "true")
+        same = sum(1 for a, b in zip(rows, orows)
+                   if a["converged"] == b["converged"] and
+                   abs(float(a["omega_fm4inv"]) - float(b["omega_fm4inv"])) <= 1e-10 * abs(float(b["omega_fm4inv"])))
+        line["cpu_baseline"] = {"value": oconv / dt, "unit": "rows/s", "cores": threads, "kind": "port",
+                                "sample": f"the whole scan ({len(orows)} rows) through the same driver"}
+        line["rows_agreeing_with_oracle"] = {"rows": len(rows), "same_convergence_and_omega_1e-10": same}
+    print(json.dumps(line))
+    eng.close()
+
+
 def run_orders(args):
     """Mixed quadrature orders in one graph launch: the 32 x 32 (T 50-300 MeV, mu 0-400 MeV, xi = 0)
     grid solved with MultiSeed (6 candidates, min-Omega) in mixed precision at p = 64, 128 and 256
@@ -462,10 +553,12 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=("gpu", "reference"))
     ap.add_argument("--workload", default="first_order_2048x2048x9",
                     choices=("first_order_2048x2048x9", "aniso_scan_256x256x9", "surrogate_eval_2p20", "iso_scan_32x32"))
-    ap.add_argument("--mode", default="surrogate", choices=("surrogate", "multiseed", "orders"),
+    ap.add_argument("--mode", default="surrogate", choices=("surrogate", "multiseed", "orders", "scan"),
                     help="surrogate: learned seed + mixed precision (headline); multiseed: the MultiSeed table; "
                          "orders: the 32 x 32 isotropic grid at p = 64, 128, 256 in one CUDA graph (mixed "
-                         "precision, errors against the FP64 solve of the same kernel)")
+                         "precision, errors against the FP64 solve of the same kernel); scan: the drop-in "
+                         "gap-transport scan driver end to end (32 x 32 x 3, continuation seeds) beside the same "
+                         "driver over the oracle")
     ap.add_argument("--precision", default=None, choices=("fp64", "mixed"),
                     help="precision of the timed arm (default: mixed for surrogate, fp64 for multiseed)")
     ap.add_argument("--chunks", type=int, default=None,
@@ -512,6 +605,9 @@ def main():
 
     if args.mode == "orders":
         run_orders(args)
+        return
+    if args.mode == "scan":
+        run_scan(args)
         return
 
     dist = None

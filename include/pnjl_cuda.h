@@ -252,6 +252,17 @@ int pnjl_set_pipeline(pnjl_ctx *ctx, int32_t chunks);
  * scan; the autotuner tries 0..4).  Results do not depend on it. */
 int pnjl_set_cert_warps(pnjl_ctx *ctx, int32_t warps);
 int pnjl_get_cert_warps(const pnjl_ctx *ctx, int32_t *warps);
+/* Bounds of the fused kernel's waits (no counterpart in the reference, which has no GPU code):
+ * a warp that has taken a listed slot's task or a queued certification polls the entry's
+ * ready flag, written by a running warp of the same launch, at most ready_polls times (64 ns
+ * apart; default 2^24, about 1 s); a seed whose FP32 root an earlier seed is still certifying
+ * polls that verdict at most verdict_polls times (128 ns apart; default 2^20).  A ready wait
+ * that runs out leaves the task undone and is counted in pnjl_stats.device_wait_timeouts, and
+ * the host-array solves then return PNJL_ERR_CUDA ("results incomplete") -- the context stays
+ * usable; a verdict wait that runs out makes the waiting seed certify the root itself (same
+ * result).  0 means no polls: a flag not set at the first read gives up at once. */
+int pnjl_set_wait_limits(pnjl_ctx *ctx, uint32_t ready_polls, uint32_t verdict_polls);
+int pnjl_get_wait_limits(const pnjl_ctx *ctx, uint32_t *ready_polls, uint32_t *verdict_polls);
 int pnjl_get_tuning(const pnjl_ctx *ctx, int32_t *lanes_per_point, int32_t *blocks_per_sm, int32_t *chunks);
 
 /* One launch shape and its measured solve time (device time of the solve kernels, CUDA events). */

@@ -150,6 +150,8 @@ SIGNATURES = {
     "pnjl_autotune": (C.c_int, [C.c_void_p, C.c_int64, dp, dp, dp, dp, dp, C.POINTER(pnjl_solve_opts),
                                 C.POINTER(pnjl_result_soa), C.c_int32, C.c_int32, C.POINTER(pnjl_tuning),
                                 C.POINTER(pnjl_tuning), C.c_int32, C.POINTER(C.c_int32)]),
+    "pnjl_set_wait_limits": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32]),
+    "pnjl_get_wait_limits": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     "pnjl_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "pnjl_probe_peak": (C.c_int, [C.c_void_p, C.c_int32, dp]),
     "pnjl_f64_math": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64, dp, dp]),

@@ -54,6 +54,8 @@ struct pnjl_ctx {
     int blocks_per_sm = 0;  // 0 = occupancy maximum
     int pipeline_chunks = 0;  // mixed per-point solves: chunks over two streams (0 = automatic)
     int cert_warps = pnjl::kDefaultCertWarps;  // fused kernel: certifying warps per block
+    unsigned ready_polls = pnjl::kReadyPollsDefault;      // bounds of the fused kernel's waits
+    unsigned verdict_polls = pnjl::kVerdictPollsDefault;  // (pnjl_set_wait_limits)
     cudaStream_t stream2 = nullptr;  // second stream of the chunk pipeline
     cudaEvent_t ev_chunk[pnjl::kMaxPipelineChunks] = {};
     cudaEvent_t ev_join = nullptr;
@@ -835,6 +837,8 @@ static cudaError_t solve_enqueue(const pnjl_ctx *ctx, const pnjl::KernelNodes &n
     a.hot_T_MeV = opts->hot_T_MeV;
     a.point_seeds = opts->point_seeds;
     pnjl::fill_solve_opts(opts, a.opts);
+    a.opts.ready_polls = ctx->ready_polls;
+    a.opts.verdict_polls = ctx->verdict_polls;
     if (pnjl::verify_map_cells(opts)) a.opts.vmap = r.vmap;
     a.out = d_out;
     a.queue = r.ctrl;
@@ -1449,6 +1453,20 @@ int pnjl_set_cert_warps(pnjl_ctx *ctx, int32_t warps) {
 int pnjl_get_cert_warps(const pnjl_ctx *ctx, int32_t *warps) {
     if (!ctx || !warps) return PNJL_ERR_INVALID_ARGUMENT;
     *warps = ctx->cert_warps;
+    return PNJL_OK;
+}
+
+int pnjl_set_wait_limits(pnjl_ctx *ctx, uint32_t ready_polls, uint32_t verdict_polls) {
+    if (!ctx) return PNJL_ERR_INVALID_ARGUMENT;
+    ctx->ready_polls = ready_polls;
+    ctx->verdict_polls = verdict_polls;
+    return PNJL_OK;
+}
+
+int pnjl_get_wait_limits(const pnjl_ctx *ctx, uint32_t *ready_polls, uint32_t *verdict_polls) {
+    if (!ctx || !ready_polls || !verdict_polls) return PNJL_ERR_INVALID_ARGUMENT;
+    *ready_polls = ctx->ready_polls;
+    *verdict_polls = ctx->verdict_polls;
     return PNJL_OK;
 }
 

@@ -54,7 +54,16 @@ struct SolveOpts {
     const unsigned char *vmap;  // device copy of pnjl_solve_opts::verify_map, or null
     int vn[3];
     double vlo[3], vhi[3];
+    // bounds of the fused kernel's waits on flags written by running warps of the same launch
+    // (pnjl_set_wait_limits): polls of a listed slot's / queued job's ready flag, and of an
+    // earlier seed's pending verdict; a wait that runs out gives up as documented there
+    unsigned ready_polls, verdict_polls;
 };
+
+// Default wait bounds: 2^24 polls of 64 ns (about 1 s) for a ready flag, 2^20 polls of 128 ns
+// for a pending verdict.
+constexpr unsigned kReadyPollsDefault = 1u << 24;
+constexpr unsigned kVerdictPollsDefault = 1u << 20;
 
 // The reference's POLYAKOV_EPS (Integrals.jl:151) and log(POLYAKOV_EPS)
 static constexpr double kPolyakovEps = 1e-16;

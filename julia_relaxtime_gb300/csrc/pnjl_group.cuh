@@ -860,14 +860,13 @@ struct Group {
 constexpr int kRootNone = 0, kRootPending = 1, kRootUsable = 2;
 // A pending root's verdict comes at the end of one seed's certification (FP64 passes and at
 // most the rest of its iteration budget): polled with a sleep, and given up after about
-// kVerdictPolls x kVerdictSleepNs (then the waiting seed certifies the root itself, the result
-// it reaches without waiting).
-constexpr unsigned kVerdictPolls = 1u << 20;
+// SolveOpts::verdict_polls x kVerdictSleepNs (then the waiting seed certifies the root itself,
+// the result it reaches without waiting).
 constexpr unsigned kVerdictSleepNs = 128;
 
-__device__ __forceinline__ int wait_verdict(const int *flag) {
+__device__ __forceinline__ int wait_verdict(const int *flag, unsigned polls) {
     int f = *(volatile const int *)flag;
-    for (unsigned k = 0; f == kRootPending && k < kVerdictPolls; ++k) {
+    for (unsigned k = 0; f == kRootPending && k < polls; ++k) {
         __nanosleep(kVerdictSleepNs);
         f = *(volatile const int *)flag;
     }
@@ -928,6 +927,7 @@ struct PublishedRoots {
     double prior_omega;   // Omega of `prior` (NaN when there is none)
     LocalRoots own;
     bool wait_pending = false;  // wait for the verdict on an earlier seed's pending root
+    unsigned verdict_polls = kVerdictPollsDefault;  // bound of that wait
     __device__ double omega_bound() const { return prior_omega; }
     __device__ const double *prior_root() const { return prior; }
     // a per-point seed (no slot), whose root may be sent to the verification seeds
@@ -947,7 +947,7 @@ struct PublishedRoots {
                     // seed q is certifying this root: its verdict decides, as it would had q
                     // finished first (skipped when q's root is usable, refined otherwise)
                     if (!wait_pending || !same_root(x, y)) continue;
-                    f = wait_verdict(&flag[base + q]);
+                    f = wait_verdict(&flag[base + q], verdict_polls);
                     if (f != kRootUsable) continue;
                     __threadfence();
                     for (int i = 0; i < 5; ++i) y[i] = __ldcg(&roots[5 * (base + q) + i]);

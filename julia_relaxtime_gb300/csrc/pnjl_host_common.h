@@ -163,6 +163,8 @@ inline void fill_solve_opts(const pnjl_solve_opts *o, SolveOpts &d) {
     d.verify_T_max_MeV = o->verify_T_max_MeV;
     d.verify_max_step = o->verify_max_step;
     d.vmap = nullptr;  // set by the caller to the device copy of o->verify_map
+    d.ready_polls = kReadyPollsDefault;
+    d.verdict_polls = kVerdictPollsDefault;
     for (int k = 0; k < 3; ++k) {
         d.vn[k] = o->verify_map ? o->verify_map_dims[k] : 0;
         d.vlo[k] = o->verify_map_lo[k];

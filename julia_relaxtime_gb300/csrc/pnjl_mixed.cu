@@ -34,14 +34,13 @@ namespace pnjl {
 
 // Ready flags of the device lists (list_mode, job_ready) are written last, after a fence, by
 // the lane that wrote the entry; a reader that has taken an entry polls its flag (the writer
-// is a running group a few stores away from setting it; the limit is never reached in
-// practice) and reads the entry through L2.
-constexpr unsigned kReadyPolls = 1u << 24;
+// is a running group a few stores away from setting it; the default limit, SolveOpts::
+// ready_polls, is never reached in practice) and reads the entry through L2.
 constexpr unsigned kReadySleepNs = 64;
 
-__device__ __forceinline__ int wait_ready(const int *flag) {
+__device__ __forceinline__ int wait_ready(const int *flag, unsigned polls) {
     int m = *(volatile const int *)flag;
-    for (unsigned k = 0; m == 0 && k < kReadyPolls; ++k) {
+    for (unsigned k = 0; m == 0 && k < polls; ++k) {
         __nanosleep(kReadySleepNs);
         m = *(volatile const int *)flag;
     }
@@ -173,7 +172,7 @@ __device__ __forceinline__ bool task_slot(const SolveArgs &a, int64_t t, bool ta
         return true;
     }
     int m = 0;
-    if (gl == 0) m = wait_ready(&a.list_mode[slot]);
+    if (gl == 0) m = wait_ready(&a.list_mode[slot], a.opts.ready_polls);
     m = __shfl_sync(mask, m, leader);
     if (m == 0) {
         cnt.v[kStatWaitTimeouts] += 1;
@@ -279,6 +278,7 @@ __device__ void task_step(Group<G> &grp, const SolveArgs &a, int64_t t, bool tab
     for (int k = 0; k < 5; ++k) x0[k] = row[k];
     PublishedRoots dd = task_roots(a, slot, s, mode, prior, mask, leader, gl);
     dd.wait_pending = !defer;
+    dd.verdict_polls = a.opts.verdict_polls;
     Candidate c;
     bool conv, dup;
     CertState cs;
@@ -296,7 +296,7 @@ __device__ void job_step(Group<G> &grp, const SolveArgs &a, long long j, int gl,
                          Counters &cnt) {
     const SolveOpts &o = a.opts;
     int ready = 0;
-    if (gl == 0) ready = wait_ready(&a.job_ready[j]);
+    if (gl == 0) ready = wait_ready(&a.job_ready[j], o.ready_polls);
     ready = __shfl_sync(mask, ready, leader);
     if (!ready) {
         cnt.v[kStatWaitTimeouts] += 1;

@@ -337,6 +337,16 @@ class GapEngine:
             self._check(self._lib.pnjl_get_kernel_stats(self._ctx, int(kernel), C.byref(st)), "pnjl_get_kernel_stats")
         return {k: getattr(st, k) for k, _ in api.pnjl_stats._fields_}
 
+    def set_wait_limits(self, ready_polls: int, verdict_polls: int):
+        """Bounds of the fused kernel's waits on flags of the same launch (pnjl_set_wait_limits)."""
+        self._check(self._lib.pnjl_set_wait_limits(self._ctx, int(ready_polls), int(verdict_polls)),
+                    "pnjl_set_wait_limits")
+
+    def wait_limits(self) -> tuple[int, int]:
+        r, v = C.c_uint32(), C.c_uint32()
+        self._check(self._lib.pnjl_get_wait_limits(self._ctx, C.byref(r), C.byref(v)), "pnjl_get_wait_limits")
+        return int(r.value), int(v.value)
+
     def sm_count(self) -> int:
         return int(self._lib.pnjl_device_sm_count(self._ctx))
 
