@@ -570,6 +570,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-parity", action="store_true", help="skip the oracle check of the arms' roots")
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default launch shape")
+    ap.add_argument("--train-epochs", type=int, default=None, help="training epochs of the network (default 400)")
+    ap.add_argument("--train-batch", type=int, default=None, help="training batch (default 512)")
+    ap.add_argument("--train-lr", type=float, default=None, help="peak learning rate (default 2e-3)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -627,6 +630,11 @@ def main():
         # set-up, untimed: label the 64 x 64 x 5 training grid with the multi-seed solver and
         # train the network on it (both on this GPU); reported as train_s
         tc = grid["train"]
+        import dataclasses
+
+        over = {k: v for k, v in (("epochs", args.train_epochs), ("batch", args.train_batch), ("lr", args.train_lr))
+                if v is not None}
+        tc = dataclasses.replace(tc, **over) if over else tc
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         ls = train_learned_seed(eng, tc)
@@ -634,10 +642,11 @@ def main():
                  "labels": f"64 x 64 x 5 (T {tc.T_MeV[0]:g}-{tc.T_MeV[1]:g} MeV, mu {tc.mu_MeV[0]:g}-{tc.mu_MeV[1]:g} "
                            f"MeV, xi {tc.xi[0]:g}..{tc.xi[1]:g}) grid, mu_s = {tc.mu_s_ratio:g} mu_u, "
                            f"MultiSeed ({tc.label_seeds + len(tc.label_extra)}) mixed",
-                 "epochs": tc.epochs}
+                 "epochs": tc.epochs, "batch": tc.batch, "lr": tc.lr}
         arm = Arm("surrogate", eng, table, hot,
                   default_learned_opts(ftol=1e-10, precision=precision, verify_map=ls.verify_map), True)
         train["verify_map_cells_flagged"] = ls.verify_map.fraction()
+        train["breakdown"] = ls.timings
         train["verify_map_criteria"] = {"coexisting_phase_within_fm4": tc.map_gap_max, "label_jump_above": tc.map_jump,
                                         "grow_cells": tc.map_grow}
     else:
@@ -869,6 +878,8 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if precision == "fp64" else "f32+f64",
             "data": "synthetic", "config": config, "e2e": e2e, "gpu_launches": int(launches),
             "roofline": roof, "clocks": main_rec["clocks"], "solved": main_rec["solved"], "tuning": tuning,
+            "step_ms": {"min": min(main_rec["step_ms"]), "median": statistics.median(main_rec["step_ms"]),
+                        "max": max(main_rec["step_ms"])},
             "work_per_step": {k: v / args.steps for k, v in main_rec["kinds"].items()}}
     if train is not None:
         # the whole grid's rate with the set-up (labels, training, verification map) included

@@ -615,12 +615,77 @@ struct Group {
     // Without the float-float tables, or when their residuals are not finite, every residual is
     // FP64.  The seed's iteration budget (max_iter less the FP32 phase's iterations, as the
     // reference's NLsolve counts one budget per seed) bounds the steps; a seed that spends it
-    // is not converged.  Steps that stop contracting even with fresh FP32 Jacobians hand the
-    // rest of the budget to FP64 Newton steps (FP64 Hessian passes) from the best state.
+    // is not converged.  Steps that stop contracting even with fresh float-float Jacobians
+    // hand the rest of the budget to newton_rescue from the best state.
     // The refinement stops at its first certification attempt and returns true: c.x is the
     // state to certify (certify(), at once or by a certifying warp), *th_valid whether c's
     // thermo fields are those of c.x.  False: c is final (an FP64-only refinement).
     static constexpr int kMaxRefreshJ = 12;
+
+    // The rescue of a mixed-precision seed whose refinement stopped contracting, or whose
+    // refined state the FP64 residual did not certify: Newton steps x <- x - J^-1 F with F the
+    // FP64 residual of the certification pass (the residual that accepts a root) and J the
+    // float-float Jacobian (~1e-12 relative, from the FP32 pipe), NLsolve's stop rules
+    // (||F||_inf < ftol, ||dx||_inf < xtol, non-finite values, the budget), then the outputs
+    // from the float-float thermo pass.  A Jacobian accurate to 1e-12 keeps Newton's
+    // convergence, and one certification pass plus one float-float pass cost a single warp
+    // about a third of an FP64 Hessian pass: the rescue is often the last work of a launch.
+    // Without the float-float tables it is the FP64 Newton iteration.
+    __device__ __noinline__ void newton_rescue(const PointIn &pt, const double *x0, const SolveOpts &o,
+                                               Candidate &c, int max_iter) {
+        double x[5], xold[5], p[5], F[5], Fj[5], J[25];
+        for (int i = 0; i < 5; ++i) { x[i] = x0[i]; xold[i] = qnan(); }
+        if (!eval_newton_ff(pt, x, Fj, J)) {
+            newton(pt, x0, o, c, max_iter);
+            return;
+        }
+        eval_grad64(pt, x, F);
+        c.exception = !all_finite5(F);
+        if (c.exception) {
+            for (int i = 0; i < 5; ++i) c.x[i] = x0[i];
+            c.residual_norm = qnan();
+            c.iterations = 0;
+            c.f_converged = false;
+            c.phys = false;
+            return;
+        }
+        int it = 0;
+        bool xconv = false, fconv = norm_inf5(F) < o.ftol;
+        bool stopped = any_nan5(x) || any_nan5(F);
+        bool converged = fconv;
+        while (!stopped && !converged && it < max_iter) {
+            ++it;
+            if (lu_solve5(J, F, p)) {
+                for (int i = 0; i < 5; ++i) p[i] = -p[i];
+            } else {
+                levenberg_step(J, F, p);
+            }
+            symmetrize_step(pt, x, p);
+            for (int i = 0; i < 5; ++i) { xold[i] = x[i]; x[i] += p[i]; }
+            eval_grad64(pt, x, F);
+            double dx = 0.0;
+            bool dxn = false;
+            for (int i = 0; i < 5; ++i) {
+                const double d = fabs(x[i] - xold[i]);
+                dxn |= isnan(d);
+                dx = d > dx ? d : dx;
+            }
+            xconv = !any_nan5(xold) && !dxn && dx < o.xtol;
+            fconv = norm_inf5(F) < o.ftol;
+            stopped = any_nan5(x) || any_nan5(F);
+            converged = xconv || fconv;
+            if (!stopped && !converged && it < max_iter && !eval_newton_ff(pt, x, Fj, J)) {
+                double Fd[5];
+                eval_newton(pt, x, Fd, J);  // float-float not finite here: an FP64 Jacobian
+            }
+        }
+        for (int i = 0; i < 5; ++i) c.x[i] = x[i];
+        c.residual_norm = norm_inf5(F);
+        c.iterations = it;
+        c.f_converged = fconv;
+        if (!eval_thermo_ff(pt, o, c)) eval_thermo(pt, o, c);
+    }
+
     __device__ bool refine64(const PointIn &pt, const SolveOpts &o, const double *J32, const double *x32, Candidate &c,
                              int &steps, int budget, int *th_out) {
         double F[5], Fo[5], p[5], B[25], xb[5], Jn[25];
@@ -665,7 +730,7 @@ struct Group {
             if (bad || (stalled && refresh >= kMaxRefreshJ)) {
                 const int used = steps;
                 cnt.v[kStatRescue64] += 1;
-                newton(pt, xb, o, c, budget - used);
+                newton_rescue(pt, xb, o, c, budget - used);
                 steps = used + c.iterations;
                 return false;
             }
@@ -776,8 +841,8 @@ struct Group {
 
     // FP64 certification of the refined state c.x (refine64 returned true): the root is
     // accepted when the FP64 residual ||grad_x Omega||_inf < ftol.  A state it does not
-    // certify (float-float and FP64 disagree, rare) is finished by FP64 Newton steps for the
-    // rest of the seed's budget.  `steps` counts the refinement steps on entry and on exit.
+    // certify (float-float and FP64 disagree, rare) is finished by newton_rescue for the rest
+    // of the seed's budget.  `steps` counts the refinement steps on entry and on exit.
     __device__ void certify(const PointIn &pt, const SolveOpts &o, Candidate &c, int &steps, int budget, int th_valid) {
         double F[5];
         eval_grad64(pt, c.x, F);
@@ -792,7 +857,7 @@ struct Group {
         for (int k = 0; k < 5; ++k) xs[k] = c.x[k];
         cnt.v[kStatRescue64] += 1;
         if (budget < 2) budget = 2;
-        newton(pt, xs, o, c, max(budget - steps, 1));
+        newton_rescue(pt, xs, o, c, max(budget - steps, 1));
         steps += c.iterations;
     }
 

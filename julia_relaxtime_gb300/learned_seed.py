@@ -85,6 +85,7 @@ class LearnedSeed(SeedStrategy):
         self._lib = api.lib()
         self._check(self._lib.pnjl_mlp_init(engine._ctx, int(seed)), "pnjl_mlp_init")
         self.trained = False
+        self.timings = {}
         self.last_loss = None
         self.scaling = None
         self.verify_map: VerifyMap | None = None  # where the MultiSeed candidates verify a solution
@@ -278,10 +279,16 @@ def coexistence_map(engine: GapEngine, cfg: TrainConfig, labels, *, distinct: fl
 def train_learned_seed(engine: GapEngine, cfg: TrainConfig | None = None) -> LearnedSeed:
     """Label the grid with the multi-seed solver, train the network on the labels and build its
     verification map."""
+    import time
+
     cfg = cfg or TrainConfig()
+    t0 = time.perf_counter()
     T, mu, xi, x, res = label_grid(engine, cfg)
+    t1 = time.perf_counter()
     ls = LearnedSeed(engine, seed=cfg.seed)
     ls.default_scaling(x, cfg)
     ls.fit(T, mu, xi, x, epochs=cfg.epochs, batch=cfg.batch, lr=cfg.lr, shuffle_seed=cfg.seed + 1)
+    t2 = time.perf_counter()
     ls.verify_map = coexistence_map(engine, cfg, res, gap_max=cfg.map_gap_max, jump=cfg.map_jump, grow=cfg.map_grow)
+    ls.timings = {"labels_s": t1 - t0, "fit_s": t2 - t1, "map_s": time.perf_counter() - t2}
     return ls
