@@ -623,33 +623,71 @@ struct Group {
     static constexpr int kMaxRefreshJ = 12;
 
     // The rescue of a mixed-precision seed whose refinement stopped contracting, or whose
-    // refined state the FP64 residual did not certify: Newton steps x <- x - J^-1 F with F the
-    // FP64 residual of the certification pass (the residual that accepts a root) and J the
-    // float-float Jacobian (~1e-12 relative, from the FP32 pipe), NLsolve's stop rules
-    // (||F||_inf < ftol, ||dx||_inf < xtol, non-finite values, the budget), then the outputs
-    // from the float-float thermo pass.  A Jacobian accurate to 1e-12 keeps Newton's
-    // convergence, and one certification pass plus one float-float pass cost a single warp
-    // about a third of an FP64 Hessian pass: the rescue is often the last work of a launch.
+    // refined state the FP64 residual did not certify.  Such roots are nearly singular:
+    // Newton converges on them, but linearly.  With ff_first (a stalled refinement) Newton
+    // steps run first on the float-float pass alone -- residual and Jacobian at once, ~1e-12
+    // accurate, on the FP32 pipe -- until its residual is below ftol/10 (or stops falling
+    // below ftol), as in the refinement; then Newton steps x <- x - J^-1 F with F the FP64
+    // residual of the certification pass and J the float-float Jacobian, under NLsolve's stop
+    // rules (||F||_inf < ftol, ||dx||_inf < xtol, non-finite values, the budget): at a root
+    // the first FP64 residual certifies it.  The outputs come from the float-float thermo
+    // pass.  A float-float step costs a single warp about a quarter of a certification pass
+    // and a tenth of an FP64 Hessian pass: a rescue is often the last work of a launch.
     // Without the float-float tables it is the FP64 Newton iteration.
     __device__ __noinline__ void newton_rescue(const PointIn &pt, const double *x0, const SolveOpts &o,
-                                               Candidate &c, int max_iter) {
+                                               Candidate &c, int max_iter, bool ff_first) {
         double x[5], xold[5], p[5], F[5], Fj[5], J[25];
         for (int i = 0; i < 5; ++i) { x[i] = x0[i]; xold[i] = qnan(); }
         if (!eval_newton_ff(pt, x, Fj, J)) {
             newton(pt, x0, o, c, max_iter);
             return;
         }
+        int it = 0;
+        if (ff_first) {
+            double fprev = 1e300;
+            while (it < max_iter) {
+                const double fn = norm_inf5(Fj);
+                if (!(fn == fn) || any_nan5(x)) break;
+                if (fn < 0.1 * o.ftol || (fn < o.ftol && !(fn < 0.5 * fprev))) break;
+                if (lu_solve5(J, Fj, p)) {
+                    for (int i = 0; i < 5; ++i) p[i] = -p[i];
+                } else {
+                    levenberg_step(J, Fj, p);
+                }
+                symmetrize_step(pt, x, p);
+                double dx = 0.0;
+                for (int i = 0; i < 5; ++i) {
+                    x[i] += p[i];
+                    dx = fabs(p[i]) > dx ? fabs(p[i]) : dx;
+                }
+                ++it;
+                fprev = fn;
+                if (!eval_newton_ff(pt, x, Fj, J)) {  // float-float not finite here: an FP64 Jacobian
+                    double Fd[5];
+                    eval_newton(pt, x, Fd, J);
+                    break;
+                }
+                if (!(dx >= o.xtol)) break;
+            }
+            if (any_nan5(x)) {  // back to the best state known; the FP64 steps take over
+                for (int i = 0; i < 5; ++i) x[i] = x0[i];
+                if (!eval_newton_ff(pt, x, Fj, J)) {
+                    newton(pt, x0, o, c, max(max_iter - it, 1));
+                    c.iterations += it;
+                    return;
+                }
+            }
+        }
         eval_grad64(pt, x, F);
         c.exception = !all_finite5(F);
         if (c.exception) {
             for (int i = 0; i < 5; ++i) c.x[i] = x0[i];
             c.residual_norm = qnan();
-            c.iterations = 0;
+            c.iterations = it;
             c.f_converged = false;
             c.phys = false;
             return;
         }
-        int it = 0;
         bool xconv = false, fconv = norm_inf5(F) < o.ftol;
         bool stopped = any_nan5(x) || any_nan5(F);
         bool converged = fconv;
@@ -730,7 +768,7 @@ struct Group {
             if (bad || (stalled && refresh >= kMaxRefreshJ)) {
                 const int used = steps;
                 cnt.v[kStatRescue64] += 1;
-                newton_rescue(pt, xb, o, c, budget - used);
+                newton_rescue(pt, xb, o, c, budget - used, true);
                 steps = used + c.iterations;
                 return false;
             }
@@ -857,7 +895,7 @@ struct Group {
         for (int k = 0; k < 5; ++k) xs[k] = c.x[k];
         cnt.v[kStatRescue64] += 1;
         if (budget < 2) budget = 2;
-        newton_rescue(pt, xs, o, c, max(budget - steps, 1));
+        newton_rescue(pt, xs, o, c, max(budget - steps, 1), false);
         steps += c.iterations;
     }
 

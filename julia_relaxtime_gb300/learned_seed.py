@@ -35,8 +35,8 @@ class TrainConfig:
     mu_MeV: tuple = (0.0, 400.0, 64)
     xi: tuple = (-0.5, 0.5, 5)
     epochs: int = 400
-    batch: int = 512
-    lr: float = 2e-3
+    batch: int = 1024
+    lr: float = 3e-3
     seed: int = 20240611
     label_seeds: int = 6          # MultiSeed candidates used to label the grid
     label_precision: str = "mixed"
@@ -222,6 +222,39 @@ def candidate_roots(engine: GapEngine, cfg: TrainConfig):
     return np.stack(roots, axis=1), np.stack(omegas, axis=1)
 
 
+def candidates_and_labels(engine: GapEngine, cfg: TrainConfig):
+    """Every MultiSeed candidate alone at every label-grid point, in ONE launch (S x N points,
+    each with its candidate as the per-point seed, no fallback), and the labels the MultiSeed
+    solve would give: at each point the converged candidate of lowest Omega, the earliest among
+    Omegas within omega_tie_rtol (solve_multi, ImplicitSolver.jl:532-559).  Returns
+    (roots [N, S, 5] NaN where not converged, omegas [N, S], labels {"x", "converged", "omega"})."""
+    T, mu, xi = grid_points(cfg)
+    mu3 = np.asarray(flavour_mu(cfg, mu), dtype=np.float64)
+    table, hot = label_table(cfg)
+    S, N = table.shape[0], T.size
+    hot_pt = T * HBARC_MEV_FM >= 300.0  # DefaultSeed's hot row (SeedStrategies.jl:212-220)
+    seeds = np.where(hot_pt[None, :, None], hot[:, None, :], table[:, None, :]).reshape(-1, 5)
+    mu_all = np.tile(mu3, S) if mu3.ndim == 1 else np.tile(mu3, (S, 1))
+    opts = SolveOptions(iterations=40, ftol=1e-10, precision=cfg.label_precision, auto_multiseed_fallback=False)
+    r = engine.solve(np.tile(T, S), mu_all, np.tile(xi, S), seed_table=table, seed_table_hot=hot,
+                     point_seeds=seeds, opts=opts)
+    conv = np.asarray(r["converged"], dtype=bool).reshape(S, N)
+    x = np.asarray(r["x"]).reshape(S, N, 5)
+    om = np.asarray(r["omega"]).reshape(S, N)
+    roots = np.where(conv[:, :, None], x, np.nan).transpose(1, 0, 2)
+    omegas = np.where(conv, om, np.nan).T
+    lab_x = np.full((N, 5), np.nan)
+    lab_om = np.full(N, np.nan)
+    lab_ok = np.zeros(N, dtype=bool)
+    tie = SolveOptions().omega_tie_rtol
+    for s_ in range(S):  # seed order: a later seed replaces the kept one only when clearly lower
+        better = conv[s_] & (~lab_ok | (om[s_] < lab_om - tie * np.abs(lab_om)))
+        lab_x[better] = x[s_][better]
+        lab_om[better] = om[s_][better]
+        lab_ok |= conv[s_]
+    return roots, omegas, {"x": lab_x, "converged": lab_ok, "omega": lab_om}
+
+
 def coexistence_map(engine: GapEngine, cfg: TrainConfig, labels, *, distinct: float = 0.05, gap_max: float = 1.0,
                     jump: float = 0.25, grow: int = 1, roots=None) -> VerifyMap:
     """Verification map on the label grid's cells.  A grid node is flagged where two MultiSeed
@@ -283,12 +316,17 @@ def train_learned_seed(engine: GapEngine, cfg: TrainConfig | None = None) -> Lea
 
     cfg = cfg or TrainConfig()
     t0 = time.perf_counter()
-    T, mu, xi, x, res = label_grid(engine, cfg)
+    # labels and every candidate's own root (the verification map's input) from one launch
+    R, Om, res = candidates_and_labels(engine, cfg)
+    Tg, mug, xig = grid_points(cfg)
+    ok = res["converged"]
+    T, mu, xi, x = Tg[ok], mug[ok], xig[ok], res["x"][ok]
     t1 = time.perf_counter()
     ls = LearnedSeed(engine, seed=cfg.seed)
     ls.default_scaling(x, cfg)
     ls.fit(T, mu, xi, x, epochs=cfg.epochs, batch=cfg.batch, lr=cfg.lr, shuffle_seed=cfg.seed + 1)
     t2 = time.perf_counter()
-    ls.verify_map = coexistence_map(engine, cfg, res, gap_max=cfg.map_gap_max, jump=cfg.map_jump, grow=cfg.map_grow)
-    ls.timings = {"labels_s": t1 - t0, "fit_s": t2 - t1, "map_s": time.perf_counter() - t2}
+    ls.verify_map = coexistence_map(engine, cfg, res, roots=(R, Om), gap_max=cfg.map_gap_max, jump=cfg.map_jump,
+                                    grow=cfg.map_grow)
+    ls.timings = {"labels_and_candidates_s": t1 - t0, "fit_s": t2 - t1, "map_s": time.perf_counter() - t2}
     return ls

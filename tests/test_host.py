@@ -414,3 +414,35 @@ def test_training_box_of_the_first_order_scan():
     s0, c0 = box_scaling(TrainConfig())
     np.testing.assert_allclose(s0, [175.0 / HBARC, 200.0 / HBARC, 0.0], rtol=1e-14, atol=1e-15)
     np.testing.assert_allclose(c0, [125.0 / HBARC, 200.0 / HBARC, 0.5], rtol=1e-14)
+
+
+def test_candidates_and_labels_select_like_solve_multi():
+    """The one-launch labels: every candidate alone as a per-point seed, then per point the
+    converged candidate of lowest Omega, the earliest among Omegas within the tie tolerance
+    (solve_multi, ImplicitSolver.jl:532-559); hot rows at T >= 300 MeV."""
+    from julia_relaxtime_gb300.learned_seed import TrainConfig, candidates_and_labels
+
+    cfg = TrainConfig(T_MeV=(250.0, 300.0, 2), mu_MeV=(0.0, 100.0, 2), xi=(0.0, 0.0, 1), label_seeds=3)
+    N, S = 4, 3
+    om = np.array([[-5.0, -5.0, -7.0, np.nan], [-6.0, -5.0 - 1e-13, -7.5, -1.0], [-6.0, -4.0, -7.5 + 1e-14, -2.0]])
+    conv = ~np.isnan(om)
+
+    class FakeEngine:
+        def solve(self, T, mu, xi, *, seed_table, seed_table_hot, point_seeds, opts):
+            assert T.size == S * N and point_seeds.shape == (S * N, 5) and not opts.auto_multiseed_fallback
+            self.seeds = point_seeds.reshape(S, N, 5)
+            x = np.repeat(np.arange(S * N, dtype=float)[:, None], 5, axis=1)
+            return {"converged": conv.ravel(), "x": x, "omega": np.nan_to_num(om, nan=0.0).ravel()}
+
+    eng = FakeEngine()
+    R, Om, lab = candidates_and_labels(eng, cfg)
+    assert R.shape == (N, S, 5) and Om.shape == (N, S)
+    # point 0: seed 1 (-6) beats seed 0 (-5), seed 2 ties seed 1 -> seed 1; point 1: seed 1 is
+    # within the tie of seed 0 -> seed 0; point 2: seed 1; point 3: seed 2 (-2 < -1)
+    assert list(lab["x"][:, 0].astype(int)) == [1 * N + 0, 0 * N + 1, 1 * N + 2, 2 * N + 3]
+    assert lab["converged"].all()
+    # the hot table's rows at T = 300 MeV (points 2, 3 of the T-major grid)
+    from julia_relaxtime_gb300.learned_seed import label_table
+
+    table, hot = label_table(cfg)
+    assert np.array_equal(eng.seeds[:, 0], table) and np.array_equal(eng.seeds[:, 3], hot)
