@@ -620,7 +620,20 @@ struct Group {
     // The refinement stops at its first certification attempt and returns true: c.x is the
     // state to certify (certify(), at once or by a certifying warp), *th_valid whether c's
     // thermo fields are those of c.x.  False: c is final (an FP64-only refinement).
+    // Plateau: with `bound` (the Omega of a certified candidate of the same point that this
+    // seed must beat; NaN when there is none) a seed whose float-float Newton steps -- fresh
+    // float-float Jacobians -- have twice in a row failed to halve a residual still above
+    // 1e3 ftol is abandoned, not converged, when the Omega of its best state lies above the
+    // bound by more than 1e-4 |bound|.  Such a state is a spinodal ghost: just past the
+    // point where a metastable root merges with the unstable branch, |grad Omega| has a
+    // minimum of ~1e-6 and no root; FP64 Newton from the same seed stalls on it for its whole
+    // budget (and so does its trust-region fallback), and the candidate ends unconverged
+    // either way.  Continuing could only change the min-Omega selection by reaching a root
+    // more than 1e-4 |bound| below the state's Omega from a point where |grad Omega| is a few
+    // 1e-6.  The test costs one float-float thermo pass, once per seed.
     static constexpr int kMaxRefreshJ = 12;
+    static constexpr int kPlateauSteps = 2;
+    static constexpr double kPlateauFtol = 1e3;
 
     // The rescue of a mixed-precision seed whose refinement stopped contracting, or whose
     // refined state the FP64 residual did not certify.  Such roots are nearly singular:
@@ -725,8 +738,11 @@ struct Group {
     }
 
     __device__ bool refine64(const PointIn &pt, const SolveOpts &o, const double *J32, const double *x32, Candidate &c,
-                             int &steps, int budget, int *th_out) {
+                             int &steps, int budget, int *th_out, double bound) {
         double F[5], Fo[5], p[5], B[25], xb[5], Jn[25];
+        bool fresh = false;    // the last step used a float-float Jacobian computed at its start
+        int plateau = 0;       // consecutive such steps that did not halve the residual
+        bool judged = !(bound == bound);  // the plateau test has run (or cannot)
         for (int i = 0; i < 25; ++i) B[i] = J32[i];
         for (int i = 0; i < 5; ++i) c.x[i] = xb[i] = x32[i];
         c.exception = false;
@@ -765,6 +781,21 @@ struct Group {
                 if (!is64) { eval_grad64(pt, c.x, F); c.residual_norm = norm_inf5(F); }
                 break;
             }
+            if (stalled && fresh) ++plateau;
+            else if (!stalled) plateau = 0;
+            if (!judged && plateau >= kPlateauSteps && fb > kPlateauFtol * o.ftol) {
+                judged = true;  // the plateau test (see above), at the best state
+                double xc[5];
+                for (int i = 0; i < 5; ++i) { xc[i] = c.x[i]; c.x[i] = xb[i]; }
+                if (eval_thermo_ff(pt, o, c) && c.omega > bound + kPruneTightRtol * fmax(fabs(bound), 1.0)) {
+                    cnt.v[kStatPruned] += 1;
+                    c.f_converged = false;
+                    c.residual_norm = fb;
+                    return false;
+                }
+                for (int i = 0; i < 5; ++i) c.x[i] = xc[i];
+                th_valid = false;
+            }
             if (bad || (stalled && refresh >= kMaxRefreshJ)) {
                 const int used = steps;
                 cnt.v[kStatRescue64] += 1;
@@ -772,12 +803,14 @@ struct Group {
                 steps = used + c.iterations;
                 return false;
             }
+            fresh = false;
             if (stalled) {
                 // a Newton step with the float-float Jacobian at x (its residual replaces F:
                 // same accuracy); without float-float, a fresh FP32 Jacobian
                 double Fn[5];
                 if (use_ff && eval_newton_ff(pt, c.x, Fn, Jn)) {
                     for (int i = 0; i < 5; ++i) F[i] = Fn[i];
+                    fresh = true;
                 } else {
                     eval_newton32(pt, c.x, Fn, Jn);
                 }
@@ -853,7 +886,7 @@ struct Group {
             s.steps = 0;
             // only where the result may be verified; J32 before the refinement's Broyden updates
             s.unstable = o.verify_seeds > 0 && dd.per_point() && det5_negative(J32) ? 1 : 0;
-            if (refine64(pt, o, J32, x32, out, s.steps, o.max_iter - it32, &s.th_valid)) {
+            if (refine64(pt, o, J32, x32, out, s.steps, o.max_iter - it32, &s.th_valid, dd.omega_bound())) {
                 for (int k = 0; k < 5; ++k) s.x32[k] = x32[k];
                 s.it32 = it32;
                 if (cs) {
@@ -930,7 +963,8 @@ struct Group {
                 Candidate f;
                 const bool unst = o.verify_seeds > 0 && dd.per_point() && det5_negative(K32);
                 int st = 0, th = 0;
-                if (refine64(pt, o, K32, y32, f, st, o.max_iter - itt, &th)) certify(pt, o, f, st, o.max_iter - itt, th);
+                if (refine64(pt, o, K32, y32, f, st, o.max_iter - itt, &th, dd.omega_bound()))
+                    certify(pt, o, f, st, o.max_iter - itt, th);
                 f.iterations = itt + st;
                 f.unstable = unst;
                 if (cand_good(f, o.residual_norm_max)) dd.publish(y32);
