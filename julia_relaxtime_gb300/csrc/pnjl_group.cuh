@@ -620,20 +620,28 @@ struct Group {
     // The refinement stops at its first certification attempt and returns true: c.x is the
     // state to certify (certify(), at once or by a certifying warp), *th_valid whether c's
     // thermo fields are those of c.x.  False: c is final (an FP64-only refinement).
-    // Plateau: with `bound` (the Omega of a certified candidate of the same point that this
-    // seed must beat; NaN when there is none) a seed whose float-float Newton steps -- fresh
-    // float-float Jacobians -- have twice in a row failed to halve a residual still above
-    // 1e3 ftol is abandoned, not converged, when the Omega of its best state lies above the
-    // bound by more than 1e-4 |bound|.  Such a state is a spinodal ghost: just past the
-    // point where a metastable root merges with the unstable branch, |grad Omega| has a
-    // minimum of ~1e-6 and no root; FP64 Newton from the same seed stalls on it for its whole
-    // budget (and so does its trust-region fallback), and the candidate ends unconverged
-    // either way.  Continuing could only change the min-Omega selection by reaching a root
-    // more than 1e-4 |bound| below the state's Omega from a point where |grad Omega| is a few
-    // 1e-6.  The test costs one float-float thermo pass, once per seed.
+    // `bound` is the Omega of a certified candidate of the same point that this seed must
+    // beat (NaN when there is none).  Two tests drop a seed that cannot win, not converged:
+    // * Omega prune: a state reached by a contracting step (residual halved, now below 1e-5)
+    //   whose float-float Omega -- computed at every step with the residual -- lies above the
+    //   bound by more than 1e-9 |bound| plus 20 |F|inf |p|inf (p the last step): Newton's
+    //   remaining path to the root is at most a few such steps long, |grad Omega| below |F|
+    //   on it, so the root's Omega stays above the bound.  This drops the metastable roots of
+    //   verification seeds before their FP64 certification.
+    // * Plateau: float-float Newton steps with fresh float-float Jacobians have twice in a row
+    //   failed to halve a residual still above 1e3 ftol.  Such a state is a spinodal ghost:
+    //   just past the point where a metastable root merges with the unstable branch,
+    //   |grad Omega| has a minimum of ~1e-6 and no root; FP64 Newton from the same seed stalls
+    //   on it for its whole budget (and so does its trust-region fallback), and the candidate
+    //   ends unconverged either way.  The seed is abandoned when the Omega of its best state
+    //   lies above the bound by more than 1e-4 |bound| (continuing could only change the
+    //   selection by reaching a root that far below from a point where |grad Omega| is a few
+    //   1e-6), or at once with `give_up` -- a per-point seed whose point the MultiSeed
+    //   candidates judge when it fails (the learned seed).  One float-float thermo pass, once.
     static constexpr int kMaxRefreshJ = 12;
     static constexpr int kPlateauSteps = 2;
     static constexpr double kPlateauFtol = 1e3;
+    static constexpr double kPruneNear = 1e-5, kPruneFFRtol = 1e-9, kPruneFFSlack = 20.0;
 
     // The rescue of a mixed-precision seed whose refinement stopped contracting, or whose
     // refined state the FP64 residual did not certify.  Such roots are nearly singular:
@@ -738,11 +746,12 @@ struct Group {
     }
 
     __device__ bool refine64(const PointIn &pt, const SolveOpts &o, const double *J32, const double *x32, Candidate &c,
-                             int &steps, int budget, int *th_out, double bound) {
+                             int &steps, int budget, int *th_out, double bound, bool give_up) {
         double F[5], Fo[5], p[5], B[25], xb[5], Jn[25];
+        double plast = 0.0;    // |p|inf of the last step
         bool fresh = false;    // the last step used a float-float Jacobian computed at its start
         int plateau = 0;       // consecutive such steps that did not halve the residual
-        bool judged = !(bound == bound);  // the plateau test has run (or cannot)
+        bool judged = !give_up && !(bound == bound);  // the plateau test has run (or cannot)
         for (int i = 0; i < 25; ++i) B[i] = J32[i];
         for (int i = 0; i < 5; ++i) c.x[i] = xb[i] = x32[i];
         c.exception = false;
@@ -771,6 +780,12 @@ struct Group {
                 for (int i = 0; i < 5; ++i) xb[i] = c.x[i];
                 fb = fn;
             }
+            if (!bad && !is64 && th_valid && bound == bound && steps > 0 && fn < kPruneNear && fn < 0.5 * fprev &&
+                c.omega > bound + kPruneFFRtol * fmax(fabs(bound), 1.0) + kPruneFFSlack * fn * fmax(plast, 1e-3)) {
+                cnt.v[kStatPruned] += 1;  // the Omega prune (see above)
+                c.f_converged = false;
+                return false;
+            }
             if (!bad && !is64 && (fn < 0.1 * o.ftol || (fn < o.ftol && !(fn < 0.5 * fprev)))) {
                 *th_out = th_valid ? 1 : 0;  // certification attempt at the current state
                 return true;
@@ -787,7 +802,7 @@ struct Group {
                 judged = true;  // the plateau test (see above), at the best state
                 double xc[5];
                 for (int i = 0; i < 5; ++i) { xc[i] = c.x[i]; c.x[i] = xb[i]; }
-                if (eval_thermo_ff(pt, o, c) && c.omega > bound + kPruneTightRtol * fmax(fabs(bound), 1.0)) {
+                if (eval_thermo_ff(pt, o, c) && (give_up || c.omega > bound + kPruneTightRtol * fmax(fabs(bound), 1.0))) {
                     cnt.v[kStatPruned] += 1;
                     c.f_converged = false;
                     c.residual_norm = fb;
@@ -824,7 +839,12 @@ struct Group {
                 levenberg_step(B, F, p);
             }
             symmetrize_step(pt, c.x, p);
-            for (int i = 0; i < 5; ++i) { c.x[i] += p[i]; Fo[i] = F[i]; }
+            plast = 0.0;
+            for (int i = 0; i < 5; ++i) {
+                c.x[i] += p[i];
+                Fo[i] = F[i];
+                plast = fabs(p[i]) > plast ? fabs(p[i]) : plast;
+            }
             ++steps;
             // after a correction step the state is usually final: the float-float pass also
             // returns the outputs at it
@@ -886,7 +906,8 @@ struct Group {
             s.steps = 0;
             // only where the result may be verified; J32 before the refinement's Broyden updates
             s.unstable = o.verify_seeds > 0 && dd.per_point() && det5_negative(J32) ? 1 : 0;
-            if (refine64(pt, o, J32, x32, out, s.steps, o.max_iter - it32, &s.th_valid, dd.omega_bound())) {
+            if (refine64(pt, o, J32, x32, out, s.steps, o.max_iter - it32, &s.th_valid, dd.omega_bound(),
+                         o.verify_seeds > 0 && dd.per_point())) {
                 for (int k = 0; k < 5; ++k) s.x32[k] = x32[k];
                 s.it32 = it32;
                 if (cs) {
@@ -963,7 +984,7 @@ struct Group {
                 Candidate f;
                 const bool unst = o.verify_seeds > 0 && dd.per_point() && det5_negative(K32);
                 int st = 0, th = 0;
-                if (refine64(pt, o, K32, y32, f, st, o.max_iter - itt, &th, dd.omega_bound()))
+                if (refine64(pt, o, K32, y32, f, st, o.max_iter - itt, &th, dd.omega_bound(), o.verify_seeds > 0 && dd.per_point()))
                     certify(pt, o, f, st, o.max_iter - itt, th);
                 f.iterations = itt + st;
                 f.unstable = unst;
