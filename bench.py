@@ -19,7 +19,7 @@ network's seed per point (BF16 tensor-core inference kernel), one mixed-precisio
 where a second phase can exist (the cells of the network's verification map, roots far from
 the seed, roots on an unstable branch), MultiSeed fallback where the learned seed fails.  The
 network is trained in an untimed set-up on this GPU (labels: a 64 x 64 x 5 (T, mu, xi)
-multi-seed solve over the workload's box; 400 epochs), reported as ``surrogate.train``, and
+multi-seed solve over the workload's box; 300 epochs), reported as ``surrogate.train``, and
 ``surrogate.amortised`` is the whole grid's rate with that set-up included.  The same chunks
 are then solved by the plain FP64 multi-seed Newton (the workload's candidates, min-Omega
 selection, trust-region fallback): ``plain_fp64`` holds its rate, the speed-up, and the phase
@@ -570,9 +570,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-parity", action="store_true", help="skip the oracle check of the arms' roots")
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default launch shape")
-    ap.add_argument("--train-epochs", type=int, default=None, help="training epochs of the network (default 400)")
-    ap.add_argument("--train-batch", type=int, default=None, help="training batch (default 512)")
-    ap.add_argument("--train-lr", type=float, default=None, help="peak learning rate (default 2e-3)")
+    ap.add_argument("--train-epochs", type=int, default=None, help="training epochs of the network (default 300)")
+    ap.add_argument("--train-batch", type=int, default=None, help="training batch (default 1024)")
+    ap.add_argument("--train-lr", type=float, default=None, help="peak learning rate (default 4e-3)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -34,9 +34,9 @@ class TrainConfig:
     T_MeV: tuple = (50.0, 300.0, 64)
     mu_MeV: tuple = (0.0, 400.0, 64)
     xi: tuple = (-0.5, 0.5, 5)
-    epochs: int = 400
+    epochs: int = 300
     batch: int = 1024
-    lr: float = 3e-3
+    lr: float = 4e-3
     seed: int = 20240611
     label_seeds: int = 6          # MultiSeed candidates used to label the grid
     label_precision: str = "mixed"
