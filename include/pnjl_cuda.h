@@ -439,9 +439,9 @@ int pnjl_derivs_batch_device(pnjl_ctx *ctx, int64_t n, const double *d_x, const 
  * counters, queue head, node and seed tables) is one static device array of about 6 MB that
  * every GPU loading this library holds until exit; batches beyond PNJL_NOALLOC_MAX_TASKS
  * tasks return PNJL_ERR_TOO_LARGE.  The call is asynchronous on `stream` (NULL = the legacy
- * default stream) and runs on the current device.  Its first call on a device looks up the
- * array's device address (cudaGetSymbolAddress) and loads the kernel module, so make that
- * first call before any stream capture.  All calls share the one array and it keeps the last
+ * default stream) and runs on the current device.  Its first call on a device also looks up
+ * the array's device address (cudaGetSymbolAddress) and loads the kernel module.  All calls
+ * share the one array and it keeps the last
  * call's contents (the counters are cleared by each call): calls that overlap on the GPU --
  * on two streams, or from two threads -- race and must not be issued. */
 int pnjl_solve_batch_noalloc(const pnjl_params *params, int32_t p_num, int32_t t_num, double p_max, int64_t n,
