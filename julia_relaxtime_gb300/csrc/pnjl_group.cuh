@@ -618,8 +618,10 @@ struct Group {
     // is not converged.  Steps that stop contracting even with fresh float-float Jacobians
     // hand the rest of the budget to newton_rescue from the best state.
     // The refinement stops at its first certification attempt and returns true: c.x is the
-    // state to certify (certify(), at once or by a certifying warp), *th_valid whether c's
-    // thermo fields are those of c.x.  False: c is final (an FP64-only refinement).
+    // state to certify (certify(), at once or by a certifying warp), *th_out whether c's
+    // thermo fields are those of c.x.  False: c is final; *th_out = -1 when the Omega prune
+    // below dropped the seed (its Newton iteration converges, so, as in the reference, no
+    // trust-region fallback follows).
     // `bound` is the Omega of a certified candidate of the same point that this seed must
     // beat (NaN when there is none).  Two tests drop a seed that cannot win, not converged:
     // * Omega prune: a state reached by a contracting step (residual halved, now below 1e-5)
@@ -784,6 +786,7 @@ struct Group {
                 c.omega > bound + kPruneFFRtol * fmax(fabs(bound), 1.0) + kPruneFFSlack * fn * fmax(plast, 1e-3)) {
                 cnt.v[kStatPruned] += 1;  // the Omega prune (see above)
                 c.f_converged = false;
+                *th_out = -1;  // converging to a root that cannot win: no fallback either
                 return false;
             }
             if (!bad && !is64 && (fn < 0.1 * o.ftol || (fn < o.ftol && !(fn < 0.5 * fprev)))) {
@@ -904,6 +907,7 @@ struct Group {
             if (!cs) dd.pending(x32);
             CertState s;
             s.steps = 0;
+            s.th_valid = 0;
             // only where the result may be verified; J32 before the refinement's Broyden updates
             s.unstable = o.verify_seeds > 0 && dd.per_point() && det5_negative(J32) ? 1 : 0;
             if (refine64(pt, o, J32, x32, out, s.steps, o.max_iter - it32, &s.th_valid, dd.omega_bound(),
@@ -919,6 +923,7 @@ struct Group {
             }
             out.iterations = it32 + s.steps;
             dd.withdraw();
+            if (s.th_valid < 0) { dup = true; converged = false; return false; }  // cannot win
         } else {
             for (int i = 0; i < 5; ++i) out.x[i] = x32[i];
             out.f_converged = false;
