@@ -621,7 +621,7 @@ struct Group {
     // state to certify (certify(), at once or by a certifying warp), *th_out whether c's
     // thermo fields are those of c.x.  False: c is final; *th_out = -1 when the Omega prune
     // below dropped the seed (its Newton iteration converges, so, as in the reference, no
-    // trust-region fallback follows).
+    // trust-region fallback follows), -2 / -3 for the give-up and plateau exits.
     // `bound` is the Omega of a certified candidate of the same point that this seed must
     // beat (NaN when there is none).  Two tests drop a seed that cannot win, not converged:
     // * Omega prune: a state reached by a contracting step (residual halved, now below 1e-5)
@@ -640,7 +640,15 @@ struct Group {
     //   selection by reaching a root that far below from a point where |grad Omega| is a few
     //   1e-6), or at once with `give_up` -- a per-point seed whose point the MultiSeed
     //   candidates judge when it fails (the learned seed).  One float-float thermo pass, once.
+    //   Its trust-region fallback then skips a result on the same plateau (seed_fallback).
+    // * Give-up: with `give_up` the seed is also abandoned when it still stalls after
+    //   kGiveUpRefresh float-float Jacobians (a slowly converging, nearly singular root): the
+    //   learned seed is a stand-in for the MultiSeed initial guess, and where it is slow the
+    //   MultiSeed candidates decide, as the reference does (no trust-region run of the learned
+    //   seed itself).
+    // *th_out on these exits: -2 the per-point seed gave up, -3 a plateau above the bound.
     static constexpr int kMaxRefreshJ = 12;
+    static constexpr int kGiveUpRefresh = 3;
     static constexpr int kPlateauSteps = 2;
     static constexpr double kPlateauFtol = 1e3;
     static constexpr double kPruneNear = 1e-5, kPruneFFRtol = 1e-9, kPruneFFSlack = 20.0;
@@ -801,7 +809,8 @@ struct Group {
             }
             if (stalled && fresh) ++plateau;
             else if (!stalled) plateau = 0;
-            if (!judged && plateau >= kPlateauSteps && fb > kPlateauFtol * o.ftol) {
+            const bool slow = give_up && stalled && refresh >= kGiveUpRefresh;
+            if (!judged && ((plateau >= kPlateauSteps && fb > kPlateauFtol * o.ftol) || slow)) {
                 judged = true;  // the plateau test (see above), at the best state
                 double xc[5];
                 for (int i = 0; i < 5; ++i) { xc[i] = c.x[i]; c.x[i] = xb[i]; }
@@ -809,6 +818,7 @@ struct Group {
                     cnt.v[kStatPruned] += 1;
                     c.f_converged = false;
                     c.residual_norm = fb;
+                    *th_out = give_up ? -2 : -3;
                     return false;
                 }
                 for (int i = 0; i < 5; ++i) c.x[i] = xc[i];
@@ -923,7 +933,14 @@ struct Group {
             }
             out.iterations = it32 + s.steps;
             dd.withdraw();
-            if (s.th_valid < 0) { dup = true; converged = false; return false; }  // cannot win
+            if (s.th_valid == -1) { dup = true; converged = false; return false; }  // cannot win
+            if (s.th_valid == -2) { converged = false; return false; }  // the MultiSeed candidates decide
+            if (s.th_valid == -3) {  // a plateau above the bound: skip a fallback root on it
+                double xp[5];
+                for (int k = 0; k < 5; ++k) xp[k] = out.x[k];
+                seed_fallback(pt, x0, o, out, converged, dd, xp);
+                return false;
+            }
         } else {
             for (int i = 0; i < 5; ++i) out.x[i] = x32[i];
             out.f_converged = false;
@@ -973,16 +990,22 @@ struct Group {
 
     // The reference's trust-region fallback for an unusable Newton result
     // (ImplicitSolver.jl:130-151, FP32 passes here) and the seed's final verdict.
+    // With `plateau` (the state where the Newton result was abandoned on a plateau above the
+    // bound), a trust-region result within 1e-3 of it is on the same plateau and is not
+    // refined: its Omega is as far above the bound.
     template <class D>
     __device__ void seed_fallback(const PointIn &pt, const double *x0, const SolveOpts &o, Candidate &out,
-                                  bool &converged, D &dd) {
+                                  bool &converged, D &dd, const double *plateau = nullptr) {
         if (!cand_good(out, o.residual_norm_max) && o.trust_region_fallback) {
             cnt.v[kStatTrRuns] += 1;
             double y32[5], K32[25];
             int itt = 0;
             if (tr32(pt, x0, o, y32, K32, itt) > 0 && !dd.seen(y32)) {
                 dd.remember(y32);
-                if (cannot_win(pt, y32, dd.omega_bound())) {  // the Newton result stays, unusable
+                bool same = plateau != nullptr;
+                for (int k = 0; k < 5 && same; ++k) same = fabs(y32[k] - plateau[k]) <= 1e-3 * (1.0 + fabs(plateau[k]));
+                if (same || cannot_win(pt, y32, dd.omega_bound())) {  // the Newton result stays, unusable
+                    if (same) cnt.v[kStatPruned] += 1;
                     converged = false;
                     return;
                 }
@@ -1076,9 +1099,12 @@ struct LocalRoots {
 // Waits point only to earlier seeds that are certifying, which wait for nothing before their
 // verdict, so every wait ends.  omega_bound() is the per-point candidate's Omega (verification mode)
 // -- a bound fixed before any task of the slot starts, so which candidates are discarded as
-// unable to win does not depend on timing; in MultiSeed table mode there is none.  The leader
-// lane reads and writes; answers are broadcast.  With roots = null (a per-point seed, which
-// has no slot) it is LocalRoots alone.
+// unable to win does not depend on timing; in MultiSeed table mode there is none.  (A bound
+// from the seeds of the slot certified so far was tried: with it a candidate dropped on a
+// plateau in one run could, in a run where that bound came later, leave the plateau and
+// reach a root tied with the minimum -- 18 of 3,000 points chose another of the tied seeds
+// between launch forms.)  The leader lane reads and writes; answers are broadcast.  With
+// roots = null (a per-point seed, which has no slot) it is LocalRoots alone.
 struct PublishedRoots {
     double *roots;        // [slots*S*5]
     int *flag;            // [slots*S]
