@@ -737,6 +737,8 @@ static pnjl::SolveArgs chunk_args(const pnjl::SolveArgs &a, int64_t lo, int64_t 
     c.done = sh(a.done, 1);
     c.roots = sh(a.roots, 5 * S);
     c.root_flag = sh(a.root_flag, S);
+    c.anchor_state = sh(a.anchor_state, 1);
+    c.anchor_omega = sh(a.anchor_omega, 1);
     c.list = sh(a.list, 1);
     c.list_mode = sh(a.list_mode, 1);
     c.queue = ctrl3;
@@ -774,8 +776,9 @@ static size_t solve_scratch_bytes(int64_t n, const pnjl_solve_opts *o) {
         return al256(nn * sizeof(int)) + nn * o->n_seeds * sizeof(pnjl::CandRec);
     if (mixed && S > 0)
         return al256(nn * sizeof(int)) + al256(nn * S * sizeof(int)) + al256(nn * sizeof(int)) +
-               al256(nn * (S + 1) * sizeof(int)) + al256(nn * (S + 1) * sizeof(pnjl::CandRec)) +
-               al256(nn * S * 5 * sizeof(double)) + al256(nn * sizeof(long long)) +
+               al256(nn * (S + 1) * sizeof(int)) + al256(nn * sizeof(int)) +
+               al256(nn * (S + 1) * sizeof(pnjl::CandRec)) + al256(nn * S * 5 * sizeof(double)) +
+               al256(nn * sizeof(long long)) + al256(nn * sizeof(double)) +
                al256(nn * (S + 1) * sizeof(pnjl::CertJob));
     return 0;
 }
@@ -803,6 +806,7 @@ static cudaError_t solve_enqueue(const pnjl_ctx *ctx, const pnjl::KernelNodes &n
         const size_t nn = (size_t)n;
         const size_t b_done = al256(nn * sizeof(int)), b_flag = al256(nn * S * sizeof(int));
         const size_t b_mode = al256(nn * sizeof(int)), b_ready = al256(nn * (S + 1) * sizeof(int));
+        const size_t b_anchor = al256(nn * sizeof(int));
         const size_t b_cand = al256(nn * (S + 1) * sizeof(pnjl::CandRec)), b_roots = al256(nn * S * 5 * sizeof(double));
         const size_t b_list = al256(nn * sizeof(long long));
         unsigned char *q = r.scratch;
@@ -814,15 +818,20 @@ static cudaError_t solve_enqueue(const pnjl_ctx *ctx, const pnjl::KernelNodes &n
         q += b_mode;
         a.job_ready = (int *)q;
         q += b_ready;
+        a.anchor_state = (int *)q;
+        q += b_anchor;
         a.cand = (pnjl::CandRec *)q;
         q += b_cand;
         a.roots = (double *)q;
         q += b_roots;
         a.list = (long long *)q;
         q += b_list;
+        a.anchor_omega = (double *)q;
+        q += al256(nn * sizeof(double));
         a.jobs = (pnjl::CertJob *)q;
-        // done, root_flag, list_mode and job_ready are adjacent: one memset clears them
-        if ((e = cudaMemsetAsync(r.scratch, 0, b_done + b_flag + b_mode + b_ready, s)) != cudaSuccess) return e;
+        // done, root_flag, list_mode, job_ready and anchor_state are adjacent: one memset clears them
+        if ((e = cudaMemsetAsync(r.scratch, 0, b_done + b_flag + b_mode + b_ready + b_anchor, s)) != cudaSuccess)
+            return e;
     }
     if ((e = cudaMemsetAsync(r.ctrl, 0, pnjl::kCtrlSlots * sizeof(long long), s)) != cudaSuccess) return e;
     a.P = ctx->dp;

@@ -49,6 +49,21 @@ __device__ __forceinline__ double qnan() { return __longlong_as_double(0x7ff8000
 
 __device__ __forceinline__ bool same_root(const double *x, const double *y);
 
+// The plateau bound of a slot that has no per-point root (MultiSeed table and fallback
+// mode): the Omega of the slot's seed 0 once that seed is certified usable.  Seeds s > 0 wait
+// for seed 0's verdict (bounded by `polls` sleeps of 128 ns; a wait that runs out is counted
+// and leaves the seed without a bound) only when their Newton refinement reaches a plateau,
+// on the warp that runs the task.  Seed 0 waits for no later seed, and its task was taken
+// before theirs (tasks are taken in order) by a warp that runs it to its end or queues its
+// certification for the certifying warps, which never wait here; so every wait ends.  The
+// bound is fixed per slot: what it drops does not depend on timing.
+struct Anchor {
+    const int *state;      // the slot's anchor_state
+    const double *omega;   // the slot's anchor_omega
+    unsigned polls;
+};
+constexpr unsigned kAnchorSleepNs = 128;
+
 template <int G>
 struct Group {
     const DevParams &P;
@@ -603,6 +618,26 @@ struct Group {
         return fr < kLoose32 ? 1 : 0;
     }
 
+    // Seed 0's certified Omega for the plateau test of a slot without a per-point root (NaN:
+    // seed 0 is not usable, or the wait ran out).
+    __device__ double anchor_bound(const Anchor &an) {
+        double b = qnan();
+        if (gl == 0) {
+            int st = *(volatile const int *)an.state;
+            for (unsigned k = 0; st == 0 && k < an.polls; ++k) {
+                __nanosleep(kAnchorSleepNs);
+                st = *(volatile const int *)an.state;
+            }
+            if (st == 1) {
+                __threadfence();
+                b = __ldcg(an.omega);
+            } else if (st == 0) {
+                cnt.v[kStatWaitTimeouts] += 1;
+            }
+        }
+        return __shfl_sync(mask, b, leader());
+    }
+
     // Refinement and FP64 certification of an FP32 solution; fills c.
     // Steps x <- x - B^-1 F run on the FP32 pipe: F is the float-float residual (~1e-12
     // accurate), B starts as the FP32 Jacobian, gets Broyden's rank-one secant update
@@ -647,6 +682,9 @@ struct Group {
     //   MultiSeed candidates decide, as the reference does (no trust-region run of the learned
     //   seed itself).
     // *th_out on these exits: -2 the per-point seed gave up, -3 a plateau above the bound.
+    // Without a per-point root, the plateau test takes seed 0's certified Omega as its bound
+    // (`anc`, see Anchor).  (Using it in the Omega prune as well made no difference to the
+    // bench steps and added waits in MultiSeed table mode.)
     static constexpr int kMaxRefreshJ = 12;
     static constexpr int kGiveUpRefresh = 3;
     static constexpr int kPlateauSteps = 2;
@@ -756,12 +794,13 @@ struct Group {
     }
 
     __device__ bool refine64(const PointIn &pt, const SolveOpts &o, const double *J32, const double *x32, Candidate &c,
-                             int &steps, int budget, int *th_out, double bound, bool give_up) {
+                             int &steps, int budget, int *th_out, double bound, bool give_up,
+                             const Anchor *anc = nullptr) {
         double F[5], Fo[5], p[5], B[25], xb[5], Jn[25];
         double plast = 0.0;    // |p|inf of the last step
         bool fresh = false;    // the last step used a float-float Jacobian computed at its start
         int plateau = 0;       // consecutive such steps that did not halve the residual
-        bool judged = !give_up && !(bound == bound);  // the plateau test has run (or cannot)
+        bool judged = !give_up && !(bound == bound) && !anc;  // the plateau test has run (or cannot)
         for (int i = 0; i < 25; ++i) B[i] = J32[i];
         for (int i = 0; i < 5; ++i) c.x[i] = xb[i] = x32[i];
         c.exception = false;
@@ -812,9 +851,11 @@ struct Group {
             const bool slow = give_up && stalled && refresh >= kGiveUpRefresh;
             if (!judged && ((plateau >= kPlateauSteps && fb > kPlateauFtol * o.ftol) || slow)) {
                 judged = true;  // the plateau test (see above), at the best state
+                const double pb = (bound == bound || !anc) ? bound : anchor_bound(*anc);
                 double xc[5];
                 for (int i = 0; i < 5; ++i) { xc[i] = c.x[i]; c.x[i] = xb[i]; }
-                if (eval_thermo_ff(pt, o, c) && (give_up || c.omega > bound + kPruneTightRtol * fmax(fabs(bound), 1.0))) {
+                if ((give_up || pb == pb) && eval_thermo_ff(pt, o, c) &&
+                    (give_up || c.omega > pb + kPruneTightRtol * fmax(fabs(pb), 1.0))) {
                     cnt.v[kStatPruned] += 1;
                     c.f_converged = false;
                     c.residual_norm = fb;
@@ -920,8 +961,10 @@ struct Group {
             s.th_valid = 0;
             // only where the result may be verified; J32 before the refinement's Broyden updates
             s.unstable = o.verify_seeds > 0 && dd.per_point() && det5_negative(J32) ? 1 : 0;
+            Anchor an;
+            const bool has_an = dd.plateau_anchor(an);
             if (refine64(pt, o, J32, x32, out, s.steps, o.max_iter - it32, &s.th_valid, dd.omega_bound(),
-                         o.verify_seeds > 0 && dd.per_point())) {
+                         o.verify_seeds > 0 && dd.per_point(), has_an ? &an : nullptr)) {
                 for (int k = 0; k < 5; ++k) s.x32[k] = x32[k];
                 s.it32 = it32;
                 if (cs) {
@@ -1012,6 +1055,8 @@ struct Group {
                 Candidate f;
                 const bool unst = o.verify_seeds > 0 && dd.per_point() && det5_negative(K32);
                 int st = 0, th = 0;
+                // (no seed-0 bound here: this also runs on certifying warps, which must not wait
+                // for a seed whose certification may be queued for them)
                 if (refine64(pt, o, K32, y32, f, st, o.max_iter - itt, &th, dd.omega_bound(), o.verify_seeds > 0 && dd.per_point()))
                     certify(pt, o, f, st, o.max_iter - itt, th);
                 f.iterations = itt + st;
@@ -1081,6 +1126,7 @@ struct LocalRoots {
         ++n;
     }
     __device__ double omega_bound() const { return __longlong_as_double(0x7ff8000000000000ll); }
+    __device__ bool plateau_anchor(Anchor &) const { return false; }
     __device__ const double *prior_root() const { return nullptr; }
     __device__ bool per_point() const { return true; }
     __device__ void publish(const double *) {}
@@ -1116,8 +1162,18 @@ struct PublishedRoots {
     double prior_omega;   // Omega of `prior` (NaN when there is none)
     LocalRoots own;
     bool wait_pending = false;  // wait for the verdict on an earlier seed's pending root
-    unsigned verdict_polls = kVerdictPollsDefault;  // bound of that wait
+    unsigned verdict_polls = kVerdictPollsDefault;  // bound of that wait and of the anchor wait
+    const int *anchor_state = nullptr;     // this slot's seed-0 verdict (Anchor), or null
+    const double *anchor_omega = nullptr;
     __device__ double omega_bound() const { return prior_omega; }
+    // The plateau bound of a slot without a per-point root, for seeds after seed 0.
+    __device__ bool plateau_anchor(Anchor &an) const {
+        if (!anchor_state || s == 0 || prior_omega == prior_omega) return false;
+        an.state = anchor_state;
+        an.omega = anchor_omega;
+        an.polls = verdict_polls;
+        return true;
+    }
     __device__ const double *prior_root() const { return prior; }
     // a per-point seed (no slot), whose root may be sent to the verification seeds
     __device__ bool per_point() const { return roots == nullptr; }

@@ -87,6 +87,8 @@ struct SolveArgs {
     int cert_warps;
     CertJob *jobs;                // [n * (n_seeds + 1)] deferred seeds
     int *job_ready;               // [n * (n_seeds + 1)] 1 once jobs[j] is written (zeroed)
+    int *anchor_state;            // [n] seed 0's verdict: 0 pending, 1 certified usable, 2 not (zeroed)
+    double *anchor_omega;         // [n] seed 0's Omega once anchor_state is 1
     long long *job_count;         // jobs reserved (zeroed)
     long long *job_head;          // jobs taken (zeroed)
 };

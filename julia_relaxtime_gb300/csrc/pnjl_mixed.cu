@@ -197,6 +197,12 @@ __device__ void task_complete(const SolveArgs &a, const PointIn &pt, int64_t i, 
     if (gl == 0) {
         store_record(&rec[s], c, conv);
         if (dup) rec[s].flags |= 16;
+        if (s == 0 && a.anchor_state) {  // seed 0's verdict: the slot's plateau bound (Anchor)
+            const bool usable = conv && !dup && c.omega == c.omega;
+            if (usable) a.anchor_omega[slot] = c.omega;
+            __threadfence();
+            atomicExch(&a.anchor_state[slot], usable ? 1 : 2);
+        }
         __threadfence();
         old = atomicAdd(&a.done[slot], 1);
     }
@@ -248,8 +254,13 @@ __device__ __forceinline__ PublishedRoots task_roots(const SolveArgs &a, int64_t
         for (int k = 0; k < 5; ++k) prior[k] = __ldcg(&rec[S].x[k]);
         prior_omega = __ldcg(&rec[S].omega);
     }
-    return PublishedRoots{a.roots, a.root_flag, slot * S, s, mode == kListVerify ? prior : nullptr, mask, leader, gl,
-                          prior_omega};
+    PublishedRoots dd{a.roots, a.root_flag, slot * S, s, mode == kListVerify ? prior : nullptr, mask, leader, gl,
+                      prior_omega};
+    if (a.anchor_state) {
+        dd.anchor_state = a.anchor_state + slot;
+        dd.anchor_omega = a.anchor_omega + slot;
+    }
+    return dd;
 }
 
 // Task t = (slot, seed) of the task list.  With certifying warps (defer) a seed that reaches
