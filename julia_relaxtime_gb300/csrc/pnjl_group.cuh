@@ -658,7 +658,7 @@ struct Group {
     // below dropped the seed (its Newton iteration converges, so, as in the reference, no
     // trust-region fallback follows), -2 / -3 for the give-up and plateau exits.
     // `bound` is the Omega of a certified candidate of the same point that this seed must
-    // beat (NaN when there is none).  Two tests drop a seed that cannot win, not converged:
+    // beat (NaN when there is none).  These tests drop a seed, not converged:
     // * Omega prune: a state reached by a contracting step (residual halved, now below 1e-5)
     //   whose float-float Omega -- computed at every step with the residual -- lies above the
     //   bound by more than 1e-9 |bound| plus 20 |F|inf |p|inf (p the last step): Newton's
