@@ -256,11 +256,14 @@ int pnjl_get_cert_warps(const pnjl_ctx *ctx, int32_t *warps);
  * a warp that has taken a listed slot's task or a queued certification polls the entry's
  * ready flag, written by a running warp of the same launch, at most ready_polls times (64 ns
  * apart; default 2^24, about 1 s); a seed whose FP32 root an earlier seed is still certifying
- * polls that verdict at most verdict_polls times (128 ns apart; default 2^20).  A ready wait
- * that runs out leaves the task undone and is counted in pnjl_stats.device_wait_timeouts, and
- * the host-array solves then return PNJL_ERR_CUDA ("results incomplete") -- the context stays
- * usable; a verdict wait that runs out makes the waiting seed certify the root itself (same
- * result).  0 means no polls: a flag not set at the first read gives up at once. */
+ * polls that verdict at most verdict_polls times (128 ns apart; default 2^20), and so does a
+ * seed of a point without a per-point root that reaches a residual plateau and waits for seed
+ * 0's verdict (its plateau bound).  A ready wait that runs out leaves the task undone, a
+ * seed-0 wait that runs out leaves the seed without a bound; both are counted in
+ * pnjl_stats.device_wait_timeouts, and the host-array solves then return PNJL_ERR_CUDA
+ * (results incomplete, or not reproducible) -- the context stays usable; a verdict wait that runs out makes the
+ * waiting seed certify the root itself (same result).  0 means no polls: a flag not set at
+ * the first read gives up at once. */
 int pnjl_set_wait_limits(pnjl_ctx *ctx, uint32_t ready_polls, uint32_t verdict_polls);
 int pnjl_get_wait_limits(const pnjl_ctx *ctx, uint32_t *ready_polls, uint32_t *verdict_polls);
 int pnjl_get_tuning(const pnjl_ctx *ctx, int32_t *lanes_per_point, int32_t *blocks_per_sm, int32_t *chunks);

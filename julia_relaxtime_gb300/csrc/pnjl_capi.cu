@@ -1332,7 +1332,7 @@ static int solve_batch_host(pnjl_ctx *ctx, int64_t n, const double *T, const dou
     PNJL_CUDA_TRY(ctx, cudaStreamSynchronize(s));
     if (pnjl_get_stats(ctx, &ctx->stats) != PNJL_OK) return PNJL_ERR_CUDA;
     if (ctx->stats.device_wait_timeouts)
-        return fail(ctx, PNJL_ERR_CUDA, "a solve kernel gave up waiting on a listed point (results incomplete)");
+        return fail(ctx, PNJL_ERR_CUDA, "a solve kernel gave up waiting on a listed point or a plateau bound (results incomplete or not reproducible)");
     return PNJL_OK;
 }
 
