@@ -76,3 +76,35 @@ def test_verification_on_ghost_points_matches_multiseed(engine_factory, start):
     assert st["pruned_candidates"] > 0
     if start == "minimum":
         assert (r["chosen_seed"] == -1).all()  # the per-point root is the minimum and is kept
+
+
+def test_ghost_points_identical_across_launch_forms(engine_factory):
+    """The rules for slow seeds -- the learned seed's give-up, the plateau test with the per-point
+    root or seed 0's Omega as bound -- depend only on values fixed per point, never on which
+    seed finishes first: the same results, bit for bit, from every launch form (the fused
+    kernel with 0 or 2 certifying warps, the two kernels, the chunk pipeline) and over repeats.
+    Each point is solved from its ghost (fallback mode: the MultiSeed candidates with seed 0's
+    bound) and from its minimum (verification mode: the per-point root as bound)."""
+    eng = engine_factory(128, 32)
+    T, mu, xi, ghost = _points()
+    table, hot = multiseed_table(6, (pnjl.MEDIUM_SEED_5, pnjl.HIGH_DENSITY_SEED_5))
+    ref = eng.solve(T, mu, xi, seed_table=table, seed_table_hot=hot,
+                    opts=SolveOptions(iterations=40, ftol=1e-10, precision="fp64"))
+    # every point twice, once per start, in one batch
+    T2, mu2, xi2 = np.concatenate([T, T]), np.concatenate([mu, mu]), np.concatenate([xi, xi])
+    seeds = np.concatenate([ghost, ref["x"] * (1.0 + 1e-3)])
+    opts = SolveOptions(iterations=40, ftol=1e-10, precision="mixed", verify_seeds=table.shape[0],
+                        verify_T_max_MeV=1000.0)
+    outs = []
+    for chunks, cert in ((1, 0), (1, 2), (-1, 0), (2, 0), (1, 0)):
+        eng.set_tuning(32, 0, pipeline_chunks=chunks, cert_warps=cert)
+        outs.append(eng.solve(T2, mu2, xi2, seed_table=table, seed_table_hot=hot, point_seeds=seeds, opts=opts))
+        assert eng.stats()["device_wait_timeouts"] == 0
+    eng.set_tuning(32, 0, pipeline_chunks=0, cert_warps=0)
+    for r in outs[1:]:
+        for k in ("x", "omega", "entropy", "n_q", "status", "chosen_seed", "iterations", "converged"):
+            np.testing.assert_array_equal(r[k], outs[0][k], err_msg=k)
+    n = T.size
+    for half in (slice(0, n), slice(n, 2 * n)):
+        r = {k: v[half] for k, v in outs[0].items()}
+        _same_selection(r, ref)
