@@ -193,8 +193,29 @@ class PhaseBoundaryData:
     xi: float
 
 
+_BOUNDARY_CACHE: dict = {}
+
+
+def _file_stamp(path: str):
+    try:
+        st = os.stat(path)
+        return st.st_mtime_ns, st.st_size
+    except OSError:
+        return None
+
+
 def load_phase_boundary(xi: float, boundary_path: str, cep_path: str) -> PhaseBoundaryData:
-    """SeedStrategies.jl:388-436 (rows with |xi_row - xi| <= 1e-6; sorted by T)."""
+    """SeedStrategies.jl:388-436 (rows with |xi_row - xi| <= 1e-6; sorted by T).  Parsed files
+    are kept by path, modification time and size (a scan makes one tracker per column); the
+    returned data is shared and read-only."""
+    key = (float(xi), boundary_path, cep_path, _file_stamp(boundary_path), _file_stamp(cep_path))
+    data = _BOUNDARY_CACHE.get(key)
+    if data is None:
+        data = _BOUNDARY_CACHE[key] = _read_phase_boundary(xi, boundary_path, cep_path)
+    return data
+
+
+def _read_phase_boundary(xi: float, boundary_path: str, cep_path: str) -> PhaseBoundaryData:
     T_CEP = mu_CEP = float("nan")
     if os.path.isfile(cep_path):
         for line in open(cep_path):

@@ -45,7 +45,18 @@ HEADER = [
 
 def julia_string(x: float) -> str:
     """Julia's string(::Float64): shortest round-trip digits; plain notation for decimal
-    exponents -4..5 ("120.0", "0.0001"), else "d.ddde-5" / "1.0e6" (no '+', no padding)."""
+    exponents -4..5 ("120.0", "0.0001"), else "d.ddde-5" / "1.0e6" (no '+', no padding).
+    For 1e-4 <= |x| < 1e6 that is Python's repr (the same shortest digits, plain notation)."""
+    x = float(x)
+    if x != x:
+        return "NaN"
+    if 1e-4 <= abs(x) < 1e6:
+        return repr(x)
+    return _julia_string_general(x)
+
+
+def _julia_string_general(x: float) -> str:
+    """julia_string for every double, from the digits of repr."""
     x = float(x)
     if math.isnan(x):
         return "NaN"
@@ -218,7 +229,9 @@ def format_row(r: dict) -> str:
     out = []
     for k in HEADER:
         v = r[k]
-        if isinstance(v, bool):
+        if type(v) is float:  # most columns
+            out.append(julia_string(v))
+        elif isinstance(v, bool):
             out.append("true" if v else "false")
         elif isinstance(v, (int, np.integer)):
             out.append(str(int(v)))

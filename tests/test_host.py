@@ -142,6 +142,22 @@ def test_julia_string_edge_cases():
     assert julia_string(2.5e-300) == "2.5e-300"
 
 
+def test_julia_string_fast_path_matches_general():
+    """julia_string returns repr for 1e-4 <= |x| < 1e6; the general digit-by-digit routine
+    gives the same text there, on random doubles of every magnitude and at the edges."""
+    from julia_relaxtime_gb300.scan import _julia_string_general
+
+    rng = np.random.default_rng(3)
+    xs = np.concatenate([
+        rng.uniform(-1, 1, 20000) * 10.0 ** rng.integers(-8, 9, 20000),
+        rng.standard_normal(5000),
+        np.array([1e-4, -1e-4, np.nextafter(1e-4, 0), np.nextafter(1e-4, 1), 1e6, np.nextafter(1e6, 0),
+                  999999.9999999999, 0.1, 0.2, 0.3, 1.0 / 3.0, 123456.7, 5e-324, 1.7976931348623157e308]),
+    ])
+    for x in xs:
+        assert julia_string(float(x)) == _julia_string_general(float(x)), x
+
+
 def test_scan_grid_and_rows_shape(tmp_path):
     assert julia_range(50.0, 200.0, 10.0)[-1] == 200.0 and len(julia_range(50.0, 200.0, 10.0)) == 16
     assert len(julia_range(0.0, 1200.0, 60.0)) == 21
