@@ -462,3 +462,29 @@ def test_candidates_and_labels_select_like_solve_multi():
 
     table, hot = label_table(cfg)
     assert np.array_equal(eng.seeds[:, 0], table) and np.array_equal(eng.seeds[:, 3], hot)
+
+
+def test_bench_reference_arm_json_line():
+    """bench.py --impl reference (the reference algorithm on the host cores, no GPU) prints one
+    JSON line with the bench contract's keys: the metric, whole-job value, timing fields (warm-up
+    raised to 3), the CPU baseline it measured and an e2e block without host-device copies."""
+    import json
+    import subprocess
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "1",
+                          "--cpu-sample", "4"], cwd=root, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = [s for s in out.stdout.splitlines() if s.startswith("{")][-1]
+    d = json.loads(line)
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+              "vs_baseline", "dtype", "data", "config", "impl", "cpu_baseline", "e2e"):
+        assert k in d, k
+    assert d["impl"] == "reference" and d["value"] > 0 and d["unit"] == "solves/s" and d["higher_is_better"]
+    assert d["steps"] == 1 and d["warmup"] >= 3 and d["vs_baseline"] is None
+    assert d["config"]["workload"] == "first_order_2048x2048x9"
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    assert cb["single_thread"]["cores"] == 1 and cb["single_thread"]["value"] > 0
+    assert d["e2e"] == {"value": d["value"], "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
